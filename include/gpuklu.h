@@ -1,0 +1,220 @@
+/* gpuklu.h - C ABI of the GB300 Newton inner loop for RustSpice.
+ *
+ * A drop-in for the reference's `LinearSolver` trait
+ * (crates/sim-core/src/solver.rs:141-166) plus a device-stamp Newton path and
+ * a batched path. Plain pointers and sizes only; every function is callable
+ * from a Rust `extern "C"` block, ctypes, or C/C++.
+ *
+ * Threading: a handle is used by one thread at a time (the trait is `Send`,
+ * not `Sync`); many handles may coexist, each with its own CUDA stream.
+ * Host pointers are host memory unless a name ends in _device.
+ */
+#ifndef GPUKLU_H
+#define GPUKLU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. 0..6 mirror SolverError (crates/sim-core/src/solver.rs:76-92):
+ * AnalyzeFailed, FactorFailed, SolveFailed, SingularMatrix{pivot},
+ * IllConditioned{rcond}, InvalidMatrix{reason}. 7.. are device conditions. */
+enum {
+  GPUKLU_OK = 0,
+  GPUKLU_ANALYZE_FAILED = 1,
+  GPUKLU_FACTOR_FAILED = 2,
+  GPUKLU_SOLVE_FAILED = 3,
+  GPUKLU_SINGULAR = 4,
+  GPUKLU_ILL_CONDITIONED = 5,
+  GPUKLU_INVALID_MATRIX = 6,
+  GPUKLU_DEVICE_TIMEOUT = 7, /* a dependency wait hit its spin limit */
+  GPUKLU_NONFINITE = 8,      /* NaN/Inf in a Newton iterate */
+  GPUKLU_CUDA_ERROR = 9      /* CUDA runtime error; see gpuklu_last_error */
+};
+
+/* Pivot handling of the first factorization.
+ * REFERENCE: NativeKLU's rule exactly (crates/sim-core/src/native_klu.rs:
+ *   1295-1334): threshold row swaps inside the symbolic pattern computed
+ *   without pivoting; entries a swap moves outside that pattern are dropped,
+ *   and later refactorizations reuse the pivots.
+ * EXACT: the same first pass chooses the pivots, then the pattern is
+ *   recomputed for the row-permuted blocks and every factorization refactors
+ *   that exact pattern; BTF coupling blocks are applied where BTF puts them
+ *   (below the diagonal blocks). */
+enum { GPUKLU_PIVOT_REFERENCE = 0, GPUKLU_PIVOT_EXACT = 1 };
+
+typedef struct gpuklu_handle gpuklu_handle;
+
+typedef struct {
+  int64_t factor_count;   /* full factorizations (pivot discovery) */
+  int64_t refactor_count; /* refactorizations with frozen pivots */
+  int64_t nnz_l, nnz_u;   /* symbolic pattern sizes (U includes the diagonal) */
+  int64_t nblocks;        /* BTF diagonal blocks */
+  int64_t noffdiag;       /* entries in the BTF coupling blocks used by solve */
+  int64_t pivot_swaps;    /* rows whose pivot differs from the diagonal */
+  int64_t refactor_flops; /* multiply/add/divide count of one refactorization */
+  double rcond;           /* min|u_kk| / max|u_kk| (native_klu.rs:1406-1427) */
+} gpuklu_stats;
+
+/* ------------------------------------------------ LinearSolver (solver.rs:141-166) */
+
+/* NativeKluSolver::new (native_klu.rs:659-674). Returns NULL if no CUDA
+ * device is usable (the reason is printed to stderr). */
+gpuklu_handle* gpuklu_create(int64_t n);
+void gpuklu_destroy(gpuklu_handle* h);
+/* prepare (native_klu.rs:1608-1614): a new n resets the cached pattern. */
+void gpuklu_prepare(gpuklu_handle* h, int64_t n);
+/* analyze (native_klu.rs:1616-1632): no-op when (ap, ai) equal the cached
+ * pattern; ap_len != n + 1 gives GPUKLU_INVALID_MATRIX. */
+int gpuklu_analyze(gpuklu_handle* h, const int64_t* ap, int64_t ap_len, const int64_t* ai,
+                   int64_t ai_len);
+/* factor (native_klu.rs:1634-1641): re-analyzes on a pattern change, else
+ * refactors with the frozen pivots. ax has ai_len values (host memory). */
+int gpuklu_factor(gpuklu_handle* h, const int64_t* ap, int64_t ap_len, const int64_t* ai,
+                  int64_t ai_len, const double* ax);
+/* solve (native_klu.rs:1643-1655): rhs (length n) is overwritten with x.
+ * Before a factorization: GPUKLU_SOLVE_FAILED. */
+int gpuklu_solve(gpuklu_handle* h, double* rhs, int64_t len);
+/* reset_pattern (native_klu.rs:1657-1666). */
+void gpuklu_reset_pattern(gpuklu_handle* h);
+/* name (native_klu.rs:1668-1670) -> "GpuKLU". */
+const char* gpuklu_name(const gpuklu_handle* h);
+/* set_parallel_threads (native_klu.rs:1672-1674): accepted and ignored; the
+ * device decides its own parallelism. */
+void gpuklu_set_parallel_threads(gpuklu_handle* h, size_t threads);
+
+/* ------------------------------------------------ extensions */
+
+/* Pivot mode for the next analysis (default GPUKLU_PIVOT_REFERENCE). */
+int gpuklu_set_pivot_mode(gpuklu_handle* h, int mode);
+/* Counters of NativeKluStats (native_klu.rs:584-594) plus device figures. */
+int gpuklu_get_stats(gpuklu_handle* h, gpuklu_stats* out);
+/* Text of the last error on this handle ("" if none). */
+const char* gpuklu_last_error(const gpuklu_handle* h);
+/* factor/solve with values already in device memory (the device-stamp path):
+ * d_ax has the cached pattern's nnz values, d_rhs has n values. */
+int gpuklu_factor_device(gpuklu_handle* h, const double* d_ax);
+int gpuklu_solve_device(gpuklu_handle* h, double* d_rhs);
+/* Transpose solve A^T y = g with the current factors (the adjoint). No
+ * counterpart in the reference: klu_l_tsolve is bound but never called
+ * (crates/sim-core/src/solver.rs:1740-1747). g (length n) is overwritten
+ * with y. */
+int gpuklu_tsolve(gpuklu_handle* h, double* g, int64_t len);
+/* Raw CUDA stream of the handle (cudaStream_t), for callers that enqueue
+ * their own work around the solver. */
+void* gpuklu_stream(gpuklu_handle* h);
+
+/* ------------------------------------------------ device stamping + Newton */
+
+/* Device types and parameter slots (p[6] per device):
+ *   0 R  p0 = ohms                    1 V  p0 = volts
+ *   2 I  p0 = amps                    3 D  p0 = Is, p1 = N
+ *   4 M  level-1 as the reference evaluates it (bsim/evaluate.rs:285-356):
+ *        p0 = is_pmos, p1 = vth0, p2 = u0, p3 = tox, p4 = W, p5 = L
+ *   5 C  p0 = farads (open in DC, backward Euler in transient)
+ *   6 MC level-1 with a self-consistent linearisation, same parameters.
+ * nodes[4] per device: R/V/I/D/C use (a, b); M/MC use (d, g, s, b).
+ * Node 0 is ground and stays in the matrix; one aux unknown per V source. */
+typedef struct gpuklu_circuit gpuklu_circuit;
+
+/* Compiles the device list into a stamp-to-slot map: the MNA pattern the
+ * reference's build closure produces (crates/sim-core/src/engine.rs:262-283:
+ * every instance stamped in order, ground pinned, CSC not merged), and for
+ * every insert its CSC index. transient != 0 includes capacitor stamps. */
+gpuklu_circuit* gpuklu_compile_devices(int64_t node_count, int64_t ndev, const int32_t* type,
+                                       const int32_t* nodes, const double* p, int transient);
+void gpuklu_circuit_free(gpuklu_circuit* c);
+/* Matrix dimension and raw (unmerged) nonzero count of a compiled circuit. */
+int gpuklu_circuit_dims(const gpuklu_circuit* c, int64_t* n, int64_t* nnz_raw);
+/* CSC pattern of a compiled circuit (ap: n+1, ai: nnz_raw). */
+int gpuklu_circuit_pattern(const gpuklu_circuit* c, int64_t* ap, int64_t* ai);
+/* Updates device parameters in place (p has ndev*6 values). */
+int gpuklu_circuit_set_params(gpuklu_circuit* c, const double* p);
+/* Stamps the circuit at x on the device and copies the raw CSC values and
+ * the right-hand side back (tests and callers that bring their own solver).
+ * cap_v: per-device previous capacitor voltage (transient), may be NULL. */
+int gpuklu_stamp(gpuklu_handle* h, gpuklu_circuit* c, const double* x, int64_t xlen,
+                 double gmin, double source_scale, double dt, const double* cap_v,
+                 double be_sign, double* ax_out, double* rhs_out);
+
+typedef struct {
+  int64_t max_iters;     /* itl1 */
+  double abs_tol;        /* vntol */
+  double rel_tol;        /* reltol */
+  double gmin;
+  int64_t gmin_steps;    /* GminSchedule steps (newton.rs:204-237) */
+  int64_t source_steps;  /* SourceSchedule steps (newton.rs:240-265) */
+  double damping, damping_min;
+} gpuklu_newton_config;
+
+/* DC operating point (engine.rs:249-311) with run_newton_with_stepping
+ * (newton.rs:142-185): stamping, factor, solve and the Newton update all on
+ * the device. x0 (node_count values) may be NULL for the zero start. x_out
+ * receives min(x_cap, len(x)) values of the final iterate; *x_len its length
+ * (n when converged, node_count otherwise). Returns a status; *reason is the
+ * NewtonExitReason (0 converged, 1 max iterations, 2 solver failure) and
+ * *iters the iterations of the final Newton run, *iters_total all of them. */
+int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_config* cfg,
+                     const double* x0, double* x_out, int64_t x_cap, int64_t* x_len,
+                     int64_t* iters, int64_t* iters_total, int* reason);
+
+/* ------------------------------------------------ batched Newton */
+
+typedef struct gpuklu_batch gpuklu_batch;
+
+/* Many independent DC operating points in one launch. Circuits are given as
+ * concatenated device lists (dev_off[ncirc+1]); instance i runs circuit
+ * inst_circ[i] with the first parameter of device inst_dev[i] replaced by
+ * inst_val[i] (inst_dev < 0: none) from initial iterate x0 + x0_off[i]
+ * (x0_off < 0: zero start). Instances of one circuit share its analysis,
+ * pivots (exact mode, found once per circuit) and device program. */
+gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
+                                  const int64_t* node_counts, const int32_t* type,
+                                  const int32_t* nodes, const double* p, int64_t ninst,
+                                  const int64_t* inst_circ, const int64_t* inst_dev,
+                                  const double* inst_val, const double* x0,
+                                  const int64_t* x0_off, int64_t x0_len);
+void gpuklu_batch_destroy(gpuklu_batch* b);
+/* Runs every instance's Newton loop on the device (one kernel launch). */
+int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg);
+/* Results: per instance iterations (final run), total iterations, exit
+ * reason, and x (n of its circuit values, at x_out + x_off[i]; x_off may be
+ * NULL to skip). */
+int gpuklu_batch_results(gpuklu_batch* b, int64_t* iters, int64_t* iters_total, int32_t* reason,
+                         double* x_out, const int64_t* x_off);
+/* Host->device copy of new per-instance values and initial iterates
+ * (same layout as at creation; either pointer may be NULL). */
+int gpuklu_batch_update_inputs(gpuklu_batch* b, const double* inst_val, const double* x0);
+/* Last error text of the batch. */
+const char* gpuklu_batch_last_error(const gpuklu_batch* b);
+/* Launch geometry and work figures: out[0] grid, out[1] block, out[2]
+ * tiles, out[3] buffer bytes, out[4] value bytes touched per Newton
+ * iteration summed over one instance of every circuit. */
+int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out);
+void* gpuklu_batch_stream(gpuklu_batch* b);
+
+/* ------------------------------------------------ host-only diagnostics */
+
+/* The symbolic plan the handle would build for a pattern (host work only; no
+ * device needed): BTF + AMD + symbolic, and, if row_perm is not NULL, the
+ * pivot sequence installed as a first factorization would (block-local
+ * row_perm per position). Arrays are read back by name with
+ * gpuklu_plan_array: "col_ptr", "dslot", "slot_row", "upd_ptr", "upd_dst",
+ * "amap_ptr", "amap_idx", "offd_ptr", "offd_col", "offd_raw", "in_pos",
+ * "out_pos", "block_ptr", "col_single", "pcol_ptr", "pcol_raw", "pcol_q",
+ * "pos_block", "raw_slot", "row_perm", "lrow_ptr", "lrow_col", "lrow_slot",
+ * "urow_ptr", "urow_col", "urow_slot", "info" (n, nslots, nblocks, nnz_l,
+ * nnz_u, noffdiag, offd_lower, swaps). */
+typedef struct gpuklu_plan gpuklu_plan;
+gpuklu_plan* gpuklu_plan_build(int64_t n, const int64_t* ap, const int64_t* ai, int pivot_mode,
+                               const int32_t* row_perm);
+int64_t gpuklu_plan_array(const gpuklu_plan* p, const char* name, int64_t* out, int64_t cap);
+void gpuklu_plan_free(gpuklu_plan* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPUKLU_H */

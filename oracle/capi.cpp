@@ -1,0 +1,226 @@
+// Oracle (test infrastructure only): a flat C interface over the CPU
+// restatement so that tests/ and bench.py's CPU-baseline leg can drive it
+// through ctypes. Nothing in the product links this library.
+#include <atomic>
+#include <cstring>
+#include <thread>
+
+#include "oracle.h"
+
+using namespace oracle;
+
+namespace {
+Circuit make_circuit(int64_t node_count, int64_t ndev, const int32_t* type,
+                     const int32_t* nodes, const double* p) {
+  Circuit c;
+  c.node_count = (size_t)node_count;
+  c.type.assign(type, type + ndev);
+  c.nodes.assign(nodes, nodes + ndev * 4);
+  c.p.assign(p, p + ndev * NPARAM);
+  return c;
+}
+IVec ivec(const int64_t* p, int64_t n) { return IVec(p, p + n); }
+}  // namespace
+
+extern "C" {
+
+void* orc_solver_new(const char* kind, int64_t n) {
+  return make_solver(kind, (size_t)n).release();
+}
+void orc_solver_free(void* h) { delete static_cast<LinearSolver*>(h); }
+void orc_prepare(void* h, int64_t n) { static_cast<LinearSolver*>(h)->prepare((size_t)n); }
+const char* orc_name(void* h) { return static_cast<LinearSolver*>(h)->name(); }
+void orc_reset(void* h) { static_cast<LinearSolver*>(h)->reset_pattern(); }
+
+int orc_analyze(void* h, const int64_t* ap, int64_t aplen, const int64_t* ai,
+                int64_t nnz) {
+  return static_cast<LinearSolver*>(h)->analyze(ivec(ap, aplen), ivec(ai, nnz));
+}
+int orc_factor(void* h, const int64_t* ap, int64_t aplen, const int64_t* ai,
+               const double* ax, int64_t nnz) {
+  return static_cast<LinearSolver*>(h)->factor(ivec(ap, aplen), ivec(ai, nnz),
+                                               Vec(ax, ax + nnz));
+}
+int orc_solve(void* h, double* rhs, int64_t len) {
+  Vec r(rhs, rhs + len);
+  int st = static_cast<LinearSolver*>(h)->solve(r);
+  if (st == ST_OK) std::memcpy(rhs, r.data(), sizeof(double) * (size_t)len);
+  return st;
+}
+
+// NativeKLU counters: out[0..5] = factor, refactor, nnz_l, nnz_u, nblocks,
+// noffdiag; *rcond = rcond.
+int orc_klu_stats(void* h, int64_t* out, double* rcond) {
+  auto* k = dynamic_cast<NativeKluSolver*>(static_cast<LinearSolver*>(h));
+  if (!k) return -1;
+  const KluStats& s = k->stats();
+  out[0] = (int64_t)s.factor_count;
+  out[1] = (int64_t)s.refactor_count;
+  out[2] = (int64_t)s.nnz_l;
+  out[3] = (int64_t)s.nnz_u;
+  out[4] = (int64_t)s.nblocks;
+  out[5] = (int64_t)s.noffdiag;
+  *rcond = s.rcond;
+  return 0;
+}
+
+// NativeKLU pivot sequence: concatenation over blocks of row_perm (block
+// local). Returns the number written, or -1.
+int64_t orc_klu_pivots(void* h, int64_t* out, int64_t cap) {
+  auto* k = dynamic_cast<NativeKluSolver*>(static_cast<LinearSolver*>(h));
+  if (!k) return -1;
+  int64_t w = 0;
+  for (auto& nm : k->numeric())
+    for (size_t r : nm.row_perm) {
+      if (w < cap) out[w] = (int64_t)r;
+      ++w;
+    }
+  return w;
+}
+
+// NativeKLU factor values for inspection: l values then u values of block b.
+int64_t orc_klu_block_values(void* h, int64_t b, double* l, int64_t lcap,
+                             double* u, int64_t ucap, int64_t* nl, int64_t* nu) {
+  auto* k = dynamic_cast<NativeKluSolver*>(static_cast<LinearSolver*>(h));
+  if (!k || b < 0 || (size_t)b >= k->numeric().size()) return -1;
+  auto& nm = k->numeric()[(size_t)b];
+  *nl = (int64_t)nm.l_val.size();
+  *nu = (int64_t)nm.u_val.size();
+  for (int64_t i = 0; i < *nl && i < lcap; ++i) l[i] = nm.l_val[(size_t)i];
+  for (int64_t i = 0; i < *nu && i < ucap; ++i) u[i] = nm.u_val[(size_t)i];
+  return 0;
+}
+
+void orc_amd(int64_t n, const int64_t* ap, const int64_t* ai, int64_t* perm,
+             int64_t* inv) {
+  AmdResult r = amd_order((size_t)n, ap, ai);
+  for (int64_t i = 0; i < n; ++i) {
+    perm[i] = (int64_t)r.perm[(size_t)i];
+    inv[i] = (int64_t)r.inv_perm[(size_t)i];
+  }
+}
+
+// info[0..3] = num_blocks, structural_rank, num_singletons, max_block_size
+void orc_btf(int64_t n, const int64_t* ap, const int64_t* ai, int64_t* row_perm,
+             int64_t* col_perm, int64_t* block_ptr, int64_t* info) {
+  Btf b = btf_decompose((size_t)n, ap, ai);
+  for (int64_t i = 0; i < n; ++i) {
+    row_perm[i] = (int64_t)b.row_perm[(size_t)i];
+    col_perm[i] = (int64_t)b.col_perm[(size_t)i];
+  }
+  for (size_t i = 0; i < b.block_ptr.size(); ++i) block_ptr[i] = (int64_t)b.block_ptr[i];
+  info[0] = (int64_t)b.num_blocks;
+  info[1] = (int64_t)b.structural_rank;
+  info[2] = (int64_t)b.num_singletons;
+  info[3] = (int64_t)b.max_block_size;
+}
+
+// MNA system of a circuit at x.
+void* orc_mna(int64_t node_count, int64_t ndev, const int32_t* type,
+              const int32_t* nodes, const double* p, const double* x,
+              int64_t xlen, double gmin, double scale, double dt,
+              const double* cap_v, double be_sign) {
+  Circuit c = make_circuit(node_count, ndev, type, nodes, p);
+  TranState st;
+  if (cap_v) st.cap_v.assign(cap_v, cap_v + ndev);
+  auto* s = new MnaSystem(build_mna(c, Vec(x, x + xlen), gmin, scale, dt,
+                                    cap_v ? &st : nullptr, be_sign));
+  return s;
+}
+void orc_mna_dims(void* h, int64_t* n, int64_t* nnz) {
+  auto* s = static_cast<MnaSystem*>(h);
+  *n = (int64_t)s->n;
+  *nnz = (int64_t)s->ai.size();
+}
+void orc_mna_get(void* h, int64_t* ap, int64_t* ai, double* ax, double* rhs) {
+  auto* s = static_cast<MnaSystem*>(h);
+  std::memcpy(ap, s->ap.data(), sizeof(int64_t) * s->ap.size());
+  std::memcpy(ai, s->ai.data(), sizeof(int64_t) * s->ai.size());
+  std::memcpy(ax, s->ax.data(), sizeof(double) * s->ax.size());
+  std::memcpy(rhs, s->rhs.data(), sizeof(double) * s->rhs.size());
+}
+void orc_mna_free(void* h) { delete static_cast<MnaSystem*>(h); }
+
+// One DC operating point. cfg: max_iters, abs_tol, rel_tol, gmin, gmin_steps,
+// source_steps. Returns the Newton exit reason; x_out gets min(n, x_cap)
+// entries of the final x.
+int orc_dc_op(int64_t node_count, int64_t ndev, const int32_t* type,
+              const int32_t* nodes, const double* p, const char* solver_kind,
+              int64_t max_iters, double abs_tol, double rel_tol, double gmin,
+              int64_t gmin_steps, int64_t source_steps, double* x_out,
+              int64_t x_cap, int64_t* x_len, int64_t* iters) {
+  Circuit c = make_circuit(node_count, ndev, type, nodes, p);
+  NewtonConfig cfg;
+  cfg.max_iters = (size_t)max_iters;
+  cfg.abs_tol = abs_tol;
+  cfg.rel_tol = rel_tol;
+  cfg.gmin = gmin;
+  cfg.gmin_steps = (size_t)gmin_steps;
+  cfg.source_steps = (size_t)source_steps;
+  auto solver = make_solver(solver_kind, c.node_count);
+  Vec x;
+  NewtonResult r = dc_op(c, cfg, *solver, x);
+  *x_len = (int64_t)x.size();
+  for (int64_t i = 0; i < x_cap && (size_t)i < x.size(); ++i) x_out[i] = x[(size_t)i];
+  *iters = (int64_t)r.iterations;
+  return r.reason;
+}
+
+double orc_residual(int64_t node_count, int64_t ndev, const int32_t* type,
+                    const int32_t* nodes, const double* p, const double* x,
+                    int64_t xlen, double gmin) {
+  Circuit c = make_circuit(node_count, ndev, type, nodes, p);
+  return residual_inf(c, Vec(x, x + xlen), gmin);
+}
+
+// Many independent DC operating points over a thread pool: instance i runs
+// circuit inst_circ[i] with device inst_dev[i]'s first parameter replaced by
+// inst_val[i] (inst_dev < 0: no override). Circuits are concatenated device
+// lists delimited by dev_off[ncirc + 1]. Per instance: iterations, exit
+// reason, and x (x_cap entries, zero padded).
+void orc_dc_batch(int64_t ncirc, const int64_t* dev_off, const int64_t* node_counts,
+                  const int32_t* type, const int32_t* nodes, const double* p,
+                  int64_t ninst, const int64_t* inst_circ, const int64_t* inst_dev,
+                  const double* inst_val, const char* solver_kind, int64_t max_iters,
+                  double abs_tol, double rel_tol, double gmin, int64_t gmin_steps,
+                  int64_t nthreads, int64_t* iters, int32_t* reason, double* x_out,
+                  int64_t x_cap) {
+  std::vector<Circuit> circs((size_t)ncirc);
+  for (int64_t c = 0; c < ncirc; ++c) {
+    int64_t d0 = dev_off[c], d1 = dev_off[c + 1];
+    circs[(size_t)c] = make_circuit(node_counts[c], d1 - d0, type + d0,
+                                    nodes + d0 * 4, p + d0 * NPARAM);
+  }
+  NewtonConfig cfg;
+  cfg.max_iters = (size_t)max_iters;
+  cfg.abs_tol = abs_tol;
+  cfg.rel_tol = rel_tol;
+  cfg.gmin = gmin;
+  cfg.gmin_steps = (size_t)gmin_steps;
+  std::string kind(solver_kind);
+  std::atomic<int64_t> next(0);
+  auto worker = [&]() {
+    while (true) {
+      int64_t i = next.fetch_add(1);
+      if (i >= ninst) break;
+      Circuit c = circs[(size_t)inst_circ[i]];
+      if (inst_dev[i] >= 0) c.p[(size_t)inst_dev[i] * NPARAM] = inst_val[i];
+      auto s = make_solver(kind, c.node_count);
+      Vec x;
+      NewtonResult r = dc_op(c, cfg, *s, x);
+      iters[i] = (int64_t)r.iterations;
+      reason[i] = r.reason;
+      double* xo = x_out ? x_out + i * x_cap : nullptr;
+      if (xo)
+        for (int64_t k = 0; k < x_cap; ++k)
+          xo[k] = (size_t)k < x.size() ? x[(size_t)k] : 0.0;
+    }
+  };
+  int64_t nt = nthreads < 1 ? 1 : nthreads;
+  std::vector<std::thread> th;
+  for (int64_t t = 1; t < nt; ++t) th.emplace_back(worker);
+  worker();
+  for (auto& t : th) t.join();
+}
+
+}  // extern "C"

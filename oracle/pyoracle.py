@@ -1,0 +1,212 @@
+"""ctypes wrapper over the oracle library (test infrastructure only).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
+this module, as the checker. The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_P = C.c_void_p
+_I64 = C.c_int64
+_D = C.c_double
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        L.orc_solver_new.restype = _P
+        L.orc_solver_new.argtypes = [C.c_char_p, _I64]
+        L.orc_solver_free.argtypes = [_P]
+        L.orc_prepare.argtypes = [_P, _I64]
+        L.orc_name.restype = C.c_char_p
+        L.orc_name.argtypes = [_P]
+        L.orc_reset.argtypes = [_P]
+        L.orc_analyze.argtypes = [_P, _P, _I64, _P, _I64]
+        L.orc_factor.argtypes = [_P, _P, _I64, _P, _P, _I64]
+        L.orc_solve.argtypes = [_P, _P, _I64]
+        L.orc_klu_stats.argtypes = [_P, _P, _P]
+        L.orc_klu_pivots.restype = _I64
+        L.orc_klu_pivots.argtypes = [_P, _P, _I64]
+        L.orc_klu_block_values.restype = _I64
+        L.orc_klu_block_values.argtypes = [_P, _I64, _P, _I64, _P, _I64, _P, _P]
+        L.orc_amd.argtypes = [_I64, _P, _P, _P, _P]
+        L.orc_btf.argtypes = [_I64, _P, _P, _P, _P, _P, _P]
+        L.orc_mna.restype = _P
+        L.orc_mna.argtypes = [_I64, _I64, _P, _P, _P, _P, _I64, _D, _D, _D, _P, _D]
+        L.orc_mna_dims.argtypes = [_P, _P, _P]
+        L.orc_mna_get.argtypes = [_P, _P, _P, _P, _P]
+        L.orc_mna_free.argtypes = [_P]
+        L.orc_dc_op.restype = C.c_int
+        L.orc_dc_op.argtypes = [_I64, _I64, _P, _P, _P, C.c_char_p, _I64, _D, _D, _D,
+                                _I64, _I64, _P, _I64, _P, _P]
+        L.orc_residual.restype = _D
+        L.orc_residual.argtypes = [_I64, _I64, _P, _P, _P, _P, _I64, _D]
+        L.orc_dc_batch.argtypes = [_I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, C.c_char_p,
+                                   _I64, _D, _D, _D, _I64, _I64, _P, _P, _P, _I64]
+        _lib = L
+    return _lib
+
+
+def _i64(a):
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Solver:
+    """One of the reference's LinearSolver implementations, restated."""
+
+    def __init__(self, kind: str, n: int):
+        self.h = lib().orc_solver_new(kind.encode(), n)
+        self.n = n
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_solver_free(self.h)
+            self.h = None
+
+    def prepare(self, n):
+        self.n = n
+        lib().orc_prepare(self.h, n)
+
+    def name(self):
+        return lib().orc_name(self.h).decode()
+
+    def reset_pattern(self):
+        lib().orc_reset(self.h)
+
+    def analyze(self, ap, ai):
+        ap, ai = _i64(ap), _i64(ai)
+        return lib().orc_analyze(self.h, _ptr(ap), len(ap), _ptr(ai), len(ai))
+
+    def factor(self, ap, ai, ax):
+        ap, ai, ax = _i64(ap), _i64(ai), _f64(ax)
+        return lib().orc_factor(self.h, _ptr(ap), len(ap), _ptr(ai), _ptr(ax), len(ai))
+
+    def solve(self, rhs):
+        """Solves in place on a float64 copy; returns (status, x)."""
+        x = _f64(rhs).copy()
+        st = lib().orc_solve(self.h, _ptr(x), len(x))
+        return st, x
+
+    def klu_stats(self):
+        out = np.zeros(6, np.int64)
+        rc = C.c_double()
+        if lib().orc_klu_stats(self.h, _ptr(out), C.byref(rc)) != 0:
+            return None
+        keys = ["factor_count", "refactor_count", "nnz_l", "nnz_u", "nblocks", "noffdiag"]
+        d = {k: int(v) for k, v in zip(keys, out)}
+        d["rcond"] = rc.value
+        return d
+
+    def klu_pivots(self):
+        cap = max(self.n, 1)
+        out = np.zeros(cap, np.int64)
+        w = lib().orc_klu_pivots(self.h, _ptr(out), cap)
+        return out[:w]
+
+
+def amd(n, ap, ai):
+    ap, ai = _i64(ap), _i64(ai)
+    perm = np.zeros(n, np.int64)
+    inv = np.zeros(n, np.int64)
+    lib().orc_amd(n, _ptr(ap), _ptr(ai), _ptr(perm), _ptr(inv))
+    return perm, inv
+
+
+def btf(n, ap, ai):
+    ap, ai = _i64(ap), _i64(ai)
+    rp = np.zeros(n, np.int64)
+    cp = np.zeros(n, np.int64)
+    bp = np.zeros(n + 1, np.int64)
+    info = np.zeros(4, np.int64)
+    lib().orc_btf(n, _ptr(ap), _ptr(ai), _ptr(rp), _ptr(cp), _ptr(bp), _ptr(info))
+    nb = int(info[0])
+    return dict(row_perm=rp, col_perm=cp, block_ptr=bp[:nb + 1], num_blocks=nb,
+                structural_rank=int(info[1]), num_singletons=int(info[2]),
+                max_block_size=int(info[3]))
+
+
+def _circ_arrays(c):
+    return (_i64([0]) if False else None, np.ascontiguousarray(c.type, np.int32),
+            np.ascontiguousarray(c.nodes, np.int32), _f64(c.p))
+
+
+def mna(c, x, gmin=1e-12, scale=1.0, dt=0.0, cap_v=None, be_sign=-1.0):
+    """The reference engine's MNA build at x: (n, ap, ai, ax, rhs)."""
+    _, t, nd, p = _circ_arrays(c)
+    x = _f64(x)
+    cv = _f64(cap_v) if cap_v is not None else None
+    h = lib().orc_mna(c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p), _ptr(x), len(x),
+                      gmin, scale, dt, _ptr(cv) if cv is not None else None, be_sign)
+    n = C.c_int64()
+    nnz = C.c_int64()
+    lib().orc_mna_dims(h, C.byref(n), C.byref(nnz))
+    ap = np.zeros(n.value + 1, np.int64)
+    ai = np.zeros(nnz.value, np.int64)
+    ax = np.zeros(nnz.value)
+    rhs = np.zeros(n.value)
+    lib().orc_mna_get(h, _ptr(ap), _ptr(ai), _ptr(ax), _ptr(rhs))
+    lib().orc_mna_free(h)
+    return n.value, ap, ai, ax, rhs
+
+
+REASONS = {0: "converged", 1: "maxiters", 2: "solver_failure"}
+
+
+def dc_op(c, solver="nativeklu", max_iters=100, abs_tol=1e-6, rel_tol=1e-3,
+          gmin=1e-12, gmin_steps=0, source_steps=0):
+    """Engine DC operating point. Returns (reason, iterations, x)."""
+    _, t, nd, p = _circ_arrays(c)
+    cap = c.n
+    x = np.zeros(cap)
+    xl = C.c_int64()
+    it = C.c_int64()
+    r = lib().orc_dc_op(c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p), solver.encode(),
+                        max_iters, abs_tol, rel_tol, gmin, gmin_steps, source_steps,
+                        _ptr(x), cap, C.byref(xl), C.byref(it))
+    return REASONS[r], it.value, x[:xl.value]
+
+
+def residual(c, x, gmin=1e-12):
+    _, t, nd, p = _circ_arrays(c)
+    x = _f64(x)
+    return lib().orc_residual(c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p),
+                              _ptr(x), len(x), gmin)
+
+
+def dc_batch(circuits, inst_circ, inst_dev, inst_val, solver="nativeklu", max_iters=100,
+             abs_tol=1e-6, rel_tol=1e-3, gmin=1e-12, gmin_steps=0, nthreads=1, x_cap=0):
+    """Independent DC operating points over a thread pool."""
+    dev_off = np.zeros(len(circuits) + 1, np.int64)
+    for i, c in enumerate(circuits):
+        dev_off[i + 1] = dev_off[i] + c.ndev
+    ncs = _i64([c.node_count for c in circuits])
+    t = np.ascontiguousarray(np.concatenate([c.type for c in circuits]), np.int32)
+    nd = np.ascontiguousarray(np.concatenate([c.nodes for c in circuits]), np.int32)
+    p = _f64(np.concatenate([c.p for c in circuits]))
+    ic, idv, iv = _i64(inst_circ), _i64(inst_dev), _f64(inst_val)
+    ninst = len(ic)
+    iters = np.zeros(ninst, np.int64)
+    reason = np.zeros(ninst, np.int32)
+    xo = np.zeros((ninst, max(x_cap, 1)))
+    lib().orc_dc_batch(len(circuits), _ptr(dev_off), _ptr(ncs), _ptr(t), _ptr(nd), _ptr(p),
+                       ninst, _ptr(ic), _ptr(idv), _ptr(iv), solver.encode(), max_iters,
+                       abs_tol, rel_tol, gmin, gmin_steps, nthreads, _ptr(iters),
+                       _ptr(reason), _ptr(xo) if x_cap > 0 else None, x_cap)
+    return iters, reason, (xo if x_cap > 0 else None)

@@ -1,0 +1,844 @@
+// CUDA kernels of the Newton inner loop (sm_103a).
+//
+//  * first_factor  - the reference's first numeric factorization with its
+//                    threshold pivot rule (crates/sim-core/src/native_klu.rs:
+//                    1194-1382), one warp walking the columns in order; it
+//                    discovers the pivot sequence.
+//  * refactor      - left-looking refactorization with frozen pivots. Warps
+//                    take columns in increasing order from an atomic counter
+//                    and wait on per-column completion flags of exactly the
+//                    columns they depend on (the U pattern), so independent
+//                    columns run concurrently without level barriers.
+//  * solve         - the forward (L) and backward (U) substitutions and the
+//                    BTF block coupling, one warp per row task, also driven by
+//                    per-row flags; the transpose variant solves A^T y = g.
+//  * stamp         - one thread per device instance writes its conductances
+//                    into the raw CSC slots given by the stamp-to-slot map and
+//                    its currents into per-contribution slots; a second pass
+//                    sums the right-hand side row by row in stamping order.
+//  * newton_update - convergence test, damping and the iterate update of
+//                    crates/sim-core/src/newton.rs:93-107, 187-201.
+//  * batch_newton  - thousands of independent circuits: each lane of a warp
+//                    owns one circuit instance and runs stamp, refactor, solve
+//                    and update for its whole Newton loop; the 32 lanes of a
+//                    warp share one circuit program, so every load of the
+//                    program is a broadcast and every value access is one
+//                    coalesced 256-byte transaction.
+//
+// All floating-point work is FP64 and compiled without multiply-add
+// contraction, so every product is rounded before it is added exactly as in
+// the reference; the factor and solve results are bit-identical to a scalar
+// CPU evaluation in the reference's order.
+#include <cstdio>
+
+#include "device.cuh"
+#include "kernels.cuh"
+
+namespace gk {
+
+namespace {
+constexpr unsigned FULL = 0xffffffffu;
+
+// --------------------------------------------------------------- first factor
+__global__ void k_first_factor(DPlan P, const double* __restrict__ ax, double* lu,
+                               double* work, int* rperm, int* rinv, double tol,
+                               int* status) {
+  const int lane = threadIdx.x;
+  const int n = P.n;
+  for (int i = lane; i < n; i += 32) {
+    int b0 = P.block_ptr[P.pos_block[i]];
+    rperm[i] = i - b0;
+    rinv[i] = i - b0;
+    work[i] = 0.0;
+  }
+  __syncwarp();
+  for (int k = 0; k < n; ++k) {
+    const int b0 = P.block_ptr[P.pos_block[k]];
+    const int s0 = P.col_ptr[k], ds = P.dslot[k], s1 = P.col_ptr[k + 1];
+    const int t0 = P.pcol_ptr[k], t1 = P.pcol_ptr[k + 1];
+    if (P.col_single[k]) {
+      if (lane == 0) {
+        double d = 0.0;
+        for (int t = t0; t < t1; ++t) d += ax[P.pcol_raw[t]];
+        lu[ds] = perturb(d, true);
+      }
+      __syncwarp();
+      continue;
+    }
+    if (lane == 0)  // duplicates accumulate in CSC order
+      for (int t = t0; t < t1; ++t) {
+        int w = b0 + rinv[b0 + P.pcol_q[t]];
+        work[w] += ax[P.pcol_raw[t]];
+      }
+    __syncwarp();
+    for (int s = s0; s < ds; ++s) {
+      const int j = P.slot_row[s];
+      const double u = work[j];
+      if (u != 0.0) {
+        const int q1 = P.col_ptr[j + 1];
+        for (int q = P.dslot[j] + 1 + lane; q < q1; q += 32) {
+          int r = P.slot_row[q];
+          work[r] = work[r] - lu[q] * u;
+        }
+      }
+      __syncwarp();
+    }
+    // threshold pivot search inside the symbolic pattern: the first row with
+    // the largest magnitude wins; the diagonal wins ties
+    const double dabs = fabs(work[k]);
+    double best = -1.0;
+    int bidx = 0x7fffffff;
+    for (int q = ds + 1 + lane; q < s1; q += 32) {
+      double v = fabs(work[P.slot_row[q]]);
+      if (v > best) {
+        best = v;
+        bidx = q;
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      double ov = __shfl_down_sync(FULL, best, off);
+      int oi = __shfl_down_sync(FULL, bidx, off);
+      if (ov > best || (ov == best && oi < bidx)) {
+        best = ov;
+        bidx = oi;
+      }
+    }
+    best = __shfl_sync(FULL, best, 0);
+    bidx = __shfl_sync(FULL, bidx, 0);
+    if (lane == 0 && bidx != 0x7fffffff && best > dabs && dabs < tol * best) {
+      const int mr = P.slot_row[bidx];
+      double tmp = work[k];
+      work[k] = work[mr];
+      work[mr] = tmp;
+      int ok = rperm[k], om = rperm[mr];
+      rperm[k] = om;
+      rperm[mr] = ok;
+      rinv[b0 + ok] = mr - b0;
+      rinv[b0 + om] = k - b0;
+    }
+    __syncwarp();
+    for (int s = s0 + lane; s < ds; s += 32) lu[s] = work[P.slot_row[s]];
+    const double diag = perturb(work[k], false);
+    if (lane == 0) lu[ds] = diag;
+    for (int q = ds + 1 + lane; q < s1; q += 32) lu[q] = work[P.slot_row[q]] / diag;
+    __syncwarp();
+    if (lane == 0)
+      for (int t = t0; t < t1; ++t) work[b0 + rinv[b0 + P.pcol_q[t]]] = 0.0;
+    for (int q = s0 + lane; q < s1; q += 32) work[P.slot_row[q]] = 0.0;
+    __syncwarp();
+    if (lane == 0) work[k] = 0.0;
+    __syncwarp();
+  }
+  (void)status;
+}
+
+// --------------------------------------------------------------- refactor
+__global__ void k_refactor(DPlan P, const double* __restrict__ ax, double* lu,
+                           unsigned* flags, unsigned epoch, unsigned* counter,
+                           int* status) {
+  const int lane = threadIdx.x & 31;
+  const int n = P.n;
+  while (true) {
+    int k = 0;
+    if (lane == 0) k = (int)atomicAdd(counter, 1u);
+    k = __shfl_sync(FULL, k, 0);
+    if (k >= n) return;
+    const int s0 = P.col_ptr[k], ds = P.dslot[k], s1 = P.col_ptr[k + 1];
+    // A(:,k) into the column's slots; duplicates summed in CSC order
+    for (int s = s0 + lane; s < s1; s += 32) {
+      double v = 0.0;
+      for (int t = P.amap_ptr[s]; t < P.amap_ptr[s + 1]; ++t) v += ax[P.amap_idx[t]];
+      lu[s] = v;
+    }
+    __syncwarp();
+    for (int s = s0; s < ds; ++s) {
+      const int j = P.slot_row[s];
+      int ok = 1;
+      if (lane == 0) ok = wait_flag(&flags[j], epoch, status);
+      ok = __shfl_sync(FULL, ok, 0);
+      if (!ok) return;
+      const double u = ld_cg(&lu[s]);
+      if (u != 0.0) {
+        const int q0 = P.dslot[j] + 1, q1 = P.col_ptr[j + 1];
+        const int* dst = P.upd_dst + P.upd_ptr[s] - q0;
+        for (int q = q0 + lane; q < q1; q += 32) {
+          const int d = dst[q];
+          lu[d] = ld_cg(&lu[d]) - ld_cg(&lu[q]) * u;
+        }
+      }
+      __syncwarp();
+    }
+    const double diag = perturb(ld_cg(&lu[ds]), P.col_single[k] != 0);
+    for (int q = ds + 1 + lane; q < s1; q += 32) lu[q] = ld_cg(&lu[q]) / diag;
+    if (lane == 0) lu[ds] = diag;
+    __syncwarp();
+    __threadfence();
+    if (lane == 0) st_release(&flags[k], epoch);
+  }
+}
+
+// --------------------------------------------------------------- solve
+// v - sum_e coef(e) * val(dep(e)) over e in [e0, e1), subtracted in order.
+// Each lane waits for and multiplies one entry of a 32-entry chunk; lane 0
+// then subtracts the rounded products in order.
+template <class Coef, class Dep>
+__device__ __forceinline__ bool ordered_dot(double& v, int e0, int e1, Coef coef, Dep dep,
+                                            const unsigned* flag, const double* val,
+                                            unsigned epoch, int* status) {
+  const int lane = threadIdx.x & 31;
+  for (int base = e0; base < e1; base += 32) {
+    const int e = base + lane;
+    double prod = 0.0;
+    int ok = 1;
+    if (e < e1) {
+      const int d = dep(e);
+      ok = wait_flag(&flag[d], epoch, status);
+      if (ok) prod = coef(e) * ld_cg(&val[d]);
+    }
+    if (!__all_sync(FULL, ok)) return false;
+    const int cnt = min(32, e1 - base);
+    for (int t = 0; t < cnt; ++t) {
+      double pt = __shfl_sync(FULL, prod, t);
+      v = v - pt;
+    }
+  }
+  return true;
+}
+
+__global__ void k_solve(DPlan P, const double* __restrict__ rhs, const double* __restrict__ ax,
+                        const double* __restrict__ lu, double* z, double* x, double* out,
+                        unsigned* zflag, unsigned* xflag, unsigned epoch, unsigned* counter,
+                        int* status) {
+  const int lane = threadIdx.x & 31;
+  while (true) {
+    int t = 0;
+    if (lane == 0) t = (int)atomicAdd(counter, 1u);
+    t = __shfl_sync(FULL, t, 0);
+    if (t >= P.ntask) return;
+    const int code = P.task[t];
+    const int i = code >> 1;
+    if ((code & 1) == 0) {  // forward: block coupling, then L
+      double v = rhs[P.in_row[i]];
+      bool ok = ordered_dot(
+          v, P.offd_ptr[i], P.offd_ptr[i + 1], [&](int e) { return ax[P.offd_raw[e]]; },
+          [&](int e) { return P.offd_col[e]; }, xflag, x, epoch, status);
+      if (ok)
+        ok = ordered_dot(
+            v, P.lrow_ptr[i], P.lrow_ptr[i + 1], [&](int e) { return lu[P.lrow_slot[e]]; },
+            [&](int e) { return P.lrow_col[e]; }, zflag, z, epoch, status);
+      if (!ok) return;
+      if (lane == 0) {
+        z[i] = v;
+        __threadfence();
+        st_release(&zflag[i], epoch);
+      }
+    } else {  // backward: U
+      int ok = 1;
+      if (lane == 0) ok = wait_flag(&zflag[i], epoch, status);
+      if (!__shfl_sync(FULL, ok, 0)) return;
+      double v = ld_cg(&z[i]);
+      ok = ordered_dot(
+          v, P.urow_ptr[i], P.urow_ptr[i + 1], [&](int e) { return lu[P.urow_slot[e]]; },
+          [&](int e) { return P.urow_col[e]; }, xflag, x, epoch, status);
+      if (!ok) return;
+      if (lane == 0) {
+        v = v / lu[P.dslot[i]];
+        x[i] = v;
+        out[P.out_col[i]] = v;
+        __threadfence();
+        st_release(&xflag[i], epoch);
+      }
+    }
+  }
+}
+
+// A^T y = g with the same factors: U^T forward (U columns as rows), then
+// L^T backward (L columns as rows). Task codes as in k_solve; the input is
+// indexed by original column and the output by original row.
+__global__ void k_tsolve(DPlan P, const double* __restrict__ g, const double* __restrict__ lu,
+                         double* z, double* x, double* out, unsigned* zflag, unsigned* xflag,
+                         unsigned epoch, unsigned* counter, int* status) {
+  const int lane = threadIdx.x & 31;
+  while (true) {
+    int t = 0;
+    if (lane == 0) t = (int)atomicAdd(counter, 1u);
+    t = __shfl_sync(FULL, t, 0);
+    if (t >= P.ntask) return;
+    const int code = P.task[t];
+    const int k = code >> 1;
+    if ((code & 1) == 0) {  // U^T row k = U column k
+      double v = g[P.out_col[k]];
+      bool ok = ordered_dot(
+          v, P.col_ptr[k], P.dslot[k], [&](int e) { return lu[e]; },
+          [&](int e) { return P.slot_row[e]; }, zflag, z, epoch, status);
+      if (!ok) return;
+      if (lane == 0) {
+        v = v / lu[P.dslot[k]];
+        z[k] = v;
+        __threadfence();
+        st_release(&zflag[k], epoch);
+      }
+    } else {  // L^T row k = L column k
+      int ok = 1;
+      if (lane == 0) ok = wait_flag(&zflag[k], epoch, status);
+      if (!__shfl_sync(FULL, ok, 0)) return;
+      double v = ld_cg(&z[k]);
+      ok = ordered_dot(
+          v, P.dslot[k] + 1, P.col_ptr[k + 1], [&](int e) { return lu[e]; },
+          [&](int e) { return P.slot_row[e]; }, xflag, x, epoch, status);
+      if (!ok) return;
+      if (lane == 0) {
+        x[k] = v;
+        out[P.in_row[k]] = v;
+        __threadfence();
+        st_release(&xflag[k], epoch);
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------- devices
+// Level-1 MOSFET exactly as the reference evaluates it
+// (crates/sim-devices/src/bsim/evaluate.rs:285-356 via mod.rs:440-455).
+__device__ void mos_reference(const double* p, double vd, double vg, double vs, double& gm,
+                              double& gds, double& ieq) {
+  const double lambda = 0.02, gmin_dev = 1e-12;
+  const bool pm = p[0] != 0.0;
+  const double beta = p[2] * 1e-4 * ((3.9 * 8.854e-12) / p[3]);
+  double vdi = pm ? -vs : vd, vgi = pm ? -vg : vg, vsi = pm ? -vd : vs;
+  double vgs = vgi - vsi, vds = vdi - vsi;
+  if (vds < 0.0) {
+    vds = -vds;
+    vgs = vgi - vdi;
+  }
+  const double vth = pm ? -fabs(p[1]) : fabs(p[1]);
+  const double beff = beta * p[4] / p[5];
+  double ids;
+  if (vgs <= vth) {
+    ids = 0.0;
+    gm = 0.0;
+    gds = gmin_dev;
+  } else if (vds < vgs - vth) {
+    ids = beff * ((vgs - vth) * vds - 0.5 * vds * vds);
+    gm = beff * vds;
+    gds = fmax(beff * ((vgs - vth) - vds), gmin_dev);
+  } else {
+    const double t = vgs - vth;
+    ids = 0.5 * beff * (t * t) * (1.0 + lambda * vds);
+    gm = beff * (vgs - vth) * (1.0 + lambda * vds);
+    gds = fmax(0.5 * beff * (t * t) * lambda, gmin_dev);
+  }
+  const double ids_s = pm ? -ids : ids;
+  ieq = ids_s - gm * (vg - vs) - gds * (vd - vs);
+}
+
+// Level-1 MOSFET with a self-consistent linearisation: drain current and its
+// partials with respect to (vg, vd, vs).
+__device__ void mos_consistent(const double* p, double vd, double vg, double vs, double& id,
+                               double& ddg, double& ddd, double& dds) {
+  const double lambda = 0.02, gmin_dev = 1e-12;
+  const double pol = p[0] != 0.0 ? -1.0 : 1.0;
+  const double beta = p[2] * 1e-4 * ((3.9 * 8.854e-12) / p[3]);
+  const double vgs = pol * (vg - vs), vds = pol * (vd - vs);
+  const bool rev = vds < 0.0;
+  const double vgse = rev ? vgs - vds : vgs, vdse = rev ? -vds : vds;
+  const double vth = fabs(p[1]);
+  const double beff = beta * p[4] / p[5];
+  double ids, gm, gds;
+  if (vgse <= vth) {
+    ids = 0.0;
+    gm = 0.0;
+    gds = gmin_dev;
+  } else if (vdse < vgse - vth) {
+    ids = beff * ((vgse - vth) * vdse - 0.5 * vdse * vdse);
+    gm = beff * vdse;
+    gds = fmax(beff * ((vgse - vth) - vdse), gmin_dev);
+  } else {
+    const double t = vgse - vth;
+    ids = 0.5 * beff * (t * t) * (1.0 + lambda * vdse);
+    gm = beff * (vgse - vth) * (1.0 + lambda * vdse);
+    gds = fmax(0.5 * beff * (t * t) * lambda, gmin_dev);
+  }
+  if (!rev) {
+    id = pol * ids;
+    ddg = gm;
+    ddd = gds;
+    dds = -(gm + gds);
+  } else {
+    id = -pol * ids;
+    ddg = -gm;
+    ddd = gm + gds;
+    dds = -gds;
+  }
+}
+
+// One device's matrix inserts (in the reference's insert order) and its
+// right-hand-side contributions. Returns the number of matrix values.
+template <class XGet>
+__device__ __forceinline__ int eval_device(int type, const int* nd, const double* p, XGet xg,
+                                           double gmin, double scale, double dt, double vprev,
+                                           double be_sign, double* m, double* r, int& nr) {
+  nr = 0;
+  switch (type) {
+    case 0: {  // R
+      const double g = 1.0 / p[0];
+      m[0] = g;
+      m[1] = g;
+      m[2] = -g;
+      m[3] = -g;
+      return 4;
+    }
+    case 1: {  // V
+      m[0] = 1.0;
+      m[1] = -1.0;
+      m[2] = 1.0;
+      m[3] = -1.0;
+      r[0] = p[0] * scale;
+      nr = 1;
+      return 4;
+    }
+    case 2: {  // I
+      const double v = p[0] * scale;
+      r[0] = -v;
+      r[1] = v;
+      nr = 2;
+      return 0;
+    }
+    case 3: {  // D, crates/sim-core/src/stamp.rs:351-387
+      const double gf = gmin > 0.0 ? gmin : 1e-12;
+      const double vt = 0.02585 * p[1];
+      const double vd = xg(nd[0]) - xg(nd[1]);
+      const double e = exp(vd / vt);
+      const double id = p[0] * (e - 1.0);
+      const double gd = (p[0] / vt) * e;
+      const double g = fmax(gd, gf);
+      const double ieq = id - gd * vd;
+      m[0] = g;
+      m[1] = g;
+      m[2] = -g;
+      m[3] = -g;
+      r[0] = -ieq;
+      r[1] = ieq;
+      nr = 2;
+      return 4;
+    }
+    case 4: {  // M, crates/sim-core/src/stamp.rs:511-545
+      const double gf = gmin > 0.0 ? gmin : 1e-12;
+      double gm, gds, ieq;
+      mos_reference(p, xg(nd[0]), xg(nd[1]), xg(nd[2]), gm, gds, ieq);
+      gds = fmax(gds, gf);
+      m[0] = gds;
+      m[1] = gds;
+      m[2] = -gds;
+      m[3] = -gds;
+      m[4] = gm;
+      m[5] = -gm;
+      m[6] = -gm;
+      m[7] = gm;
+      r[0] = -ieq;
+      r[1] = ieq;
+      nr = 2;
+      return 8;
+    }
+    case 6: {  // MC: same 8 inserts, exact partials
+      const double vd = xg(nd[0]), vg = xg(nd[1]), vs = xg(nd[2]);
+      double id, ddg, ddd, dds;
+      mos_consistent(p, vd, vg, vs, id, ddg, ddd, dds);
+      const double ieq = id - (ddg * vg + ddd * vd + dds * vs);
+      m[0] = ddd;
+      m[1] = -dds;
+      m[2] = dds;
+      m[3] = -ddd;
+      m[4] = ddg;
+      m[5] = 0.0;
+      m[6] = -ddg;
+      m[7] = 0.0;
+      r[0] = -ieq;
+      r[1] = ieq;
+      nr = 2;
+      return 8;
+    }
+    case 5: {  // C: backward Euler companion in transient, open in DC
+      if (dt <= 0.0) return 0;
+      const double g = p[0] / dt;
+      const double ieq = g * vprev;
+      m[0] = g;
+      m[1] = g;
+      m[2] = -g;
+      m[3] = -g;
+      r[0] = be_sign * ieq;
+      r[1] = -be_sign * ieq;
+      nr = 2;
+      return 4;
+    }
+  }
+  return 0;
+}
+
+__global__ void k_stamp(DCircuit C, const double* __restrict__ x, int xlen, double gmin,
+                        double scale, double dt, const double* __restrict__ cap_v,
+                        double be_sign, double* ax, double* rhs_c) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d == 0 && C.pin_raw >= 0) ax[C.pin_raw] = 1.0;
+  if (d >= C.ndev) return;
+  const int* nd = C.nodes + 4 * d;
+  auto xg = [&](int i) { return (i >= 0 && i < xlen) ? x[i] : 0.0; };
+  double m[8], r[2];
+  int nr;
+  const double vprev = cap_v ? cap_v[d] : 0.0;
+  const int nm = eval_device(C.type[d], nd, C.p + 6 * d, xg, gmin, scale, dt, vprev, be_sign,
+                             m, r, nr);
+  const int* raw = C.raw + 8 * d;
+  for (int e = 0; e < nm; ++e)
+    if (raw[e] >= 0) ax[raw[e]] = m[e];
+  const int* rs = C.rhs_slot + 2 * d;
+  for (int e = 0; e < nr; ++e)
+    if (rs[e] >= 0) rhs_c[rs[e]] = r[e];
+}
+
+__global__ void k_rhs_sum(DCircuit C, const double* __restrict__ rhs_c, double* rhs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= C.n) return;
+  double v = 0.0;
+  for (int t = C.rhs_ptr[i]; t < C.rhs_ptr[i + 1]; ++t) v += rhs_c[C.rhs_src[t]];
+  rhs[i] = v;
+}
+
+// --------------------------------------------------------------- Newton
+__global__ void k_newton_update(int m, int n, double* x, const double* __restrict__ xn,
+                                NewtonState* st, NewtonCfg cfg, int* status) {
+  __shared__ double ssum[32];
+  __shared__ int sconv[32], sfin[32];
+  const int tid = threadIdx.x;
+  double acc = 0.0;
+  int conv = 1, fin = 1;
+  for (int i = tid; i < m; i += blockDim.x) {
+    const double a = xn[i], dx = a - x[i];
+    acc += dx * dx;
+    if (!(fabs(dx) <= cfg.abs_tol + cfg.rel_tol * fabs(a))) conv = 0;
+    if (!isfinite(a)) fin = 0;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    acc += __shfl_down_sync(FULL, acc, off);
+    conv &= __shfl_down_sync(FULL, conv, off);
+    fin &= __shfl_down_sync(FULL, fin, off);
+  }
+  if ((tid & 31) == 0) {
+    ssum[tid >> 5] = acc;
+    sconv[tid >> 5] = conv;
+    sfin[tid >> 5] = fin;
+  }
+  __syncthreads();
+  if (tid < 32) {
+    const int nw = blockDim.x >> 5;
+    acc = tid < nw ? ssum[tid] : 0.0;
+    conv = tid < nw ? sconv[tid] : 1;
+    fin = tid < nw ? sfin[tid] : 1;
+    for (int off = 16; off > 0; off >>= 1) {
+      acc += __shfl_down_sync(FULL, acc, off);
+      conv &= __shfl_down_sync(FULL, conv, off);
+      fin &= __shfl_down_sync(FULL, fin, off);
+    }
+    if (tid == 0) {
+      const double dxn = sqrt(acc);
+      st->iter += 1;
+      st->converged = conv;
+      if (!fin) atomicCAS(status, DS_OK, DS_NONFINITE);
+      if (!conv) {
+        if (dxn > st->prev_dx_norm && st->damping > cfg.damping_min)
+          st->damping = fmax(st->damping * 0.5, cfg.damping_min);
+        st->prev_dx_norm = dxn;
+      }
+      ssum[0] = st->damping;
+      sconv[0] = conv;
+    }
+  }
+  __syncthreads();
+  const double damp = ssum[0];
+  if (sconv[0]) {
+    for (int i = tid; i < n; i += blockDim.x) x[i] = xn[i];
+  } else {
+    for (int i = tid; i < m; i += blockDim.x) x[i] = x[i] + damp * (xn[i] - x[i]);
+  }
+}
+
+__global__ void k_rcond(DPlan P, const double* __restrict__ lu, double* out) {
+  __shared__ double smin[32], smax[32];
+  const int tid = threadIdx.x;
+  double mn = 1.7976931348623157e308, mx = 0.0;
+  for (int k = tid; k < P.n; k += blockDim.x) {
+    const double a = fabs(lu[P.dslot[k]]);
+    mn = fmin(mn, a);
+    mx = fmax(mx, a);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    mn = fmin(mn, __shfl_down_sync(FULL, mn, off));
+    mx = fmax(mx, __shfl_down_sync(FULL, mx, off));
+  }
+  if ((tid & 31) == 0) {
+    smin[tid >> 5] = mn;
+    smax[tid >> 5] = mx;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      mn = fmin(mn, smin[w]);
+      mx = fmax(mx, smax[w]);
+    }
+    out[0] = fmin(mn, smin[0]);
+    out[1] = fmax(mx, smax[0]);
+  }
+}
+
+// --------------------------------------------------------------- batched
+// Per-lane state lives in the warp's buffer, value index v of lane l at
+// buf[v * 32 + l]: [0, nslots+noffd) matrix values, then rhs[n], t[n], x[nc].
+__global__ void __launch_bounds__(128)
+    k_batch_newton(const GroupHdr* __restrict__ groups, const Tile* __restrict__ tiles,
+                   int ntiles, unsigned* tile_counter, const int* __restrict__ dev_type,
+                   const int* __restrict__ dev_nodes, const double* __restrict__ dev_p,
+                   const int* __restrict__ dev_slot, const int* __restrict__ g_col_ptr,
+                   const int* __restrict__ g_dslot, const int* __restrict__ g_col_single,
+                   const int* __restrict__ g_in_row, const int* __restrict__ g_out_pos,
+                   const int* __restrict__ g_offd_ptr, const int* __restrict__ g_slot_row,
+                   const int* __restrict__ g_upd_ptr, const int* __restrict__ g_upd_dst,
+                   const int* __restrict__ g_offd_col, const int* __restrict__ g_block_ptr,
+                   const int* __restrict__ inst_ov_dev, const double* __restrict__ inst_ov_val,
+                   const long long* __restrict__ inst_x0_off, const double* __restrict__ x0,
+                   NewtonCfg cfg, double* buf_all, long long buf_stride, int* iters,
+                   int* iters_total, int* reason, const long long* __restrict__ inst_x_off,
+                   double* x_out, int* status) {
+  const int lane = threadIdx.x & 31;
+  const long long warp_global = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  double* buf = buf_all + warp_global * buf_stride;
+  while (true) {
+    int ti = 0;
+    if (lane == 0) ti = (int)atomicAdd(tile_counter, 1u);
+    ti = __shfl_sync(FULL, ti, 0);
+    if (ti >= ntiles) return;
+    const Tile tl = tiles[ti];
+    const GroupHdr G = groups[tl.group];
+    const bool live = lane < tl.count;
+    const int inst = tl.first + (live ? lane : 0);
+    const int nv = G.nslots + G.noffd;
+    double* V = buf + lane;                 // V[s * 32]
+    double* R = buf + (long long)nv * 32 + lane;
+    double* T = R + (long long)G.n * 32;
+    double* X = T + (long long)G.n * 32;
+    const int* col_ptr = g_col_ptr + G.col_off;
+    const int* dslot = g_dslot + G.col_off;
+    const int* csing = g_col_single + G.col_off;
+    const int* in_row = g_in_row + G.col_off;
+    const int* out_pos = g_out_pos + G.col_off;
+    const int* offd_ptr = g_offd_ptr + G.col_off;
+    const int* slot_row = g_slot_row + G.slot_off;
+    const int* upd_ptr = g_upd_ptr + G.slot_off;
+    const int* upd_dst = g_upd_dst + G.upd_off;
+    const int* offd_col = g_offd_col + G.offd_off;
+    const int* bptr = g_block_ptr + G.blk_off;
+    const int ov_dev = live ? inst_ov_dev[inst] : -1;
+    const double ov_val = live ? inst_ov_val[inst] : 0.0;
+    const int nc = G.node_count;
+    // initial iterate
+    if (live) {
+      const double* x0p = inst_x0_off[inst] >= 0 ? x0 + inst_x0_off[inst] : nullptr;
+      for (int i = 0; i < nc; ++i) X[i * 32] = x0p ? x0p[i] : 0.0;
+    }
+    int done = live ? 0 : 1, it = 0, total = 0, gstep = 0, rsn = 1;
+    double damp = cfg.damping, prev = 1.7976931348623157e308;
+    const double gstart = fmax(cfg.gmin * 1e3, 1e-6);
+    double gmin = cfg.gmin_steps == 0 ? cfg.gmin : gstart;
+    while (__any_sync(FULL, !done)) {
+      if (!done) {
+        // ---- stamp: device order, accumulating into slots as the reference's
+        // scatter sums duplicate CSC entries
+        for (int s = 0; s < nv; ++s) V[s * 32] = 0.0;
+        for (int i = 0; i < G.n; ++i) R[i * 32] = 0.0;
+        auto xg = [&](int i) { return (i >= 0 && i < nc) ? X[i * 32] : 0.0; };
+        for (int d = 0; d < G.ndev; ++d) {
+          const int dg = G.dev_off + d;
+          const int type = dev_type[dg];
+          const int* nd = dev_nodes + 4 * dg;
+          double pl[6];
+#pragma unroll
+          for (int q = 0; q < 6; ++q) pl[q] = dev_p[6 * dg + q];
+          if (d == ov_dev) pl[0] = ov_val;
+          double m[8], r[2];
+          int nr;
+          const int nm = eval_device(type, nd, pl, xg, gmin, 1.0, 0.0, 0.0, -1.0, m, r, nr);
+          const int* sl = dev_slot + 8 * dg;
+          for (int e = 0; e < nm; ++e) {
+            const int s = sl[e];
+            if (s >= 0) V[s * 32] = V[s * 32] + m[e];
+          }
+          if (nr) {  // rows: V -> its aux row; M -> drain, source; others -> a, b
+            const int ra = type == 1 ? nd[2] : nd[0];
+            const int rb = (type == 4 || type == 6) ? nd[2] : nd[1];
+            if (ra < G.n) R[ra * 32] = R[ra * 32] + r[0];
+            if (nr > 1 && rb < G.n) R[rb * 32] = R[rb * 32] + r[1];
+          }
+        }
+        if (G.pin_slot >= 0) V[G.pin_slot * 32] = V[G.pin_slot * 32] + 1.0;
+        // ---- refactor with frozen pivots (left-looking, columns in order)
+        for (int k = 0; k < G.n; ++k) {
+          const int s0 = col_ptr[k], ds = dslot[k], s1 = col_ptr[k + 1];
+          for (int s = s0; s < ds; ++s) {
+            const double u = V[s * 32];
+            if (u != 0.0) {
+              const int j = slot_row[s];
+              const int q0 = dslot[j] + 1, q1 = col_ptr[j + 1];
+              const int* dst = upd_dst + upd_ptr[s] - q0;
+              for (int q = q0; q < q1; ++q) {
+                const int dd = dst[q];
+                V[dd * 32] = V[dd * 32] - V[q * 32] * u;
+              }
+            }
+          }
+          const double diag = perturb(V[ds * 32], csing[k] != 0);
+          V[ds * 32] = diag;
+          for (int q = ds + 1; q < s1; ++q) V[q * 32] = V[q * 32] / diag;
+        }
+        // ---- solve
+        for (int i = 0; i < G.n; ++i) T[i * 32] = R[in_row[i] * 32];
+        for (int bb = 0; bb < G.nblocks; ++bb) {
+          const int b = G.offd_lower ? bb : G.nblocks - 1 - bb;
+          const int b0 = bptr[b], b1 = bptr[b + 1];
+          for (int i = b0; i < b1; ++i)
+            for (int e = offd_ptr[i]; e < offd_ptr[i + 1]; ++e)
+              T[i * 32] = T[i * 32] - V[(G.nslots + e) * 32] * T[offd_col[e] * 32];
+          for (int k = b0; k < b1; ++k) {
+            const double zk = T[k * 32];
+            for (int q = dslot[k] + 1; q < col_ptr[k + 1]; ++q)
+              T[slot_row[q] * 32] = T[slot_row[q] * 32] - V[q * 32] * zk;
+          }
+          for (int k = b1 - 1; k >= b0; --k) {
+            const double xk = T[k * 32] / V[dslot[k] * 32];
+            T[k * 32] = xk;
+            for (int s = col_ptr[k]; s < dslot[k]; ++s)
+              T[slot_row[s] * 32] = T[slot_row[s] * 32] - V[s * 32] * xk;
+          }
+        }
+        // ---- Newton update (crates/sim-core/src/newton.rs:93-107)
+        ++it;
+        ++total;
+        double ss = 0.0;
+        bool conv = true, fin = true;
+        for (int c = 0; c < nc; ++c) {
+          const double a = T[out_pos[c] * 32];
+          const double dx = a - X[c * 32];
+          ss += dx * dx;
+          if (!(fabs(dx) <= cfg.abs_tol + cfg.rel_tol * fabs(a))) conv = false;
+          if (!isfinite(a)) fin = false;
+        }
+        if (conv) {
+          done = 1;
+          rsn = 0;
+          const long long xo = inst_x_off[inst];
+          if (xo >= 0)
+            for (int c = 0; c < G.n; ++c) x_out[xo + c] = T[out_pos[c] * 32];
+        } else {
+          const double dxn = sqrt(ss);
+          if (dxn > prev && damp > cfg.damping_min) damp = fmax(damp * 0.5, cfg.damping_min);
+          prev = dxn;
+          for (int c = 0; c < nc; ++c) {
+            const double a = T[out_pos[c] * 32];
+            X[c * 32] = X[c * 32] + damp * (a - X[c * 32]);
+          }
+          if (!fin) {
+            done = 1;
+            rsn = 1;
+          } else if (it >= cfg.max_iters) {
+            if (gstep < cfg.gmin_steps) {  // next gmin step, fresh damping state
+              ++gstep;
+              gmin = gstart + (cfg.gmin - gstart) * ((double)gstep / (double)cfg.gmin_steps);
+              it = 0;
+              damp = cfg.damping;
+              prev = 1.7976931348623157e308;
+            } else {
+              done = 1;
+              rsn = 1;
+            }
+          }
+        }
+        if (done && live) {
+          iters[inst] = it;
+          iters_total[inst] = total;
+          reason[inst] = rsn;
+          if (rsn != 0) {
+            const long long xo = inst_x_off[inst];
+            if (xo >= 0)
+              for (int c = 0; c < G.n; ++c) x_out[xo + c] = c < nc ? X[c * 32] : 0.0;
+          }
+        }
+      }
+    }
+  }
+  (void)status;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launches
+void launch_first_factor(const DPlan& P, const double* ax, double* lu, double* work,
+                         int* rperm, int* rinv, double tol, int* status, cudaStream_t s) {
+  k_first_factor<<<1, 32, 0, s>>>(P, ax, lu, work, rperm, rinv, tol, status);
+}
+
+void launch_refactor(const DPlan& P, const double* ax, double* lu, unsigned* flags,
+                     unsigned epoch, unsigned* counter, int* status, int grid,
+                     cudaStream_t s) {
+  cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
+  k_refactor<<<grid, 128, 0, s>>>(P, ax, lu, flags, epoch, counter, status);
+}
+
+void launch_solve(const DPlan& P, const double* rhs, const double* ax, const double* lu,
+                  double* z, double* x, double* out, unsigned* zflag, unsigned* xflag,
+                  unsigned epoch, unsigned* counter, int* status, int grid, bool transpose,
+                  cudaStream_t s) {
+  cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
+  if (transpose)
+    k_tsolve<<<grid, 128, 0, s>>>(P, rhs, lu, z, x, out, zflag, xflag, epoch, counter, status);
+  else
+    k_solve<<<grid, 128, 0, s>>>(P, rhs, ax, lu, z, x, out, zflag, xflag, epoch, counter,
+                                 status);
+}
+
+void launch_stamp(const DCircuit& C, const double* x, int xlen, double gmin, double scale,
+                  double dt, const double* cap_v, double be_sign, double* ax, double* rhs_c,
+                  double* rhs, cudaStream_t s) {
+  const int nb = (C.ndev + 255) / 256;
+  k_stamp<<<nb > 0 ? nb : 1, 256, 0, s>>>(C, x, xlen, gmin, scale, dt, cap_v, be_sign, ax,
+                                          rhs_c);
+  k_rhs_sum<<<(C.n + 255) / 256, 256, 0, s>>>(C, rhs_c, rhs);
+}
+
+void launch_newton_update(int m, int n, double* x, const double* xnew, NewtonState* st,
+                          NewtonCfg cfg, int* status, cudaStream_t s) {
+  k_newton_update<<<1, 1024, 0, s>>>(m, n, x, xnew, st, cfg, status);
+}
+
+void launch_rcond(const DPlan& P, const double* lu, double* out2, cudaStream_t s) {
+  k_rcond<<<1, 1024, 0, s>>>(P, lu, out2);
+}
+
+void launch_batch_newton(const GroupHdr* groups, const Tile* tiles, int ntiles,
+                         unsigned* tile_counter, const int* dev_type, const int* dev_nodes,
+                         const double* dev_p, const int* dev_slot, const int* col_ptr,
+                         const int* dslot, const int* col_single, const int* in_row,
+                         const int* out_col, const int* offd_ptr, const int* slot_row,
+                         const int* upd_ptr, const int* upd_dst, const int* offd_col,
+                         const int* block_ptr, const int* inst_ov_dev,
+                         const double* inst_ov_val, const long long* inst_x0_off,
+                         const double* x0, NewtonCfg cfg, double* buf, long long buf_stride,
+                         int* iters, int* iters_total, int* reason,
+                         const long long* inst_x_off, double* x_out, int* status, int grid,
+                         int block, cudaStream_t s) {
+  cudaMemsetAsync(tile_counter, 0, sizeof(unsigned), s);
+  k_batch_newton<<<grid, block, 0, s>>>(
+      groups, tiles, ntiles, tile_counter, dev_type, dev_nodes, dev_p, dev_slot, col_ptr, dslot,
+      col_single, in_row, out_col, offd_ptr, slot_row, upd_ptr, upd_dst, offd_col, block_ptr,
+      inst_ov_dev, inst_ov_val, inst_x0_off, x0, cfg, buf, buf_stride, iters, iters_total,
+      reason, inst_x_off, x_out, status);
+}
+
+}  // namespace gk

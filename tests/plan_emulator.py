@@ -1,0 +1,155 @@
+"""Scalar CPU emulation of the device algorithms over a host Plan.
+
+Test infrastructure: it runs the exact operation sequence of the CUDA kernels
+(first factor with the reference pivot rule, frozen-pivot refactor, block
+solve) on the integer plan the library builds, so the plan itself (slot maps,
+update lists, permutations, block coupling) can be checked against the
+oracle on a machine without a GPU.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from rustspice_gb300 import native
+
+
+def _perturb(d, single):
+    if single:
+        return 1e-14 if abs(d) < 1e-300 else d
+    if abs(d) < 1e-14:
+        return 1e-14 if d >= 0.0 else -1e-14
+    return d
+
+
+def first_factor(P: native.Plan, ax, tol=0.001):
+    n = P.n
+    lu = np.zeros(P.nslots)
+    work = np.zeros(n)
+    b0s = P.block_ptr[P.pos_block]
+    rperm = (np.arange(n) - b0s).astype(np.int64)
+    rinv = rperm.copy()
+    for k in range(n):
+        b0 = b0s[k]
+        s0, ds, s1 = P.col_ptr[k], P.dslot[k], P.col_ptr[k + 1]
+        t0, t1 = P.pcol_ptr[k], P.pcol_ptr[k + 1]
+        if P.col_single[k]:
+            d = 0.0
+            for t in range(t0, t1):
+                d += ax[P.pcol_raw[t]]
+            lu[ds] = _perturb(d, True)
+            continue
+        for t in range(t0, t1):
+            work[b0 + rinv[b0 + P.pcol_q[t]]] += ax[P.pcol_raw[t]]
+        for s in range(s0, ds):
+            j = P.slot_row[s]
+            u = work[j]
+            if u != 0.0:
+                for q in range(P.dslot[j] + 1, P.col_ptr[j + 1]):
+                    r = P.slot_row[q]
+                    work[r] = work[r] - lu[q] * u
+        dabs = abs(work[k])
+        best, bq = -1.0, -1
+        for q in range(ds + 1, s1):
+            v = abs(work[P.slot_row[q]])
+            if v > best:
+                best, bq = v, q
+        if bq >= 0 and best > dabs and dabs < tol * best:
+            mr = P.slot_row[bq]
+            work[k], work[mr] = work[mr], work[k]
+            ok, om = rperm[k], rperm[mr]
+            rperm[k], rperm[mr] = om, ok
+            rinv[b0 + ok] = mr - b0
+            rinv[b0 + om] = k - b0
+        for s in range(s0, ds):
+            lu[s] = work[P.slot_row[s]]
+        diag = _perturb(work[k], False)
+        lu[ds] = diag
+        for q in range(ds + 1, s1):
+            lu[q] = work[P.slot_row[q]] / diag
+        for t in range(t0, t1):
+            work[b0 + rinv[b0 + P.pcol_q[t]]] = 0.0
+        for q in range(s0, s1):
+            work[P.slot_row[q]] = 0.0
+        work[k] = 0.0
+    return lu, rperm
+
+
+def refactor(P: native.Plan, ax):
+    lu = np.zeros(P.nslots)
+    for k in range(P.n):
+        s0, ds, s1 = P.col_ptr[k], P.dslot[k], P.col_ptr[k + 1]
+        for s in range(s0, s1):
+            v = 0.0
+            for t in range(P.amap_ptr[s], P.amap_ptr[s + 1]):
+                v += ax[P.amap_idx[t]]
+            lu[s] = v
+        for s in range(s0, ds):
+            j = P.slot_row[s]
+            u = lu[s]
+            if u != 0.0:
+                q0 = P.dslot[j] + 1
+                for q in range(q0, P.col_ptr[j + 1]):
+                    d = P.upd_dst[P.upd_ptr[s] + q - q0]
+                    lu[d] = lu[d] - lu[q] * u
+        diag = _perturb(lu[ds], bool(P.col_single[k]))
+        lu[ds] = diag
+        for q in range(ds + 1, s1):
+            lu[q] = lu[q] / diag
+    return lu
+
+
+def solve(P: native.Plan, ax, lu, rhs):
+    """Row-oriented dependency order, as the device solve computes it."""
+    n = P.n
+    in_row = np.zeros(n, np.int64)
+    in_row[P.in_pos] = np.arange(n)
+    z = np.zeros(n)
+    x = np.zeros(n)
+    nb = P.nblocks
+    order = range(nb) if P.offd_lower else range(nb - 1, -1, -1)
+    for b in order:
+        b0, b1 = P.block_ptr[b], P.block_ptr[b + 1]
+        for i in range(b0, b1):
+            v = rhs[in_row[i]]
+            for e in range(P.offd_ptr[i], P.offd_ptr[i + 1]):
+                v = v - ax[P.offd_raw[e]] * x[P.offd_col[e]]
+            for e in range(P.lrow_ptr[i], P.lrow_ptr[i + 1]):
+                v = v - lu[P.lrow_slot[e]] * z[P.lrow_col[e]]
+            z[i] = v
+        for i in range(b1 - 1, b0 - 1, -1):
+            v = z[i]
+            for e in range(P.urow_ptr[i], P.urow_ptr[i + 1]):
+                v = v - lu[P.urow_slot[e]] * x[P.urow_col[e]]
+            x[i] = v / lu[P.dslot[i]]
+    out = np.zeros(n)
+    out[:] = x[P.out_pos]
+    return out
+
+
+class EmulatedSolver:
+    """LinearSolver call sequence over the emulated kernels."""
+
+    def __init__(self, mode=native.PIVOT_REFERENCE):
+        self.mode = mode
+        self.plan = None
+        self.key = None
+        self.lu = None
+        self.factored = False
+
+    def factor(self, n, ap, ai, ax):
+        key = (n, ap.tobytes(), ai.tobytes())
+        if key != self.key:
+            self.key = key
+            self.plan = native.Plan(n, ap, ai, self.mode)
+            self.factored = False
+        if not self.factored:
+            lu, rperm = first_factor(self.plan, ax)
+            self.plan = native.Plan(n, ap, ai, self.mode, row_perm=rperm)
+            self.lu = lu if self.mode == native.PIVOT_REFERENCE else refactor(self.plan, ax)
+            self.factored = True
+        else:
+            self.lu = refactor(self.plan, ax)
+        self.ax = np.asarray(ax, np.float64)
+
+    def solve(self, rhs):
+        return solve(self.plan, self.ax, self.lu, np.asarray(rhs, np.float64))
