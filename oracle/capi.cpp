@@ -147,7 +147,7 @@ void orc_mna_free(void* h) { delete static_cast<MnaSystem*>(h); }
 int orc_dc_op(int64_t node_count, int64_t ndev, const int32_t* type,
               const int32_t* nodes, const double* p, const char* solver_kind,
               int64_t max_iters, double abs_tol, double rel_tol, double gmin,
-              int64_t gmin_steps, int64_t source_steps, double* x_out,
+              int64_t gmin_steps, int64_t source_steps, const double* x0, double* x_out,
               int64_t x_cap, int64_t* x_len, int64_t* iters) {
   Circuit c = make_circuit(node_count, ndev, type, nodes, p);
   NewtonConfig cfg;
@@ -159,7 +159,7 @@ int orc_dc_op(int64_t node_count, int64_t ndev, const int32_t* type,
   cfg.source_steps = (size_t)source_steps;
   auto solver = make_solver(solver_kind, c.node_count);
   Vec x;
-  NewtonResult r = dc_op(c, cfg, *solver, x);
+  NewtonResult r = dc_op(c, cfg, *solver, x, x0);
   *x_len = (int64_t)x.size();
   for (int64_t i = 0; i < x_cap && (size_t)i < x.size(); ++i) x_out[i] = x[(size_t)i];
   *iters = (int64_t)r.iterations;
@@ -183,8 +183,8 @@ void orc_dc_batch(int64_t ncirc, const int64_t* dev_off, const int64_t* node_cou
                   int64_t ninst, const int64_t* inst_circ, const int64_t* inst_dev,
                   const double* inst_val, const char* solver_kind, int64_t max_iters,
                   double abs_tol, double rel_tol, double gmin, int64_t gmin_steps,
-                  int64_t nthreads, int64_t* iters, int32_t* reason, double* x_out,
-                  int64_t x_cap) {
+                  const double* x0, const int64_t* x0_off, int64_t nthreads, int64_t* iters,
+                  int32_t* reason, double* x_out, int64_t x_cap) {
   std::vector<Circuit> circs((size_t)ncirc);
   for (int64_t c = 0; c < ncirc; ++c) {
     int64_t d0 = dev_off[c], d1 = dev_off[c + 1];
@@ -207,7 +207,8 @@ void orc_dc_batch(int64_t ncirc, const int64_t* dev_off, const int64_t* node_cou
       if (inst_dev[i] >= 0) c.p[(size_t)inst_dev[i] * NPARAM] = inst_val[i];
       auto s = make_solver(kind, c.node_count);
       Vec x;
-      NewtonResult r = dc_op(c, cfg, *s, x);
+      const double* xi = (x0 && x0_off && x0_off[i] >= 0) ? x0 + x0_off[i] : nullptr;
+      NewtonResult r = dc_op(c, cfg, *s, x, xi);
       iters[i] = (int64_t)r.iterations;
       reason[i] = r.reason;
       double* xo = x_out ? x_out + i * x_cap : nullptr;

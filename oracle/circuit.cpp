@@ -369,8 +369,10 @@ MnaSystem dc_build(void* p, const Vec& x, double gmin, double scale) {
 }  // namespace
 
 NewtonResult dc_op(const Circuit& c, const NewtonConfig& cfg,
-                   LinearSolver& solver, Vec& x) {  // engine.rs:249-283
+                   LinearSolver& solver, Vec& x, const double* x0) {  // engine.rs:249-283
   x.assign(c.node_count, 0.0);
+  if (x0)  // an initial iterate (nodeset) in place of the zero start
+    for (size_t i = 0; i < c.node_count; ++i) x[i] = x0[i];
   solver.prepare(c.node_count);
   DcCtx ctx{&c};
   return run_newton_with_stepping(cfg, x, dc_build, &ctx, solver);

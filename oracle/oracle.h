@@ -330,7 +330,7 @@ NewtonResult run_newton_with_stepping(const NewtonConfig& cfg, Vec& x,
 // Engine DC operating point (crates/sim-core/src/engine.rs:249-311) on a
 // circuit. `x` returns the solution (length n when converged).
 NewtonResult dc_op(const Circuit& c, const NewtonConfig& cfg,
-                   LinearSolver& solver, Vec& x);
+                   LinearSolver& solver, Vec& x, const double* x0 = nullptr);
 
 // Nonlinear residual F(x) = A(x) x - b(x) with the stamps at x, in the
 // infinity norm, divided by max(|b|_inf, 1).

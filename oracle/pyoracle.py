@@ -51,11 +51,11 @@ def lib():
         L.orc_mna_free.argtypes = [_P]
         L.orc_dc_op.restype = C.c_int
         L.orc_dc_op.argtypes = [_I64, _I64, _P, _P, _P, C.c_char_p, _I64, _D, _D, _D,
-                                _I64, _I64, _P, _I64, _P, _P]
+                                _I64, _I64, _P, _P, _I64, _P, _P]
         L.orc_residual.restype = _D
         L.orc_residual.argtypes = [_I64, _I64, _P, _P, _P, _P, _I64, _D]
         L.orc_dc_batch.argtypes = [_I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, C.c_char_p,
-                                   _I64, _D, _D, _D, _I64, _I64, _P, _P, _P, _I64]
+                                   _I64, _D, _D, _D, _I64, _P, _P, _I64, _P, _P, _P, _I64]
         _lib = L
     return _lib
 
@@ -170,16 +170,18 @@ REASONS = {0: "converged", 1: "maxiters", 2: "solver_failure"}
 
 
 def dc_op(c, solver="nativeklu", max_iters=100, abs_tol=1e-6, rel_tol=1e-3,
-          gmin=1e-12, gmin_steps=0, source_steps=0):
+          gmin=1e-12, gmin_steps=0, source_steps=0, x0=None):
     """Engine DC operating point. Returns (reason, iterations, x)."""
     _, t, nd, p = _circ_arrays(c)
+    x0a = _f64(x0) if x0 is not None else None
     cap = c.n
     x = np.zeros(cap)
     xl = C.c_int64()
     it = C.c_int64()
     r = lib().orc_dc_op(c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p), solver.encode(),
                         max_iters, abs_tol, rel_tol, gmin, gmin_steps, source_steps,
-                        _ptr(x), cap, C.byref(xl), C.byref(it))
+                        _ptr(x0a) if x0a is not None else None, _ptr(x), cap, C.byref(xl),
+                        C.byref(it))
     return REASONS[r], it.value, x[:xl.value]
 
 
@@ -191,8 +193,11 @@ def residual(c, x, gmin=1e-12):
 
 
 def dc_batch(circuits, inst_circ, inst_dev, inst_val, solver="nativeklu", max_iters=100,
-             abs_tol=1e-6, rel_tol=1e-3, gmin=1e-12, gmin_steps=0, nthreads=1, x_cap=0):
+             abs_tol=1e-6, rel_tol=1e-3, gmin=1e-12, gmin_steps=0, nthreads=1, x_cap=0,
+             x0=None, x0_off=None):
     """Independent DC operating points over a thread pool."""
+    x0a = _f64(x0) if x0 is not None else None
+    x0o = _i64(x0_off) if x0_off is not None else None
     dev_off = np.zeros(len(circuits) + 1, np.int64)
     for i, c in enumerate(circuits):
         dev_off[i + 1] = dev_off[i] + c.ndev
@@ -207,6 +212,8 @@ def dc_batch(circuits, inst_circ, inst_dev, inst_val, solver="nativeklu", max_it
     xo = np.zeros((ninst, max(x_cap, 1)))
     lib().orc_dc_batch(len(circuits), _ptr(dev_off), _ptr(ncs), _ptr(t), _ptr(nd), _ptr(p),
                        ninst, _ptr(ic), _ptr(idv), _ptr(iv), solver.encode(), max_iters,
-                       abs_tol, rel_tol, gmin, gmin_steps, nthreads, _ptr(iters),
+                       abs_tol, rel_tol, gmin, gmin_steps,
+                       _ptr(x0a) if x0a is not None else None,
+                       _ptr(x0o) if x0o is not None else None, nthreads, _ptr(iters),
                        _ptr(reason), _ptr(xo) if x_cap > 0 else None, x_cap)
     return iters, reason, (xo if x_cap > 0 else None)

@@ -1,0 +1,267 @@
+"""Python face of libgpuklu, shaped like the reference's Rust API.
+
+* ``GpuKluSolver`` mirrors the ``LinearSolver`` trait
+  (crates/sim-core/src/solver.rs:141-166): prepare / analyze / factor /
+  solve / reset_pattern / name / set_parallel_threads, with the same error
+  behaviour (``SolverError`` is raised with the status of the C ABI).
+* ``DeviceCircuit`` is the compiled device-stamp plan and ``newton_dc`` the
+  device-resident DC operating point (crates/sim-core/src/engine.rs:249-311).
+* ``Batch`` runs many independent operating points in one kernel launch.
+
+Everything numeric runs on the GPU; constructing any of these without a CUDA
+device raises ``RuntimeError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+
+import numpy as np
+
+from . import native as N
+from .circuits import Circuit
+
+STATUS_NAMES = {0: "Ok", 1: "AnalyzeFailed", 2: "FactorFailed", 3: "SolveFailed",
+                4: "SingularMatrix", 5: "IllConditioned", 6: "InvalidMatrix",
+                7: "DeviceTimeout", 8: "NonFinite", 9: "CudaError"}
+
+
+class SolverError(RuntimeError):
+    """Mirror of SolverError (crates/sim-core/src/solver.rs:76-92)."""
+
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+class GpuKluSolver:
+    """Drop-in for NativeKluSolver / KluSolver behind the LinearSolver trait."""
+
+    def __init__(self, n: int = 0, pivot_mode: int = N.PIVOT_REFERENCE):
+        L = N.lib()
+        self._h = L.gpuklu_create(n)
+        if not self._h:
+            raise RuntimeError("gpuklu_create failed: no usable CUDA device")
+        self._n = n
+        if pivot_mode != N.PIVOT_REFERENCE:
+            L.gpuklu_set_pivot_mode(self._h, pivot_mode)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().gpuklu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, st: int):
+        if st != N.OK:
+            raise SolverError(st, N.lib().gpuklu_last_error(self._h).decode())
+
+    # -- trait
+    def prepare(self, n: int) -> None:
+        self._n = n
+        N.lib().gpuklu_prepare(self._h, n)
+
+    def analyze(self, ap, ai) -> None:
+        ap, ai = N.i64(ap), N.i64(ai)
+        self._check(N.lib().gpuklu_analyze(self._h, N.ptr(ap), len(ap), N.ptr(ai), len(ai)))
+
+    def factor(self, ap, ai, ax) -> None:
+        ap, ai, ax = N.i64(ap), N.i64(ai), N.f64(ax)
+        if len(ax) != len(ai):
+            raise SolverError(N.INVALID_MATRIX, "ax and ai lengths differ")
+        self._check(N.lib().gpuklu_factor(self._h, N.ptr(ap), len(ap), N.ptr(ai), len(ai),
+                                          N.ptr(ax)))
+
+    def solve(self, rhs: np.ndarray) -> None:
+        """Overwrites ``rhs`` (a float64 numpy array) with x."""
+        if not (isinstance(rhs, np.ndarray) and rhs.dtype == np.float64 and rhs.flags.c_contiguous):
+            raise TypeError("rhs must be a contiguous float64 numpy array")
+        self._check(N.lib().gpuklu_solve(self._h, N.ptr(rhs), len(rhs)))
+
+    def tsolve(self, g: np.ndarray) -> None:
+        """Overwrites ``g`` with y solving A^T y = g (adjoint)."""
+        self._check(N.lib().gpuklu_tsolve(self._h, N.ptr(g), len(g)))
+
+    def reset_pattern(self) -> None:
+        N.lib().gpuklu_reset_pattern(self._h)
+
+    def name(self) -> str:
+        return N.lib().gpuklu_name(self._h).decode()
+
+    def set_parallel_threads(self, threads: int) -> None:
+        N.lib().gpuklu_set_parallel_threads(self._h, threads)
+
+    # -- extensions
+    def set_pivot_mode(self, mode: int) -> None:
+        self._check(N.lib().gpuklu_set_pivot_mode(self._h, mode))
+
+    def stats(self) -> dict:
+        s = N.Stats()
+        self._check(N.lib().gpuklu_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in N.Stats._fields_}
+
+
+class DeviceCircuit:
+    """A circuit compiled into its stamp-to-slot map on the device."""
+
+    def __init__(self, c: Circuit, transient: bool = False):
+        self.circuit = c
+        t, nd, p = N.i32(c.type), N.i32(c.nodes), N.f64(c.p)
+        self._h = N.lib().gpuklu_compile_devices(c.node_count, c.ndev, N.ptr(t), N.ptr(nd),
+                                                 N.ptr(p), 1 if transient else 0)
+        if not self._h:
+            raise RuntimeError("gpuklu_compile_devices failed")
+        n = C.c_int64()
+        nnz = C.c_int64()
+        N.lib().gpuklu_circuit_dims(self._h, C.byref(n), C.byref(nnz))
+        self.n, self.nnz_raw = n.value, nnz.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().gpuklu_circuit_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def pattern(self):
+        ap = np.zeros(self.n + 1, np.int64)
+        ai = np.zeros(self.nnz_raw, np.int64)
+        N.lib().gpuklu_circuit_pattern(self._h, N.ptr(ap), N.ptr(ai))
+        return ap, ai
+
+    def set_params(self, p):
+        p = N.f64(p)
+        if N.lib().gpuklu_circuit_set_params(self._h, N.ptr(p)) != N.OK:
+            raise RuntimeError("set_params failed")
+
+    def stamp(self, solver: GpuKluSolver, x, gmin=1e-12, source_scale=1.0, dt=0.0,
+              cap_v=None, be_sign=-1.0):
+        """Device stamp at x: (ax_raw, rhs) copied back."""
+        x = N.f64(x)
+        ax = np.zeros(self.nnz_raw)
+        rhs = np.zeros(self.n)
+        cv = N.f64(cap_v) if cap_v is not None else None
+        st = N.lib().gpuklu_stamp(solver.handle, self._h, N.ptr(x), len(x), gmin, source_scale,
+                                  dt, N.ptr(cv) if cv is not None else None, be_sign,
+                                  N.ptr(ax), N.ptr(rhs))
+        solver._check(st)
+        return ax, rhs
+
+
+@dataclasses.dataclass
+class NewtonResult:
+    converged: bool
+    iterations: int
+    iterations_total: int
+    reason: str
+    x: np.ndarray
+
+
+REASONS = {0: "converged", 1: "maxiters", 2: "solver_failure"}
+
+
+def newton_dc(solver: GpuKluSolver, dc: DeviceCircuit, cfg: N.NewtonConfig,
+              x0=None) -> NewtonResult:
+    """Device-resident DC operating point through ``solver``."""
+    n = dc.n
+    x = np.zeros(n)
+    xl = C.c_int64()
+    it = C.c_int64()
+    itt = C.c_int64()
+    rs = C.c_int()
+    x0a = N.f64(x0) if x0 is not None else None
+    st = N.lib().gpuklu_newton_dc(solver.handle, dc.handle, C.byref(cfg),
+                                  N.ptr(x0a) if x0a is not None else None, N.ptr(x), n,
+                                  C.byref(xl), C.byref(it), C.byref(itt), C.byref(rs))
+    solver._check(st)
+    return NewtonResult(rs.value == 0, it.value, itt.value, REASONS[rs.value], x[:xl.value])
+
+
+class Batch:
+    """Independent DC operating points of many circuit instances.
+
+    ``circuits``: list of Circuit; ``inst_circ[i]``: circuit of instance i
+    (instances of one circuit must be consecutive); ``inst_dev[i]`` / ``inst_val[i]``:
+    device whose first parameter is overridden and its value (-1: none);
+    ``x0``/``x0_off``: flat initial iterates and their offsets (-1: zero start).
+    """
+
+    def __init__(self, circuits, inst_circ, inst_dev=None, inst_val=None, x0=None, x0_off=None):
+        self.circuits = circuits
+        ninst = len(inst_circ)
+        dev_off = np.zeros(len(circuits) + 1, np.int64)
+        for i, c in enumerate(circuits):
+            dev_off[i + 1] = dev_off[i] + c.ndev
+        ncs = N.i64([c.node_count for c in circuits])
+        t = N.i32(np.concatenate([c.type for c in circuits]))
+        nd = N.i32(np.concatenate([c.nodes for c in circuits]))
+        p = N.f64(np.concatenate([c.p for c in circuits]))
+        self.inst_circ = N.i64(inst_circ)
+        idev = N.i64(inst_dev if inst_dev is not None else -np.ones(ninst))
+        ival = N.f64(inst_val if inst_val is not None else np.zeros(ninst))
+        x0a = N.f64(x0) if x0 is not None else None
+        x0o = N.i64(x0_off) if x0_off is not None else None
+        self._h = N.lib().gpuklu_batch_create(
+            len(circuits), N.ptr(dev_off), N.ptr(ncs), N.ptr(t), N.ptr(nd), N.ptr(p), ninst,
+            N.ptr(self.inst_circ), N.ptr(idev), N.ptr(ival),
+            N.ptr(x0a) if x0a is not None else None, N.ptr(x0o) if x0o is not None else None,
+            len(x0a) if x0a is not None else 0)
+        if not self._h:
+            raise RuntimeError("gpuklu_batch_create failed")
+        self.ninst = ninst
+        ns = np.array([c.n for c in circuits], np.int64)[self.inst_circ]
+        self.x_off = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
+        self.x_len = int(ns.sum())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().gpuklu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def run(self, cfg: N.NewtonConfig):
+        st = N.lib().gpuklu_batch_run(self._h, C.byref(cfg))
+        if st != N.OK:
+            raise SolverError(st, N.lib().gpuklu_batch_last_error(self._h).decode())
+
+    def update_inputs(self, inst_val=None, x0=None):
+        iv = N.f64(inst_val) if inst_val is not None else None
+        xa = N.f64(x0) if x0 is not None else None
+        st = N.lib().gpuklu_batch_update_inputs(self._h, N.ptr(iv) if iv is not None else None,
+                                                N.ptr(xa) if xa is not None else None)
+        if st != N.OK:
+            raise SolverError(st, N.lib().gpuklu_batch_last_error(self._h).decode())
+
+    def results(self, with_x: bool = True):
+        it = np.zeros(self.ninst, np.int64)
+        itt = np.zeros(self.ninst, np.int64)
+        rs = np.zeros(self.ninst, np.int32)
+        x = np.zeros(self.x_len) if with_x else None
+        st = N.lib().gpuklu_batch_results(self._h, N.ptr(it), N.ptr(itt), N.ptr(rs),
+                                          N.ptr(x) if with_x else None,
+                                          N.ptr(self.x_off) if with_x else None)
+        if st != N.OK:
+            raise SolverError(st, N.lib().gpuklu_batch_last_error(self._h).decode())
+        return it, itt, rs, x
+
+    def info(self) -> dict:
+        out = np.zeros(5, np.int64)
+        N.lib().gpuklu_batch_info(self._h, N.ptr(out))
+        return dict(grid=int(out[0]), block=int(out[1]), tiles=int(out[2]),
+                    buffer_bytes=int(out[3]), bytes_per_iter_all_circuits=int(out[4]))
+
+    def stream(self) -> int:
+        return N.lib().gpuklu_batch_stream(self._h) or 0

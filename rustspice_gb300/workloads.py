@@ -1,0 +1,76 @@
+"""The seeded workloads the bench and the parity tests run.
+
+``inverter_batch`` is the batched Monte-Carlo DC case: uneven CMOS inverter
+chains (8..256 stages), each solved at every input voltage of a 0..1.2 V
+sweep as an independent DC operating point. The reference's Newton
+(crates/sim-core/src/newton.rs:65-117) has no device limiting, so from the
+engine's zero start it diverges on CMOS chains; each instance therefore
+starts from a logic-level nodeset: every stage output at the rail an ideal
+inverter with threshold ``vm`` would give. The instance's Newton then runs
+exactly as the reference's.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+from . import circuits as cz
+
+VDD = 1.2
+
+
+def chain_nodeset(stages: int, vin: float, vm: float = 0.585) -> np.ndarray:
+    """Logic-level initial iterate of an inverter chain (node order of
+    ``circuits.inverter_chain``)."""
+    x = np.zeros(stages + 3)
+    x[1] = VDD
+    x[2] = vin
+    v = vin
+    for k in range(stages):
+        v = VDD if v < vm else 0.0
+        x[3 + k] = v
+    return x
+
+
+@dataclasses.dataclass
+class InverterBatch:
+    circuits: list
+    inst_circ: np.ndarray
+    inst_dev: np.ndarray
+    inst_val: np.ndarray
+    x0: np.ndarray
+    x0_off: np.ndarray
+    stages: np.ndarray
+    vin: np.ndarray
+
+    @property
+    def ninst(self) -> int:
+        return len(self.inst_circ)
+
+
+def inverter_batch(nchains: int = 4096, nvin: int = 61, seed: int = 3,
+                   lo: int = 8, hi: int = 256, mos_model: str = "consistent") -> InverterBatch:
+    """nchains chains x nvin input points; instance i = (chain i // nvin,
+    vin point i % nvin). The input source is device 1 of every chain."""
+    stages = cz.chain_lengths(nchains, lo, hi, seed)
+    vins = cz.vin_points(nvin)
+    circuits = [cz.inverter_chain(int(s), 0.0, seed=seed, chain_id=i, mos_model=mos_model)
+                for i, s in enumerate(stages)]
+    ninst = nchains * nvin
+    inst_circ = np.repeat(np.arange(nchains, dtype=np.int64), nvin)
+    inst_dev = np.full(ninst, 1, np.int64)
+    inst_val = np.tile(vins, nchains)
+    sizes = np.repeat(stages + 3, nvin)
+    x0_off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    x0 = np.concatenate([chain_nodeset(int(stages[i // nvin]), float(inst_val[i]))
+                         for i in range(ninst)])
+    return InverterBatch(circuits, inst_circ, inst_dev, inst_val, x0, x0_off, stages,
+                         inst_val.copy())
+
+
+# Newton settings of the parity and bench runs: the engine's option names
+# (crates/sim-core/src/engine.rs:987-999) with tolerances tightened so the
+# converged iterate's residual is at the FP64 floor.
+TIGHT = dict(max_iters=100, abs_tol=1e-12, rel_tol=1e-10, gmin=1e-12, gmin_steps=0,
+             source_steps=0, damping=1.0, damping_min=0.1)

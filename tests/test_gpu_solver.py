@@ -1,0 +1,182 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle.
+
+Factor and solve results are compared bit for bit where the arithmetic is the
+same (both compile without multiply-add contraction and follow the
+reference's operation order); device stamps of diodes use CUDA's exp, so
+those are compared to 1e-14 relative. Newton results use the north-star
+tolerance: relative solution error <= 1e-10.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import pyoracle as po
+from rustspice_gb300 import circuits as cz
+from rustspice_gb300 import native as N
+from rustspice_gb300 import workloads as wl
+from rustspice_gb300.solver import Batch, DeviceCircuit, GpuKluSolver, SolverError, newton_dc
+
+pytestmark = pytest.mark.gpu
+
+MODES = [(N.PIVOT_REFERENCE, "nativeklu"), (N.PIVOT_EXACT, "nativeklu_exact")]
+
+
+def _systems():
+    out = []
+    c = cz.mesh_dc()
+    out.append(("mesh32", po.mna(c, np.zeros(c.node_count))))
+    for s, v in [(8, 0.3), (40, 0.7), (256, 0.55)]:
+        c = cz.inverter_chain(s, v)
+        out.append((f"chain{s}", po.mna(c, wl.chain_nodeset(s, v))))
+    return out
+
+
+def _block_lower(n=300, seed=0):
+    """Random diagonally dominant matrix in block lower triangular form with
+    shuffled rows/columns, so BTF finds many blocks and coupling entries."""
+    rng = np.random.default_rng(seed)
+    A = np.zeros((n, n))
+    b0 = 0
+    while b0 < n:
+        bs = int(rng.integers(1, 9))
+        b1 = min(n, b0 + bs)
+        A[b0:b1, b0:b1] = rng.standard_normal((b1 - b0, b1 - b0)) * (rng.random((b1 - b0, b1 - b0)) < 0.6)
+        b0 = b1
+    A += np.tril(rng.standard_normal((n, n)) * (rng.random((n, n)) < 0.01), -8)
+    A[np.arange(n), np.arange(n)] += 5.0
+    p = rng.permutation(n)
+    q = rng.permutation(n)
+    A = A[p][:, q]
+    M = sp.csc_matrix(A)
+    M.sort_indices()
+    return n, M.indptr.astype(np.int64), M.indices.astype(np.int64), M.data.copy(), rng.standard_normal(n)
+
+
+@pytest.mark.parametrize("mode,kind", MODES)
+def test_factor_solve_bitexact(mode, kind):
+    for name, (n, ap, ai, ax, rhs) in _systems() + [("blocklower", _block_lower())]:
+        g = GpuKluSolver(n, pivot_mode=mode)
+        o = po.Solver(kind, n)
+        o.prepare(n)
+        g.prepare(n)
+        rng = np.random.default_rng(1)
+        for it, a in enumerate([ax, ax * (1 + 0.05 * rng.standard_normal(len(ax))), ax]):
+            g.analyze(ap, ai)
+            assert o.analyze(ap, ai) == 0
+            g.factor(ap, ai, a)
+            assert o.factor(ap, ai, a) == 0
+            xg = rhs.copy()
+            g.solve(xg)
+            st, xo = o.solve(rhs)
+            assert st == 0
+            assert np.array_equal(xg, xo), (name, kind, it, np.max(np.abs(xg - xo)))
+        s = g.stats()
+        ks = o.klu_stats()
+        assert s["factor_count"] == 1 and s["refactor_count"] == 2
+        assert s["nblocks"] == ks["nblocks"]
+        if mode == N.PIVOT_REFERENCE:
+            assert (s["nnz_l"], s["nnz_u"]) == (ks["nnz_l"], ks["nnz_u"])
+        assert s["rcond"] == pytest.approx(ks["rcond"], rel=0, abs=0)
+        g.close()
+
+
+def test_exact_mode_solves_the_system():
+    for name, (n, ap, ai, ax, rhs) in _systems() + [("blocklower", _block_lower())]:
+        g = GpuKluSolver(n, pivot_mode=N.PIVOT_EXACT)
+        g.factor(ap, ai, ax)
+        x = rhs.copy()
+        g.solve(x)
+        A = sp.csc_matrix((ax, ai, ap), shape=(n, n))
+        xr = np.linalg.solve(A.toarray(), rhs)
+        assert np.max(np.abs(x - xr)) <= 1e-10 * max(1.0, np.max(np.abs(xr))), name
+        # adjoint: A^T y = g
+        if g.stats()["noffdiag"] == 0:
+            y = rhs.copy()
+            g.tsolve(y)
+            yr = np.linalg.solve(A.toarray().T, rhs)
+            assert np.max(np.abs(y - yr)) <= 1e-10 * max(1.0, np.max(np.abs(yr))), name
+
+
+def test_error_behaviour():
+    n, ap, ai, ax, rhs = _systems()[1][1]
+    g = GpuKluSolver(n)
+    with pytest.raises(SolverError) as e:
+        g.solve(rhs.copy())
+    assert e.value.status == N.SOLVE_FAILED
+    with pytest.raises(SolverError) as e:
+        g.analyze(ap[:-1], ai)
+    assert e.value.status == N.INVALID_MATRIX
+    g.factor(ap, ai, ax)
+    with pytest.raises(SolverError) as e:
+        g.solve(np.zeros(n + 1))
+    assert e.value.status == N.INVALID_MATRIX
+    assert g.name() == "GpuKLU"
+    g.prepare(n + 1)  # size change resets the pattern
+    with pytest.raises(SolverError):
+        g.solve(np.zeros(n + 1))
+
+
+@pytest.mark.parametrize("model", ["reference", "consistent"])
+def test_device_stamps(model):
+    rng = np.random.default_rng(2)
+    cases = [cz.mesh_dc(), cz.inverter_chain(20, 0.4, mos_model=model),
+             cz.ring_oscillator(11, mos_model=model)]
+    g = GpuKluSolver(1)
+    for c in cases:
+        dc = DeviceCircuit(c)
+        ap, ai = dc.pattern()
+        x = rng.uniform(-0.2, 1.3, c.node_count)
+        x[0] = 0.0
+        for gmin in (1e-12, 1e-6):
+            ax, rhs = dc.stamp(g, x, gmin=gmin)
+            n, ap_o, ai_o, ax_o, rhs_o = po.mna(c, x, gmin=gmin)
+            assert dc.n == n
+            assert np.array_equal(ap, ap_o) and np.array_equal(ai, ai_o)
+            np.testing.assert_allclose(ax, ax_o, rtol=1e-14, atol=0)
+            np.testing.assert_allclose(rhs, rhs_o, rtol=1e-14, atol=1e-300)
+            if not np.any(c.type == cz.DEV_D):
+                assert np.array_equal(ax, ax_o) and np.array_equal(rhs, rhs_o)
+
+
+def test_newton_dc_mesh():
+    c = cz.mesh_dc()
+    cfg = dict(wl.TIGHT, gmin_steps=10)
+    ocfg = {k: cfg[k] for k in ("max_iters", "abs_tol", "rel_tol", "gmin", "gmin_steps",
+                                "source_steps")}
+    r_o, it_o, x_o = po.dc_op(c, "nativeklu_exact", **ocfg)
+    g = GpuKluSolver(1, pivot_mode=N.PIVOT_EXACT)
+    dc = DeviceCircuit(c)
+    res = newton_dc(g, dc, N.newton_config(**cfg))
+    assert res.converged and r_o == "converged"
+    assert res.iterations == it_o
+    assert np.max(np.abs(res.x - x_o)) <= 1e-10 * np.max(np.abs(x_o))
+    assert po.residual(c, res.x, 1e-6) <= 1e-12
+    # reference pivot rule: same iterates as the reference's NativeKLU
+    r_r, it_r, x_r = po.dc_op(c, "nativeklu", **ocfg)
+    g2 = GpuKluSolver(1, pivot_mode=N.PIVOT_REFERENCE)
+    res2 = newton_dc(g2, DeviceCircuit(c), N.newton_config(**cfg))
+    assert res2.iterations == it_r and res2.reason == r_r
+    assert np.max(np.abs(res2.x - x_r)) <= 1e-10 * np.max(np.abs(x_r))
+
+
+def test_batch_matches_oracle():
+    B = wl.inverter_batch(12, 61, seed=11)
+    it_o, rs_o, x_o = po.dc_batch(B.circuits, B.inst_circ, B.inst_dev, B.inst_val,
+                                  "nativeklu_exact", nthreads=4,
+                                  x_cap=max(c.n for c in B.circuits), x0=B.x0,
+                                  x0_off=B.x0_off, **{k: v for k, v in wl.TIGHT.items()
+                                                      if k in ("max_iters", "abs_tol",
+                                                               "rel_tol", "gmin", "gmin_steps")})
+    bt = Batch(B.circuits, B.inst_circ, B.inst_dev, B.inst_val, B.x0, B.x0_off)
+    bt.run(N.newton_config(**wl.TIGHT))
+    it, itt, rs, x = bt.results()
+    conv = rs_o == 0
+    assert np.mean(conv) > 0.9
+    assert np.array_equal(rs == 0, conv)
+    agree = np.mean(it[conv] == it_o[conv])
+    assert agree > 0.98, agree
+    for i in np.flatnonzero(conv):
+        n = B.circuits[B.inst_circ[i]].n
+        xg = x[bt.x_off[i]:bt.x_off[i] + n]
+        xo = x_o[i, :n]
+        assert np.max(np.abs(xg - xo)) <= 1e-10 * max(1.0, np.max(np.abs(xo))), i
