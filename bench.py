@@ -1,0 +1,402 @@
+"""Benchmark: batched circuit-Newton iterations/s on one GB300 (FP64).
+
+Workload (one "step"): the batched Monte-Carlo DC case - 4096 CMOS inverter
+chains of 8..256 stages (level-1 card, KP_n=120u, KP_p=40u, VTO ~ N(+-0.45,
+0.03), W jittered +-5%), each solved at 61 input voltages 0..1.2 V as an
+independent DC operating point: 249,856 Newton solves, every Newton iteration
+= device stamp + frozen-pivot refactor + forward/backward solve + update, all
+in one kernel launch. Synthetic seeded data (the reference publishes none).
+
+``value``   Newton iterations/s with inputs resident in device memory.
+``e2e``     the same through the public API from pinned host buffers: the
+            per-step copy of the inputs (input voltages and initial iterates)
+            and the read-back of every solution are inside the timed region.
+``--impl reference`` times the reference's CPU algorithm (the oracle's C++
+restatement of NativeKLU, the exact-pivot variant, with the same Newton
+loop) on the host cores over a bounded sample of the same instances.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "circuit-Newton iters/s, batched vs one-at-a-time on GB300 (FP64, resid<=1e-10)"
+UNIT = "iters/s"
+WORKLOAD = "batched Monte-Carlo DC: 4096 CMOS inverter chains (8-256 stages) x 61 Vin"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpuklu", choices=["gpuklu", "reference"])
+    ap.add_argument("--chains", type=int, default=4096)
+    ap.add_argument("--nvin", type=int, default=61)
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="instances timed on the host cores (0: sized for ~15 s)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    lrank = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, lrank
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def _alg_bytes_per_iter(batch_circuits):
+    """Algorithmic bytes of one Newton iteration of one instance, as defined
+    for the roofline: stamp 8*nnz_A + 8*n + per-device bytes (diode 104 B,
+    level-1 MOSFET 184 B); refactor 8*nnz_A + 12*(nnz_L+nnz_U); solve
+    12*(nnz_L+nnz_U) + 24*n; update 32*n. nnz counts from the GPU solver's
+    own symbolic analysis (host-side plan, no device work)."""
+    from rustspice_gb300 import native as N
+    from rustspice_gb300.solver import DeviceCircuit
+    out = {}
+    for c in batch_circuits:
+        key = (c.ndev, c.node_count)
+        if key in out:
+            continue
+        dc = DeviceCircuit(c)
+        ap, ai = dc.pattern()
+        n = dc.n
+        dc.close()
+        plan = N.Plan(n, ap, ai, N.PIVOT_EXACT)
+        nnz_a = len(ai)
+        nlu = plan.nnz_l + plan.nnz_u
+        nmos = int(np.count_nonzero((c.type == 4) | (c.type == 6)))
+        ndio = int(np.count_nonzero(c.type == 3))
+        b = (8 * nnz_a + 8 * n + 104 * ndio + 184 * nmos) + (8 * nnz_a + 12 * nlu) + \
+            (12 * nlu + 24 * n) + 32 * n
+        out[key] = b
+    return out
+
+
+def _residual_sample(B, bt, rs, count=64):
+    import scipy.sparse as sp
+    from rustspice_gb300.solver import DeviceCircuit, GpuKluSolver
+    _, _, _, xs = bt.results(with_x=True)
+    conv = np.flatnonzero(rs == 0)
+    idx = conv[:: max(1, len(conv) // count)][:count]
+    g = GpuKluSolver(1)
+    worst = 0.0
+    for i in idx:
+        c0 = B.circuits[B.inst_circ[i]]
+        c = c0.__class__(**{**c0.__dict__})
+        c.p = c0.p.copy()
+        c.p[B.inst_dev[i], 0] = B.inst_val[i]
+        dc = DeviceCircuit(c)
+        x = xs[bt.x_off[i]:bt.x_off[i] + dc.n]
+        ax, rhs = dc.stamp(g, x[:c.node_count])
+        ap, ai = dc.pattern()
+        A = sp.csc_matrix((ax, ai, ap), shape=(dc.n, dc.n))
+        r = A @ x - rhs
+        den = abs(A).sum(axis=1).max() * np.max(np.abs(x)) + np.max(np.abs(rhs))
+        worst = max(worst, float(np.max(np.abs(r)) / den))
+        dc.close()
+    g.close()
+    return worst
+
+
+def run_gpu(a):
+    import torch
+    from rustspice_gb300 import native as N
+    from rustspice_gb300 import workloads as wl
+    from rustspice_gb300.solver import Batch, DeviceCircuit, GpuKluSolver, newton_dc
+
+    ws, rank, lrank = _dist()
+    torch.cuda.set_device(lrank)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", lrank)
+    B = wl.inverter_batch(a.chains, a.nvin, seed=3)
+    bt = Batch(B.circuits, B.inst_circ, B.inst_dev, B.inst_val, B.x0, B.x0_off)
+    cfg = N.newton_config(**wl.TIGHT)
+    stream = torch.cuda.ExternalStream(bt.stream(), device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def step():
+        flush.fill_(1)
+        bt.run(cfg)
+
+    with torch.cuda.stream(stream):
+        for _ in range(a.warmup):
+            step()
+        stream.synchronize()
+        it, itt, rs, _ = bt.results(with_x=False)
+        iters_per_step = int(itt.sum())
+        # device-resident timing
+        clk = ClockSampler(lrank)
+        clk.start()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        evs = []
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            flush.fill_(1)
+            e0.record(stream)
+            bt.run(cfg)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        clocks = clk.stop()
+        kern_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+        ms_step = float(np.mean(kern_ms))
+        if ws > 1:
+            t = torch.tensor([ms_step], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms_step = float(t.item())
+        value = iters_per_step * ws / (ms_step * 1e-3)
+
+        # end-to-end: pinned host inputs -> device, run, every solution -> host
+        val_h = torch.from_numpy(np.ascontiguousarray(B.inst_val)).pin_memory()
+        x0_h = torch.from_numpy(np.ascontiguousarray(B.x0)).pin_memory()
+        e2e_ms = []
+        for _ in range(max(2, a.steps)):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            bt.update_inputs(val_h.numpy(), x0_h.numpy())
+            bt.run(cfg)
+            it2, itt2, rs2, x2 = bt.results(with_x=True)
+            e2e_ms.append((time.perf_counter() - t1) * 1e3)
+        e2e_step = float(np.median(e2e_ms))
+        h2d = val_h.numel() * 8 + x0_h.numel() * 8
+        d2h = len(x2) * 8 + 3 * 8 * len(it2)
+    conv = float(np.mean(rs == 0))
+    it_final = it
+
+    # Newton residual F(x) = A(x) x - b(x) of a sample of converged solutions,
+    # stamped at x by the device and evaluated on the host, normwise relative
+    resid = _residual_sample(B, bt, rs)
+
+    # roofline
+    hbm_peak, peak_src = _measured_peaks()
+    per_key = _alg_bytes_per_iter(B.circuits)
+    keys = [(B.circuits[c].ndev, B.circuits[c].node_count) for c in B.inst_circ]
+    alg_bytes = float(sum(per_key[k] * t for k, t in zip(keys, itt)))
+    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    flops, _ = bt.work()
+    fp64 = float(np.sum(flops.astype(np.float64) * itt))
+    fp64_tflops = fp64 / (ms_step * 1e-3) / 1e12
+    fp64_peak = float(N.lib().gpuklu_fp64_peak_tflops())
+
+    # one-at-a-time GpuKluSolver on a sample (the metric's comparison)
+    rng = np.random.default_rng(0)
+    sample = rng.choice(B.ninst, 24, replace=False)
+    t_one, it_one = 0.0, 0
+    g = GpuKluSolver(1, pivot_mode=N.PIVOT_EXACT)
+    for i in sample:
+        c = B.circuits[B.inst_circ[i]]
+        c2 = c.__class__(**{**c.__dict__})
+        c2.p = c.p.copy()
+        c2.p[1, 0] = B.inst_val[i]
+        dc = DeviceCircuit(c2)
+        x0 = B.x0[B.x0_off[i]:B.x0_off[i] + c.node_count]
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        r = newton_dc(g, dc, cfg, x0=x0)
+        t_one += time.perf_counter() - t1
+        it_one += r.iterations_total
+        g.reset_pattern()
+    one_at_a_time = it_one / t_one
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded circuits; the reference publishes no dataset)",
+        "config": {"workload": WORKLOAD, "chains": a.chains, "vin_points": a.nvin,
+                   "instances": int(B.ninst), "newton_iterations_per_step": iters_per_step,
+                   "converged_fraction": conv, "max_final_residual": resid,
+                   "newton": dict(wl.TIGHT), "mos_model": "level-1, consistent linearisation",
+                   "initial_iterate": "logic-level nodeset",
+                   "l2": "256 MB buffer written before every timed step; inputs 270 MB > L2",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": iters_per_step * ws / (e2e_step * 1e-3), "unit": UNIT,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": e2e_step},
+        "gpu_launches": a.steps,
+        "one_at_a_time": {"value": one_at_a_time, "unit": UNIT,
+                          "how": "GpuKluSolver newton_dc, one instance at a time, 24 sampled",
+                          "batched_over_one_at_a_time": value / one_at_a_time},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_step": alg_bytes},
+        "roofline_fp64": {"achieved": fp64_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
+                          "frac": fp64_tflops / fp64_peak if fp64_peak else None,
+                          "peak_source": "measured DFMA microbenchmark (gpuklu_fp64_peak_tflops)",
+                          "fp64_ops_per_step": fp64},
+        "clocks": clocks,
+        "wall_s_timed": wall,
+    }
+    if not a.no_cpu_baseline and rank == 0:
+        line["cpu_baseline"] = cpu_baseline(B, a, cfg_dict=wl.TIGHT)
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _cpu_sample(B, count, seed=1):
+    """Stratified sample of instances (every stage count represented)."""
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(B.ninst, min(count, B.ninst), replace=False))
+
+
+def _cpu_run(B, idx, threads, cfg_dict):
+    from oracle import pyoracle as po
+    circ_ids = np.unique(B.inst_circ[idx])
+    remap = {c: k for k, c in enumerate(circ_ids)}
+    circuits = [B.circuits[c] for c in circ_ids]
+    order = np.argsort(B.inst_circ[idx], kind="stable")
+    idx = idx[order]
+    ic = np.array([remap[c] for c in B.inst_circ[idx]], np.int64)
+    x0 = np.concatenate([B.x0[B.x0_off[i]:B.x0_off[i] + B.circuits[B.inst_circ[i]].node_count]
+                         for i in idx])
+    off = np.concatenate([[0], np.cumsum([B.circuits[B.inst_circ[i]].node_count
+                                          for i in idx])[:-1]]).astype(np.int64)
+    kw = {k: cfg_dict[k] for k in ("max_iters", "abs_tol", "rel_tol", "gmin", "gmin_steps")}
+    t0 = time.perf_counter()
+    it, rs, _ = po.dc_batch(circuits, ic, B.inst_dev[idx], B.inst_val[idx], "nativeklu_exact",
+                            nthreads=threads, x0=x0, x0_off=off, **kw)
+    dt = time.perf_counter() - t0
+    return int(it.sum()), dt, float(np.mean(rs == 0))
+
+
+def cpu_baseline(B, a, cfg_dict):
+    threads = os.cpu_count() or 1
+    count = a.cpu_sample or 4000
+    idx = _cpu_sample(B, count)
+    iters, dt, conv = _cpu_run(B, idx, threads, cfg_dict)
+    if not a.cpu_sample and dt < 10.0:  # grow the sample towards ~15 s of CPU work
+        count = int(min(B.ninst, count * max(1.0, 15.0 / max(dt, 1e-3))))
+        idx = _cpu_sample(B, count)
+        iters, dt, conv = _cpu_run(B, idx, threads, cfg_dict)
+    return {"value": iters / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(idx)} of {B.ninst} instances (random, seed 1), "
+                      f"{iters} Newton iterations in {dt:.2f} s, converged {conv:.4f}; "
+                      "oracle C++ NativeKLU (exact pivots) + reference Newton loop"}
+
+
+def run_reference(a):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    from rustspice_gb300 import workloads as wl
+    B = wl.inverter_batch(a.chains, a.nvin, seed=3)
+    threads = os.cpu_count() or 1
+    count = a.cpu_sample or 3000
+    idx = _cpu_sample(B, count)
+    for _ in range(max(0, min(a.warmup, 1))):
+        _cpu_run(B, idx[: max(1, len(idx) // 10)], threads, wl.TIGHT)
+    per = []
+    tot_it = 0
+    for _ in range(a.steps):
+        iters, dt, conv = _cpu_run(B, idx, threads, wl.TIGHT)
+        per.append(dt)
+        tot_it = iters
+    ms = float(np.mean(per)) * 1e3
+    value = tot_it / (ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded circuits)",
+        "config": {"workload": WORKLOAD, "chains": a.chains, "vin_points": a.nvin,
+                   "step": f"bounded sample of {len(idx)} instances per step"},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{len(idx)} of {B.ninst} instances per step (seed 1); "
+                                   "oracle C++ restatement of NativeKLU (exact pivots) and the "
+                                   "reference Newton loop"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    args = _args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)

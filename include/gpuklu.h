@@ -190,11 +190,19 @@ int gpuklu_batch_results(gpuklu_batch* b, int64_t* iters, int64_t* iters_total, 
 int gpuklu_batch_update_inputs(gpuklu_batch* b, const double* inst_val, const double* x0);
 /* Last error text of the batch. */
 const char* gpuklu_batch_last_error(const gpuklu_batch* b);
-/* Launch geometry and work figures: out[0] grid, out[1] block, out[2]
- * tiles, out[3] buffer bytes, out[4] value bytes touched per Newton
- * iteration summed over one instance of every circuit. */
+/* Launch geometry (out has 6 entries): out[0] grid, out[1] threads per
+ * block, out[2] program groups, out[3] shared-memory bytes per warp,
+ * out[4] registers per thread, out[5] resident blocks per SM. */
 int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out);
+/* Work of one Newton iteration of every instance: FP64 operations and the
+ * value bytes it moves through on-chip memory (arrays of ninst). */
+int gpuklu_batch_work(const gpuklu_batch* b, int64_t* flops, int64_t* bytes);
 void* gpuklu_batch_stream(gpuklu_batch* b);
+
+/* Measured FP64 fused multiply-add throughput of the current device in
+ * TFLOP/s (a short microbenchmark; the denominator of FP64 roofline
+ * fractions). */
+double gpuklu_fp64_peak_tflops(void);
 
 /* ------------------------------------------------ host-only diagnostics */
 

@@ -809,27 +809,215 @@ struct gpuklu_batch {
   cudaStream_t stream = nullptr;
   std::string err;
   std::vector<gk::GroupHdr> groups;
-  std::vector<gk::Tile> tiles;
-  std::vector<int> inst_n;
   DBuf<gk::GroupHdr> d_groups;
-  DBuf<gk::Tile> d_tiles;
   DBuf<unsigned> d_counter;
-  DBuf<i32> d_dev_type, d_dev_nodes, d_dev_slot, d_col_ptr, d_dslot, d_col_single, d_in_row,
-      d_out_pos, d_offd_ptr, d_slot_row, d_upd_ptr, d_upd_dst, d_offd_col, d_block_ptr,
-      d_ov_dev, d_iters, d_iters_total, d_reason, d_status;
-  DBuf<double> d_dev_p, d_ov_val, d_x0, d_buf, d_xout;
-  DBuf<long long> d_x0_off, d_x_off;
+  DBuf<i32> d_order, d_inst_group, d_dev_type, d_dev_nodes, d_dev_dv, d_amap_ptr, d_amap_code,
+      d_rmap_ptr, d_rmap_code, d_col_ptr, d_dslot, d_col_single, d_in_row, d_out_pos,
+      d_offd_ptr, d_slot_row, d_upd_ptr, d_upd_dst, d_offd_col, d_block_ptr, d_ov_dev, d_iters,
+      d_iters_total, d_reason, d_status;
+  DBuf<double> d_dparams, d_ov_val, d_x0, d_xout;
+  DBuf<long long> d_p_off, d_x0_off, d_x_off;
   std::vector<long long> x_off;
   int64_t x0_len = 0, xout_len = 0;
-  int grid = 0, block = 128;
-  long long buf_stride = 0;
-  int64_t bytes_per_iter = 0;
+  int grid = 0, warps_per_block = 2, regs = 0, blocks_per_sm = 0, region = 0;
+  int64_t flops_per_iter = 0, bytes_per_iter = 0;
+  std::vector<int64_t> group_flops, group_bytes;
+  std::vector<i32> inst_group_h;
+  gk::BatchArgs args{};
 
   int fail(const std::string& m) {
     err = m;
     return GPUKLU_CUDA_ERROR;
   }
 };
+
+namespace {
+// Program of one circuit as flat arrays; circuits with equal programs share
+// a group (only their constants and inputs differ).
+struct Program {
+  gk::GroupHdr h{};
+  std::vector<i32> dev_type, dev_nodes, dev_dv, amap_ptr, amap_code, rmap_ptr, rmap_code,
+      col_ptr, dslot, col_single, in_row, out_pos, offd_ptr, slot_row, upd_ptr, upd_dst,
+      offd_col, block_ptr;
+  int64_t flops = 0, bytes = 0;
+  std::string key() const {
+    std::string k;
+    auto app = [&k](const std::vector<i32>& v) {
+      int32_t sz = (int32_t)v.size();
+      k.append((const char*)&sz, 4);
+      k.append((const char*)v.data(), v.size() * 4);
+    };
+    int32_t hdr[7] = {h.n, h.node_count, h.nslots, h.noffd, h.ndev, h.nblocks, h.ndv};
+    k.append((const char*)hdr, sizeof(hdr));
+    for (auto* v : {&dev_type, &dev_nodes, &dev_dv, &amap_ptr, &amap_code, &rmap_ptr,
+                    &rmap_code, &col_ptr, &dslot, &col_single, &in_row, &out_pos, &offd_ptr,
+                    &slot_row, &upd_ptr, &upd_dst, &offd_col, &block_ptr})
+      app(*v);
+    return k;
+  }
+};
+
+int record_size(int type) {
+  switch (type) {
+    case 3: return 2;
+    case 4: return 3;
+    case 6: return 4;
+    case 5: return 0;
+    default: return 1;
+  }
+}
+
+// Contribution codes of every matrix insert and rhs add of one device, in
+// the reference's insert order (see compile_circuit).
+void device_codes(int type, int dv, int m[8], int r[2]) {
+  auto c = [dv](int k, int kind) { return ((dv + k) << 3) | kind; };
+  for (int e = 0; e < 8; ++e) m[e] = -1;
+  r[0] = r[1] = -1;
+  switch (type) {
+    case 0:
+      m[0] = c(0, 0); m[1] = c(0, 0); m[2] = c(0, 1); m[3] = c(0, 1);
+      break;
+    case 1:
+      m[0] = 2; m[1] = 3; m[2] = 2; m[3] = 3;
+      r[0] = c(0, 0);
+      break;
+    case 2:
+      r[0] = c(0, 1); r[1] = c(0, 0);
+      break;
+    case 3:
+      m[0] = c(0, 0); m[1] = c(0, 0); m[2] = c(0, 1); m[3] = c(0, 1);
+      r[0] = c(1, 1); r[1] = c(1, 0);
+      break;
+    case 4:
+      m[0] = c(0, 0); m[1] = c(0, 0); m[2] = c(0, 1); m[3] = c(0, 1);
+      m[4] = c(1, 0); m[5] = c(1, 1); m[6] = c(1, 1); m[7] = c(1, 0);
+      r[0] = c(2, 1); r[1] = c(2, 0);
+      break;
+    case 6:
+      m[0] = c(0, 0); m[1] = c(1, 1); m[2] = c(1, 0); m[3] = c(0, 1);
+      m[4] = c(2, 0); m[5] = 4; m[6] = c(2, 1); m[7] = 4;
+      r[0] = c(3, 1); r[1] = c(3, 0);
+      break;
+    default:
+      break;
+  }
+}
+
+Program make_program(const gpuklu_circuit& C, const gk::Plan& P) {
+  Program g;
+  gk::GroupHdr& h = g.h;
+  h.n = P.n;
+  h.node_count = C.node_count;
+  h.nslots = P.nslots();
+  h.noffd = (int)P.offd_raw.size();
+  h.ndev = C.ndev;
+  h.nblocks = P.nblocks;
+  std::vector<int> raw_offd(C.ai.size(), -1);
+  for (size_t e = 0; e < P.offd_raw.size(); ++e) raw_offd[P.offd_raw[e]] = (int)e;
+  const int nv = h.nslots + h.noffd;
+  std::vector<std::vector<i32>> vlist(nv), rlist(P.n);
+  int ndv = 0;
+  int64_t dev_flops = 0;
+  for (int d = 0; d < C.ndev; ++d) {
+    const int t = C.type[d];
+    g.dev_type.push_back(t);
+    for (int q = 0; q < 4; ++q) g.dev_nodes.push_back(C.nodes[(size_t)d * 4 + q]);
+    g.dev_dv.push_back(ndv);
+    int m[8], r[2];
+    device_codes(t, ndv, m, r);
+    for (int e = 0; e < 8; ++e) {
+      const int raw = C.raw[(size_t)d * 8 + e];
+      if (raw < 0 || m[e] < 0) continue;
+      const int v = P.raw_slot[raw] >= 0 ? P.raw_slot[raw]
+                                         : (raw_offd[raw] >= 0 ? h.nslots + raw_offd[raw] : -1);
+      if (v >= 0) vlist[v].push_back(m[e]);
+    }
+    const int* nd = &C.nodes[(size_t)d * 4];
+    const int ra = t == 1 ? nd[2] : nd[0];
+    const int rb = (t == 4 || t == 6) ? nd[2] : nd[1];
+    if (r[0] >= 0) rlist[ra].push_back(r[0]);
+    if (r[1] >= 0) rlist[rb].push_back(r[1]);
+    ndv += record_size(t);
+    dev_flops += t == 6 ? 32 : t == 4 ? 30 : t == 3 ? 30 : 0;
+  }
+  if (C.pin_raw >= 0 && P.raw_slot[C.pin_raw] >= 0) vlist[P.raw_slot[C.pin_raw]].push_back(2);
+  h.ndv = std::max(ndv, h.node_count);
+  int64_t nadd = 0;
+  g.amap_ptr.push_back(0);
+  for (int v = 0; v < nv; ++v) {
+    g.amap_code.insert(g.amap_code.end(), vlist[v].begin(), vlist[v].end());
+    g.amap_ptr.push_back((i32)g.amap_code.size());
+    nadd += (int64_t)vlist[v].size();
+  }
+  g.rmap_ptr.push_back(0);
+  for (int i = 0; i < P.n; ++i) {
+    g.rmap_code.insert(g.rmap_code.end(), rlist[i].begin(), rlist[i].end());
+    g.rmap_ptr.push_back((i32)g.rmap_code.size());
+    nadd += (int64_t)rlist[i].size();
+  }
+  g.in_row.assign(P.n + 1, 0);
+  for (int k = 0; k <= P.n; ++k) {
+    g.col_ptr.push_back(P.col_ptr[k]);
+    g.dslot.push_back(k < P.n ? P.dslot[k] : 0);
+    g.col_single.push_back(k < P.n ? P.col_single[k] : 0);
+    g.out_pos.push_back(k < P.n ? P.out_pos[k] : 0);
+    g.offd_ptr.push_back(P.offd_ptr[k]);
+  }
+  for (int r = 0; r < P.n; ++r) g.in_row[P.in_pos[r]] = r;
+  for (int s = 0; s <= P.nslots(); ++s) {
+    g.slot_row.push_back(s < P.nslots() ? P.slot_row[s] : 0);
+    g.upd_ptr.push_back(P.upd_ptr[s]);
+  }
+  g.upd_dst = P.upd_dst;
+  g.offd_col = P.offd_col;
+  g.block_ptr.assign(P.block_ptr.begin(), P.block_ptr.end());
+  // FP64 operations of one Newton iteration: device evaluation, assembly
+  // additions, refactorization, both substitutions, block coupling, update
+  const int64_t nl = P.nnz_l, nu = P.nnz_u - P.n;
+  g.flops = dev_flops + nadd + P.flops_refactor + 2 * (nl + nu) + P.n + 2 * h.noffd +
+            6LL * h.node_count;
+  // value bytes a Newton iteration moves through on-chip memory
+  g.bytes = 8LL * (h.ndv + 2 * nadd + 3 * (int64_t)P.upd_dst.size() + 2 * nv +
+                   6 * (nl + nu) + 6LL * P.n + 4LL * h.node_count);
+  h.cost = (int)std::min<int64_t>(g.flops, 0x7fffffff);
+  return g;
+}
+
+// Circuit constants (4 per device) with the reference's arithmetic:
+// R 1/R (stamp.rs:253); D Is, 0.02585*N, Is/vt (stamp.rs:360-370); level-1
+// beff = (u0*1e-4*(EPSILON_OX/tox))*W/L (bsim/mod.rs:445, params.rs:10,
+// 460-462, evaluate.rs:318).
+void circuit_constants(int64_t ndev, const int32_t* type, const double* p,
+                       std::vector<double>& out) {
+  const double eps_ox = 3.9 * 8.854e-12;
+  for (int64_t d = 0; d < ndev; ++d) {
+    const double* q = p + 6 * d;
+    double c[4] = {0.0, 0.0, 0.0, 0.0};
+    switch (type[d]) {
+      case 0: c[0] = 1.0 / q[0]; break;
+      case 1:
+      case 2: c[0] = q[0]; break;
+      case 3: {
+        const double vt = 0.02585 * q[1];
+        c[0] = q[0];
+        c[1] = vt;
+        c[2] = q[0] / vt;
+        break;
+      }
+      case 4:
+      case 6: {
+        const double beta = q[2] * 1e-4 * (eps_ox / q[3]);
+        c[0] = type[d] == 4 ? q[0] : (q[0] != 0.0 ? -1.0 : 1.0);
+        c[1] = type[d] == 4 ? q[1] : std::fabs(q[1]);
+        c[2] = beta * q[4] / q[5];
+        break;
+      }
+      default: c[0] = q[0]; break;
+    }
+    out.insert(out.end(), c, c + 4);
+  }
+}
+}  // namespace
 
 extern "C" {
 
@@ -846,37 +1034,38 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
   gpuklu_handle* H = gpuklu_create(1);
   if (!H) return nullptr;
   gpuklu_set_pivot_mode(H, GPUKLU_PIVOT_EXACT);
-  // first instance of every circuit: its iterate is used for pivot discovery
   std::vector<int64_t> first(ncirc, -1);
-  std::vector<std::vector<int64_t>> members(ncirc);
   for (int64_t i = 0; i < ninst; ++i) {
     if (inst_circ[i] < 0 || inst_circ[i] >= ncirc) {
       fprintf(stderr, "gpuklu_batch_create: instance %ld has no circuit\n", (long)i);
       gpuklu_destroy(H);
       return nullptr;
     }
-    members[inst_circ[i]].push_back(i);
     if (first[inst_circ[i]] < 0) first[inst_circ[i]] = i;
   }
-  std::vector<i32> dtype, dnodes, dslotv, col_ptr, dslot, csing, in_row, out_pos, offd_ptr,
-      slot_row, upd_ptr, upd_dst, offd_col, block_ptr;
-  std::vector<double> dp;
-  long long maxbuf = 0;
+  std::vector<Program> progs;
+  std::vector<std::string> keys;
+  std::vector<int> circ_group(ncirc, -1);
+  std::vector<long long> circ_poff(ncirc, 0);
+  std::vector<double> dparams;
   for (int64_t c = 0; c < ncirc; ++c) {
     const int64_t d0 = dev_off[c], nd = dev_off[c + 1] - d0;
+    circ_poff[c] = (long long)dparams.size();
+    circuit_constants(nd, type + d0, p + 6 * d0, dparams);
+    if (first[c] < 0) continue;
     gpuklu_circuit* C = gpuklu_compile_devices(node_counts[c], nd, type + d0, nodes + 4 * d0,
                                                p + 6 * d0, 0);
     if (!C) {
       gpuklu_destroy(H);
       return nullptr;
     }
-    const int64_t rep = first[c];
     // pivot discovery on the representative instance's first matrix
+    const int64_t rep = first[c];
     std::vector<double> pc(C->p);
-    if (rep >= 0 && inst_dev[rep] >= 0) pc[(size_t)inst_dev[rep] * 6] = inst_val[rep];
+    if (inst_dev && inst_dev[rep] >= 0) pc[(size_t)inst_dev[rep] * 6] = inst_val[rep];
     gpuklu_circuit_set_params(C, pc.data());
     std::vector<double> xr(C->node_count, 0.0);
-    if (rep >= 0 && x0 && x0_off[rep] >= 0)
+    if (x0 && x0_off && x0_off[rep] >= 0)
       std::copy(x0 + x0_off[rep], x0 + x0_off[rep] + C->node_count, xr.begin());
     std::vector<double> ax(C->ai.size()), rhs(C->n);
     gpuklu_prepare(H, C->n);
@@ -892,122 +1081,121 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
       gpuklu_destroy(H);
       return nullptr;
     }
-    const gk::Plan& P = H->plan;
-    std::vector<int> raw_offd(C->ai.size(), -1);
-    for (size_t e = 0; e < P.offd_raw.size(); ++e) raw_offd[P.offd_raw[e]] = (int)e;
-    gk::GroupHdr G{};
-    G.n = P.n;
-    G.node_count = C->node_count;
-    G.nslots = P.nslots();
-    G.noffd = (int)P.offd_raw.size();
-    G.ndev = (int)nd;
-    G.nblocks = P.nblocks;
-    G.dev_off = (int)dtype.size();
-    G.col_off = (int)col_ptr.size();
-    G.slot_off = (int)slot_row.size();
-    G.upd_off = (int)upd_dst.size();
-    G.offd_off = (int)offd_col.size();
-    G.blk_off = (int)block_ptr.size();
-    G.pin_slot = C->pin_raw >= 0 ? P.raw_slot[C->pin_raw] : -1;
-    G.offd_lower = P.offd_lower ? 1 : 0;
-    for (int64_t d = 0; d < nd; ++d) {
-      dtype.push_back(C->type[d]);
-      for (int q = 0; q < 4; ++q) dnodes.push_back(C->nodes[d * 4 + q]);
-      for (int q = 0; q < 6; ++q) dp.push_back(C->p[d * 6 + q]);
-      for (int q = 0; q < 8; ++q) {
-        int r = C->raw[d * 8 + q];
-        int s = -1;
-        if (r >= 0) s = P.raw_slot[r] >= 0 ? P.raw_slot[r] : (raw_offd[r] >= 0 ? G.nslots + raw_offd[r] : -1);
-        dslotv.push_back(s);
+    Program pr = make_program(*C, H->plan);
+    std::string k = pr.key();
+    int gid = -1;
+    for (size_t q = 0; q < keys.size(); ++q)
+      if (keys[q].size() == k.size() && keys[q] == k) {
+        gid = (int)q;
+        break;
       }
+    if (gid < 0) {
+      gid = (int)progs.size();
+      progs.push_back(std::move(pr));
+      keys.push_back(std::move(k));
     }
-    // column arrays: col_ptr (n+1) and the n-sized ones padded to n+1
-    for (int k = 0; k <= P.n; ++k) {
-      col_ptr.push_back(P.col_ptr[k]);
-      dslot.push_back(k < P.n ? P.dslot[k] : 0);
-      csing.push_back(k < P.n ? P.col_single[k] : 0);
-      in_row.push_back(0);
-      out_pos.push_back(k < P.n ? P.out_pos[k] : 0);
-      offd_ptr.push_back(P.offd_ptr[k]);
-    }
-    for (int r = 0; r < P.n; ++r) in_row[G.col_off + P.in_pos[r]] = r;
-    for (int s = 0; s <= P.nslots(); ++s) {
-      slot_row.push_back(s < P.nslots() ? P.slot_row[s] : 0);
-      upd_ptr.push_back(P.upd_ptr[s]);
-    }
-    upd_dst.insert(upd_dst.end(), P.upd_dst.begin(), P.upd_dst.end());
-    offd_col.insert(offd_col.end(), P.offd_col.begin(), P.offd_col.end());
-    block_ptr.insert(block_ptr.end(), P.block_ptr.begin(), P.block_ptr.end());
-    G.cost = G.nslots + (int)P.upd_dst.size() + 4 * G.ndev;
-    const long long need = 32LL * (G.nslots + G.noffd + 2LL * G.n + G.node_count);
-    maxbuf = std::max(maxbuf, need);
-    B->bytes_per_iter += 8LL * (2 * (G.nslots + G.noffd) + (long long)P.upd_dst.size() * 3 +
-                                4LL * G.n + 2LL * G.node_count) +
-                         4LL * ((long long)P.upd_dst.size() + G.nslots + 2LL * G.n);
-    const int gid = (int)B->groups.size();
-    B->groups.push_back(G);
-    auto& mem = members[c];
-    for (size_t t0 = 0; t0 < mem.size(); t0 += 32) {
-      // instances of a tile must be consecutive: build them from the member list
-      gk::Tile T{gid, (int)mem[t0], (int)std::min<size_t>(32, mem.size() - t0)};
-      bool contiguous = true;
-      for (int q = 1; q < T.count; ++q)
-        if (mem[t0 + q] != mem[t0] + q) contiguous = false;
-      if (!contiguous) {
-        fprintf(stderr, "gpuklu_batch_create: instances of a circuit must be consecutive\n");
-        gpuklu_circuit_free(C);
-        gpuklu_destroy(H);
-        return nullptr;
-      }
-      B->tiles.push_back(T);
-    }
+    circ_group[c] = gid;
     gpuklu_circuit_free(C);
   }
   gpuklu_destroy(H);
-  // longest programs first
-  std::stable_sort(B->tiles.begin(), B->tiles.end(), [&](const gk::Tile& a, const gk::Tile& b) {
-    return B->groups[a.group].cost > B->groups[b.group].cost;
+  const int ng = (int)progs.size();
+  std::vector<i32> dev_type, dev_nodes, dev_dv, amap_ptr, amap_code, rmap_ptr, rmap_code,
+      col_ptr, dslot, col_single, in_row, out_pos, offd_ptr, slot_row, upd_ptr, upd_dst,
+      offd_col, block_ptr;
+  auto cat = [](std::vector<i32>& dst, const std::vector<i32>& src) {
+    dst.insert(dst.end(), src.begin(), src.end());
+  };
+  int region = 0;
+  for (int g = 0; g < ng; ++g) {
+    Program& pr = progs[g];
+    gk::GroupHdr h = pr.h;
+    h.dev_off = (int)dev_type.size();
+    h.col_off = (int)col_ptr.size();
+    h.slot_off = (int)slot_row.size();
+    h.upd_off = (int)upd_dst.size();
+    h.offd_off = (int)offd_col.size();
+    h.blk_off = (int)block_ptr.size();
+    h.amap_off = (int)amap_ptr.size();
+    h.amap_code_off = (int)amap_code.size();
+    h.rmap_off = (int)rmap_ptr.size();
+    h.rmap_code_off = (int)rmap_code.size();
+    cat(dev_type, pr.dev_type);
+    cat(dev_nodes, pr.dev_nodes);
+    cat(dev_dv, pr.dev_dv);
+    cat(amap_ptr, pr.amap_ptr);
+    cat(amap_code, pr.amap_code);
+    cat(rmap_ptr, pr.rmap_ptr);
+    cat(rmap_code, pr.rmap_code);
+    cat(col_ptr, pr.col_ptr);
+    cat(dslot, pr.dslot);
+    cat(col_single, pr.col_single);
+    cat(in_row, pr.in_row);
+    cat(out_pos, pr.out_pos);
+    cat(offd_ptr, pr.offd_ptr);
+    cat(slot_row, pr.slot_row);
+    cat(upd_ptr, pr.upd_ptr);
+    cat(upd_dst, pr.upd_dst);
+    cat(offd_col, pr.offd_col);
+    cat(block_ptr, pr.block_ptr);
+    B->groups.push_back(h);
+    B->group_flops.push_back(pr.flops);
+    B->group_bytes.push_back(pr.bytes);
+    region = std::max(region, h.node_count + h.n + h.ndv + h.nslots + h.noffd);
+  }
+  // instances, most expensive program first
+  std::vector<i32> order(ninst);
+  B->inst_group_h.assign(ninst, 0);
+  for (int64_t i = 0; i < ninst; ++i) {
+    order[i] = (i32)i;
+    B->inst_group_h[i] = circ_group[inst_circ[i]];
+  }
+  std::stable_sort(order.begin(), order.end(), [&](i32 a, i32 b) {
+    return B->groups[B->inst_group_h[a]].cost > B->groups[B->inst_group_h[b]].cost;
   });
-  // outputs: n values per instance
   B->x_off.assign(ninst, 0);
   long long off = 0;
   for (int64_t i = 0; i < ninst; ++i) {
     B->x_off[i] = off;
-    off += B->groups[inst_circ[i]].n;
+    off += progs[circ_group[inst_circ[i]]].h.n;
   }
   B->xout_len = off;
   B->x0_len = x0 ? x0_len : 0;
-  // launch geometry: enough resident warps to cover the SMs several times
-  int occ = 0;
-  B->block = 128;
-  B->grid = sm_count() * 8;
-  (void)occ;
-  const long long nwarps = (long long)B->grid * (B->block / 32);
-  B->buf_stride = maxbuf;
+  B->region = (region + 1) & ~1;
+  gk::batch_kernel_info(B->warps_per_block, B->region, &B->regs, &B->blocks_per_sm);
+  if (B->blocks_per_sm <= 0) {
+    fprintf(stderr, "gpuklu_batch_create: a circuit needs %d KB of shared memory per warp\n",
+            (int)(B->region * 8 / 1024));
+    return nullptr;
+  }
+  B->grid = sm_count() * B->blocks_per_sm;
   cudaStream_t s = B->stream;
   cudaError_t e = cudaSuccess;
   std::vector<i32> ov_dev(ninst);
   std::vector<double> ov_val(ninst);
-  std::vector<long long> x0o(ninst, -1);
+  std::vector<long long> x0o(ninst, -1), poff(ninst);
   for (int64_t i = 0; i < ninst; ++i) {
-    ov_dev[i] = inst_dev[i] >= 0 ? (i32)inst_dev[i] : -1;
+    ov_dev[i] = inst_dev ? (i32)inst_dev[i] : -1;
     ov_val[i] = inst_val ? inst_val[i] : 0.0;
     if (x0 && x0_off) x0o[i] = x0_off[i];
+    poff[i] = circ_poff[inst_circ[i]];
   }
 #define UP(buf, vec) \
   if (e == cudaSuccess) e = B->buf.upload(vec, s);
-  UP(d_groups, B->groups) UP(d_tiles, B->tiles) UP(d_dev_type, dtype) UP(d_dev_nodes, dnodes)
-  UP(d_dev_slot, dslotv) UP(d_dev_p, dp) UP(d_col_ptr, col_ptr) UP(d_dslot, dslot)
-  UP(d_col_single, csing) UP(d_in_row, in_row) UP(d_out_pos, out_pos) UP(d_offd_ptr, offd_ptr)
-  UP(d_slot_row, slot_row) UP(d_upd_ptr, upd_ptr) UP(d_upd_dst, upd_dst)
-  UP(d_offd_col, offd_col) UP(d_block_ptr, block_ptr) UP(d_ov_dev, ov_dev)
-  UP(d_ov_val, ov_val) UP(d_x0_off, x0o) UP(d_x_off, B->x_off)
+  UP(d_groups, B->groups) UP(d_order, order) UP(d_inst_group, B->inst_group_h)
+  UP(d_dev_type, dev_type) UP(d_dev_nodes, dev_nodes) UP(d_dev_dv, dev_dv)
+  UP(d_amap_ptr, amap_ptr) UP(d_amap_code, amap_code) UP(d_rmap_ptr, rmap_ptr)
+  UP(d_rmap_code, rmap_code) UP(d_col_ptr, col_ptr) UP(d_dslot, dslot)
+  UP(d_col_single, col_single) UP(d_in_row, in_row) UP(d_out_pos, out_pos)
+  UP(d_offd_ptr, offd_ptr) UP(d_slot_row, slot_row) UP(d_upd_ptr, upd_ptr)
+  UP(d_upd_dst, upd_dst) UP(d_offd_col, offd_col) UP(d_block_ptr, block_ptr)
+  UP(d_dparams, dparams) UP(d_p_off, poff) UP(d_ov_dev, ov_dev) UP(d_ov_val, ov_val)
+  UP(d_x0_off, x0o) UP(d_x_off, B->x_off)
 #undef UP
   if (e == cudaSuccess) {
-    std::vector<double> x0v(x0 ? x0 : nullptr, x0 ? x0 + B->x0_len : nullptr);
+    std::vector<double> x0v;
+    if (x0) x0v.assign(x0, x0 + B->x0_len);
     e = B->d_x0.upload(x0v, s);
   }
-  if (e == cudaSuccess) e = B->d_buf.resize((size_t)(nwarps * B->buf_stride));
   if (e == cudaSuccess) e = B->d_xout.resize(std::max<int64_t>(B->xout_len, 1));
   if (e == cudaSuccess) e = B->d_iters.resize(std::max<int64_t>(ninst, 1));
   if (e == cudaSuccess) e = B->d_iters_total.resize(std::max<int64_t>(ninst, 1));
@@ -1020,6 +1208,43 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
     fprintf(stderr, "gpuklu_batch_create: %s\n", cudaGetErrorString(e));
     return nullptr;
   }
+  gk::BatchArgs& a = B->args;
+  a.groups = B->d_groups.p;
+  a.ninst = (int)ninst;
+  a.counter = B->d_counter.p;
+  a.order = B->d_order.p;
+  a.inst_group = B->d_inst_group.p;
+  a.dev_type = B->d_dev_type.p;
+  a.dev_nodes = B->d_dev_nodes.p;
+  a.dev_dv = B->d_dev_dv.p;
+  a.amap_ptr = B->d_amap_ptr.p;
+  a.amap_code = B->d_amap_code.p;
+  a.rmap_ptr = B->d_rmap_ptr.p;
+  a.rmap_code = B->d_rmap_code.p;
+  a.col_ptr = B->d_col_ptr.p;
+  a.dslot = B->d_dslot.p;
+  a.col_single = B->d_col_single.p;
+  a.in_row = B->d_in_row.p;
+  a.out_pos = B->d_out_pos.p;
+  a.offd_ptr = B->d_offd_ptr.p;
+  a.slot_row = B->d_slot_row.p;
+  a.upd_ptr = B->d_upd_ptr.p;
+  a.upd_dst = B->d_upd_dst.p;
+  a.offd_col = B->d_offd_col.p;
+  a.block_ptr = B->d_block_ptr.p;
+  a.inst_p_off = B->d_p_off.p;
+  a.dparams = B->d_dparams.p;
+  a.inst_ov_dev = B->d_ov_dev.p;
+  a.inst_ov_val = B->d_ov_val.p;
+  a.inst_x0_off = B->d_x0_off.p;
+  a.x0 = B->d_x0.p;
+  a.region = B->region;
+  a.iters = B->d_iters.p;
+  a.iters_total = B->d_iters_total.p;
+  a.reason = B->d_reason.p;
+  a.inst_x_off = B->d_x_off.p;
+  a.x_out = B->d_xout.p;
+  a.status = B->d_status.p;
   return B.release();
 }
 
@@ -1041,14 +1266,8 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
   c.gmin = cfg->gmin;
   c.damping = cfg->damping;
   c.damping_min = cfg->damping_min;
-  gk::launch_batch_newton(
-      b->d_groups.p, b->d_tiles.p, (int)b->tiles.size(), b->d_counter.p, b->d_dev_type.p,
-      b->d_dev_nodes.p, b->d_dev_p.p, b->d_dev_slot.p, b->d_col_ptr.p, b->d_dslot.p,
-      b->d_col_single.p, b->d_in_row.p, b->d_out_pos.p, b->d_offd_ptr.p, b->d_slot_row.p,
-      b->d_upd_ptr.p, b->d_upd_dst.p, b->d_offd_col.p, b->d_block_ptr.p, b->d_ov_dev.p,
-      b->d_ov_val.p, b->d_x0_off.p, b->d_x0.p, c, b->d_buf.p, b->buf_stride, b->d_iters.p,
-      b->d_iters_total.p, b->d_reason.p, b->d_x_off.p, b->d_xout.p, b->d_status.p, b->grid,
-      b->block, b->stream);
+  b->args.cfg = c;
+  gk::launch_batch_newton(b->args, b->grid, b->warps_per_block, b->stream);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return b->fail(cuda_msg(e, "batch launch"));
   return GPUKLU_OK;
@@ -1059,25 +1278,23 @@ int gpuklu_batch_results(gpuklu_batch* b, int64_t* iters, int64_t* iters_total, 
   if (!b) return GPUKLU_INVALID_MATRIX;
   const int64_t ni = b->ninst;
   std::vector<i32> it(ni), itt(ni), rs(ni);
-  std::vector<double> xo(b->xout_len);
+  std::vector<double> xo;
   cudaStream_t s = b->stream;
   cudaError_t e = cudaMemcpyAsync(it.data(), b->d_iters.p, ni * 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(itt.data(), b->d_iters_total.p, ni * 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(rs.data(), b->d_reason.p, ni * 4, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess && x_out && b->xout_len)
+  if (e == cudaSuccess && x_out && b->xout_len) {
+    xo.resize(b->xout_len);
     e = cudaMemcpyAsync(xo.data(), b->d_xout.p, b->xout_len * 8, cudaMemcpyDeviceToHost, s);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return b->fail(cuda_msg(e, "batch results"));
   for (int64_t i = 0; i < ni; ++i) {
     if (iters) iters[i] = it[i];
     if (iters_total) iters_total[i] = itt[i];
     if (reason) reason[i] = rs[i];
-    if (x_out && x_off) {
-      const int gn = b->groups[0].n;  // replaced below per instance
-      (void)gn;
-    }
   }
   if (x_out && x_off) {
     for (int64_t i = 0; i < ni; ++i) {
@@ -1107,10 +1324,20 @@ const char* gpuklu_batch_last_error(const gpuklu_batch* b) { return b ? b->err.c
 int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out) {
   if (!b) return GPUKLU_INVALID_MATRIX;
   out[0] = b->grid;
-  out[1] = b->block;
-  out[2] = (int64_t)b->tiles.size();
-  out[3] = (int64_t)b->d_buf.n * 8;
-  out[4] = b->bytes_per_iter;
+  out[1] = 32 * b->warps_per_block;
+  out[2] = (int64_t)b->groups.size();
+  out[3] = (int64_t)b->region * 8;
+  out[4] = b->regs;
+  out[5] = b->blocks_per_sm;
+  return GPUKLU_OK;
+}
+
+int gpuklu_batch_work(const gpuklu_batch* b, int64_t* flops, int64_t* bytes) {
+  if (!b) return GPUKLU_INVALID_MATRIX;
+  for (int64_t i = 0; i < b->ninst; ++i) {
+    flops[i] = b->group_flops[b->inst_group_h[i]];
+    bytes[i] = b->group_bytes[b->inst_group_h[i]];
+  }
   return GPUKLU_OK;
 }
 
@@ -1125,6 +1352,8 @@ struct gpuklu_plan {
 };
 
 extern "C" {
+
+double gpuklu_fp64_peak_tflops(void) { return gk::fp64_peak_tflops(); }
 
 gpuklu_plan* gpuklu_plan_build(int64_t n, const int64_t* ap, const int64_t* ai, int pivot_mode,
                                const int32_t* row_perm) {

@@ -562,6 +562,23 @@ __global__ void k_newton_update(int m, int n, double* x, const double* __restric
   }
 }
 
+// FP64 pipe throughput probe: every thread runs 8 independent chains of
+// fused multiply-adds (explicit fma, 2 flops each); the result is stored so
+// the work cannot be removed.
+__global__ void k_dfma_peak(double* out, int iters, double a, double b) {
+  double v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = threadIdx.x * 1e-7 + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = fma(v[k], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += v[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 __global__ void k_rcond(DPlan P, const double* __restrict__ lu, double* out) {
   __shared__ double smin[32], smax[32];
   const int tid = threadIdx.x;
@@ -591,189 +608,309 @@ __global__ void k_rcond(DPlan P, const double* __restrict__ lu, double* out) {
 }
 
 // --------------------------------------------------------------- batched
-// Per-lane state lives in the warp's buffer, value index v of lane l at
-// buf[v * 32 + l]: [0, nslots+noffd) matrix values, then rhs[n], t[n], x[nc].
-__global__ void __launch_bounds__(128)
-    k_batch_newton(const GroupHdr* __restrict__ groups, const Tile* __restrict__ tiles,
-                   int ntiles, unsigned* tile_counter, const int* __restrict__ dev_type,
-                   const int* __restrict__ dev_nodes, const double* __restrict__ dev_p,
-                   const int* __restrict__ dev_slot, const int* __restrict__ g_col_ptr,
-                   const int* __restrict__ g_dslot, const int* __restrict__ g_col_single,
-                   const int* __restrict__ g_in_row, const int* __restrict__ g_out_pos,
-                   const int* __restrict__ g_offd_ptr, const int* __restrict__ g_slot_row,
-                   const int* __restrict__ g_upd_ptr, const int* __restrict__ g_upd_dst,
-                   const int* __restrict__ g_offd_col, const int* __restrict__ g_block_ptr,
-                   const int* __restrict__ inst_ov_dev, const double* __restrict__ inst_ov_val,
-                   const long long* __restrict__ inst_x0_off, const double* __restrict__ x0,
-                   NewtonCfg cfg, double* buf_all, long long buf_stride, int* iters,
-                   int* iters_total, int* reason, const long long* __restrict__ inst_x_off,
-                   double* x_out, int* status) {
-  const int lane = threadIdx.x & 31;
-  const long long warp_global = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  double* buf = buf_all + warp_global * buf_stride;
-  while (true) {
-    int ti = 0;
-    if (lane == 0) ti = (int)atomicAdd(tile_counter, 1u);
-    ti = __shfl_sync(FULL, ti, 0);
-    if (ti >= ntiles) return;
-    const Tile tl = tiles[ti];
-    const GroupHdr G = groups[tl.group];
-    const bool live = lane < tl.count;
-    const int inst = tl.first + (live ? lane : 0);
-    const int nv = G.nslots + G.noffd;
-    double* V = buf + lane;                 // V[s * 32]
-    double* R = buf + (long long)nv * 32 + lane;
-    double* T = R + (long long)G.n * 32;
-    double* X = T + (long long)G.n * 32;
-    const int* col_ptr = g_col_ptr + G.col_off;
-    const int* dslot = g_dslot + G.col_off;
-    const int* csing = g_col_single + G.col_off;
-    const int* in_row = g_in_row + G.col_off;
-    const int* out_pos = g_out_pos + G.col_off;
-    const int* offd_ptr = g_offd_ptr + G.col_off;
-    const int* slot_row = g_slot_row + G.slot_off;
-    const int* upd_ptr = g_upd_ptr + G.slot_off;
-    const int* upd_dst = g_upd_dst + G.upd_off;
-    const int* offd_col = g_offd_col + G.offd_off;
-    const int* bptr = g_block_ptr + G.blk_off;
-    const int ov_dev = live ? inst_ov_dev[inst] : -1;
-    const double ov_val = live ? inst_ov_val[inst] : 0.0;
-    const int nc = G.node_count;
-    // initial iterate
-    if (live) {
-      const double* x0p = inst_x0_off[inst] >= 0 ? x0 + inst_x0_off[inst] : nullptr;
-      for (int i = 0; i < nc; ++i) X[i * 32] = x0p ? x0p[i] : 0.0;
+// One warp owns one circuit instance at a time and keeps all of its state in
+// shared memory: iterate x[nc], solve vector t[n], device value records
+// dv[ndv] and the LU values v[nslots+noffd]. Program arrays (the group's
+// symbolic plan) and circuit constants are read through the read-only path;
+// each iteration touches global memory only for them.
+//   stamp     - lanes evaluate devices (strided) into their value records
+//   assemble  - lanes sum each LU slot's and each rhs row's contributions in
+//               stamping order (bit-identical to the reference's scatter)
+//   factor    - left-looking, column by column; a column's U entries in
+//               order, each applying L(:,j) across lanes; the forward
+//               substitution of the right-hand side is fused in
+//   backward  - U sweep, lanes over a column's U entries
+//   update    - convergence test, damping and iterate update
+__device__ __forceinline__ double contrib(const double* dv, int code) {
+  const int kind = code & 7, idx = code >> 3;
+  switch (kind) {
+    case 0: return dv[idx];
+    case 1: return -dv[idx];
+    case 2: return 1.0;
+    case 3: return -1.0;
+    default: return 0.0;
+  }
+}
+
+// Device value record (see eval): R [g]; V [value]; I [value]; D [g, ieq];
+// M [gds, gm, ieq]; MC [ddd, dds, ddg, ieq]. Circuit constants per device:
+// R [1/R]; V, I [value]; D [Is, vt, Is/vt]; M [is_pmos, vth0, beff];
+// MC [polarity, |vth0|, beff].
+__device__ __forceinline__ void eval_record(int type, const int* nd, const double* dp,
+                                            const double* X, int nc, double gmin, double* rec) {
+  auto xg = [&](int i) { return (i >= 0 && i < nc) ? X[i] : 0.0; };
+  switch (type) {
+    case 0:
+    case 1:
+    case 2:
+      rec[0] = dp[0];
+      break;
+    case 3: {  // crates/sim-core/src/stamp.rs:351-387
+      const double gf = gmin > 0.0 ? gmin : 1e-12;
+      const double vd = xg(nd[0]) - xg(nd[1]);
+      const double e = exp(vd / dp[1]);
+      const double id = dp[0] * (e - 1.0);
+      const double gd = dp[2] * e;
+      rec[0] = fmax(gd, gf);
+      rec[1] = id - gd * vd;
+      break;
     }
-    int done = live ? 0 : 1, it = 0, total = 0, gstep = 0, rsn = 1;
+    case 4: {  // level 1 as the reference evaluates it (evaluate.rs:285-356)
+      const double lambda = 0.02, gdev = 1e-12;
+      const double gf = gmin > 0.0 ? gmin : 1e-12;
+      const bool pm = dp[0] != 0.0;
+      const double vd = xg(nd[0]), vg = xg(nd[1]), vs = xg(nd[2]);
+      double vdi = pm ? -vs : vd, vgi = pm ? -vg : vg, vsi = pm ? -vd : vs;
+      double vgs = vgi - vsi, vds = vdi - vsi;
+      if (vds < 0.0) {
+        vds = -vds;
+        vgs = vgi - vdi;
+      }
+      const double vth = pm ? -fabs(dp[1]) : fabs(dp[1]);
+      const double beff = dp[2];
+      double ids, gm, gds;
+      if (vgs <= vth) {
+        ids = 0.0;
+        gm = 0.0;
+        gds = gdev;
+      } else if (vds < vgs - vth) {
+        ids = beff * ((vgs - vth) * vds - 0.5 * vds * vds);
+        gm = beff * vds;
+        gds = fmax(beff * ((vgs - vth) - vds), gdev);
+      } else {
+        const double t = vgs - vth;
+        ids = 0.5 * beff * (t * t) * (1.0 + lambda * vds);
+        gm = beff * (vgs - vth) * (1.0 + lambda * vds);
+        gds = fmax(0.5 * beff * (t * t) * lambda, gdev);
+      }
+      const double ids_s = pm ? -ids : ids;
+      rec[0] = fmax(gds, gf);
+      rec[1] = gm;
+      rec[2] = ids_s - gm * (vg - vs) - gds * (vd - vs);
+      break;
+    }
+    case 6: {  // consistent level 1
+      const double lambda = 0.02, gdev = 1e-12;
+      const double pol = dp[0];
+      const double vd = xg(nd[0]), vg = xg(nd[1]), vs = xg(nd[2]);
+      const double vgs = pol * (vg - vs), vds = pol * (vd - vs);
+      const bool rev = vds < 0.0;
+      const double vgse = rev ? vgs - vds : vgs, vdse = rev ? -vds : vds;
+      const double vth = dp[1], beff = dp[2];
+      double ids, gm, gds;
+      if (vgse <= vth) {
+        ids = 0.0;
+        gm = 0.0;
+        gds = gdev;
+      } else if (vdse < vgse - vth) {
+        ids = beff * ((vgse - vth) * vdse - 0.5 * vdse * vdse);
+        gm = beff * vdse;
+        gds = fmax(beff * ((vgse - vth) - vdse), gdev);
+      } else {
+        const double t = vgse - vth;
+        ids = 0.5 * beff * (t * t) * (1.0 + lambda * vdse);
+        gm = beff * (vgse - vth) * (1.0 + lambda * vdse);
+        gds = fmax(0.5 * beff * (t * t) * lambda, gdev);
+      }
+      double id, ddg, ddd, dds;
+      if (!rev) {
+        id = pol * ids;
+        ddg = gm;
+        ddd = gds;
+        dds = -(gm + gds);
+      } else {
+        id = -pol * ids;
+        ddg = -gm;
+        ddd = gm + gds;
+        dds = -gds;
+      }
+      rec[0] = ddd;
+      rec[1] = dds;
+      rec[2] = ddg;
+      rec[3] = id - (ddg * vg + ddd * vd + dds * vs);
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+__global__ void k_batch_newton(BatchArgs A) {
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31;
+  double* const region = smem + (size_t)(threadIdx.x >> 5) * A.region;
+  const NewtonCfg cfg = A.cfg;
+  const double gstart = fmax(cfg.gmin * 1e3, 1e-6);
+  while (true) {
+    int q = 0;
+    if (lane == 0) q = (int)atomicAdd(A.counter, 1u);
+    q = __shfl_sync(FULL, q, 0);
+    if (q >= A.ninst) return;
+    const int inst = A.order[q];
+    const GroupHdr G = A.groups[A.inst_group[inst]];
+    const int n = G.n, nc = G.node_count, nv = G.nslots + G.noffd;
+    double* const X = region;
+    double* const T = X + nc;
+    double* const DV = T + n;
+    double* const V = DV + G.ndv;
+    const int* dev_type = A.dev_type + G.dev_off;
+    const int* dev_nodes = A.dev_nodes + 4 * G.dev_off;
+    const int* dev_dv = A.dev_dv + G.dev_off;
+    const int* amap_ptr = A.amap_ptr + G.amap_off;
+    const int* amap_code = A.amap_code + G.amap_code_off;
+    const int* rmap_ptr = A.rmap_ptr + G.rmap_off;
+    const int* rmap_code = A.rmap_code + G.rmap_code_off;
+    const int* col_ptr = A.col_ptr + G.col_off;
+    const int* dslot = A.dslot + G.col_off;
+    const int* csing = A.col_single + G.col_off;
+    const int* in_row = A.in_row + G.col_off;
+    const int* out_pos = A.out_pos + G.col_off;
+    const int* offd_ptr = A.offd_ptr + G.col_off;
+    const int* slot_row = A.slot_row + G.slot_off;
+    const int* upd_ptr = A.upd_ptr + G.slot_off;
+    const int* upd_dst = A.upd_dst + G.upd_off;
+    const int* offd_col = A.offd_col + G.offd_off;
+    const int* bptr = A.block_ptr + G.blk_off;
+    const double* dparams = A.dparams + A.inst_p_off[inst];
+    const int ov_dev = A.inst_ov_dev[inst];
+    const double ov_val = A.inst_ov_val[inst];
+    {
+      const long long xo = A.inst_x0_off[inst];
+      for (int i = lane; i < nc; i += 32) X[i] = xo >= 0 ? A.x0[xo + i] : 0.0;
+    }
+    int it = 0, total = 0, gstep = 0, rsn = -1;
     double damp = cfg.damping, prev = 1.7976931348623157e308;
-    const double gstart = fmax(cfg.gmin * 1e3, 1e-6);
     double gmin = cfg.gmin_steps == 0 ? cfg.gmin : gstart;
-    while (__any_sync(FULL, !done)) {
-      if (!done) {
-        // ---- stamp: device order, accumulating into slots as the reference's
-        // scatter sums duplicate CSC entries
-        for (int s = 0; s < nv; ++s) V[s * 32] = 0.0;
-        for (int i = 0; i < G.n; ++i) R[i * 32] = 0.0;
-        auto xg = [&](int i) { return (i >= 0 && i < nc) ? X[i * 32] : 0.0; };
-        for (int d = 0; d < G.ndev; ++d) {
-          const int dg = G.dev_off + d;
-          const int type = dev_type[dg];
-          const int* nd = dev_nodes + 4 * dg;
-          double pl[6];
+    __syncwarp();
+    while (rsn < 0) {
+      // ---- stamp
+      for (int d = lane; d < G.ndev; d += 32) {
+        double dp[4];
+        const double* src = dparams + 4 * d;
 #pragma unroll
-          for (int q = 0; q < 6; ++q) pl[q] = dev_p[6 * dg + q];
-          if (d == ov_dev) pl[0] = ov_val;
-          double m[8], r[2];
-          int nr;
-          const int nm = eval_device(type, nd, pl, xg, gmin, 1.0, 0.0, 0.0, -1.0, m, r, nr);
-          const int* sl = dev_slot + 8 * dg;
-          for (int e = 0; e < nm; ++e) {
-            const int s = sl[e];
-            if (s >= 0) V[s * 32] = V[s * 32] + m[e];
-          }
-          if (nr) {  // rows: V -> its aux row; M -> drain, source; others -> a, b
-            const int ra = type == 1 ? nd[2] : nd[0];
-            const int rb = (type == 4 || type == 6) ? nd[2] : nd[1];
-            if (ra < G.n) R[ra * 32] = R[ra * 32] + r[0];
-            if (nr > 1 && rb < G.n) R[rb * 32] = R[rb * 32] + r[1];
-          }
-        }
-        if (G.pin_slot >= 0) V[G.pin_slot * 32] = V[G.pin_slot * 32] + 1.0;
-        // ---- refactor with frozen pivots (left-looking, columns in order)
-        for (int k = 0; k < G.n; ++k) {
+        for (int k = 0; k < 4; ++k) dp[k] = __ldg(src + k);
+        if (d == ov_dev) dp[0] = ov_val;
+        double rec[4];
+        const int type = dev_type[d];
+        eval_record(type, dev_nodes + 4 * d, dp, X, nc, gmin, rec);
+        const int o = dev_dv[d];
+        const int nrec = type == 6 ? 4 : type == 4 ? 3 : type == 3 ? 2 : type == 5 ? 0 : 1;
+        for (int k = 0; k < nrec; ++k) DV[o + k] = rec[k];
+      }
+      __syncwarp();
+      // ---- assemble LU slots and the permuted right-hand side
+      for (int v = lane; v < nv; v += 32) {
+        double acc = 0.0;
+        for (int t = amap_ptr[v]; t < amap_ptr[v + 1]; ++t) acc += contrib(DV, amap_code[t]);
+        V[v] = acc;
+      }
+      for (int i = lane; i < n; i += 32) {
+        const int r = in_row[i];
+        double acc = 0.0;
+        for (int t = rmap_ptr[r]; t < rmap_ptr[r + 1]; ++t) acc += contrib(DV, rmap_code[t]);
+        T[i] = acc;
+      }
+      __syncwarp();
+      // ---- factor + forward substitution, then backward, block by block
+      for (int b = 0; b < G.nblocks; ++b) {
+        const int b0 = bptr[b], b1 = bptr[b + 1];
+        for (int i = b0 + lane; i < b1; i += 32)
+          for (int e = offd_ptr[i]; e < offd_ptr[i + 1]; ++e)
+            T[i] = T[i] - V[G.nslots + e] * T[offd_col[e]];
+        __syncwarp();
+        for (int k = b0; k < b1; ++k) {
           const int s0 = col_ptr[k], ds = dslot[k], s1 = col_ptr[k + 1];
           for (int s = s0; s < ds; ++s) {
-            const double u = V[s * 32];
+            const double u = V[s];
             if (u != 0.0) {
               const int j = slot_row[s];
               const int q0 = dslot[j] + 1, q1 = col_ptr[j + 1];
               const int* dst = upd_dst + upd_ptr[s] - q0;
-              for (int q = q0; q < q1; ++q) {
-                const int dd = dst[q];
-                V[dd * 32] = V[dd * 32] - V[q * 32] * u;
+              for (int qq = q0 + lane; qq < q1; qq += 32) {
+                const int dd = dst[qq];
+                V[dd] = V[dd] - V[qq] * u;
               }
             }
+            __syncwarp();
           }
-          const double diag = perturb(V[ds * 32], csing[k] != 0);
-          V[ds * 32] = diag;
-          for (int q = ds + 1; q < s1; ++q) V[q * 32] = V[q * 32] / diag;
+          const double diag = perturb(V[ds], csing[k] != 0);
+          const double zk = T[k];
+          for (int qq = ds + 1 + lane; qq < s1; qq += 32) {
+            const double l = V[qq] / diag;
+            V[qq] = l;
+            const int r = slot_row[qq];
+            T[r] = T[r] - l * zk;
+          }
+          if (lane == 0) V[ds] = diag;
+          __syncwarp();
         }
-        // ---- solve
-        for (int i = 0; i < G.n; ++i) T[i * 32] = R[in_row[i] * 32];
-        for (int bb = 0; bb < G.nblocks; ++bb) {
-          const int b = G.offd_lower ? bb : G.nblocks - 1 - bb;
-          const int b0 = bptr[b], b1 = bptr[b + 1];
-          for (int i = b0; i < b1; ++i)
-            for (int e = offd_ptr[i]; e < offd_ptr[i + 1]; ++e)
-              T[i * 32] = T[i * 32] - V[(G.nslots + e) * 32] * T[offd_col[e] * 32];
-          for (int k = b0; k < b1; ++k) {
-            const double zk = T[k * 32];
-            for (int q = dslot[k] + 1; q < col_ptr[k + 1]; ++q)
-              T[slot_row[q] * 32] = T[slot_row[q] * 32] - V[q * 32] * zk;
+        for (int k = b1 - 1; k >= b0; --k) {
+          const double xk = T[k] / V[dslot[k]];
+          for (int s = col_ptr[k] + lane; s < dslot[k]; s += 32) {
+            const int r = slot_row[s];
+            T[r] = T[r] - V[s] * xk;
           }
-          for (int k = b1 - 1; k >= b0; --k) {
-            const double xk = T[k * 32] / V[dslot[k] * 32];
-            T[k * 32] = xk;
-            for (int s = col_ptr[k]; s < dslot[k]; ++s)
-              T[slot_row[s] * 32] = T[slot_row[s] * 32] - V[s * 32] * xk;
-          }
-        }
-        // ---- Newton update (crates/sim-core/src/newton.rs:93-107)
-        ++it;
-        ++total;
-        double ss = 0.0;
-        bool conv = true, fin = true;
-        for (int c = 0; c < nc; ++c) {
-          const double a = T[out_pos[c] * 32];
-          const double dx = a - X[c * 32];
-          ss += dx * dx;
-          if (!(fabs(dx) <= cfg.abs_tol + cfg.rel_tol * fabs(a))) conv = false;
-          if (!isfinite(a)) fin = false;
-        }
-        if (conv) {
-          done = 1;
-          rsn = 0;
-          const long long xo = inst_x_off[inst];
-          if (xo >= 0)
-            for (int c = 0; c < G.n; ++c) x_out[xo + c] = T[out_pos[c] * 32];
-        } else {
-          const double dxn = sqrt(ss);
-          if (dxn > prev && damp > cfg.damping_min) damp = fmax(damp * 0.5, cfg.damping_min);
-          prev = dxn;
-          for (int c = 0; c < nc; ++c) {
-            const double a = T[out_pos[c] * 32];
-            X[c * 32] = X[c * 32] + damp * (a - X[c * 32]);
-          }
-          if (!fin) {
-            done = 1;
-            rsn = 1;
-          } else if (it >= cfg.max_iters) {
-            if (gstep < cfg.gmin_steps) {  // next gmin step, fresh damping state
-              ++gstep;
-              gmin = gstart + (cfg.gmin - gstart) * ((double)gstep / (double)cfg.gmin_steps);
-              it = 0;
-              damp = cfg.damping;
-              prev = 1.7976931348623157e308;
-            } else {
-              done = 1;
-              rsn = 1;
-            }
-          }
-        }
-        if (done && live) {
-          iters[inst] = it;
-          iters_total[inst] = total;
-          reason[inst] = rsn;
-          if (rsn != 0) {
-            const long long xo = inst_x_off[inst];
-            if (xo >= 0)
-              for (int c = 0; c < G.n; ++c) x_out[xo + c] = c < nc ? X[c * 32] : 0.0;
-          }
+          __syncwarp();
+          if (lane == 0) T[k] = xk;
+          __syncwarp();
         }
       }
+      // ---- Newton update (crates/sim-core/src/newton.rs:93-107)
+      ++it;
+      ++total;
+      bool conv = true, fin = true;
+      for (int c = lane; c < nc; c += 32) {
+        const double a = T[out_pos[c]];
+        const double dx = a - X[c];
+        DV[c] = dx * dx;
+        if (!(fabs(dx) <= cfg.abs_tol + cfg.rel_tol * fabs(a))) conv = false;
+        if (!isfinite(a)) fin = false;
+      }
+      conv = __all_sync(FULL, conv);
+      fin = __all_sync(FULL, fin);
+      __syncwarp();
+      if (conv) {
+        rsn = 0;
+        const long long xo = A.inst_x_off[inst];
+        if (xo >= 0)
+          for (int c = lane; c < n; c += 32) A.x_out[xo + c] = T[out_pos[c]];
+      } else {
+        double ss = 0.0;  // norm2 as the reference sums it: in order
+        if (lane == 0)
+          for (int c = 0; c < nc; ++c) ss += DV[c];
+        ss = __shfl_sync(FULL, ss, 0);
+        const double dxn = sqrt(ss);
+        if (dxn > prev && damp > cfg.damping_min) damp = fmax(damp * 0.5, cfg.damping_min);
+        prev = dxn;
+        for (int c = lane; c < nc; c += 32) X[c] = X[c] + damp * (T[out_pos[c]] - X[c]);
+        if (!fin) {
+          rsn = 1;
+        } else if (it >= cfg.max_iters) {
+          if (gstep < cfg.gmin_steps) {  // next gmin step, fresh damping state
+            ++gstep;
+            gmin = gstart + (cfg.gmin - gstart) * ((double)gstep / (double)cfg.gmin_steps);
+            it = 0;
+            damp = cfg.damping;
+            prev = 1.7976931348623157e308;
+          } else {
+            rsn = 1;
+          }
+        }
+        __syncwarp();
+        if (rsn == 1) {
+          const long long xo = A.inst_x_off[inst];
+          if (xo >= 0)
+            for (int c = lane; c < n; c += 32) A.x_out[xo + c] = c < nc ? X[c] : 0.0;
+        }
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      A.iters[inst] = it;
+      A.iters_total[inst] = total;
+      A.reason[inst] = rsn;
     }
   }
-  (void)status;
 }
 
 }  // namespace
@@ -821,24 +958,48 @@ void launch_rcond(const DPlan& P, const double* lu, double* out2, cudaStream_t s
   k_rcond<<<1, 1024, 0, s>>>(P, lu, out2);
 }
 
-void launch_batch_newton(const GroupHdr* groups, const Tile* tiles, int ntiles,
-                         unsigned* tile_counter, const int* dev_type, const int* dev_nodes,
-                         const double* dev_p, const int* dev_slot, const int* col_ptr,
-                         const int* dslot, const int* col_single, const int* in_row,
-                         const int* out_col, const int* offd_ptr, const int* slot_row,
-                         const int* upd_ptr, const int* upd_dst, const int* offd_col,
-                         const int* block_ptr, const int* inst_ov_dev,
-                         const double* inst_ov_val, const long long* inst_x0_off,
-                         const double* x0, NewtonCfg cfg, double* buf, long long buf_stride,
-                         int* iters, int* iters_total, int* reason,
-                         const long long* inst_x_off, double* x_out, int* status, int grid,
-                         int block, cudaStream_t s) {
-  cudaMemsetAsync(tile_counter, 0, sizeof(unsigned), s);
-  k_batch_newton<<<grid, block, 0, s>>>(
-      groups, tiles, ntiles, tile_counter, dev_type, dev_nodes, dev_p, dev_slot, col_ptr, dslot,
-      col_single, in_row, out_col, offd_ptr, slot_row, upd_ptr, upd_dst, offd_col, block_ptr,
-      inst_ov_dev, inst_ov_val, inst_x0_off, x0, cfg, buf, buf_stride, iters, iters_total,
-      reason, inst_x_off, x_out, status);
+double fp64_peak_tflops() {
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = sms * 8, block = 256, iters = 4096;
+  double* out = nullptr;
+  if (cudaMalloc(&out, (size_t)grid * block * sizeof(double)) != cudaSuccess) return 0.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_dfma_peak<<<grid, block>>>(out, 64, 0.999999, 1e-9);  // warm-up
+  float best = 1e30f;
+  for (int r = 0; r < 5; ++r) {
+    cudaEventRecord(e0);
+    k_dfma_peak<<<grid, block>>>(out, iters, 0.999999, 1e-9);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = ms < best ? ms : best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  const double flops = 2.0 * 8.0 * iters * (double)grid * block;
+  return flops / (best * 1e-3) / 1e12;
+}
+
+void launch_batch_newton(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s) {
+  cudaMemsetAsync(a.counter, 0, sizeof(unsigned), s);
+  const size_t sm = (size_t)a.region * warps_per_block * sizeof(double);
+  k_batch_newton<<<grid, 32 * warps_per_block, sm, s>>>(a);
+}
+
+void batch_kernel_info(int warps_per_block, int region, int* regs, int* blocks_per_sm) {
+  cudaFuncAttributes fa{};
+  cudaFuncGetAttributes(&fa, k_batch_newton);
+  *regs = fa.numRegs;
+  const size_t sm = (size_t)region * warps_per_block * sizeof(double);
+  cudaFuncSetAttribute(k_batch_newton, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch_newton,
+                                                32 * warps_per_block, sm);
 }
 
 }  // namespace gk

@@ -39,22 +39,51 @@ struct NewtonState {
   int converged, iter;
 };
 
-// Batched program of one circuit group (all instances share it).
+// Batched program of one group: circuits whose device lists, analysis and
+// pivots are identical share it; only parameters and inputs differ.
 struct GroupHdr {
-  int n, node_count, nslots, noffd, ndev, nblocks;
-  int dev_off;    // device arrays (type, nodes*4, p*6, slot*8)
-  int col_off;    // n+1 column arrays (col_ptr, dslot, col_single, in_row, out_col, offd_ptr)
-  int slot_off;   // nslots(+1) slot arrays (slot_row, upd_ptr)
-  int upd_off;    // upd_dst
-  int offd_off;   // offd_col
-  int blk_off;    // block_ptr
-  int pin_slot;   // value slot of the ground pin
-  int offd_lower; // 1: blocks in forward order
-  int cost;       // scheduling weight
+  int n, node_count, nslots, noffd, ndev, nblocks, ndv;
+  int dev_off;     // program device arrays (type, nodes*4, dv)
+  int col_off;     // n+1 column arrays (col_ptr, dslot, col_single, in_row, out_pos, offd_ptr)
+  int slot_off;    // nslots+1 slot arrays (slot_row, upd_ptr)
+  int upd_off;     // upd_dst
+  int offd_off;    // offd_col
+  int blk_off;     // block_ptr
+  int amap_off;    // nslots+noffd+1 contribution pointers (values relative to amap_code base)
+  int amap_code_off;
+  int rmap_off;    // n+1 row contribution pointers
+  int rmap_code_off;
+  int cost;        // scheduling weight (FP64 operations of one Newton iteration)
 };
 
-struct Tile {
-  int group, first, count;
+// Contribution codes of the batched stamp: (index << 3) | kind with kind
+// 0 +dv[index], 1 -dv[index], 2 +1.0, 3 -1.0, 4 +0.0. A value slot (or a
+// right-hand-side row) is the sum, from 0.0 and in stamping order, of its
+// contributions, which is how the reference's scatter adds duplicate CSC
+// entries (crates/sim-core/src/native_klu.rs:1265-1274).
+struct BatchArgs {
+  const GroupHdr* groups;
+  int ninst;
+  unsigned* counter;       // next instance to hand out
+  const int* order;        // instances, most expensive first
+  const int* inst_group;
+  const int *dev_type, *dev_nodes, *dev_dv;  // dv: offset of the device's value record
+  const int *amap_ptr, *amap_code;           // per value slot (group-local ptr)
+  const int *rmap_ptr, *rmap_code;           // per original row
+  const int *col_ptr, *dslot, *col_single, *in_row, *out_pos, *offd_ptr, *slot_row,
+      *upd_ptr, *upd_dst, *offd_col, *block_ptr;
+  const long long* inst_p_off;  // offset of the instance's circuit constants (4 per device)
+  const double* dparams;
+  const int* inst_ov_dev;
+  const double* inst_ov_val;
+  const long long* inst_x0_off;
+  const double* x0;
+  NewtonCfg cfg;
+  int region;  // shared-memory doubles per warp
+  int *iters, *iters_total, *reason;
+  const long long* inst_x_off;
+  double* x_out;
+  int* status;
 };
 
 // --------------------------------------------------------------- launches
@@ -73,17 +102,11 @@ void launch_stamp(const DCircuit& C, const double* x, int xlen, double gmin, dou
 void launch_newton_update(int m, int n, double* x, const double* xnew, NewtonState* st,
                           NewtonCfg cfg, int* status, cudaStream_t s);
 void launch_rcond(const DPlan& P, const double* lu, double* out2, cudaStream_t s);
-void launch_batch_newton(const GroupHdr* groups, const Tile* tiles, int ntiles,
-                         unsigned* tile_counter, const int* dev_type, const int* dev_nodes,
-                         const double* dev_p, const int* dev_slot, const int* col_ptr,
-                         const int* dslot, const int* col_single, const int* in_row,
-                         const int* out_col, const int* offd_ptr, const int* slot_row,
-                         const int* upd_ptr, const int* upd_dst, const int* offd_col,
-                         const int* block_ptr, const int* inst_ov_dev,
-                         const double* inst_ov_val, const long long* inst_x0_off,
-                         const double* x0, NewtonCfg cfg, double* buf, long long buf_stride,
-                         int* iters, int* iters_total, int* reason,
-                         const long long* inst_x_off, double* x_out, int* status, int grid,
-                         int block, cudaStream_t s);
+// Measured FP64 fused multiply-add throughput of the current device [TFLOP/s].
+double fp64_peak_tflops();
+void launch_batch_newton(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
+// Registers per thread and resident blocks per SM of the batched kernel for
+// a block of warps_per_block warps with `region` shared doubles per warp.
+void batch_kernel_info(int warps_per_block, int region, int* regs, int* blocks_per_sm);
 
 }  // namespace gk

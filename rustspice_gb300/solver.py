@@ -258,10 +258,17 @@ class Batch:
         return it, itt, rs, x
 
     def info(self) -> dict:
-        out = np.zeros(5, np.int64)
+        out = np.zeros(6, np.int64)
         N.lib().gpuklu_batch_info(self._h, N.ptr(out))
-        return dict(grid=int(out[0]), block=int(out[1]), tiles=int(out[2]),
-                    buffer_bytes=int(out[3]), bytes_per_iter_all_circuits=int(out[4]))
+        return dict(grid=int(out[0]), block=int(out[1]), groups=int(out[2]),
+                    smem_per_warp=int(out[3]), regs=int(out[4]), blocks_per_sm=int(out[5]))
+
+    def work(self):
+        """Per instance: FP64 operations and on-chip value bytes of one iteration."""
+        f = np.zeros(self.ninst, np.int64)
+        b = np.zeros(self.ninst, np.int64)
+        N.lib().gpuklu_batch_work(self._h, N.ptr(f), N.ptr(b))
+        return f, b
 
     def stream(self) -> int:
         return N.lib().gpuklu_batch_stream(self._h) or 0
