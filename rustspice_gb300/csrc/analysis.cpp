@@ -487,23 +487,21 @@ void finalize_plan(Plan& p, const i64* ap, const i64* ai, const std::vector<Patt
   // off-diagonal block entries in (block row, block column, local column,
   // CSC) order; the reference keeps only those above the diagonal blocks,
   // the exact mode keeps those below (where BTF puts them).
-  for (int br = 0; br < p.nblocks; ++br) {
-    for (int bc = 0; bc < p.nblocks; ++bc) {
-      if (bc == br) continue;
+  // Columns in BTF position order and their entries in CSC order give every
+  // row its entries ordered by (block column, local column, CSC), the order
+  // the reference's block-pair loops visit them (native_klu.rs:800-857).
+  for (int Cc = 0; Cc < n; ++Cc) {
+    const int bc = p.pos_block[Cc];
+    const int oc = btf_col_perm[Cc];
+    for (i64 t = ap[oc]; t < ap[oc + 1]; ++t) {
+      int r = (int)ai[t];
+      if (r >= n) continue;
+      int R = p.btf_row_inv[r];
+      const int br = p.pos_block[R];
+      if (br == bc) continue;
       if (p.offd_lower ? bc > br : bc < br) continue;
-      int c0 = p.block_ptr[bc], c1 = p.block_ptr[bc + 1];
-      int r0 = p.block_ptr[br], r1 = p.block_ptr[br + 1];
-      for (int Cc = c0; Cc < c1; ++Cc) {
-        int oc = btf_col_perm[Cc];
-        for (i64 t = ap[oc]; t < ap[oc + 1]; ++t) {
-          int r = (int)ai[t];
-          if (r >= n) continue;
-          int R = p.btf_row_inv[r];
-          if (R < r0 || R >= r1) continue;
-          offd_rows[in_map(R)].push_back({out_map(Cc), (int)t});
-          ++p.noffdiag;
-        }
-      }
+      offd_rows[in_map(R)].push_back({out_map(Cc), (int)t});
+      ++p.noffdiag;
     }
   }
   p.offd_ptr.assign(n + 1, 0);
