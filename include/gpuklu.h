@@ -107,6 +107,25 @@ int gpuklu_tsolve(gpuklu_handle* h, double* g, int64_t len);
  * their own work around the solver. */
 void* gpuklu_stream(gpuklu_handle* h);
 
+/* Largest n gpuklu_solve_device_noalloc accepts. */
+#define GPUKLU_NOALLOC_MAX_N 65536
+
+/* Solve without allocating: for callers that cannot call cudaMalloc where
+ * they solve (a stream being captured into a CUDA graph, a host callback, a
+ * real-time loop with a fixed memory budget, a runtime that only lends
+ * buffers). No counterpart in the reference; it is an addition of this
+ * library. Solves A x = b with the handle's current factors: d_rhs (n
+ * values, device memory) is read, d_x (n values, device memory) receives x.
+ * The solve kernel's scratch (about 1.5 MB, held by every GPU that loads the
+ * library until the process exits) is a fixed array inside the library, not
+ * the handle's buffers, so the call allocates nothing. The first call on a
+ * device looks up that array's device address; make that first call before
+ * any stream capture. All calls share the one array: calls that overlap on
+ * the GPU (two handles on different streams at once) race, so serialise
+ * them. n above GPUKLU_NOALLOC_MAX_N gives GPUKLU_INVALID_MATRIX. Returns
+ * after the solve has finished (it waits on the handle's stream). */
+int gpuklu_solve_device_noalloc(gpuklu_handle* h, const double* d_rhs, double* d_x);
+
 /* ------------------------------------------------ device stamping + Newton */
 
 /* Device types and parameter slots (p[6] per device):

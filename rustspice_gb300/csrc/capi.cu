@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1344,6 +1345,72 @@ int gpuklu_batch_work(const gpuklu_batch* b, int64_t* flops, int64_t* bytes) {
 void* gpuklu_batch_stream(gpuklu_batch* b) { return b ? (void*)b->stream : nullptr; }
 
 }  // extern "C"
+
+// ====================================================================== no-allocation solve
+// Some callers cannot call cudaMalloc at the point where they solve: code
+// running while a stream is being captured into a CUDA graph, a simulator
+// step inside a host callback or a real-time loop with a fixed memory budget,
+// or a foreign runtime that owns all device memory and only lends buffers.
+// gpuklu_solve_device_noalloc serves them: the caller passes device buffers
+// for the right-hand side and the solution, and the solve kernel's scratch
+// (the forward and backward vectors, the per-row completion flags and the
+// task counter) lives in the file-scope array below instead of the handle's
+// buffers. Every GPU that loads the library holds this array until the
+// process exits.
+namespace {
+constexpr size_t kNoallocFlagBytes = 256 + 2 * (size_t)GPUKLU_NOALLOC_MAX_N * sizeof(unsigned);
+constexpr size_t kNoallocBytes = kNoallocFlagBytes + 2 * (size_t)GPUKLU_NOALLOC_MAX_N * sizeof(double);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+// Device address of g_noalloc_scratch per device, looked up once with that
+// device current. In host code the array's name is only a host-side handle.
+unsigned char* g_noalloc_addr[64] = {nullptr};
+std::mutex g_noalloc_mu;
+
+cudaError_t noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return cudaSuccess;
+}
+}  // namespace
+
+extern "C" int gpuklu_solve_device_noalloc(gpuklu_handle* h, const double* d_rhs, double* d_x) {
+  if (!h || h->state != gpuklu_handle::FACTORED) return GPUKLU_SOLVE_FAILED;
+  if (h->n > GPUKLU_NOALLOC_MAX_N)
+    return h->fail(GPUKLU_INVALID_MATRIX,
+                   "gpuklu_solve_device_noalloc: n = " + std::to_string(h->n) +
+                       " exceeds GPUKLU_NOALLOC_MAX_N = " +
+                       std::to_string(GPUKLU_NOALLOC_MAX_N));
+  unsigned char* base = nullptr;
+  cudaError_t e = noalloc_scratch(&base);
+  if (e != cudaSuccess) return h->cuda_fail(e, "noalloc scratch address");
+  const size_t n = (size_t)h->n;
+  unsigned* counter = reinterpret_cast<unsigned*>(base);
+  unsigned* zflag = reinterpret_cast<unsigned*>(base + 256);
+  unsigned* xflag = zflag + GPUKLU_NOALLOC_MAX_N;
+  double* z = reinterpret_cast<double*>(base + kNoallocFlagBytes);
+  double* x = z + GPUKLU_NOALLOC_MAX_N;
+  // the array keeps the previous call's flags: clear this call's rows
+  e = cudaMemsetAsync(zflag, 0, n * sizeof(unsigned), h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(xflag, 0, n * sizeof(unsigned), h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "noalloc flags");
+  const int grid = std::max(1, std::min<int>((int)((2 * n + 3) / 4), sm_count() * 16));
+  gk::launch_solve(h->pd.dp, d_rhs, h->d_ax.p, h->d_lu.p, z, x, d_x, zflag, xflag, 1u, counter,
+                   h->d_status.p, grid, false, h->stream);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return h->cuda_fail(e, "noalloc solve launch");
+  return h->check_status("solve_device_noalloc");
+}
 
 // ====================================================================== diagnostics
 struct gpuklu_plan {
