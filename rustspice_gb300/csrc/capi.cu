@@ -811,20 +811,43 @@ struct gpuklu_batch {
   std::string err;
   std::vector<gk::GroupHdr> groups;
   DBuf<gk::GroupHdr> d_groups;
-  DBuf<unsigned> d_counter;
-  DBuf<i32> d_order, d_inst_group, d_dev_type, d_dev_nodes, d_dev_dv, d_amap_ptr, d_amap_code,
+  DBuf<i32> d_order, d_dev_type, d_dev_nodes, d_dev_dv, d_amap_ptr, d_amap_code,
       d_rmap_ptr, d_rmap_code, d_col_ptr, d_dslot, d_col_single, d_in_row, d_out_pos,
-      d_offd_ptr, d_slot_row, d_upd_ptr, d_upd_dst, d_offd_col, d_block_ptr, d_ov_dev, d_iters,
+      d_offd_ptr, d_slot_row, d_upd_ptr, d_upd_dst, d_offd_col, d_block_ptr, d_heavy, d_ov_dev,
+      d_iters,
       d_iters_total, d_reason, d_status;
   DBuf<double> d_dparams, d_ov_val, d_x0, d_xout;
   DBuf<long long> d_p_off, d_x0_off, d_x_off;
   std::vector<long long> x_off;
   int64_t x0_len = 0, xout_len = 0;
-  int grid = 0, warps_per_block = 2, regs = 0, blocks_per_sm = 0, region = 0;
   int64_t flops_per_iter = 0, bytes_per_iter = 0;
   std::vector<int64_t> group_flops, group_bytes;
   std::vector<i32> inst_group_h;
+  DBuf<unsigned> d_gnext;
+  // Launch classes: groups of similar per-instance shared memory run in one
+  // launch with m instances per warp; classes run concurrently on their own
+  // streams.
+  struct Class {
+    int m = 1, region = 0, prog_ints = 0, grid = 0, warps_per_block = 1, regs = 0,
+        blocks_per_sm = 0;
+    std::vector<i32> tiles;
+    DBuf<i32> d_tiles;
+    DBuf<unsigned> d_counter;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    gk::BatchArgs args{};
+  };
+  std::vector<std::unique_ptr<Class>> classes;
+  cudaEvent_t start_ev = nullptr;
   gk::BatchArgs args{};
+
+  ~gpuklu_batch() {
+    for (auto& c : classes) {
+      if (c->stream) cudaStreamDestroy(c->stream);
+      if (c->done) cudaEventDestroy(c->done);
+    }
+    if (start_ev) cudaEventDestroy(start_ev);
+  }
 
   int fail(const std::string& m) {
     err = m;
@@ -839,7 +862,7 @@ struct Program {
   gk::GroupHdr h{};
   std::vector<i32> dev_type, dev_nodes, dev_dv, amap_ptr, amap_code, rmap_ptr, rmap_code,
       col_ptr, dslot, col_single, in_row, out_pos, offd_ptr, slot_row, upd_ptr, upd_dst,
-      offd_col, block_ptr;
+      offd_col, block_ptr, heavy;
   int64_t flops = 0, bytes = 0;
   std::string key() const {
     std::string k;
@@ -852,7 +875,7 @@ struct Program {
     k.append((const char*)hdr, sizeof(hdr));
     for (auto* v : {&dev_type, &dev_nodes, &dev_dv, &amap_ptr, &amap_code, &rmap_ptr,
                     &rmap_code, &col_ptr, &dslot, &col_single, &in_row, &out_pos, &offd_ptr,
-                    &slot_row, &upd_ptr, &upd_dst, &offd_col, &block_ptr})
+                    &slot_row, &upd_ptr, &upd_dst, &offd_col, &block_ptr, &heavy})
       app(*v);
     return k;
   }
@@ -896,7 +919,7 @@ void device_codes(int type, int dv, int m[8], int r[2]) {
       break;
     case 6:
       m[0] = c(0, 0); m[1] = c(1, 1); m[2] = c(1, 0); m[3] = c(0, 1);
-      m[4] = c(2, 0); m[5] = 4; m[6] = c(2, 1); m[7] = 4;
+      m[4] = c(2, 0); m[5] = -1; m[6] = c(2, 1); m[7] = -1;  // the +0.0 inserts add nothing
       r[0] = c(3, 1); r[1] = c(3, 0);
       break;
     default:
@@ -969,6 +992,14 @@ Program make_program(const gpuklu_circuit& C, const gk::Plan& P) {
     g.slot_row.push_back(s < P.nslots() ? P.slot_row[s] : 0);
     g.upd_ptr.push_back(P.upd_ptr[s]);
   }
+  // long contribution lists (must match the kernel's threshold of 12)
+  for (int v = 0; v < nv; ++v)
+    if (g.amap_ptr[v + 1] - g.amap_ptr[v] > 12) g.heavy.push_back(v << 1);
+  for (int i = 0; i < P.n; ++i) {
+    const int r = g.in_row[i];
+    if (g.rmap_ptr[r + 1] - g.rmap_ptr[r] > 12) g.heavy.push_back((i << 1) | 1);
+  }
+  h.nheavy = (int)g.heavy.size();
   g.upd_dst = P.upd_dst;
   g.offd_col = P.offd_col;
   g.block_ptr.assign(P.block_ptr.begin(), P.block_ptr.end());
@@ -1102,7 +1133,7 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
   const int ng = (int)progs.size();
   std::vector<i32> dev_type, dev_nodes, dev_dv, amap_ptr, amap_code, rmap_ptr, rmap_code,
       col_ptr, dslot, col_single, in_row, out_pos, offd_ptr, slot_row, upd_ptr, upd_dst,
-      offd_col, block_ptr;
+      offd_col, block_ptr, heavy;
   auto cat = [](std::vector<i32>& dst, const std::vector<i32>& src) {
     dst.insert(dst.end(), src.begin(), src.end());
   };
@@ -1118,6 +1149,8 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
     h.blk_off = (int)block_ptr.size();
     h.amap_off = (int)amap_ptr.size();
     h.amap_code_off = (int)amap_code.size();
+    h.nupd = (int)pr.upd_dst.size();
+    h.heavy_off = (int)heavy.size();
     h.rmap_off = (int)rmap_ptr.size();
     h.rmap_code_off = (int)rmap_code.size();
     cat(dev_type, pr.dev_type);
@@ -1138,21 +1171,31 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
     cat(upd_dst, pr.upd_dst);
     cat(offd_col, pr.offd_col);
     cat(block_ptr, pr.block_ptr);
+    cat(heavy, pr.heavy);
     B->groups.push_back(h);
     B->group_flops.push_back(pr.flops);
     B->group_bytes.push_back(pr.bytes);
     region = std::max(region, h.node_count + h.n + h.ndv + h.nslots + h.noffd);
   }
-  // instances, most expensive program first
-  std::vector<i32> order(ninst);
+  // instances grouped by program; each group's range in the order array
+  const int ngr = (int)B->groups.size();
+  std::vector<std::vector<i32>> members(ngr);
   B->inst_group_h.assign(ninst, 0);
   for (int64_t i = 0; i < ninst; ++i) {
-    order[i] = (i32)i;
     B->inst_group_h[i] = circ_group[inst_circ[i]];
+    members[B->inst_group_h[i]].push_back((i32)i);
   }
-  std::stable_sort(order.begin(), order.end(), [&](i32 a, i32 b) {
-    return B->groups[B->inst_group_h[a]].cost > B->groups[B->inst_group_h[b]].cost;
-  });
+  std::vector<i32> order;
+  order.reserve(ninst);
+  std::vector<int> gregion(ngr);
+  for (int g = 0; g < ngr; ++g) {
+    B->groups[g].inst_begin = (int)order.size();
+    B->groups[g].inst_count = (int)members[g].size();
+    order.insert(order.end(), members[g].begin(), members[g].end());
+    const gk::GroupHdr& h = B->groups[g];
+    gregion[g] = (h.node_count + h.n + h.ndv + h.nslots + h.noffd + 1) & ~1;
+  }
+  (void)region;
   B->x_off.assign(ninst, 0);
   long long off = 0;
   for (int64_t i = 0; i < ninst; ++i) {
@@ -1161,14 +1204,46 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
   }
   B->xout_len = off;
   B->x0_len = x0 ? x0_len : 0;
-  B->region = (region + 1) & ~1;
-  gk::batch_kernel_info(B->warps_per_block, B->region, &B->regs, &B->blocks_per_sm);
-  if (B->blocks_per_sm <= 0) {
-    fprintf(stderr, "gpuklu_batch_create: a circuit needs %d KB of shared memory per warp\n",
-            (int)(B->region * 8 / 1024));
-    return nullptr;
+  // launch classes by per-instance shared memory: small programs put four
+  // instances in a warp, medium two, large one
+  std::vector<int> gorder(ngr);
+  for (int g = 0; g < ngr; ++g) gorder[g] = g;
+  std::stable_sort(gorder.begin(), gorder.end(),
+                   [&](int x, int y) { return B->groups[x].cost > B->groups[y].cost; });
+  // instances per warp by per-instance shared memory: small programs put
+  // four instances in a warp, medium two, large one (more resident warps
+  // hide more FP64 latency than wider packing saves)
+  auto pick_m = [](int region, int prog) {
+    (void)prog;
+    return region <= 1152 ? 4 : (region <= 2304 ? 2 : 1);
+  };
+  const int mclass[4] = {1, 2, 4, 8};
+  for (int ci = 0; ci < 4; ++ci) {
+    auto C = std::make_unique<gpuklu_batch::Class>();
+    C->m = mclass[ci];
+    for (int g : gorder) {
+      const gk::GroupHdr& h = B->groups[g];
+      const int prog = (4 * h.n + 2 * h.nslots + h.nupd + 3) & ~3;
+      if (pick_m(gregion[g], prog) != C->m || h.inst_count == 0) continue;
+      C->region = std::max(C->region, gregion[g]);
+      C->prog_ints = std::max(C->prog_ints, prog);
+      for (int t = 0; t < (h.inst_count + C->m - 1) / C->m; ++t) C->tiles.push_back(g);
+    }
+    if (C->tiles.empty()) continue;
+    gk::batch_kernel_info(C->m, C->warps_per_block, C->region, C->prog_ints, &C->regs,
+                          &C->blocks_per_sm);
+    if (C->blocks_per_sm <= 0) {
+      fprintf(stderr, "gpuklu_batch_create: a circuit needs %d KB of shared memory\n",
+              (int)(C->region * 8 * C->m / 1024));
+      return nullptr;
+    }
+    C->grid = std::min<int>(sm_count() * C->blocks_per_sm, (int)C->tiles.size());
+    if (cudaStreamCreateWithFlags(&C->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&C->done, cudaEventDisableTiming) != cudaSuccess)
+      return nullptr;
+    B->classes.push_back(std::move(C));
   }
-  B->grid = sm_count() * B->blocks_per_sm;
+  if (cudaEventCreateWithFlags(&B->start_ev, cudaEventDisableTiming) != cudaSuccess) return nullptr;
   cudaStream_t s = B->stream;
   cudaError_t e = cudaSuccess;
   std::vector<i32> ov_dev(ninst);
@@ -1182,16 +1257,20 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
   }
 #define UP(buf, vec) \
   if (e == cudaSuccess) e = B->buf.upload(vec, s);
-  UP(d_groups, B->groups) UP(d_order, order) UP(d_inst_group, B->inst_group_h)
+  UP(d_groups, B->groups) UP(d_order, order)
   UP(d_dev_type, dev_type) UP(d_dev_nodes, dev_nodes) UP(d_dev_dv, dev_dv)
   UP(d_amap_ptr, amap_ptr) UP(d_amap_code, amap_code) UP(d_rmap_ptr, rmap_ptr)
   UP(d_rmap_code, rmap_code) UP(d_col_ptr, col_ptr) UP(d_dslot, dslot)
   UP(d_col_single, col_single) UP(d_in_row, in_row) UP(d_out_pos, out_pos)
   UP(d_offd_ptr, offd_ptr) UP(d_slot_row, slot_row) UP(d_upd_ptr, upd_ptr)
   UP(d_upd_dst, upd_dst) UP(d_offd_col, offd_col) UP(d_block_ptr, block_ptr)
-  UP(d_dparams, dparams) UP(d_p_off, poff) UP(d_ov_dev, ov_dev) UP(d_ov_val, ov_val)
+  UP(d_heavy, heavy) UP(d_dparams, dparams) UP(d_p_off, poff) UP(d_ov_dev, ov_dev) UP(d_ov_val, ov_val)
   UP(d_x0_off, x0o) UP(d_x_off, B->x_off)
 #undef UP
+  for (auto& C : B->classes) {
+    if (e == cudaSuccess) e = C->d_tiles.upload(C->tiles, s);
+    if (e == cudaSuccess) e = C->d_counter.resize(1);
+  }
   if (e == cudaSuccess) {
     std::vector<double> x0v;
     if (x0) x0v.assign(x0, x0 + B->x0_len);
@@ -1202,19 +1281,18 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
   if (e == cudaSuccess) e = B->d_iters_total.resize(std::max<int64_t>(ninst, 1));
   if (e == cudaSuccess) e = B->d_reason.resize(std::max<int64_t>(ninst, 1));
   if (e == cudaSuccess) e = B->d_status.resize(1);
-  if (e == cudaSuccess) e = B->d_counter.resize(1);
+  if (e == cudaSuccess) e = B->d_gnext.resize(std::max(ngr, 1));
   if (e == cudaSuccess) e = cudaMemsetAsync(B->d_status.p, 0, sizeof(int), s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     fprintf(stderr, "gpuklu_batch_create: %s\n", cudaGetErrorString(e));
     return nullptr;
   }
-  gk::BatchArgs& a = B->args;
+  gk::BatchArgs a{};
   a.groups = B->d_groups.p;
-  a.ninst = (int)ninst;
-  a.counter = B->d_counter.p;
+  a.ngroups = ngr;
+  a.gnext = B->d_gnext.p;
   a.order = B->d_order.p;
-  a.inst_group = B->d_inst_group.p;
   a.dev_type = B->d_dev_type.p;
   a.dev_nodes = B->d_dev_nodes.p;
   a.dev_dv = B->d_dev_dv.p;
@@ -1233,19 +1311,28 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
   a.upd_dst = B->d_upd_dst.p;
   a.offd_col = B->d_offd_col.p;
   a.block_ptr = B->d_block_ptr.p;
+  a.heavy = B->d_heavy.p;
   a.inst_p_off = B->d_p_off.p;
   a.dparams = B->d_dparams.p;
   a.inst_ov_dev = B->d_ov_dev.p;
   a.inst_ov_val = B->d_ov_val.p;
   a.inst_x0_off = B->d_x0_off.p;
   a.x0 = B->d_x0.p;
-  a.region = B->region;
   a.iters = B->d_iters.p;
   a.iters_total = B->d_iters_total.p;
   a.reason = B->d_reason.p;
   a.inst_x_off = B->d_x_off.p;
   a.x_out = B->d_xout.p;
   a.status = B->d_status.p;
+  B->args = a;
+  for (auto& C : B->classes) {
+    C->args = a;
+    C->args.tile_group = C->d_tiles.p;
+    C->args.ntiles = (int)C->tiles.size();
+    C->args.counter = C->d_counter.p;
+    C->args.region = C->region;
+    C->args.prog_ints = C->prog_ints;
+  }
   return B.release();
 }
 
@@ -1267,8 +1354,17 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
   c.gmin = cfg->gmin;
   c.damping = cfg->damping;
   c.damping_min = cfg->damping_min;
-  b->args.cfg = c;
-  gk::launch_batch_newton(b->args, b->grid, b->warps_per_block, b->stream);
+  cudaStream_t s = b->stream;
+  cudaMemsetAsync(b->d_gnext.p, 0, b->d_gnext.n * sizeof(unsigned), s);
+  for (auto& C : b->classes) cudaMemsetAsync(C->d_counter.p, 0, sizeof(unsigned), s);
+  cudaEventRecord(b->start_ev, s);
+  for (auto& C : b->classes) {  // largest programs first, all classes concurrent
+    cudaStreamWaitEvent(C->stream, b->start_ev, 0);
+    C->args.cfg = c;
+    gk::launch_batch_newton(C->args, C->m, C->grid, C->warps_per_block, C->stream);
+    cudaEventRecord(C->done, C->stream);
+    cudaStreamWaitEvent(s, C->done, 0);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return b->fail(cuda_msg(e, "batch launch"));
   return GPUKLU_OK;
@@ -1324,12 +1420,17 @@ const char* gpuklu_batch_last_error(const gpuklu_batch* b) { return b ? b->err.c
 
 int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out) {
   if (!b) return GPUKLU_INVALID_MATRIX;
-  out[0] = b->grid;
-  out[1] = 32 * b->warps_per_block;
+  for (int q = 0; q < 6; ++q) out[q] = 0;
   out[2] = (int64_t)b->groups.size();
-  out[3] = (int64_t)b->region * 8;
-  out[4] = b->regs;
-  out[5] = b->blocks_per_sm;
+  for (auto& C : b->classes) {  // the largest class (first) describes the launch
+    out[0] += C->grid;
+    if (out[1] == 0) {
+      out[1] = 32 * C->warps_per_block;
+      out[3] = ((int64_t)C->region * 8 * C->m + (int64_t)C->prog_ints * 4) * C->warps_per_block;
+      out[4] = C->regs;
+      out[5] = C->blocks_per_sm;
+    }
+  }
   return GPUKLU_OK;
 }
 

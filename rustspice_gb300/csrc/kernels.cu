@@ -735,20 +735,100 @@ __device__ __forceinline__ void eval_record(int type, const int* nd, const doubl
   }
 }
 
+// 1/d for the batched factorization: a single-precision seed built from d's
+// bits on the integer pipe, the hardware float reciprocal, and one FP64
+// Newton step (relative error about 1e-14). FP64 operations have a 64-cycle
+// dependent latency on this part, so this is about half the latency of the
+// correctly rounded reciprocal, which serves magnitudes outside the
+// single-precision range.
+__device__ __forceinline__ double fast_rcp(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e < 1023 - 120 || e > 1023 + 120) return __drcp_rn(d);
+  const unsigned fb = (unsigned)((b >> 32) & 0x80000000u) | ((unsigned)(e - 1023 + 127) << 23) |
+                      (unsigned)((b >> 29) & 0x7fffffu);
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(__uint_as_float(fb)));
+  const unsigned rb = __float_as_uint(rf);
+  const unsigned long long r64 =
+      ((unsigned long long)(rb & 0x80000000u) << 32) |
+      ((unsigned long long)(((rb >> 23) & 0xff) - 127 + 1023) << 52) |
+      ((unsigned long long)(rb & 0x7fffffu) << 29);
+  const double r = __longlong_as_double((long long)r64);
+  return fma(r, fma(-d, r, 1.0), r);
+}
+
+// Contribution lists longer than this are summed across the instance's
+// lanes instead of by one lane.
+constexpr int kHeavy = 12;
+
+__device__ __forceinline__ bool nonzero(double u) {
+  return (__double_as_longlong(u) << 1) != 0;
+}
+
+// The reference's pivot perturbation (native_klu.rs:1229-1231, :1345-1348)
+// on the bit pattern: integer compares instead of FP64 pipe compares.
+__device__ __forceinline__ double perturb_bits(double d, bool singleton) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned long long a = b & 0x7fffffffffffffffull;
+  if (singleton)
+    return a < (unsigned long long)__double_as_longlong(1e-300) ? 1e-14 : d;
+  if (a < (unsigned long long)__double_as_longlong(1e-14))
+    return (a == 0 || (b >> 63) == 0) ? 1e-14 : -1e-14;
+  return d;
+}
+
+// M instances per warp, 32/M lanes each; the M instances run the same
+// program (one group), so the warp's control flow is shared and every FP64
+// warp instruction of the sequential factor and solve serves M instances.
+// A block works on one group at a time and first stages the group's factor
+// and solve structure (per-column records, slot rows, update lists) in its
+// shared memory, so the sequential critical path reads only shared memory.
+template <int M>
 __global__ void k_batch_newton(BatchArgs A) {
-  extern __shared__ double smem[];
+  constexpr int LPI = 32 / M;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
-  double* const region = smem + (size_t)(threadIdx.x >> 5) * A.region;
+  const int sub = lane / LPI, sl = lane % LPI, lead = sub * LPI;
+  const unsigned leaders =
+      M == 1 ? 1u : (M == 2 ? 0x00010001u : (M == 4 ? 0x01010101u : 0x11111111u));
+  // per-warp slice: the staged program, then M instance regions
+  unsigned char* const slice =
+      smem_raw + (size_t)(threadIdx.x >> 5) * ((size_t)A.prog_ints * 4 + (size_t)M * A.region * 8);
+  int* const prog = reinterpret_cast<int*>(slice);
+  double* const region = reinterpret_cast<double*>(slice + (size_t)A.prog_ints * 4) +
+                         (size_t)sub * A.region;
   const NewtonCfg cfg = A.cfg;
   const double gstart = fmax(cfg.gmin * 1e3, 1e-6);
   while (true) {
-    int q = 0;
-    if (lane == 0) q = (int)atomicAdd(A.counter, 1u);
-    q = __shfl_sync(FULL, q, 0);
-    if (q >= A.ninst) return;
-    const int inst = A.order[q];
-    const GroupHdr G = A.groups[A.inst_group[inst]];
+    int ti = 0;
+    if (lane == 0) ti = (int)atomicAdd(A.counter, 1u);
+    ti = __shfl_sync(FULL, ti, 0);
+    if (ti >= A.ntiles) return;
+    const int g = A.tile_group[ti];
+    const GroupHdr G = A.groups[g];
     const int n = G.n, nc = G.node_count, nv = G.nslots + G.noffd;
+    // ---- stage the program: colrec[4n] = (s0, ds, s1, singleton), slot_row,
+    // upd_ptr, upd_dst
+    int4* const colrec = reinterpret_cast<int4*>(prog);
+    int* const srow = prog + 4 * n;
+    int* const uptr = srow + G.nslots;
+    int* const udst = uptr + G.nslots;
+    {
+      const int* cp = A.col_ptr + G.col_off;
+      const int* dsl = A.dslot + G.col_off;
+      const int* cs = A.col_single + G.col_off;
+      for (int k = lane; k < n; k += 32) colrec[k] = make_int4(cp[k], dsl[k], cp[k + 1], cs[k]);
+      const int* sr = A.slot_row + G.slot_off;
+      const int* up = A.upd_ptr + G.slot_off;
+      for (int q = lane; q < G.nslots; q += 32) {
+        srow[q] = sr[q];
+        uptr[q] = up[q];
+      }
+      const int* ud = A.upd_dst + G.upd_off;
+      for (int q = lane; q < G.nupd; q += 32) udst[q] = ud[q];
+    }
+    __syncwarp();
     double* const X = region;
     double* const T = X + nc;
     double* const DV = T + n;
@@ -760,156 +840,209 @@ __global__ void k_batch_newton(BatchArgs A) {
     const int* amap_code = A.amap_code + G.amap_code_off;
     const int* rmap_ptr = A.rmap_ptr + G.rmap_off;
     const int* rmap_code = A.rmap_code + G.rmap_code_off;
-    const int* col_ptr = A.col_ptr + G.col_off;
-    const int* dslot = A.dslot + G.col_off;
-    const int* csing = A.col_single + G.col_off;
     const int* in_row = A.in_row + G.col_off;
     const int* out_pos = A.out_pos + G.col_off;
     const int* offd_ptr = A.offd_ptr + G.col_off;
-    const int* slot_row = A.slot_row + G.slot_off;
-    const int* upd_ptr = A.upd_ptr + G.slot_off;
-    const int* upd_dst = A.upd_dst + G.upd_off;
     const int* offd_col = A.offd_col + G.offd_off;
     const int* bptr = A.block_ptr + G.blk_off;
-    const double* dparams = A.dparams + A.inst_p_off[inst];
-    const int ov_dev = A.inst_ov_dev[inst];
-    const double ov_val = A.inst_ov_val[inst];
-    {
-      const long long xo = A.inst_x0_off[inst];
-      for (int i = lane; i < nc; i += 32) X[i] = xo >= 0 ? A.x0[xo + i] : 0.0;
-    }
-    int it = 0, total = 0, gstep = 0, rsn = -1;
-    double damp = cfg.damping, prev = 1.7976931348623157e308;
-    double gmin = cfg.gmin_steps == 0 ? cfg.gmin : gstart;
-    __syncwarp();
-    while (rsn < 0) {
+    const int* heavy = A.heavy + G.heavy_off;
+
+    int inst = -1, it = 0, total = 0, gstep = 0, ov_dev = -1;
+    bool exhausted = false;
+    double damp = 0.0, prev = 0.0, gmin = 0.0, ov_val = 0.0;
+    const double* dparams = nullptr;
+    while (true) {
+      // ---- idle sub-groups take the group's next instances (one atomic per warp)
+      const bool need = inst < 0 && !exhausted;
+      const unsigned want = __ballot_sync(FULL, need) & leaders;
+      if (want) {
+        const int first_lane = __ffs(want) - 1;
+        int base = 0;
+        if (lane == first_lane) base = (int)atomicAdd(&A.gnext[g], (unsigned)__popc(want));
+        base = __shfl_sync(FULL, base, first_lane);
+        if (need) {
+          const int k = base + __popc(want & ((1u << lead) - 1));
+          if (k < G.inst_count) {
+            inst = A.order[G.inst_begin + k];
+            dparams = A.dparams + A.inst_p_off[inst];
+            ov_dev = A.inst_ov_dev[inst];
+            ov_val = A.inst_ov_val[inst];
+            const long long xo = A.inst_x0_off[inst];
+            for (int i = sl; i < nc; i += LPI) X[i] = xo >= 0 ? A.x0[xo + i] : 0.0;
+            it = total = gstep = 0;
+            damp = cfg.damping;
+            prev = 1.7976931348623157e308;
+            gmin = cfg.gmin_steps == 0 ? cfg.gmin : gstart;
+          } else {
+            exhausted = true;
+          }
+        }
+      }
+      if (!__any_sync(FULL, inst >= 0)) break;
+      __syncwarp();
+      const bool live = inst >= 0;
       // ---- stamp
-      for (int d = lane; d < G.ndev; d += 32) {
-        double dp[4];
-        const double* src = dparams + 4 * d;
+      if (live) {
+        for (int d = sl; d < G.ndev; d += LPI) {
+          double dp[4];
+          const double* src = dparams + 4 * d;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) dp[k] = __ldg(src + k);
-        if (d == ov_dev) dp[0] = ov_val;
-        double rec[4];
-        const int type = dev_type[d];
-        eval_record(type, dev_nodes + 4 * d, dp, X, nc, gmin, rec);
-        const int o = dev_dv[d];
-        const int nrec = type == 6 ? 4 : type == 4 ? 3 : type == 3 ? 2 : type == 5 ? 0 : 1;
-        for (int k = 0; k < nrec; ++k) DV[o + k] = rec[k];
+          for (int k = 0; k < 4; ++k) dp[k] = __ldg(src + k);
+          if (d == ov_dev) dp[0] = ov_val;
+          double rec[4];
+          const int type = dev_type[d];
+          eval_record(type, dev_nodes + 4 * d, dp, X, nc, gmin, rec);
+          const int o = dev_dv[d];
+          const int nrec = type == 6 ? 4 : type == 4 ? 3 : type == 3 ? 2 : type == 5 ? 0 : 1;
+          for (int k = 0; k < nrec; ++k) DV[o + k] = rec[k];
+        }
       }
       __syncwarp();
-      // ---- assemble LU slots and the permuted right-hand side
-      for (int v = lane; v < nv; v += 32) {
+      // ---- assemble LU slots and the permuted right-hand side: short
+      // contribution lists one lane each, long ones (the ground and supply
+      // rows and columns) reduced across the instance's lanes
+      for (int v = sl; v < nv; v += LPI) {
+        const int t0 = amap_ptr[v], t1 = amap_ptr[v + 1];
+        if (t1 - t0 > kHeavy) continue;
         double acc = 0.0;
-        for (int t = amap_ptr[v]; t < amap_ptr[v + 1]; ++t) acc += contrib(DV, amap_code[t]);
+        for (int t = t0; t < t1; ++t) acc += contrib(DV, amap_code[t]);
         V[v] = acc;
       }
-      for (int i = lane; i < n; i += 32) {
+      for (int i = sl; i < n; i += LPI) {
         const int r = in_row[i];
+        const int t0 = rmap_ptr[r], t1 = rmap_ptr[r + 1];
+        if (t1 - t0 > kHeavy) continue;
         double acc = 0.0;
-        for (int t = rmap_ptr[r]; t < rmap_ptr[r + 1]; ++t) acc += contrib(DV, rmap_code[t]);
+        for (int t = t0; t < t1; ++t) acc += contrib(DV, rmap_code[t]);
         T[i] = acc;
       }
+      for (int h = 0; h < G.nheavy; ++h) {
+        const int code = heavy[h];  // (index << 1) | is_row
+        const int idx = code >> 1;
+        const int* ptr = (code & 1) ? rmap_ptr : amap_ptr;
+        const int* cds = (code & 1) ? rmap_code : amap_code;
+        const int key = (code & 1) ? in_row[idx] : idx;
+        const int t0 = ptr[key], t1 = ptr[key + 1];
+        double acc = 0.0;
+        for (int t = t0 + sl; t < t1; t += LPI) acc += contrib(DV, cds[t]);
+#pragma unroll
+        for (int o = LPI / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
+        if (sl == 0) {
+          if (code & 1)
+            T[idx] = acc;
+          else
+            V[idx] = acc;
+        }
+      }
       __syncwarp();
-      // ---- factor + forward substitution, then backward, block by block
+      // ---- factor + forward substitution, then backward, block by block;
+      // V[dslot] holds the reciprocal of the (perturbed) pivot
       for (int b = 0; b < G.nblocks; ++b) {
         const int b0 = bptr[b], b1 = bptr[b + 1];
-        for (int i = b0 + lane; i < b1; i += 32)
+        for (int i = b0 + sl; i < b1; i += LPI)
           for (int e = offd_ptr[i]; e < offd_ptr[i + 1]; ++e)
-            T[i] = T[i] - V[G.nslots + e] * T[offd_col[e]];
+            T[i] = fma(-V[G.nslots + e], T[offd_col[e]], T[i]);
         __syncwarp();
         for (int k = b0; k < b1; ++k) {
-          const int s0 = col_ptr[k], ds = dslot[k], s1 = col_ptr[k + 1];
-          for (int s = s0; s < ds; ++s) {
+          const int4 ck = colrec[k];
+          for (int s = ck.x; s < ck.y; ++s) {
             const double u = V[s];
-            if (u != 0.0) {
-              const int j = slot_row[s];
-              const int q0 = dslot[j] + 1, q1 = col_ptr[j + 1];
-              const int* dst = upd_dst + upd_ptr[s] - q0;
-              for (int qq = q0 + lane; qq < q1; qq += 32) {
+            if (nonzero(u)) {
+              const int4 cj = colrec[srow[s]];
+              const int q0 = cj.y + 1;
+              const int* dst = udst + uptr[s] - q0;
+              for (int qq = q0 + sl; qq < cj.z; qq += LPI) {
                 const int dd = dst[qq];
-                V[dd] = V[dd] - V[qq] * u;
+                V[dd] = fma(-V[qq], u, V[dd]);
               }
             }
             __syncwarp();
           }
-          const double diag = perturb(V[ds], csing[k] != 0);
+          const double r = fast_rcp(perturb_bits(V[ck.y], ck.w != 0));
           const double zk = T[k];
-          for (int qq = ds + 1 + lane; qq < s1; qq += 32) {
-            const double l = V[qq] / diag;
+          for (int qq = ck.y + 1 + sl; qq < ck.z; qq += LPI) {
+            const double l = V[qq] * r;
             V[qq] = l;
-            const int r = slot_row[qq];
-            T[r] = T[r] - l * zk;
+            const int row = srow[qq];
+            T[row] = fma(-l, zk, T[row]);
           }
-          if (lane == 0) V[ds] = diag;
+          if (sl == 0) V[ck.y] = r;
           __syncwarp();
         }
         for (int k = b1 - 1; k >= b0; --k) {
-          const double xk = T[k] / V[dslot[k]];
-          for (int s = col_ptr[k] + lane; s < dslot[k]; s += 32) {
-            const int r = slot_row[s];
-            T[r] = T[r] - V[s] * xk;
+          const int4 ck = colrec[k];
+          const double xk = T[k] * V[ck.y];
+          for (int s = ck.x + sl; s < ck.y; s += LPI) {
+            const int row = srow[s];
+            T[row] = fma(-V[s], xk, T[row]);
           }
           __syncwarp();
-          if (lane == 0) T[k] = xk;
+          if (sl == 0) T[k] = xk;
           __syncwarp();
         }
       }
       // ---- Newton update (crates/sim-core/src/newton.rs:93-107)
-      ++it;
-      ++total;
       bool conv = true, fin = true;
-      for (int c = lane; c < nc; c += 32) {
+      for (int c = sl; c < nc; c += LPI) {
         const double a = T[out_pos[c]];
         const double dx = a - X[c];
         DV[c] = dx * dx;
         if (!(fabs(dx) <= cfg.abs_tol + cfg.rel_tol * fabs(a))) conv = false;
         if (!isfinite(a)) fin = false;
       }
-      conv = __all_sync(FULL, conv);
-      fin = __all_sync(FULL, fin);
+      const unsigned smask = (LPI == 32 ? FULL : (((1u << LPI) - 1u) << lead));
+      const unsigned nconv = __ballot_sync(FULL, !conv) & smask;
+      const unsigned nfin = __ballot_sync(FULL, !fin) & smask;
       __syncwarp();
-      if (conv) {
-        rsn = 0;
-        const long long xo = A.inst_x_off[inst];
-        if (xo >= 0)
-          for (int c = lane; c < n; c += 32) A.x_out[xo + c] = T[out_pos[c]];
-      } else {
-        double ss = 0.0;  // norm2 as the reference sums it: in order
-        if (lane == 0)
-          for (int c = 0; c < nc; ++c) ss += DV[c];
-        ss = __shfl_sync(FULL, ss, 0);
-        const double dxn = sqrt(ss);
-        if (dxn > prev && damp > cfg.damping_min) damp = fmax(damp * 0.5, cfg.damping_min);
-        prev = dxn;
-        for (int c = lane; c < nc; c += 32) X[c] = X[c] + damp * (T[out_pos[c]] - X[c]);
-        if (!fin) {
-          rsn = 1;
-        } else if (it >= cfg.max_iters) {
-          if (gstep < cfg.gmin_steps) {  // next gmin step, fresh damping state
-            ++gstep;
-            gmin = gstart + (cfg.gmin - gstart) * ((double)gstep / (double)cfg.gmin_steps);
-            it = 0;
-            damp = cfg.damping;
-            prev = 1.7976931348623157e308;
-          } else {
-            rsn = 1;
-          }
-        }
-        __syncwarp();
-        if (rsn == 1) {
+      if (live) {
+        ++it;
+        ++total;
+        int rsn = -1;
+        if (!nconv) {
+          rsn = 0;
           const long long xo = A.inst_x_off[inst];
           if (xo >= 0)
-            for (int c = lane; c < n; c += 32) A.x_out[xo + c] = c < nc ? X[c] : 0.0;
+            for (int c = sl; c < n; c += LPI) A.x_out[xo + c] = T[out_pos[c]];
+        } else {
+          double ss = 0.0;  // norm2 of dx, reduced across the instance's lanes
+          for (int c = sl; c < nc; c += LPI) ss += DV[c];
+#pragma unroll
+          for (int o = LPI / 2; o > 0; o >>= 1) ss += __shfl_xor_sync(smask, ss, o);
+          const double dxn = sqrt(ss);
+          if (dxn > prev && damp > cfg.damping_min) damp = fmax(damp * 0.5, cfg.damping_min);
+          prev = dxn;
+          for (int c = sl; c < nc; c += LPI) X[c] = fma(damp, T[out_pos[c]] - X[c], X[c]);
+          if (nfin) {
+            rsn = 1;
+          } else if (it >= cfg.max_iters) {
+            if (gstep < cfg.gmin_steps) {  // next gmin step, fresh damping state
+              ++gstep;
+              gmin = gstart + (cfg.gmin - gstart) * ((double)gstep / (double)cfg.gmin_steps);
+              it = 0;
+              damp = cfg.damping;
+              prev = 1.7976931348623157e308;
+            } else {
+              rsn = 1;
+            }
+          }
+          if (rsn == 1) {
+            const long long xo = A.inst_x_off[inst];
+            if (xo >= 0)
+              for (int c = sl; c < n; c += LPI) A.x_out[xo + c] = c < nc ? X[c] : 0.0;
+          }
+        }
+        if (rsn >= 0) {
+          if (sl == 0) {
+            A.iters[inst] = it;
+            A.iters_total[inst] = total;
+            A.reason[inst] = rsn;
+          }
+          inst = -1;
         }
       }
       __syncwarp();
     }
-    if (lane == 0) {
-      A.iters[inst] = it;
-      A.iters_total[inst] = total;
-      A.reason[inst] = rsn;
-    }
+    __syncwarp();  // done with this group's staged program
   }
 }
 
@@ -986,20 +1119,49 @@ double fp64_peak_tflops() {
   return flops / (best * 1e-3) / 1e12;
 }
 
-void launch_batch_newton(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s) {
-  cudaMemsetAsync(a.counter, 0, sizeof(unsigned), s);
-  const size_t sm = (size_t)a.region * warps_per_block * sizeof(double);
-  k_batch_newton<<<grid, 32 * warps_per_block, sm, s>>>(a);
+template <int M>
+static size_t smem_bytes(const BatchArgs& a, int warps_per_block) {
+  return ((size_t)a.prog_ints * 4 + (size_t)a.region * M * sizeof(double)) * warps_per_block;
 }
 
-void batch_kernel_info(int warps_per_block, int region, int* regs, int* blocks_per_sm) {
+template <int M>
+static void launch_m(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s) {
+  const size_t sm = smem_bytes<M>(a, warps_per_block);
+  k_batch_newton<M><<<grid, 32 * warps_per_block, sm, s>>>(a);
+}
+
+void launch_batch_newton(const BatchArgs& a, int m, int grid, int warps_per_block,
+                         cudaStream_t s) {
+  cudaMemsetAsync(a.counter, 0, sizeof(unsigned), s);
+  cudaMemsetAsync(a.gnext, 0, sizeof(unsigned) * (a.ngroups > 0 ? a.ngroups : 1), s);
+  switch (m) {
+    case 8: launch_m<8>(a, grid, warps_per_block, s); break;
+    case 4: launch_m<4>(a, grid, warps_per_block, s); break;
+    case 2: launch_m<2>(a, grid, warps_per_block, s); break;
+    default: launch_m<1>(a, grid, warps_per_block, s); break;
+  }
+}
+
+template <int M>
+static void info_m(int warps_per_block, int region, int prog_ints, int* regs,
+                   int* blocks_per_sm) {
   cudaFuncAttributes fa{};
-  cudaFuncGetAttributes(&fa, k_batch_newton);
+  cudaFuncGetAttributes(&fa, k_batch_newton<M>);
   *regs = fa.numRegs;
-  const size_t sm = (size_t)region * warps_per_block * sizeof(double);
-  cudaFuncSetAttribute(k_batch_newton, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch_newton,
+  const size_t sm = ((size_t)prog_ints * 4 + (size_t)region * M * sizeof(double)) * warps_per_block;
+  cudaFuncSetAttribute(k_batch_newton<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch_newton<M>,
                                                 32 * warps_per_block, sm);
+}
+
+void batch_kernel_info(int m, int warps_per_block, int region, int prog_ints, int* regs,
+                       int* blocks_per_sm) {
+  switch (m) {
+    case 8: info_m<8>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+    case 4: info_m<4>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+    case 2: info_m<2>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+    default: info_m<1>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+  }
 }
 
 }  // namespace gk

@@ -51,8 +51,13 @@ struct GroupHdr {
   int blk_off;     // block_ptr
   int amap_off;    // nslots+noffd+1 contribution pointers (values relative to amap_code base)
   int amap_code_off;
+  int nupd;        // update-list length
+  int heavy_off;   // slots/rows with long contribution lists
+  int nheavy;
   int rmap_off;    // n+1 row contribution pointers
   int rmap_code_off;
+  int inst_begin;  // range of the group's instances in the order array
+  int inst_count;
   int cost;        // scheduling weight (FP64 operations of one Newton iteration)
 };
 
@@ -63,15 +68,18 @@ struct GroupHdr {
 // entries (crates/sim-core/src/native_klu.rs:1265-1274).
 struct BatchArgs {
   const GroupHdr* groups;
-  int ninst;
-  unsigned* counter;       // next instance to hand out
-  const int* order;        // instances, most expensive first
-  const int* inst_group;
+  int ngroups;
+  const int* tile_group;   // warp work units: group of each tile
+  int ntiles;
+  unsigned* counter;       // next tile to hand out
+  unsigned* gnext;         // per group: next instance to hand out
+  const int* order;        // instances grouped by group
   const int *dev_type, *dev_nodes, *dev_dv;  // dv: offset of the device's value record
   const int *amap_ptr, *amap_code;           // per value slot (group-local ptr)
   const int *rmap_ptr, *rmap_code;           // per original row
   const int *col_ptr, *dslot, *col_single, *in_row, *out_pos, *offd_ptr, *slot_row,
       *upd_ptr, *upd_dst, *offd_col, *block_ptr;
+  const int* heavy;  // (value index << 1) or (position << 1 | 1), per group
   const long long* inst_p_off;  // offset of the instance's circuit constants (4 per device)
   const double* dparams;
   const int* inst_ov_dev;
@@ -79,7 +87,8 @@ struct BatchArgs {
   const long long* inst_x0_off;
   const double* x0;
   NewtonCfg cfg;
-  int region;  // shared-memory doubles per warp
+  int region;     // shared-memory doubles per instance
+  int prog_ints;  // shared-memory ints of the staged program (largest group)
   int *iters, *iters_total, *reason;
   const long long* inst_x_off;
   double* x_out;
@@ -104,9 +113,11 @@ void launch_newton_update(int m, int n, double* x, const double* xnew, NewtonSta
 void launch_rcond(const DPlan& P, const double* lu, double* out2, cudaStream_t s);
 // Measured FP64 fused multiply-add throughput of the current device [TFLOP/s].
 double fp64_peak_tflops();
-void launch_batch_newton(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
-// Registers per thread and resident blocks per SM of the batched kernel for
-// a block of warps_per_block warps with `region` shared doubles per warp.
-void batch_kernel_info(int warps_per_block, int region, int* regs, int* blocks_per_sm);
+// m: instances per warp (1, 2 or 4); region: shared doubles per instance.
+void launch_batch_newton(const BatchArgs& a, int m, int grid, int warps_per_block,
+                         cudaStream_t s);
+// Registers per thread and resident blocks per SM of the batched kernel.
+void batch_kernel_info(int m, int warps_per_block, int region, int prog_ints, int* regs,
+                       int* blocks_per_sm);
 
 }  // namespace gk
