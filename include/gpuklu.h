@@ -180,6 +180,18 @@ int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_co
                      const double* x0, double* x_out, int64_t x_cap, int64_t* x_len,
                      int64_t* iters, int64_t* iters_total, int* reason);
 
+/* Adjoint of a DC operating point (no counterpart in the reference). At the
+ * converged x (xlen values, node voltages first) it stamps and factors the
+ * exact Jacobian A(x) on the device (the consistent level-1 model without its
+ * 1e-12 S conductance floor, which cancels in the residual), solves A(x)^T lambda = dl_dx (n values) with the transpose
+ * solve, and evaluates dL/dp = -lambda^T dF/dp for every device, where
+ * F(x, p) = A(x) x - b(x) is the stamped KCL residual and p is the device's
+ * resistance (R), value (V, I), Is (D) or VTO (M, MC). lambda_out (n) and
+ * grad_out (ndev) may be NULL. */
+int gpuklu_dc_backward(gpuklu_handle* h, gpuklu_circuit* c, const double* x, int64_t xlen,
+                       const double* dl_dx, double gmin, double* lambda_out,
+                       double* grad_out);
+
 /* ------------------------------------------------ batched Newton */
 
 typedef struct gpuklu_batch gpuklu_batch;

@@ -119,12 +119,12 @@ void orc_btf(int64_t n, const int64_t* ap, const int64_t* ai, int64_t* row_perm,
 void* orc_mna(int64_t node_count, int64_t ndev, const int32_t* type,
               const int32_t* nodes, const double* p, const double* x,
               int64_t xlen, double gmin, double scale, double dt,
-              const double* cap_v, double be_sign) {
+              const double* cap_v, double be_sign, double gdev) {
   Circuit c = make_circuit(node_count, ndev, type, nodes, p);
   TranState st;
   if (cap_v) st.cap_v.assign(cap_v, cap_v + ndev);
   auto* s = new MnaSystem(build_mna(c, Vec(x, x + xlen), gmin, scale, dt,
-                                    cap_v ? &st : nullptr, be_sign));
+                                    cap_v ? &st : nullptr, be_sign, gdev));
   return s;
 }
 void orc_mna_dims(void* h, int64_t* n, int64_t* nnz) {

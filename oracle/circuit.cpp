@@ -125,7 +125,7 @@ MosOut eval_level1(double vth0, double u0, double tox, double w, double l,
 
 MosJ eval_level1_consistent(double vth0, double u0, double tox, double w,
                             double l, double vd, double vg, double vs,
-                            bool is_pmos) {
+                            bool is_pmos, double gdev) {
   // Same level-1 equations and constants as eval_level1; the polarity is
   // applied to every terminal voltage and the drain/source roles swap when
   // vds < 0, so (ddg, ddd, dds) are the exact partials of id.
@@ -142,16 +142,16 @@ MosJ eval_level1_consistent(double vth0, double u0, double tox, double w,
   if (vgse <= vth) {
     ids = 0.0;
     gm = 0.0;
-    gds = kGmin;
+    gds = gdev;
   } else if (vdse < vgse - vth) {
     ids = beff * ((vgse - vth) * vdse - 0.5 * vdse * vdse);
     gm = beff * vdse;
-    gds = std::fmax(beff * ((vgse - vth) - vdse), kGmin);
+    gds = std::fmax(beff * ((vgse - vth) - vdse), gdev);
   } else {
     double t = vgse - vth;
     ids = 0.5 * beff * (t * t) * (1.0 + lambda * vdse);
     gm = beff * (vgse - vth) * (1.0 + lambda * vdse);
-    gds = std::fmax(0.5 * beff * (t * t) * lambda, kGmin);
+    gds = std::fmax(0.5 * beff * (t * t) * lambda, gdev);
   }
   MosJ j;
   if (!rev) {
@@ -170,7 +170,7 @@ MosJ eval_level1_consistent(double vth0, double u0, double tox, double w,
 
 MnaSystem build_mna(const Circuit& c, const Vec& x, double gmin,
                     double source_scale, double dt, const TranState* st,
-                    double be_sign) {
+                    double be_sign, double gdev) {
   MnaSystem s;
   Builder b(c.node_count);
   s.rhs.assign(c.node_count, 0.0);
@@ -244,7 +244,7 @@ MnaSystem build_mna(const Circuit& c, const Vec& x, double gmin,
         size_t dr = (size_t)nd[0], gt = (size_t)nd[1], sr = (size_t)nd[2];
         double vd = xget(x, dr), vg = xget(x, gt), vs = xget(x, sr);
         MosJ j = eval_level1_consistent(p[1], p[2], p[3], p[4], p[5], vd, vg, vs,
-                                        p[0] != 0.0);
+                                        p[0] != 0.0, gdev);
         double ieq = j.id - (j.ddg * vg + j.ddd * vd + j.dds * vs);
         ctx.add(dr, dr, j.ddd);
         ctx.add(sr, sr, -j.dds);

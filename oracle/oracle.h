@@ -280,9 +280,12 @@ struct TranState {
 // When `dt > 0` capacitors use the backward-Euler companion
 // (crates/sim-core/src/stamp.rs:759-787) with `be_sign` = -1 for the
 // reference's sign and +1 for the physical one; dt <= 0 is DC (C open).
+// gdev: the consistent MOSFET model's conductance floor (1e-12; 0 gives the
+// exact Jacobian of the residual).
 MnaSystem build_mna(const Circuit& c, const Vec& x, double gmin,
                     double source_scale, double dt = 0.0,
-                    const TranState* st = nullptr, double be_sign = -1.0);
+                    const TranState* st = nullptr, double be_sign = -1.0,
+                    double gdev = 1e-12);
 
 // Level-1 MOSFET, crates/sim-devices/src/bsim/evaluate.rs:285-356 via
 // evaluate_mos, crates/sim-devices/src/bsim/mod.rs:430-476.
@@ -298,7 +301,7 @@ struct MosJ {
 };
 MosJ eval_level1_consistent(double vth0, double u0, double tox, double w,
                             double l, double vd, double vg, double vs,
-                            bool is_pmos);
+                            bool is_pmos, double gdev = 1e-12);
 
 // ---------------------------------------------------------------- Newton
 // crates/sim-core/src/newton.rs:1-265

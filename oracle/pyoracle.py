@@ -45,7 +45,7 @@ def lib():
         L.orc_amd.argtypes = [_I64, _P, _P, _P, _P]
         L.orc_btf.argtypes = [_I64, _P, _P, _P, _P, _P, _P]
         L.orc_mna.restype = _P
-        L.orc_mna.argtypes = [_I64, _I64, _P, _P, _P, _P, _I64, _D, _D, _D, _P, _D]
+        L.orc_mna.argtypes = [_I64, _I64, _P, _P, _P, _P, _I64, _D, _D, _D, _P, _D, _D]
         L.orc_mna_dims.argtypes = [_P, _P, _P]
         L.orc_mna_get.argtypes = [_P, _P, _P, _P, _P]
         L.orc_mna_free.argtypes = [_P]
@@ -147,13 +147,13 @@ def _circ_arrays(c):
             np.ascontiguousarray(c.nodes, np.int32), _f64(c.p))
 
 
-def mna(c, x, gmin=1e-12, scale=1.0, dt=0.0, cap_v=None, be_sign=-1.0):
+def mna(c, x, gmin=1e-12, scale=1.0, dt=0.0, cap_v=None, be_sign=-1.0, gdev=1e-12):
     """The reference engine's MNA build at x: (n, ap, ai, ax, rhs)."""
     _, t, nd, p = _circ_arrays(c)
     x = _f64(x)
     cv = _f64(cap_v) if cap_v is not None else None
     h = lib().orc_mna(c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p), _ptr(x), len(x),
-                      gmin, scale, dt, _ptr(cv) if cv is not None else None, be_sign)
+                      gmin, scale, dt, _ptr(cv) if cv is not None else None, be_sign, gdev)
     n = C.c_int64()
     nnz = C.c_int64()
     lib().orc_mna_dims(h, C.byref(n), C.byref(nnz))

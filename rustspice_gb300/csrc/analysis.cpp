@@ -514,6 +514,22 @@ void finalize_plan(Plan& p, const i64* ap, const i64* ai, const std::vector<Patt
     }
     p.offd_ptr[i + 1] = (int)p.offd_col.size();
   }
+  {
+    std::vector<std::vector<std::pair<int, int>>> cols(n);
+    for (int i = 0; i < n; ++i)
+      for (int e = p.offd_ptr[i]; e < p.offd_ptr[i + 1]; ++e)
+        cols[p.offd_col[e]].push_back({i, p.offd_raw[e]});
+    p.offdT_ptr.assign(n + 1, 0);
+    p.offdT_row.clear();
+    p.offdT_raw.clear();
+    for (int c = 0; c < n; ++c) {
+      for (auto& e : cols[c]) {
+        p.offdT_row.push_back(e.first);
+        p.offdT_raw.push_back(e.second);
+      }
+      p.offdT_ptr[c + 1] = (int)p.offdT_row.size();
+    }
+  }
   // raw entries summed into each slot, in CSC order
   std::vector<int> cnt(ns + 1, 0);
   for (i64 t = 0; t < p.nnz_raw; ++t)

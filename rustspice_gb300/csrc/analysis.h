@@ -82,6 +82,9 @@ struct Plan {
   std::vector<i32> offd_ptr;     // [n+1]
   std::vector<i32> offd_col;     // position column
   std::vector<i32> offd_raw;     // raw CSC index
+  // The same entries grouped by position column (for A^T solves): rows and
+  // raw indices, rows ascending.
+  std::vector<i32> offdT_ptr, offdT_row, offdT_raw;
   bool offd_lower = false;       // true: forward block order (exact mode)
 
   // Row-oriented views of L and U for the dependency-driven solve.

@@ -83,7 +83,8 @@ std::vector<i32> make_tasks(const gk::Plan& p, bool transpose) {
 // Device copy of a Plan.
 struct PlanDev {
   DBuf<i32> col_ptr, dslot, slot_row, upd_ptr, upd_dst, col_single, amap_ptr, amap_idx,
-      offd_ptr, offd_col, offd_raw, lrow_ptr, lrow_col, lrow_slot, urow_ptr, urow_col,
+      offd_ptr, offd_col, offd_raw, offdT_ptr, offdT_row, offdT_raw, lrow_ptr, lrow_col,
+      lrow_slot, urow_ptr, urow_col,
       urow_slot, in_row, out_col, pcol_ptr, pcol_raw, pcol_q, pos_block, block_ptr, task,
       ttask;
   gk::DPlan dp{}, dpt{};
@@ -98,7 +99,8 @@ struct PlanDev {
     UP(col_ptr, p.col_ptr) UP(dslot, p.dslot) UP(slot_row, p.slot_row) UP(upd_ptr, p.upd_ptr)
     UP(upd_dst, p.upd_dst) UP(col_single, p.col_single) UP(amap_ptr, p.amap_ptr)
     UP(amap_idx, p.amap_idx) UP(offd_ptr, p.offd_ptr) UP(offd_col, p.offd_col)
-    UP(offd_raw, p.offd_raw) UP(lrow_ptr, p.lrow_ptr) UP(lrow_col, p.lrow_col)
+    UP(offd_raw, p.offd_raw) UP(offdT_ptr, p.offdT_ptr) UP(offdT_row, p.offdT_row)
+    UP(offdT_raw, p.offdT_raw) UP(lrow_ptr, p.lrow_ptr) UP(lrow_col, p.lrow_col)
     UP(lrow_slot, p.lrow_slot) UP(urow_ptr, p.urow_ptr) UP(urow_col, p.urow_col)
     UP(urow_slot, p.urow_slot) UP(in_row, h_in_row) UP(out_col, h_out_col)
     UP(pcol_ptr, p.pcol_ptr) UP(pcol_raw, p.pcol_raw) UP(pcol_q, p.pcol_q)
@@ -123,6 +125,9 @@ struct PlanDev {
     d.offd_ptr = offd_ptr.p;
     d.offd_col = offd_col.p;
     d.offd_raw = offd_raw.p;
+    d.offdT_ptr = offdT_ptr.p;
+    d.offdT_row = offdT_row.p;
+    d.offdT_raw = offdT_raw.p;
     d.lrow_ptr = lrow_ptr.p;
     d.lrow_col = lrow_col.p;
     d.lrow_slot = lrow_slot.p;
@@ -456,8 +461,6 @@ struct gpuklu_handle {
 
   // Solve with rhs in d_rhs; result in d_out (original column order).
   int solve_on_device(bool transpose, bool sync) {
-    if (transpose && plan.noffdiag > 0)
-      return fail(GPUKLU_SOLVE_FAILED, "transpose solve with BTF coupling blocks");
     unsigned ep = sepoch + 1;
     if (ep == 0) ep = 1;
     sepoch = ep;
@@ -800,6 +803,43 @@ int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_co
   if (iters_total) *iters_total = total;
   if (reason) *reason = rsn;
   return GPUKLU_OK;
+}
+
+int gpuklu_dc_backward(gpuklu_handle* h, gpuklu_circuit* c, const double* x, int64_t xlen,
+                       const double* dl_dx, double gmin, double* lambda_out,
+                       double* grad_out) {
+  if (!h || !c || !x || !dl_dx) return GPUKLU_INVALID_MATRIX;
+  const int n = c->n;
+  gpuklu_prepare(h, n);
+  int st = gpuklu_analyze(h, c->ap.data(), (int64_t)c->ap.size(), c->ai.data(),
+                          (int64_t)c->ai.size());
+  if (st) return st;
+  DBuf<double> dx, dgrad;
+  cudaError_t e = dx.resize(std::max<int64_t>(xlen, 1));
+  if (e == cudaSuccess) e = dgrad.resize(std::max(c->ndev, 1));
+  if (e == cudaSuccess) e = h->d_rhs_c.resize(std::max(c->ncontrib, 1));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dx.p, x, xlen * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "backward upload");
+  // A at the solution: stamp and factor (refactor when the pivots are known)
+  // exact Jacobian: no level-1 conductance floor (it cancels in the residual)
+  gk::launch_stamp(c->dc, dx.p, (int)std::min<int64_t>(xlen, c->node_count), gmin, 1.0, 0.0,
+                   nullptr, -1.0, h->d_ax.p, h->d_rhs_c.p, h->d_rhs.p, h->stream, 0.0);
+  st = h->factor_on_device(true);
+  if (st) return st;
+  e = cudaMemcpyAsync(h->d_rhs.p, dl_dx, n * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "backward upload");
+  st = h->solve_on_device(true, false);
+  if (st) return st;
+  gk::launch_param_grad(c->dc, dx.p, (int)xlen, h->d_out.p, dgrad.p, h->stream);
+  if (lambda_out)
+    e = cudaMemcpyAsync(lambda_out, h->d_out.p, n * sizeof(double), cudaMemcpyDeviceToHost,
+                        h->stream);
+  if (e == cudaSuccess && grad_out)
+    e = cudaMemcpyAsync(grad_out, dgrad.p, c->ndev * sizeof(double), cudaMemcpyDeviceToHost,
+                        h->stream);
+  if (e != cudaSuccess) return h->cuda_fail(e, "backward download");
+  return h->check_status("dc_backward");
 }
 
 }  // extern "C"

@@ -255,9 +255,10 @@ __global__ void k_solve(DPlan P, const double* __restrict__ rhs, const double* _
 // A^T y = g with the same factors: U^T forward (U columns as rows), then
 // L^T backward (L columns as rows). Task codes as in k_solve; the input is
 // indexed by original column and the output by original row.
-__global__ void k_tsolve(DPlan P, const double* __restrict__ g, const double* __restrict__ lu,
-                         double* z, double* x, double* out, unsigned* zflag, unsigned* xflag,
-                         unsigned epoch, unsigned* counter, int* status) {
+__global__ void k_tsolve(DPlan P, const double* __restrict__ g, const double* __restrict__ ax,
+                         const double* __restrict__ lu, double* z, double* x, double* out,
+                         unsigned* zflag, unsigned* xflag, unsigned epoch, unsigned* counter,
+                         int* status) {
   const int lane = threadIdx.x & 31;
   while (true) {
     int t = 0;
@@ -266,11 +267,15 @@ __global__ void k_tsolve(DPlan P, const double* __restrict__ g, const double* __
     if (t >= P.ntask) return;
     const int code = P.task[t];
     const int k = code >> 1;
-    if ((code & 1) == 0) {  // U^T row k = U column k
+    if ((code & 1) == 0) {  // coupling^T, then U^T row k = U column k
       double v = g[P.out_col[k]];
       bool ok = ordered_dot(
-          v, P.col_ptr[k], P.dslot[k], [&](int e) { return lu[e]; },
-          [&](int e) { return P.slot_row[e]; }, zflag, z, epoch, status);
+          v, P.offdT_ptr[k], P.offdT_ptr[k + 1], [&](int e) { return ax[P.offdT_raw[e]]; },
+          [&](int e) { return P.offdT_row[e]; }, xflag, x, epoch, status);
+      if (ok)
+        ok = ordered_dot(
+            v, P.col_ptr[k], P.dslot[k], [&](int e) { return lu[e]; },
+            [&](int e) { return P.slot_row[e]; }, zflag, z, epoch, status);
       if (!ok) return;
       if (lane == 0) {
         v = v / lu[P.dslot[k]];
@@ -335,8 +340,8 @@ __device__ void mos_reference(const double* p, double vd, double vg, double vs, 
 // Level-1 MOSFET with a self-consistent linearisation: drain current and its
 // partials with respect to (vg, vd, vs).
 __device__ void mos_consistent(const double* p, double vd, double vg, double vs, double& id,
-                               double& ddg, double& ddd, double& dds) {
-  const double lambda = 0.02, gmin_dev = 1e-12;
+                               double& ddg, double& ddd, double& dds, double gmin_dev) {
+  const double lambda = 0.02;
   const double pol = p[0] != 0.0 ? -1.0 : 1.0;
   const double beta = p[2] * 1e-4 * ((3.9 * 8.854e-12) / p[3]);
   const double vgs = pol * (vg - vs), vds = pol * (vd - vs);
@@ -374,10 +379,14 @@ __device__ void mos_consistent(const double* p, double vd, double vg, double vs,
 
 // One device's matrix inserts (in the reference's insert order) and its
 // right-hand-side contributions. Returns the number of matrix values.
+// gdev is the level-1 conductance floor of the consistent model: 1e-12 as
+// the reference's evaluator uses, or 0 for the exact Jacobian of the
+// residual (the floor cancels in the residual but not in the matrix).
 template <class XGet>
 __device__ __forceinline__ int eval_device(int type, const int* nd, const double* p, XGet xg,
                                            double gmin, double scale, double dt, double vprev,
-                                           double be_sign, double* m, double* r, int& nr) {
+                                           double be_sign, double* m, double* r, int& nr,
+                                           double gdev = 1e-12) {
   nr = 0;
   switch (type) {
     case 0: {  // R
@@ -443,7 +452,7 @@ __device__ __forceinline__ int eval_device(int type, const int* nd, const double
     case 6: {  // MC: same 8 inserts, exact partials
       const double vd = xg(nd[0]), vg = xg(nd[1]), vs = xg(nd[2]);
       double id, ddg, ddd, dds;
-      mos_consistent(p, vd, vg, vs, id, ddg, ddd, dds);
+      mos_consistent(p, vd, vg, vs, id, ddg, ddd, dds, gdev);
       const double ieq = id - (ddg * vg + ddd * vd + dds * vs);
       m[0] = ddd;
       m[1] = -dds;
@@ -477,7 +486,7 @@ __device__ __forceinline__ int eval_device(int type, const int* nd, const double
 
 __global__ void k_stamp(DCircuit C, const double* __restrict__ x, int xlen, double gmin,
                         double scale, double dt, const double* __restrict__ cap_v,
-                        double be_sign, double* ax, double* rhs_c) {
+                        double be_sign, double* ax, double* rhs_c, double gdev) {
   const int d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d == 0 && C.pin_raw >= 0) ax[C.pin_raw] = 1.0;
   if (d >= C.ndev) return;
@@ -487,13 +496,87 @@ __global__ void k_stamp(DCircuit C, const double* __restrict__ x, int xlen, doub
   int nr;
   const double vprev = cap_v ? cap_v[d] : 0.0;
   const int nm = eval_device(C.type[d], nd, C.p + 6 * d, xg, gmin, scale, dt, vprev, be_sign,
-                             m, r, nr);
+                             m, r, nr, gdev);
   const int* raw = C.raw + 8 * d;
   for (int e = 0; e < nm; ++e)
     if (raw[e] >= 0) ax[raw[e]] = m[e];
   const int* rs = C.rhs_slot + 2 * d;
   for (int e = 0; e < nr; ++e)
     if (rs[e] >= 0) rhs_c[rs[e]] = r[e];
+}
+
+// dL/dp of every device at a DC solution x, given the adjoint lambda
+// (A^T lambda = dL/dx): dL/dp = -lambda^T dF/dp with F(x, p) = A(x) x - b(x)
+// the stamped KCL residual. p is the resistance for R, the value for V and
+// I, Is for D, and VTO for the MOSFETs (threshold |VTO| for both models).
+__global__ void k_param_grad(DCircuit C, const double* __restrict__ x, int xlen,
+                             const double* __restrict__ lam, double* grad) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= C.ndev) return;
+  const int* nd = C.nodes + 4 * d;
+  const double* p = C.p + 6 * d;
+  auto xg = [&](int i) { return (i >= 0 && i < xlen) ? x[i] : 0.0; };
+  auto lg = [&](int i) { return (i >= 0 && i < C.n) ? lam[i] : 0.0; };
+  double gr = 0.0;
+  switch (C.type[d]) {
+    case 0: {  // F_a += (va - vb)/R
+      const double v = xg(nd[0]) - xg(nd[1]);
+      gr = (lg(nd[0]) - lg(nd[1])) * v / (p[0] * p[0]);
+      break;
+    }
+    case 1:  // aux row: va - vb - V
+      gr = lg(nd[2]);
+      break;
+    case 2:  // F_a += I, F_b -= I
+      gr = -(lg(nd[0]) - lg(nd[1]));
+      break;
+    case 3: {  // F_a += Is (exp(vd/vt) - 1)
+      const double vt = 0.02585 * p[1];
+      const double e = exp((xg(nd[0]) - xg(nd[1])) / vt);
+      gr = -(lg(nd[0]) - lg(nd[1])) * (e - 1.0);
+      break;
+    }
+    case 4:
+    case 6: {  // F_d += id, F_s -= id; d id / d vth = -(frame sign) * gm
+      const bool pm = p[0] != 0.0;
+      const double vd = xg(nd[0]), vg = xg(nd[1]), vs = xg(nd[2]);
+      const double beff = p[2] * 1e-4 * ((3.9 * 8.854e-12) / p[3]) * p[4] / p[5];
+      double vgs, vds, vth, sgn;
+      if (C.type[d] == 6) {
+        const double pol = pm ? -1.0 : 1.0;
+        vgs = pol * (vg - vs);
+        vds = pol * (vd - vs);
+        const bool rev = vds < 0.0;
+        if (rev) {
+          vgs = vgs - vds;
+          vds = -vds;
+        }
+        vth = fabs(p[1]);
+        sgn = rev ? -pol : pol;
+      } else {  // the reference's frame (evaluate.rs:299-316)
+        double vdi = pm ? -vs : vd, vgi = pm ? -vg : vg, vsi = pm ? -vd : vs;
+        vgs = vgi - vsi;
+        vds = vdi - vsi;
+        if (vds < 0.0) {
+          vds = -vds;
+          vgs = vgi - vdi;
+        }
+        vth = pm ? -fabs(p[1]) : fabs(p[1]);
+        sgn = pm ? -1.0 : 1.0;
+      }
+      double gm = 0.0;
+      if (vgs > vth) gm = vds < vgs - vth ? beff * vds : beff * (vgs - vth) * (1.0 + 0.02 * vds);
+      // dvth/dVTO: |VTO| -> sign(VTO); the reference's PMOS uses -|VTO|
+      double dvth = p[1] >= 0.0 ? 1.0 : -1.0;
+      if (C.type[d] == 4 && pm) dvth = -dvth;
+      const double did = sgn * (-gm) * dvth;
+      gr = -(lg(nd[0]) - lg(nd[2])) * did;
+      break;
+    }
+    default:
+      break;
+  }
+  grad[d] = gr;
 }
 
 __global__ void k_rhs_sum(DCircuit C, const double* __restrict__ rhs_c, double* rhs) {
@@ -1067,7 +1150,8 @@ void launch_solve(const DPlan& P, const double* rhs, const double* ax, const dou
                   cudaStream_t s) {
   cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
   if (transpose)
-    k_tsolve<<<grid, 128, 0, s>>>(P, rhs, lu, z, x, out, zflag, xflag, epoch, counter, status);
+    k_tsolve<<<grid, 128, 0, s>>>(P, rhs, ax, lu, z, x, out, zflag, xflag, epoch, counter,
+                                  status);
   else
     k_solve<<<grid, 128, 0, s>>>(P, rhs, ax, lu, z, x, out, zflag, xflag, epoch, counter,
                                  status);
@@ -1075,11 +1159,17 @@ void launch_solve(const DPlan& P, const double* rhs, const double* ax, const dou
 
 void launch_stamp(const DCircuit& C, const double* x, int xlen, double gmin, double scale,
                   double dt, const double* cap_v, double be_sign, double* ax, double* rhs_c,
-                  double* rhs, cudaStream_t s) {
+                  double* rhs, cudaStream_t s, double gdev) {
   const int nb = (C.ndev + 255) / 256;
   k_stamp<<<nb > 0 ? nb : 1, 256, 0, s>>>(C, x, xlen, gmin, scale, dt, cap_v, be_sign, ax,
-                                          rhs_c);
+                                          rhs_c, gdev);
   k_rhs_sum<<<(C.n + 255) / 256, 256, 0, s>>>(C, rhs_c, rhs);
+}
+
+void launch_param_grad(const DCircuit& C, const double* x, int xlen, const double* lam,
+                       double* grad, cudaStream_t s) {
+  k_param_grad<<<(C.ndev + 255) / 256 > 0 ? (C.ndev + 255) / 256 : 1, 256, 0, s>>>(C, x, xlen, lam,
+                                                                                  grad);
 }
 
 void launch_newton_update(int m, int n, double* x, const double* xnew, NewtonState* st,

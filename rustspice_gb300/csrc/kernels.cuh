@@ -11,6 +11,7 @@ struct DPlan {
   const int *col_ptr, *dslot, *slot_row, *upd_ptr, *upd_dst, *col_single;
   const int *amap_ptr, *amap_idx;
   const int *offd_ptr, *offd_col, *offd_raw;
+  const int *offdT_ptr, *offdT_row, *offdT_raw;
   const int *lrow_ptr, *lrow_col, *lrow_slot, *urow_ptr, *urow_col, *urow_slot;
   const int *in_row, *out_col;  // position -> original row / original column
   const int *pcol_ptr, *pcol_raw, *pcol_q, *pos_block, *block_ptr;
@@ -107,7 +108,10 @@ void launch_solve(const DPlan& P, const double* rhs, const double* ax, const dou
                   cudaStream_t s);
 void launch_stamp(const DCircuit& C, const double* x, int xlen, double gmin, double scale,
                   double dt, const double* cap_v, double be_sign, double* ax, double* rhs_c,
-                  double* rhs, cudaStream_t s);
+                  double* rhs, cudaStream_t s, double gdev = 1e-12);
+// dL/dp per device from the adjoint lambda at a DC solution x.
+void launch_param_grad(const DCircuit& C, const double* x, int xlen, const double* lam,
+                       double* grad, cudaStream_t s);
 void launch_newton_update(int m, int n, double* x, const double* xnew, NewtonState* st,
                           NewtonCfg cfg, int* status, cudaStream_t s);
 void launch_rcond(const DPlan& P, const double* lu, double* out2, cudaStream_t s);

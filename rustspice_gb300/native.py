@@ -32,7 +32,7 @@ SYMBOLS = [
     "gpuklu_circuit_set_params", "gpuklu_stamp", "gpuklu_newton_dc", "gpuklu_batch_create",
     "gpuklu_batch_destroy", "gpuklu_batch_run", "gpuklu_batch_results",
     "gpuklu_batch_update_inputs", "gpuklu_batch_last_error", "gpuklu_batch_info",
-    "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_fp64_peak_tflops", "gpuklu_solve_device_noalloc", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free",
+    "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_fp64_peak_tflops", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free",
 ]
 
 
@@ -101,6 +101,7 @@ def lib(build_if_missing: bool = True):
         "gpuklu_batch_work": (C.c_int, [_P, _P, _P]),
         "gpuklu_fp64_peak_tflops": (_D, []),
         "gpuklu_solve_device_noalloc": (C.c_int, [_P, _P, _P]),
+        "gpuklu_dc_backward": (C.c_int, [_P, _P, _P, _I64, _P, _D, _P, _P]),
         "gpuklu_plan_build": (_P, [_I64, _P, _P, C.c_int, _P]),
         "gpuklu_plan_array": (_I64, [_P, C.c_char_p, _P, _I64]),
         "gpuklu_plan_free": (None, [_P]),

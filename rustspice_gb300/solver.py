@@ -188,6 +188,25 @@ def newton_dc(solver: GpuKluSolver, dc: DeviceCircuit, cfg: N.NewtonConfig,
     return NewtonResult(rs.value == 0, it.value, itt.value, REASONS[rs.value], x[:xl.value])
 
 
+def dc_forward(solver: GpuKluSolver, dc: DeviceCircuit, cfg: N.NewtonConfig,
+               x0=None) -> NewtonResult:
+    """Forward half of the DC operating-point function pair (newton_dc)."""
+    return newton_dc(solver, dc, cfg, x0)
+
+
+def dc_backward(solver: GpuKluSolver, dc: DeviceCircuit, x, dl_dx, gmin: float = 1e-12):
+    """Backward half: (lambda, dL/dp per device) at the converged x."""
+    x = N.f64(x)
+    g = N.f64(dl_dx)
+    if len(g) != dc.n:
+        raise ValueError("dl_dx must have n values")
+    lam = np.zeros(dc.n)
+    grad = np.zeros(dc.circuit.ndev)
+    solver._check(N.lib().gpuklu_dc_backward(solver.handle, dc.handle, N.ptr(x), len(x),
+                                             N.ptr(g), gmin, N.ptr(lam), N.ptr(grad)))
+    return lam, grad
+
+
 class Batch:
     """Independent DC operating points of many circuit instances.
 
