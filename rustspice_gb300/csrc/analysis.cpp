@@ -37,8 +37,8 @@ void amd_order(int n, const i64* ap, const i64* ai, std::vector<int>& perm,
     deg[i] = (int)nb[i].size();
     pq.push({deg[i], i});
   }
-  std::vector<unsigned> stamp(n, 0);
-  unsigned tick = 0;
+  std::vector<unsigned> stamp(n, 0), inp(n, 0);
+  unsigned tick = 0, ptick = 0;
   int done = 0;
   std::vector<int> vars, els;
   while (done < n && !pq.empty()) {
@@ -72,13 +72,18 @@ void amd_order(int n, const i64* ap, const i64* ai, std::vector<int>& perm,
         }
     elem[p] = 1;
     nb[p] = vars;
+    ++ptick;  // inp[v] == ptick <=> v is in nb[p]
+    for (int v : vars) inp[v] = ptick;
     for (int e : els) {  // absorb e into p
       if (e == p) continue;
       std::vector<int> moved;
       moved.swap(nb[e]);
       for (int v : moved) {
         if (elem[v]) continue;
-        if (!has(nb[p], v)) nb[p].push_back(v);
+        if (inp[v] != ptick) {
+          inp[v] = ptick;
+          nb[p].push_back(v);
+        }
         auto it = std::find(nb[v].begin(), nb[v].end(), e);
         if (it != nb[v].end()) *it = p;
       }
@@ -246,6 +251,108 @@ BtfResult btf_decompose(int n, const i64* ap, const i64* ai) {
   return b;
 }
 
+// True when the matrix has a perfect matching and its column graph under that
+// matching is strongly connected: a single irreducible block. The block
+// structure of a structurally nonsingular matrix does not depend on which
+// perfect matching is used, so this answers "does the BTF keep more than one
+// block" without the row-order augmenting search above, whose matching is
+// only needed when there are blocks to order. The matching here uses a
+// look-ahead scan of each row before descending (MC21-style).
+bool structurally_irreducible(int n, const i64* ap, const i64* ai) {
+  if (n <= 1) return true;
+  std::vector<int> rp(n + 1, 0), rc;
+  for (int c = 0; c < n; ++c)
+    for (i64 t = ap[c]; t < ap[c + 1]; ++t)
+      if (ai[t] < n) ++rp[(int)ai[t] + 1];
+  for (int r = 0; r < n; ++r) rp[r + 1] += rp[r];
+  rc.resize(rp[n]);
+  {
+    std::vector<int> fill(rp.begin(), rp.end() - 1);
+    for (int c = 0; c < n; ++c)
+      for (i64 t = ap[c]; t < ap[c + 1]; ++t)
+        if (ai[t] < n) rc[fill[(int)ai[t]]++] = c;
+  }
+  std::vector<int> cmatch(n, -1), seen(n, -1), look(n), nxt(n);
+  for (int r = 0; r < n; ++r) look[r] = rp[r];
+  std::vector<int> stk;
+  for (int root = 0; root < n; ++root) {
+    stk.assign(1, root);
+    nxt[root] = rp[root];
+    bool found = false;
+    while (!stk.empty() && !found) {
+      int r = stk.back();
+      for (; look[r] < rp[r + 1]; ++look[r]) {  // look-ahead for a free column
+        int c = rc[look[r]];
+        if (cmatch[c] < 0) {
+          found = true;
+          // augment along the stack: each row takes the column it descended through
+          cmatch[c] = r;
+          for (size_t k = stk.size() - 1; k-- > 0;) {
+            int rr = stk[k];
+            int cc = rc[nxt[rr] - 1];
+            cmatch[cc] = rr;
+          }
+          break;
+        }
+      }
+      if (found) break;
+      int go = -1;
+      while (nxt[r] < rp[r + 1]) {
+        int c = rc[nxt[r]++];
+        if (seen[c] == root) continue;
+        seen[c] = root;
+        go = cmatch[c];
+        break;
+      }
+      if (go >= 0) {
+        nxt[go] = rp[go];
+        stk.push_back(go);
+      } else {
+        stk.pop_back();
+      }
+    }
+    if (!found) return false;  // structurally singular
+  }
+  // column graph: i -> j when column i has an entry in the row matched to j
+  // (edges of the reference's BTF graph); strongly connected <=> node 0
+  // reaches everything forwards and backwards.
+  std::vector<int> rowmatch(n);
+  for (int c = 0; c < n; ++c) rowmatch[cmatch[c]] = c;
+  std::vector<char> vis(n, 0);
+  std::vector<int> q;
+  // forward: from column i, edge to j = rowmatch[r] for every row r of column i
+  q.assign(1, 0);
+  vis[0] = 1;
+  for (size_t h = 0; h < q.size(); ++h) {
+    int i = q[h];
+    for (i64 t = ap[i]; t < ap[i + 1]; ++t) {
+      if (ai[t] >= n) continue;
+      int j = rowmatch[(int)ai[t]];
+      if (!vis[j]) {
+        vis[j] = 1;
+        q.push_back(j);
+      }
+    }
+  }
+  if ((int)q.size() != n) return false;
+  // backward: into column j from every column i having an entry in row cmatch[j]
+  std::fill(vis.begin(), vis.end(), 0);
+  q.assign(1, 0);
+  vis[0] = 1;
+  for (size_t h = 0; h < q.size(); ++h) {
+    int j = q[h];
+    int r = cmatch[j];
+    for (int t = rp[r]; t < rp[r + 1]; ++t) {
+      int i = rc[t];
+      if (!vis[i]) {
+        vis[i] = 1;
+        q.push_back(i);
+      }
+    }
+  }
+  return (int)q.size() == n;
+}
+
 // ------------------------------------------------------------------ symbolic
 // Column k's pattern is the set of rows reachable from A(:,k) through the L
 // columns of earlier columns (Gilbert-Peierls), split into U (< k, plus the
@@ -329,7 +436,7 @@ std::string analyze(int n, const i64* ap, const i64* ai, int pivot_mode, Plan& p
   }
   BtfResult b;
   bool keep = false;
-  if (n >= 4) {
+  if (n >= 4 && !structurally_irreducible(n, ap, ai)) {
     b = btf_decompose(n, ap, ai);
     keep = b.nblocks >= 2 && b.max_block < n;
   }

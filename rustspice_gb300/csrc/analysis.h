@@ -31,6 +31,7 @@ struct BtfResult {
   int nblocks = 0, max_block = 0;
 };
 BtfResult btf_decompose(int n, const i64* ap, const i64* ai);
+bool structurally_irreducible(int n, const i64* ap, const i64* ai);
 
 // Symbolic L/U pattern of an already permuted block, column by column.
 struct Pattern {

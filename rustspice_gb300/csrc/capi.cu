@@ -323,6 +323,14 @@ struct gpuklu_handle {
   gk::Plan plan;
   PlanDev pd;
   std::vector<i64> last_ap, last_ai;
+  // The ordering and symbolic pattern are functions of the sparsity pattern
+  // alone, so the plan analyze() built last (before any pivots were applied)
+  // is kept across reset(): a prepare(n) that changes n and comes back, as
+  // the engine's DC entry does, then costs a pattern compare instead of BTF,
+  // AMD and the symbolic pass. The first factor still chooses fresh pivots.
+  gk::Plan sym_plan;
+  std::vector<i64> sym_ap, sym_ai;
+  int sym_mode = -1;
   cudaStream_t stream = nullptr;
   DBuf<double> d_ax, d_lu, d_z, d_x, d_out, d_rhs, d_work, d_rc, d_rhs_c, d_xnew, d_newx,
       d_scratch2;
@@ -373,8 +381,18 @@ struct gpuklu_handle {
                                              " != expected " + std::to_string(n + 1));
     if (ap[n] != ai_len || ap[0] != 0)
       return fail(GPUKLU_INVALID_MATRIX, "ap[n] does not match the row index count");
-    std::string m = gk::analyze((int)n, ap, ai, pivot_mode, plan);
-    if (!m.empty()) return fail(GPUKLU_INVALID_MATRIX, m);
+    if (sym_mode == pivot_mode && sym_plan.n == n && (int64_t)sym_ap.size() == ap_len &&
+        (int64_t)sym_ai.size() == ai_len && std::equal(sym_ap.begin(), sym_ap.end(), ap) &&
+        std::equal(sym_ai.begin(), sym_ai.end(), ai)) {
+      plan = sym_plan;
+    } else {
+      std::string m = gk::analyze((int)n, ap, ai, pivot_mode, plan);
+      if (!m.empty()) return fail(GPUKLU_INVALID_MATRIX, m);
+      sym_plan = plan;
+      sym_ap.assign(ap, ap + ap_len);
+      sym_ai.assign(ai, ai + ai_len);
+      sym_mode = pivot_mode;
+    }
     last_ap.assign(ap, ap + ap_len);
     last_ai.assign(ai, ai + ai_len);
     int st = upload_plan();
