@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import re
 import os
 import subprocess
 import sys
@@ -172,9 +173,24 @@ def _residual_sample(B, bt, rs, count=64):
     return worst
 
 
+def _ncu_traffic(iters_per_step):
+    """DRAM bytes of one batch run, scaled from the committed ncu summary of
+    k_batch_newton (dram__bytes_read.sum + dram__bytes_write.sum over all size
+    classes of a smaller batch, per Newton iteration)."""
+    path = os.path.join(ROOT, "profiles", "k_batch_newton_inverter_chains.txt")
+    try:
+        with open(path) as f:
+            m = re.search(r"^dram_bytes_per_newton_iteration:\s*([0-9.eE+-]+)", f.read(), re.M)
+        per = float(m.group(1))
+    except (OSError, AttributeError, ValueError):
+        return None, "no ncu summary"
+    return per * iters_per_step, f"{os.path.relpath(path, ROOT)} ({per:.1f} B per iteration)"
+
+
 def run_gpu(a):
     import torch
     from rustspice_gb300 import native as N
+    from rustspice_gb300 import ranks
     from rustspice_gb300 import workloads as wl
     from rustspice_gb300.solver import Batch, DeviceCircuit, GpuKluSolver, newton_dc
 
@@ -184,7 +200,8 @@ def run_gpu(a):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     dev = torch.device("cuda", lrank)
-    B = wl.inverter_batch(a.chains, a.nvin, seed=3)
+    # every rank solves its own seeded batch of the same size (weak scaling)
+    B = wl.inverter_batch(a.chains, a.nvin, seed=ranks.shard_seed(rank))
     bt = Batch(B.circuits, B.inst_circ, B.inst_dev, B.inst_val, B.x0, B.x0_off)
     cfg = N.newton_config(**wl.TIGHT)
     stream = torch.cuda.ExternalStream(bt.stream(), device=dev)
@@ -220,12 +237,9 @@ def run_gpu(a):
         wall = time.perf_counter() - t0
         clocks = clk.stop()
         kern_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-        ms_step = float(np.mean(kern_ms))
-        if ws > 1:
-            t = torch.tensor([ms_step], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms_step = float(t.item())
-        value = iters_per_step * ws / (ms_step * 1e-3)
+        ms_step = ranks.max_over_ranks(float(np.mean(kern_ms)), dev)
+        iters_all = int(ranks.sum_over_ranks(iters_per_step, dev))
+        value = iters_all / (ms_step * 1e-3)
 
         # end-to-end: pinned host inputs -> device, run, every solution -> host
         val_h = torch.from_numpy(np.ascontiguousarray(B.inst_val)).pin_memory()
@@ -239,7 +253,7 @@ def run_gpu(a):
             bt.run(cfg)
             it2, itt2, rs2, x2 = bt.results(with_x=True)
             e2e_ms.append((time.perf_counter() - t1) * 1e3)
-        e2e_step = float(np.median(e2e_ms))
+        e2e_step = ranks.max_over_ranks(float(np.median(e2e_ms)), dev)
         h2d = val_h.numel() * 8 + x0_h.numel() * 8
         d2h = len(x2) * 8 + 3 * 8 * len(it2)
     conv = float(np.mean(rs == 0))
@@ -255,6 +269,7 @@ def run_gpu(a):
     keys = [(B.circuits[c].ndev, B.circuits[c].node_count) for c in B.inst_circ]
     alg_bytes = float(sum(per_key[k] * t for k, t in zip(keys, itt)))
     achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    traffic, traffic_src = _ncu_traffic(iters_per_step)
     flops, _ = bt.work()
     fp64 = float(np.sum(flops.astype(np.float64) * itt))
     fp64_tflops = fp64 / (ms_step * 1e-3) / 1e12
@@ -292,15 +307,16 @@ def run_gpu(a):
                    "initial_iterate": "logic-level nodeset",
                    "l2": "256 MB buffer written before every timed step; inputs 270 MB > L2",
                    "parallelism": f"replicas x{ws}"},
-        "e2e": {"value": iters_per_step * ws / (e2e_step * 1e-3), "unit": UNIT,
+        "e2e": {"value": iters_all / (e2e_step * 1e-3), "unit": UNIT,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": e2e_step},
-        "gpu_launches": a.steps,
+        "gpu_launches": a.steps * bt.info()["launches"],
         "one_at_a_time": {"value": one_at_a_time, "unit": UNIT,
                           "how": "GpuKluSolver newton_dc, one instance at a time, 24 sampled",
                           "batched_over_one_at_a_time": value / one_at_a_time},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "traffic_source": traffic_src,
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                      "algorithmic_bytes_per_step": alg_bytes},
         "roofline_fp64": {"achieved": fp64_tflops, "peak": fp64_peak, "unit": "TFLOP/s",

@@ -221,9 +221,11 @@ int gpuklu_batch_results(gpuklu_batch* b, int64_t* iters, int64_t* iters_total, 
 int gpuklu_batch_update_inputs(gpuklu_batch* b, const double* inst_val, const double* x0);
 /* Last error text of the batch. */
 const char* gpuklu_batch_last_error(const gpuklu_batch* b);
-/* Launch geometry (out has 6 entries): out[0] grid, out[1] threads per
+/* Launch geometry (out has 8 entries): out[0] grid, out[1] threads per
  * block, out[2] program groups, out[3] shared-memory bytes per warp,
- * out[4] registers per thread, out[5] resident blocks per SM. */
+ * out[4] registers per thread, out[5] resident blocks per SM (out[1], out[3..5]
+ * describe the largest class), out[6] kernel launches per gpuklu_batch_run
+ * (one per size class), out[7] reserved (0). */
 int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out);
 /* Work of one Newton iteration of every instance: FP64 operations and the
  * value bytes it moves through on-chip memory (arrays of ninst). */

@@ -320,15 +320,22 @@ struct gpuklu_handle {
   int64_t n = 0;
   int pivot_mode = GPUKLU_PIVOT_REFERENCE;
   State state = EMPTY;
+  // Two plans, both resident on the device. sym_plan is what analyze()
+  // builds from the pattern alone (orderings, pivot-free symbolic pattern);
+  // the first factor runs on it and picks the pivots. plan is sym_plan with
+  // those pivots applied; refactor and solves run on it. Both are functions
+  // of (pattern, mode) and (pattern, mode, pivots) only, so they are kept
+  // across reset(): a prepare(n) that changes n and comes back, as the
+  // engine's DC entry does, costs a pattern compare, and a first factor that
+  // picks the same pivots as last time costs a pivot compare. The first
+  // factor itself always runs, as in the reference.
   gk::Plan plan;
   PlanDev pd;
-  std::vector<i64> last_ap, last_ai;
-  // The ordering and symbolic pattern are functions of the sparsity pattern
-  // alone, so the plan analyze() built last (before any pivots were applied)
-  // is kept across reset(): a prepare(n) that changes n and comes back, as
-  // the engine's DC entry does, then costs a pattern compare instead of BTF,
-  // AMD and the symbolic pass. The first factor still chooses fresh pivots.
   gk::Plan sym_plan;
+  PlanDev pd_sym;
+  bool pd_sym_ok = false, piv_ok = false;
+  std::vector<i32> piv_rperm;
+  std::vector<i64> last_ap, last_ai;
   std::vector<i64> sym_ap, sym_ai;
   int sym_mode = -1;
   cudaStream_t stream = nullptr;
@@ -356,7 +363,6 @@ struct gpuklu_handle {
     state = EMPTY;
     last_ap.clear();
     last_ai.clear();
-    plan = gk::Plan();
     factor_count = refactor_count = 0;
     rcond = 0.0;
     rcond_valid = false;
@@ -375,29 +381,34 @@ struct gpuklu_handle {
     return GPUKLU_OK;
   }
 
+  const gk::Plan& cur_plan() const { return state == FACTORED ? plan : sym_plan; }
+
   int do_analyze(const int64_t* ap, int64_t ap_len, const int64_t* ai, int64_t ai_len) {
     if (ap_len != n + 1)
       return fail(GPUKLU_INVALID_MATRIX, "Column pointer length " + std::to_string(ap_len) +
                                              " != expected " + std::to_string(n + 1));
     if (ap[n] != ai_len || ap[0] != 0)
       return fail(GPUKLU_INVALID_MATRIX, "ap[n] does not match the row index count");
-    if (sym_mode == pivot_mode && sym_plan.n == n && (int64_t)sym_ap.size() == ap_len &&
-        (int64_t)sym_ai.size() == ai_len && std::equal(sym_ap.begin(), sym_ap.end(), ap) &&
-        std::equal(sym_ai.begin(), sym_ai.end(), ai)) {
-      plan = sym_plan;
-    } else {
-      std::string m = gk::analyze((int)n, ap, ai, pivot_mode, plan);
+    if (!(sym_mode == pivot_mode && sym_plan.n == n && (int64_t)sym_ap.size() == ap_len &&
+          (int64_t)sym_ai.size() == ai_len && std::equal(sym_ap.begin(), sym_ap.end(), ap) &&
+          std::equal(sym_ai.begin(), sym_ai.end(), ai))) {
+      pd_sym_ok = piv_ok = false;
+      sym_mode = -1;
+      std::string m = gk::analyze((int)n, ap, ai, pivot_mode, sym_plan);
       if (!m.empty()) return fail(GPUKLU_INVALID_MATRIX, m);
-      sym_plan = plan;
       sym_ap.assign(ap, ap + ap_len);
       sym_ai.assign(ai, ai + ai_len);
       sym_mode = pivot_mode;
     }
     last_ap.assign(ap, ap + ap_len);
     last_ai.assign(ai, ai + ai_len);
-    int st = upload_plan();
-    if (st) return st;
     cudaError_t e = cudaSuccess;
+    if (!pd_sym_ok) {
+      e = pd_sym.upload(sym_plan, stream);
+      if (e != cudaSuccess) return cuda_fail(e, "upload plan");
+      pd_sym_ok = true;
+    }
+    e = d_lu.resize(std::max(sym_plan.nslots(), 1));
     size_t nn = (size_t)std::max<int64_t>(n, 1);
     if (e == cudaSuccess) e = d_ax.resize(std::max<int64_t>(ai_len, 1));
     for (auto* b : {&d_z, &d_x, &d_out, &d_rhs, &d_work, &d_xnew, &d_newx})
@@ -455,7 +466,7 @@ struct gpuklu_handle {
       return check_status("refactor");
     }
     // First factorization: the reference's pivot pass.
-    gk::launch_first_factor(pd.dp, d_ax.p, d_lu.p, d_work.p, d_rperm.p, d_rinv.p, 0.001,
+    gk::launch_first_factor(pd_sym.dp, d_ax.p, d_lu.p, d_work.p, d_rperm.p, d_rinv.p, 0.001,
                             d_status.p, stream);
     std::vector<i32> rperm(n);
     cudaError_t e = cudaMemcpyAsync(rperm.data(), d_rperm.p, n * sizeof(i32),
@@ -464,9 +475,15 @@ struct gpuklu_handle {
     if (e != cudaSuccess) return cuda_fail(e, "first factor");
     int st = check_status("first factor");
     if (st) return st;
-    gk::set_pivots(plan, last_ap.data(), last_ai.data(), rperm);
-    st = upload_plan();
-    if (st) return st;
+    if (!(piv_ok && rperm == piv_rperm)) {
+      piv_ok = false;
+      plan = sym_plan;
+      gk::set_pivots(plan, last_ap.data(), last_ai.data(), rperm);
+      st = upload_plan();
+      if (st) return st;
+      piv_rperm.swap(rperm);
+      piv_ok = true;
+    }
     if (pivot_mode == GPUKLU_PIVOT_EXACT) {  // refactor the exact pattern
       unsigned ep = next_epoch(epoch, d_flags);
       gk::launch_refactor(pd.dp, d_ax.p, d_lu.p, d_flags.p, ep, d_counter.p, d_status.p,
@@ -629,12 +646,13 @@ int gpuklu_get_stats(gpuklu_handle* h, gpuklu_stats* out) {
   }
   out->factor_count = h->factor_count;
   out->refactor_count = h->refactor_count;
-  out->nnz_l = h->plan.nnz_l;
-  out->nnz_u = h->plan.nnz_u;
-  out->nblocks = h->plan.nblocks;
-  out->noffdiag = h->plan.noffdiag;
-  out->pivot_swaps = h->plan.swaps;
-  out->refactor_flops = h->plan.flops_refactor;
+  const gk::Plan& P = h->cur_plan();
+  out->nnz_l = P.nnz_l;
+  out->nnz_u = P.nnz_u;
+  out->nblocks = P.nblocks;
+  out->noffdiag = P.noffdiag;
+  out->pivot_swaps = P.swaps;
+  out->refactor_flops = P.flops_refactor;
   out->rcond = h->state == gpuklu_handle::FACTORED ? h->rcond : 0.0;
   return GPUKLU_OK;
 }
@@ -1478,8 +1496,9 @@ const char* gpuklu_batch_last_error(const gpuklu_batch* b) { return b ? b->err.c
 
 int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out) {
   if (!b) return GPUKLU_INVALID_MATRIX;
-  for (int q = 0; q < 6; ++q) out[q] = 0;
+  for (int q = 0; q < 8; ++q) out[q] = 0;
   out[2] = (int64_t)b->groups.size();
+  out[6] = (int64_t)b->classes.size();
   for (auto& C : b->classes) {  // the largest class (first) describes the launch
     out[0] += C->grid;
     if (out[1] == 0) {

@@ -277,10 +277,11 @@ class Batch:
         return it, itt, rs, x
 
     def info(self) -> dict:
-        out = np.zeros(6, np.int64)
+        out = np.zeros(8, np.int64)
         N.lib().gpuklu_batch_info(self._h, N.ptr(out))
         return dict(grid=int(out[0]), block=int(out[1]), groups=int(out[2]),
-                    smem_per_warp=int(out[3]), regs=int(out[4]), blocks_per_sm=int(out[5]))
+                    smem_per_warp=int(out[3]), regs=int(out[4]), blocks_per_sm=int(out[5]),
+                    launches=int(out[6]))
 
     def work(self):
         """Per instance: FP64 operations and on-chip value bytes of one iteration."""
