@@ -232,6 +232,37 @@ int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out);
 int gpuklu_batch_work(const gpuklu_batch* b, int64_t* flops, int64_t* bytes);
 void* gpuklu_batch_stream(gpuklu_batch* b);
 
+/* ------------------------------------------ batched transient + adjoint */
+/* Fixed-step backward-Euler transient of many circuits, one instance per
+ * circuit, and the discrete adjoint of the loss
+ *   L_i = sum_{t=1..steps} (x_t[probe_i] - target)^2
+ * by checkpointing. This is the transient the reference's engine runs with a
+ * fixed step and BE (crates/sim-core/src/engine.rs:463-602,
+ * stamp.rs:759-787), except that the capacitor companion current has the
+ * physical sign (rhs[a] += (C/dt) v_prev; the reference subtracts it,
+ * stamp.rs:777-784). No reference counterpart exists for the adjoint.
+ * Circuits are given as for gpuklu_batch_create; x_init/x_init_off: each
+ * instance's initial node voltages; every ckpt_every steps the forward run
+ * keeps the state, and the backward run recomputes each segment from it.
+ * The handle is released with gpuklu_batch_destroy. */
+gpuklu_batch* gpuklu_tran_create(int64_t ncirc, const int64_t* dev_off,
+                                 const int64_t* node_counts, const int32_t* type,
+                                 const int32_t* nodes, const double* p, const double* x_init,
+                                 const int64_t* x_init_off, int64_t x_init_len, double dt,
+                                 int64_t steps, int64_t ckpt_every, const int64_t* probe,
+                                 double target);
+/* Forward run: per instance the loss, optionally the probe waveform
+ * (ninst x steps), the Newton iterations and the reason (0 every step
+ * converged, 1 a step failed; its loss is NaN). */
+int gpuklu_tran_forward(gpuklu_batch* b, const gpuklu_newton_config* cfg, double* loss_out,
+                        double* wave_out, int64_t* iters_out, int32_t* reason_out);
+/* Backward run after a forward run with the same cfg: dL_i/dC for every
+ * capacitor of instance i (0 for other devices), concatenated over the
+ * instances in device order; iters_out: Newton iterations of the
+ * recomputation. */
+int gpuklu_tran_backward(gpuklu_batch* b, const gpuklu_newton_config* cfg, double* grad_out,
+                         int64_t* iters_out);
+
 /* Measured FP64 fused multiply-add throughput of the current device in
  * TFLOP/s (a short microbenchmark; the denominator of FP64 roofline
  * fractions). */

@@ -166,6 +166,37 @@ int orc_dc_op(int64_t node_count, int64_t ndev, const int32_t* type,
   return r.reason;
 }
 
+// Fixed-step backward Euler (tran_be). states: (steps+1) * node_count.
+int orc_tran(int64_t node_count, int64_t ndev, const int32_t* type, const int32_t* nodes,
+             const double* p, const char* solver_kind, int64_t max_iters, double abs_tol,
+             double rel_tol, double gmin, double dt, int64_t steps, const double* x_init,
+             double* states, int64_t* iters) {
+  Circuit c = make_circuit(node_count, ndev, type, nodes, p);
+  NewtonConfig cfg;
+  cfg.max_iters = (size_t)max_iters;
+  cfg.abs_tol = abs_tol;
+  cfg.rel_tol = rel_tol;
+  cfg.gmin = gmin;
+  Vec st;
+  size_t it = 0;
+  int r = tran_be(c, cfg, solver_kind, dt, (size_t)steps, x_init, st, it);
+  std::copy(st.begin(), st.end(), states);
+  *iters = (int64_t)it;
+  return r;
+}
+
+// Discrete adjoint of orc_tran's loss (tran_adjoint); grad has ndev entries.
+int orc_tran_adjoint(int64_t node_count, int64_t ndev, const int32_t* type,
+                     const int32_t* nodes, const double* p, double dt, int64_t steps,
+                     const double* states, int64_t probe, double target, double gmin,
+                     double* grad) {
+  Circuit c = make_circuit(node_count, ndev, type, nodes, p);
+  Vec st(states, states + (size_t)(steps + 1) * (size_t)node_count), g;
+  int r = tran_adjoint(c, dt, (size_t)steps, st, (size_t)probe, target, gmin, g);
+  std::copy(g.begin(), g.end(), grad);
+  return r;
+}
+
 double orc_residual(int64_t node_count, int64_t ndev, const int32_t* type,
                     const int32_t* nodes, const double* p, const double* x,
                     int64_t xlen, double gmin) {

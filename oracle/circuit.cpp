@@ -126,9 +126,14 @@ MosOut eval_level1(double vth0, double u0, double tox, double w, double l,
 MosJ eval_level1_consistent(double vth0, double u0, double tox, double w,
                             double l, double vd, double vg, double vs,
                             bool is_pmos, double gdev) {
-  // Same level-1 equations and constants as eval_level1; the polarity is
-  // applied to every terminal voltage and the drain/source roles swap when
-  // vds < 0, so (ddg, ddd, dds) are the exact partials of id.
+  // Level 1 with the constants of eval_level1 (lambda 0.02, beta from u0
+  // and tox) in the Shichman-Hodges form: the (1 + lambda vds) factor
+  // multiplies the current in the linear region too, so the current and its
+  // partials are continuous where the linear and saturation regions meet
+  // (the reference's linear region omits the factor, a 2 % current step
+  // there on which Newton can cycle). The polarity is applied to every
+  // terminal voltage and the drain/source roles swap when vds < 0, so
+  // (ddg, ddd, dds) are the exact partials of id.
   const double lambda = 0.02;
   double beta = u0 * 1e-4 * (kEpsOx / tox);
   double pol = is_pmos ? -1.0 : 1.0;
@@ -144,9 +149,11 @@ MosJ eval_level1_consistent(double vth0, double u0, double tox, double w,
     gm = 0.0;
     gds = gdev;
   } else if (vdse < vgse - vth) {
-    ids = beff * ((vgse - vth) * vdse - 0.5 * vdse * vdse);
-    gm = beff * vdse;
-    gds = std::fmax(beff * ((vgse - vth) - vdse), gdev);
+    const double k = 1.0 + lambda * vdse;
+    const double q = (vgse - vth) * vdse - 0.5 * vdse * vdse;
+    ids = beff * q * k;
+    gm = beff * vdse * k;
+    gds = std::fmax(beff * ((vgse - vth) - vdse) * k + lambda * beff * q, gdev);
   } else {
     double t = vgse - vth;
     ids = 0.5 * beff * (t * t) * (1.0 + lambda * vdse);
@@ -398,6 +405,127 @@ double residual_inf(const Circuit& c, const Vec& x, double gmin) {
   }
   double den = an * xn + bn;
   return den > 0.0 ? rn / den : rn;
+}
+
+
+// ---------------------------------------------------------------- transient
+namespace {
+struct TranCtx {
+  const Circuit* c;
+  double dt;
+  TranState st;
+};
+MnaSystem tran_build(void* p, const Vec& x, double gmin, double scale) {
+  auto* t = static_cast<TranCtx*>(p);
+  return build_mna(*t->c, x, gmin, scale, t->dt, &t->st, 1.0);
+}
+
+// Dense LU with partial pivoting (row-major), in place; piv[k] = row swapped
+// into k. Returns false on an exactly zero pivot.
+bool dense_lu(std::vector<double>& a, size_t n, std::vector<size_t>& piv) {
+  piv.resize(n);
+  for (size_t k = 0; k < n; ++k) {
+    size_t p = k;
+    double best = std::fabs(a[k * n + k]);
+    for (size_t i = k + 1; i < n; ++i)
+      if (std::fabs(a[i * n + k]) > best) {
+        best = std::fabs(a[i * n + k]);
+        p = i;
+      }
+    if (best == 0.0) return false;
+    piv[k] = p;
+    if (p != k)
+      for (size_t j = 0; j < n; ++j) std::swap(a[k * n + j], a[p * n + j]);
+    for (size_t i = k + 1; i < n; ++i) {
+      const double l = a[i * n + k] / a[k * n + k];
+      a[i * n + k] = l;
+      for (size_t j = k + 1; j < n; ++j) a[i * n + j] -= l * a[k * n + j];
+    }
+  }
+  return true;
+}
+
+// Solves A^T y = b with P A = L U: U^T z = b, L^T w = z, y = P^T w.
+void dense_tsolve(const std::vector<double>& lu, size_t n, const std::vector<size_t>& piv,
+                  Vec& b) {
+  for (size_t k = 0; k < n; ++k) {
+    double s = b[k];
+    for (size_t j = 0; j < k; ++j) s -= lu[j * n + k] * b[j];
+    b[k] = s / lu[k * n + k];
+  }
+  for (size_t k = n; k-- > 0;) {
+    double s = b[k];
+    for (size_t i = k + 1; i < n; ++i) s -= lu[i * n + k] * b[i];
+    b[k] = s;
+  }
+  for (size_t k = n; k-- > 0;)
+    if (piv[k] != k) std::swap(b[k], b[piv[k]]);
+}
+}  // namespace
+
+int tran_be(const Circuit& c, const NewtonConfig& cfg, const std::string& solver_kind,
+            double dt, size_t steps, const double* x_init, Vec& states, size_t& iters) {
+  const size_t nc = c.node_count;
+  states.assign((steps + 1) * nc, 0.0);
+  Vec x(x_init, x_init + nc);
+  std::copy(x.begin(), x.end(), states.begin());
+  TranCtx ctx{&c, dt, {}};
+  ctx.st.cap_v.assign(c.ndev(), 0.0);
+  auto solver = make_solver(solver_kind, nc);
+  iters = 0;
+  for (size_t t = 1; t <= steps; ++t) {
+    for (size_t d = 0; d < c.ndev(); ++d)
+      if (c.type[d] == DEV_C) {
+        const int a = c.nodes[d * 4], b = c.nodes[d * 4 + 1];
+        ctx.st.cap_v[d] = x[(size_t)a] - x[(size_t)b];
+      }
+    Vec xn(x.begin(), x.begin() + nc);
+    NewtonResult r = run_newton(cfg, xn, tran_build, &ctx, cfg.gmin, 1.0, *solver);
+    iters += r.iterations;
+    if (!r.converged) return r.reason == NR_CONVERGED ? NR_MAXITERS : r.reason;
+    std::copy(xn.begin(), xn.begin() + nc, x.begin());
+    std::copy(x.begin(), x.end(), states.begin() + t * nc);
+  }
+  return 0;
+}
+
+int tran_adjoint(const Circuit& c, double dt, size_t steps, const Vec& states, size_t probe,
+                 double target, double gmin, Vec& grad) {
+  const size_t nc = c.node_count;
+  grad.assign(c.ndev(), 0.0);
+  Vec lam_next;  // lambda_{t+1}
+  TranState st;
+  st.cap_v.assign(c.ndev(), 0.0);
+  for (size_t t = steps; t >= 1; --t) {
+    Vec xt(states.begin() + t * nc, states.begin() + (t + 1) * nc);
+    MnaSystem s = build_mna(c, xt, gmin, 1.0, dt, &st, 1.0, 0.0);
+    const size_t n = s.n;
+    std::vector<double> a(n * n, 0.0);
+    for (size_t col = 0; col < n; ++col)
+      for (i64 q = s.ap[col]; q < s.ap[col + 1]; ++q) a[(size_t)s.ai[q] * n + col] += s.ax[q];
+    std::vector<size_t> piv;
+    if (!dense_lu(a, n, piv)) return 1;
+    if (lam_next.empty()) lam_next.assign(n, 0.0);
+    Vec rhs(n, 0.0);
+    rhs[probe] += 2.0 * (xt[probe] - target);
+    for (size_t d = 0; d < c.ndev(); ++d)
+      if (c.type[d] == DEV_C) {
+        const size_t ca = (size_t)c.nodes[d * 4], cb = (size_t)c.nodes[d * 4 + 1];
+        const double gl = c.p[d * NPARAM] / dt * (lam_next[ca] - lam_next[cb]);
+        rhs[ca] += gl;
+        rhs[cb] -= gl;
+      }
+    dense_tsolve(a, n, piv, rhs);
+    const double* xp = &states[(t - 1) * nc];
+    for (size_t d = 0; d < c.ndev(); ++d)
+      if (c.type[d] == DEV_C) {
+        const size_t ca = (size_t)c.nodes[d * 4], cb = (size_t)c.nodes[d * 4 + 1];
+        const double dv = (xt[ca] - xt[cb]) - (xp[ca] - xp[cb]);
+        grad[d] -= (rhs[ca] - rhs[cb]) * dv / dt;
+      }
+    lam_next = rhs;
+  }
+  return 0;
 }
 
 }  // namespace oracle

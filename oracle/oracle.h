@@ -247,8 +247,9 @@ enum DevType : int32_t {
   // terminal voltages and the drain/source roles swapped when vds < 0. The
   // reference's evaluator flips PMOS into a frame where the stamped gm/gds are
   // not the derivatives of the stamped current, so its Newton diverges on
-  // CMOS circuits; this type is the documented physical alternative. Same
-  // parameters as DEV_M.
+  // CMOS circuits; this type is the documented physical alternative, in the
+  // Shichman-Hodges form (lambda factor in the linear region too, so the
+  // current is continuous between regions). Same parameters as DEV_M.
   DEV_MC = 6,
 };
 constexpr int NPARAM = 6;
@@ -340,5 +341,27 @@ NewtonResult dc_op(const Circuit& c, const NewtonConfig& cfg,
 double residual_inf(const Circuit& c, const Vec& x, double gmin);
 
 std::unique_ptr<LinearSolver> make_solver(const std::string& kind, size_t n);
+
+// ---------------------------------------------------------------- transient
+// Fixed-step backward Euler with the physical companion sign (the transient
+// the reference's engine would run with `.tran dt` and BE, crates/sim-core/
+// src/engine.rs:463-602 with stamp.rs:759-787, fixed step, no LTE control):
+// every step is a Newton solve from the previous time point, capacitor
+// voltages from the previous time point, one solver whose pivots freeze at
+// the first factorization. `states` returns (steps + 1) x node_count values
+// (the initial state first). Returns the first failing step's Newton reason
+// (0 when every step converged); `iters` sums the Newton iterations.
+int tran_be(const Circuit& c, const NewtonConfig& cfg, const std::string& solver_kind,
+            double dt, size_t steps, const double* x_init, Vec& states, size_t& iters);
+
+// Discrete adjoint of tran_be for L = sum_{t=1..steps} (x_t[probe] - target)^2:
+// lambda_t solves J_t^T lambda_t = dL/dx_t + G_C lambda_{t+1} with the exact
+// Jacobian J_t at x_t (level-1 floor 0) and G_C the capacitor conductances;
+// dL/dC_d = -sum_t (lambda_t[a] - lambda_t[b]) (dv_t - dv_{t-1}) / dt.
+// grad[d] receives dL/dp[d][0] for capacitors (0 elsewhere). Dense LU with
+// partial pivoting for the transposed solves. Returns 0, or 1 on a singular
+// Jacobian.
+int tran_adjoint(const Circuit& c, double dt, size_t steps, const Vec& states, size_t probe,
+                 double target, double gmin, Vec& grad);
 
 }  // namespace oracle

@@ -52,6 +52,11 @@ def lib():
         L.orc_dc_op.restype = C.c_int
         L.orc_dc_op.argtypes = [_I64, _I64, _P, _P, _P, C.c_char_p, _I64, _D, _D, _D,
                                 _I64, _I64, _P, _P, _I64, _P, _P]
+        L.orc_tran.restype = C.c_int
+        L.orc_tran.argtypes = [_I64, _I64, _P, _P, _P, C.c_char_p, _I64, _D, _D, _D, _D, _I64,
+                               _P, _P, _P]
+        L.orc_tran_adjoint.restype = C.c_int
+        L.orc_tran_adjoint.argtypes = [_I64, _I64, _P, _P, _P, _D, _I64, _P, _I64, _D, _D, _P]
         L.orc_residual.restype = _D
         L.orc_residual.argtypes = [_I64, _I64, _P, _P, _P, _P, _I64, _D]
         L.orc_dc_batch.argtypes = [_I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, C.c_char_p,
@@ -183,6 +188,32 @@ def dc_op(c, solver="nativeklu", max_iters=100, abs_tol=1e-6, rel_tol=1e-3,
                         _ptr(x0a) if x0a is not None else None, _ptr(x), cap, C.byref(xl),
                         C.byref(it))
     return REASONS[r], it.value, x[:xl.value]
+
+
+def tran(c, x_init, dt, steps, solver="nativeklu_exact", max_iters=100, abs_tol=1e-12,
+         rel_tol=1e-10, gmin=1e-12):
+    """Fixed-step backward Euler. Returns (reason, iterations, states[steps+1, nc])."""
+    _, t, nd, p = _circ_arrays(c)
+    xi = _f64(x_init)
+    st = np.zeros((steps + 1) * c.node_count)
+    it = C.c_int64()
+    r = lib().orc_tran(c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p), solver.encode(),
+                       max_iters, abs_tol, rel_tol, gmin, dt, steps, _ptr(xi), _ptr(st),
+                       C.byref(it))
+    return r, it.value, st.reshape(steps + 1, c.node_count)
+
+
+def tran_adjoint(c, states, dt, probe, target, gmin=1e-12):
+    """dL/dC per device (capacitors) for L = sum_t (x_t[probe] - target)^2."""
+    _, t, nd, p = _circ_arrays(c)
+    st = _f64(states).ravel()
+    steps = states.shape[0] - 1
+    g = np.zeros(c.ndev)
+    r = lib().orc_tran_adjoint(c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p), dt, steps,
+                               _ptr(st), probe, target, gmin, _ptr(g))
+    if r != 0:
+        raise RuntimeError("singular Jacobian in the transient adjoint")
+    return g
 
 
 def residual(c, x, gmin=1e-12):

@@ -21,11 +21,15 @@ MC     as M
 ``M`` is the reference's level-1 evaluator exactly (crates/sim-devices/src/
 bsim/evaluate.rs:285-356). Its PMOS branch negates and swaps the terminals
 into a frame where the stamped gm and gds are not the derivatives of the
-stamped current, so Newton diverges on CMOS inverters from a zero start.
-``MC`` ("consistent") keeps the same level-1 equations and constants but
-applies the polarity to every terminal voltage and swaps the drain/source
-roles for vds < 0, so the stamp is an exact linearisation. The CMOS
-workloads use ``MC`` by default; ``mos_model="reference"`` selects ``M``.
+stamped current, so Newton diverges on CMOS inverters from a zero start, and
+its linear region omits the (1 + lambda vds) factor, so the current steps by
+~2 % where the linear and saturation regions meet (Newton can cycle on that
+step in a transient). ``MC`` ("consistent") keeps the reference's constants
+(lambda 0.02, beta from u0 and tox) in the Shichman-Hodges form (the factor
+in both regions), applies the polarity to every terminal voltage and swaps
+the drain/source roles for vds < 0, so the current is continuous and the
+stamp is its exact linearisation. The CMOS workloads use ``MC`` by default;
+``mos_model="reference"`` selects ``M``.
 
 Random numbers come from a counter-based splitmix64 stream, so a circuit
 depends only on its seed and is identical on every host.

@@ -1,0 +1,413 @@
+// Building blocks of the batched kernels (DC Newton, transient forward and
+// transient adjoint). One warp works on M instances of one circuit program
+// at a time, LPI = 32/M lanes per instance, with every value of an instance
+// in shared memory:
+//   X[nc]   iterate (node voltages)      XP[nc] previous time point
+//   T[n]    permuted right-hand side / solution
+//   DV[ndv] device value records         V[nv]  LU values + BTF coupling
+// The group's program (column records, slot rows, update lists) is staged in
+// the warp's shared memory; everything else of the program is read through
+// the read-only path.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace gk {
+namespace bt {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// Contribution lists longer than this are summed across the instance's
+// lanes instead of by one lane.
+constexpr int kHeavy = 12;
+
+__device__ __forceinline__ double contrib(const double* dv, int code) {
+  const int kind = code & 7, idx = code >> 3;
+  switch (kind) {
+    case 0: return dv[idx];
+    case 1: return -dv[idx];
+    case 2: return 1.0;
+    case 3: return -1.0;
+    default: return 0.0;
+  }
+}
+
+// Device value record: R [g]; V [value]; I [value]; D [g, ieq];
+// M [gds, gm, ieq]; MC [ddd, dds, ddg, ieq]; C (transient) [g, ieq].
+// Circuit constants per device: R [1/R]; V, I [value]; D [Is, vt, Is/vt];
+// M [is_pmos, vth0, beff]; MC [polarity, |vth0|, beff]; C [C, C/dt].
+// gdev is the level-1 conductance floor (1e-12 as the reference has it; 0
+// for the exact Jacobian of the adjoint).
+__device__ __forceinline__ void eval_record(int type, const int* nd, const double* dp,
+                                            const double* X, const double* XP, int nc,
+                                            double gmin, double gdev, double* rec) {
+  auto xg = [&](int i) { return (i >= 0 && i < nc) ? X[i] : 0.0; };
+  switch (type) {
+    case 0:
+    case 1:
+    case 2:
+      rec[0] = dp[0];
+      break;
+    case 3: {  // crates/sim-core/src/stamp.rs:351-387
+      const double gf = gmin > 0.0 ? gmin : 1e-12;
+      const double vd = xg(nd[0]) - xg(nd[1]);
+      const double e = exp(vd / dp[1]);
+      const double id = dp[0] * (e - 1.0);
+      const double gd = dp[2] * e;
+      rec[0] = fmax(gd, gf);
+      rec[1] = id - gd * vd;
+      break;
+    }
+    case 4: {  // level 1 as the reference evaluates it (evaluate.rs:285-356)
+      const double lambda = 0.02;
+      const double gf = gmin > 0.0 ? gmin : 1e-12;
+      const bool pm = dp[0] != 0.0;
+      const double vd = xg(nd[0]), vg = xg(nd[1]), vs = xg(nd[2]);
+      double vdi = pm ? -vs : vd, vgi = pm ? -vg : vg, vsi = pm ? -vd : vs;
+      double vgs = vgi - vsi, vds = vdi - vsi;
+      if (vds < 0.0) {
+        vds = -vds;
+        vgs = vgi - vdi;
+      }
+      const double vth = pm ? -fabs(dp[1]) : fabs(dp[1]);
+      const double beff = dp[2];
+      double ids, gm, gds;
+      if (vgs <= vth) {
+        ids = 0.0;
+        gm = 0.0;
+        gds = gdev;
+      } else if (vds < vgs - vth) {
+        ids = beff * ((vgs - vth) * vds - 0.5 * vds * vds);
+        gm = beff * vds;
+        gds = fmax(beff * ((vgs - vth) - vds), gdev);
+      } else {
+        const double t = vgs - vth;
+        ids = 0.5 * beff * (t * t) * (1.0 + lambda * vds);
+        gm = beff * (vgs - vth) * (1.0 + lambda * vds);
+        gds = fmax(0.5 * beff * (t * t) * lambda, gdev);
+      }
+      const double ids_s = pm ? -ids : ids;
+      rec[0] = fmax(gds, gf);
+      rec[1] = gm;
+      rec[2] = ids_s - gm * (vg - vs) - gds * (vd - vs);
+      break;
+    }
+    case 5: {  // backward-Euler capacitor companion, physical sign
+      const double g = dp[1];
+      const double vp = ((nd[0] >= 0 && nd[0] < nc) ? XP[nd[0]] : 0.0) -
+                        ((nd[1] >= 0 && nd[1] < nc) ? XP[nd[1]] : 0.0);
+      rec[0] = g;
+      rec[1] = g * vp;
+      break;
+    }
+    case 6: {  // consistent level 1, Shichman-Hodges form
+      const double lambda = 0.02;
+      const double pol = dp[0];
+      const double vd = xg(nd[0]), vg = xg(nd[1]), vs = xg(nd[2]);
+      const double vgs = pol * (vg - vs), vds = pol * (vd - vs);
+      const bool rev = vds < 0.0;
+      const double vgse = rev ? vgs - vds : vgs, vdse = rev ? -vds : vds;
+      const double vth = dp[1], beff = dp[2];
+      double ids, gm, gds;
+      if (vgse <= vth) {
+        ids = 0.0;
+        gm = 0.0;
+        gds = gdev;
+      } else if (vdse < vgse - vth) {  // Shichman-Hodges: (1 + lambda vds) here too
+        const double k = 1.0 + lambda * vdse;
+        const double q = (vgse - vth) * vdse - 0.5 * vdse * vdse;
+        ids = beff * q * k;
+        gm = beff * vdse * k;
+        gds = fmax(beff * ((vgse - vth) - vdse) * k + lambda * beff * q, gdev);
+      } else {
+        const double t = vgse - vth;
+        ids = 0.5 * beff * (t * t) * (1.0 + lambda * vdse);
+        gm = beff * (vgse - vth) * (1.0 + lambda * vdse);
+        gds = fmax(0.5 * beff * (t * t) * lambda, gdev);
+      }
+      double id, ddg, ddd, dds;
+      if (!rev) {
+        id = pol * ids;
+        ddg = gm;
+        ddd = gds;
+        dds = -(gm + gds);
+      } else {
+        id = -pol * ids;
+        ddg = -gm;
+        ddd = gm + gds;
+        dds = -gds;
+      }
+      rec[0] = ddd;
+      rec[1] = dds;
+      rec[2] = ddg;
+      rec[3] = id - (ddg * vg + ddd * vd + dds * vs);
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+__device__ __forceinline__ int record_len(int type, bool transient) {
+  return type == 6 ? 4 : type == 4 ? 3 : type == 3 ? 2 : type == 5 ? (transient ? 2 : 0) : 1;
+}
+
+// 1/d for the batched factorization: a single-precision seed built from d's
+// bits on the integer pipe, the hardware float reciprocal, and one FP64
+// Newton step (relative error about 1e-14). FP64 operations have a 64-cycle
+// dependent latency on this part, so this is about half the latency of the
+// correctly rounded reciprocal, which serves magnitudes outside the
+// single-precision range.
+__device__ __forceinline__ double fast_rcp(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e < 1023 - 120 || e > 1023 + 120) return __drcp_rn(d);
+  const unsigned fb = (unsigned)((b >> 32) & 0x80000000u) | ((unsigned)(e - 1023 + 127) << 23) |
+                      (unsigned)((b >> 29) & 0x7fffffu);
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(__uint_as_float(fb)));
+  const unsigned rb = __float_as_uint(rf);
+  const unsigned long long r64 =
+      ((unsigned long long)(rb & 0x80000000u) << 32) |
+      ((unsigned long long)(((rb >> 23) & 0xff) - 127 + 1023) << 52) |
+      ((unsigned long long)(rb & 0x7fffffu) << 29);
+  const double r = __longlong_as_double((long long)r64);
+  return fma(r, fma(-d, r, 1.0), r);
+}
+
+__device__ __forceinline__ bool nonzero(double u) {
+  return (__double_as_longlong(u) << 1) != 0;
+}
+
+// The reference's pivot perturbation (native_klu.rs:1229-1231, :1345-1348)
+// on the bit pattern: integer compares instead of FP64 pipe compares.
+__device__ __forceinline__ double perturb_bits(double d, bool singleton) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned long long a = b & 0x7fffffffffffffffull;
+  if (singleton)
+    return a < (unsigned long long)__double_as_longlong(1e-300) ? 1e-14 : d;
+  if (a < (unsigned long long)__double_as_longlong(1e-14))
+    return (a == 0 || (b >> 63) == 0) ? 1e-14 : -1e-14;
+  return d;
+}
+
+// One group's program as the phases below read it.
+struct Prog {
+  const int4* colrec;  // staged: (s0, dslot, s1, singleton) per column
+  const int* srow;     // staged: slot rows
+  const int* uptr;     // staged: update-list offsets per slot
+  const int* udst;     // staged: update destinations
+  const int *dev_type, *dev_nodes, *dev_dv, *amap_ptr, *amap_code, *rmap_ptr, *rmap_code,
+      *in_row, *out_pos, *offd_ptr, *offd_col, *bptr, *heavy;
+  int n, nc, nv, nslots, ndev, nblocks, nheavy;
+};
+
+// Stages the group's factor and solve structure into the warp's shared
+// memory and returns the program view.
+__device__ __forceinline__ Prog stage_program(const BatchArgs& A, const GroupHdr& G, int* prog,
+                                              int lane) {
+  Prog P;
+  const int n = G.n;
+  int4* const colrec = reinterpret_cast<int4*>(prog);
+  int* const srow = prog + 4 * n;
+  int* const uptr = srow + G.nslots;
+  int* const udst = uptr + G.nslots;
+  {
+    const int* cp = A.col_ptr + G.col_off;
+    const int* dsl = A.dslot + G.col_off;
+    const int* cs = A.col_single + G.col_off;
+    for (int k = lane; k < n; k += 32) colrec[k] = make_int4(cp[k], dsl[k], cp[k + 1], cs[k]);
+    const int* sr = A.slot_row + G.slot_off;
+    const int* up = A.upd_ptr + G.slot_off;
+    for (int q = lane; q < G.nslots; q += 32) {
+      srow[q] = sr[q];
+      uptr[q] = up[q];
+    }
+    const int* ud = A.upd_dst + G.upd_off;
+    for (int q = lane; q < G.nupd; q += 32) udst[q] = ud[q];
+  }
+  __syncwarp();
+  P.colrec = colrec;
+  P.srow = srow;
+  P.uptr = uptr;
+  P.udst = udst;
+  P.dev_type = A.dev_type + G.dev_off;
+  P.dev_nodes = A.dev_nodes + 4 * G.dev_off;
+  P.dev_dv = A.dev_dv + G.dev_off;
+  P.amap_ptr = A.amap_ptr + G.amap_off;
+  P.amap_code = A.amap_code + G.amap_code_off;
+  P.rmap_ptr = A.rmap_ptr + G.rmap_off;
+  P.rmap_code = A.rmap_code + G.rmap_code_off;
+  P.in_row = A.in_row + G.col_off;
+  P.out_pos = A.out_pos + G.col_off;
+  P.offd_ptr = A.offd_ptr + G.col_off;
+  P.offd_col = A.offd_col + G.offd_off;
+  P.bptr = A.block_ptr + G.blk_off;
+  P.heavy = A.heavy + G.heavy_off;
+  P.n = n;
+  P.nc = G.node_count;
+  P.nslots = G.nslots;
+  P.nv = G.nslots + G.noffd;
+  P.ndev = G.ndev;
+  P.nblocks = G.nblocks;
+  P.nheavy = G.nheavy;
+  return P;
+}
+
+// Device evaluation of one instance into its value records (lanes over
+// devices). ov_dev/ov_val override the first constant of one device.
+template <int LPI>
+__device__ __forceinline__ void stamp_devices(const Prog& P, const double* dparams, int ov_dev,
+                                              double ov_val, const double* X, const double* XP,
+                                              double gmin, double gdev, bool transient,
+                                              double* DV, int sl) {
+  for (int d = sl; d < P.ndev; d += LPI) {
+    double dp[4];
+    const double* src = dparams + 4 * d;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) dp[k] = __ldg(src + k);
+    if (d == ov_dev) dp[0] = ov_val;
+    double rec[4];
+    const int type = P.dev_type[d];
+    eval_record(type, P.dev_nodes + 4 * d, dp, X, XP, P.nc, gmin, gdev, rec);
+    const int o = P.dev_dv[d];
+    const int nrec = record_len(type, transient);
+    for (int k = 0; k < nrec; ++k) DV[o + k] = rec[k];
+  }
+}
+
+// LU slot values and the permuted right-hand side from the value records:
+// short contribution lists one lane each, long ones (the ground and supply
+// rows and columns) reduced across the instance's lanes.
+template <int LPI>
+__device__ __forceinline__ void assemble(const Prog& P, const double* DV, double* V, double* T,
+                                         int sl) {
+  for (int v = sl; v < P.nv; v += LPI) {
+    const int t0 = P.amap_ptr[v], t1 = P.amap_ptr[v + 1];
+    if (t1 - t0 > kHeavy) continue;
+    double acc = 0.0;
+    for (int t = t0; t < t1; ++t) acc += contrib(DV, P.amap_code[t]);
+    V[v] = acc;
+  }
+  for (int i = sl; i < P.n; i += LPI) {
+    const int r = P.in_row[i];
+    const int t0 = P.rmap_ptr[r], t1 = P.rmap_ptr[r + 1];
+    if (t1 - t0 > kHeavy) continue;
+    double acc = 0.0;
+    for (int t = t0; t < t1; ++t) acc += contrib(DV, P.rmap_code[t]);
+    T[i] = acc;
+  }
+  for (int h = 0; h < P.nheavy; ++h) {
+    const int code = P.heavy[h];  // (index << 1) | is_row
+    const int idx = code >> 1;
+    const int* ptr = (code & 1) ? P.rmap_ptr : P.amap_ptr;
+    const int* cds = (code & 1) ? P.rmap_code : P.amap_code;
+    const int key = (code & 1) ? P.in_row[idx] : idx;
+    const int t0 = ptr[key], t1 = ptr[key + 1];
+    double acc = 0.0;
+    for (int t = t0 + sl; t < t1; t += LPI) acc += contrib(DV, cds[t]);
+#pragma unroll
+    for (int o = LPI / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if (sl == 0) {
+      if (code & 1)
+        T[idx] = acc;
+      else
+        V[idx] = acc;
+    }
+  }
+}
+
+// Factor + forward substitution, then backward substitution, block by block
+// (blocks in order; the BTF coupling lies below the diagonal blocks).
+// Afterwards V[dslot] holds the reciprocal of the (perturbed) pivot and T
+// the permuted solution.
+template <int LPI>
+__device__ __forceinline__ void factor_solve(const Prog& P, double* V, double* T, int sl) {
+  for (int b = 0; b < P.nblocks; ++b) {
+    const int b0 = P.bptr[b], b1 = P.bptr[b + 1];
+    for (int i = b0 + sl; i < b1; i += LPI)
+      for (int e = P.offd_ptr[i]; e < P.offd_ptr[i + 1]; ++e)
+        T[i] = fma(-V[P.nslots + e], T[P.offd_col[e]], T[i]);
+    __syncwarp();
+    for (int k = b0; k < b1; ++k) {
+      const int4 ck = P.colrec[k];
+      for (int s = ck.x; s < ck.y; ++s) {
+        const double u = V[s];
+        if (nonzero(u)) {
+          const int4 cj = P.colrec[P.srow[s]];
+          const int q0 = cj.y + 1;
+          const int* dst = P.udst + P.uptr[s] - q0;
+          for (int qq = q0 + sl; qq < cj.z; qq += LPI) {
+            const int dd = dst[qq];
+            V[dd] = fma(-V[qq], u, V[dd]);
+          }
+        }
+        __syncwarp();
+      }
+      const double r = fast_rcp(perturb_bits(V[ck.y], ck.w != 0));
+      const double zk = T[k];
+      for (int qq = ck.y + 1 + sl; qq < ck.z; qq += LPI) {
+        const double l = V[qq] * r;
+        V[qq] = l;
+        const int row = P.srow[qq];
+        T[row] = fma(-l, zk, T[row]);
+      }
+      if (sl == 0) V[ck.y] = r;
+      __syncwarp();
+    }
+    for (int k = b1 - 1; k >= b0; --k) {
+      const int4 ck = P.colrec[k];
+      const double xk = T[k] * V[ck.y];
+      for (int s = ck.x + sl; s < ck.y; s += LPI) {
+        const int row = P.srow[s];
+        T[row] = fma(-V[s], xk, T[row]);
+      }
+      __syncwarp();
+      if (sl == 0) T[k] = xk;
+      __syncwarp();
+    }
+  }
+}
+
+// Transpose solve with the factors factor_solve left in V: on entry T holds
+// the right-hand side in permuted column order (T[out_pos[c]] = g[c]); on
+// exit T holds w with lambda[in_row[i]] = w[i]. Blocks in reverse order:
+// U^T forward, L^T backward, then the block's coupling scattered into the
+// earlier blocks by one lane (few entries).
+template <int LPI>
+__device__ __forceinline__ void tsolve(const Prog& P, const double* V, double* T, int sl) {
+  constexpr unsigned smask = kFull;  // all M instances of the warp run in step
+  for (int b = P.nblocks - 1; b >= 0; --b) {
+    const int b0 = P.bptr[b], b1 = P.bptr[b + 1];
+    for (int k = b0; k < b1; ++k) {  // U^T y = r
+      const int4 ck = P.colrec[k];
+      double acc = 0.0;
+      for (int s = ck.x + sl; s < ck.y; s += LPI) acc = fma(V[s], T[P.srow[s]], acc);
+#pragma unroll
+      for (int o = LPI / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(smask, acc, o);
+      const double yk = (T[k] - acc) * V[ck.y];
+      __syncwarp(smask);
+      if (sl == 0) T[k] = yk;
+      __syncwarp(smask);
+    }
+    for (int k = b1 - 1; k >= b0; --k) {  // L^T w = y
+      const int4 ck = P.colrec[k];
+      double acc = 0.0;
+      for (int q = ck.y + 1 + sl; q < ck.z; q += LPI) acc = fma(V[q], T[P.srow[q]], acc);
+#pragma unroll
+      for (int o = LPI / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(smask, acc, o);
+      const double wk = T[k] - acc;
+      __syncwarp(smask);
+      if (sl == 0) T[k] = wk;
+      __syncwarp(smask);
+    }
+    if (sl == 0)
+      for (int i = b0; i < b1; ++i)
+        for (int e = P.offd_ptr[i]; e < P.offd_ptr[i + 1]; ++e)
+          T[P.offd_col[e]] = fma(-V[P.nslots + e], T[i], T[P.offd_col[e]]);
+    __syncwarp(smask);
+  }
+}
+
+}  // namespace bt
+}  // namespace gk

@@ -916,6 +916,18 @@ struct gpuklu_batch {
   std::vector<std::unique_ptr<Class>> classes;
   cudaEvent_t start_ev = nullptr;
   gk::BatchArgs args{};
+  // transient
+  int transient = 0;
+  double dt = 0.0;
+  int64_t steps = 0, ckpt_every = 0;
+  int tran_region = 0, tran_prog = 0, tran_grid_f = 0, tran_grid_b = 0;
+  std::vector<long long> grad_off_h;
+  int64_t grad_len = 0;
+  DBuf<i32> d_inst_group, d_probe;
+  DBuf<double> d_loss, d_wave, d_ckpt, d_seg, d_grad;
+  DBuf<long long> d_ckpt_off, d_seg_off, d_grad_off;
+  DBuf<unsigned> d_tcounter;
+  bool tran_fwd_done = false;
 
   ~gpuklu_batch() {
     for (auto& c : classes) {
@@ -957,19 +969,19 @@ struct Program {
   }
 };
 
-int record_size(int type) {
+int record_size(int type, bool transient) {
   switch (type) {
     case 3: return 2;
     case 4: return 3;
     case 6: return 4;
-    case 5: return 0;
+    case 5: return transient ? 2 : 0;
     default: return 1;
   }
 }
 
 // Contribution codes of every matrix insert and rhs add of one device, in
 // the reference's insert order (see compile_circuit).
-void device_codes(int type, int dv, int m[8], int r[2]) {
+void device_codes(int type, int dv, bool transient, int m[8], int r[2]) {
   auto c = [dv](int k, int kind) { return ((dv + k) << 3) | kind; };
   for (int e = 0; e < 8; ++e) m[e] = -1;
   r[0] = r[1] = -1;
@@ -998,6 +1010,12 @@ void device_codes(int type, int dv, int m[8], int r[2]) {
       m[4] = c(2, 0); m[5] = -1; m[6] = c(2, 1); m[7] = -1;  // the +0.0 inserts add nothing
       r[0] = c(3, 1); r[1] = c(3, 0);
       break;
+    case 5:  // backward-Euler companion [g, ieq], physical sign: rhs a += ieq
+      if (transient) {
+        m[0] = c(0, 0); m[1] = c(0, 0); m[2] = c(0, 1); m[3] = c(0, 1);
+        r[0] = c(1, 0); r[1] = c(1, 1);
+      }
+      break;
     default:
       break;
   }
@@ -1024,7 +1042,7 @@ Program make_program(const gpuklu_circuit& C, const gk::Plan& P) {
     for (int q = 0; q < 4; ++q) g.dev_nodes.push_back(C.nodes[(size_t)d * 4 + q]);
     g.dev_dv.push_back(ndv);
     int m[8], r[2];
-    device_codes(t, ndv, m, r);
+    device_codes(t, ndv, C.transient != 0, m, r);
     for (int e = 0; e < 8; ++e) {
       const int raw = C.raw[(size_t)d * 8 + e];
       if (raw < 0 || m[e] < 0) continue;
@@ -1037,8 +1055,8 @@ Program make_program(const gpuklu_circuit& C, const gk::Plan& P) {
     const int rb = (t == 4 || t == 6) ? nd[2] : nd[1];
     if (r[0] >= 0) rlist[ra].push_back(r[0]);
     if (r[1] >= 0) rlist[rb].push_back(r[1]);
-    ndv += record_size(t);
-    dev_flops += t == 6 ? 32 : t == 4 ? 30 : t == 3 ? 30 : 0;
+    ndv += record_size(t, C.transient != 0);
+    dev_flops += t == 6 ? 32 : t == 4 ? 30 : t == 3 ? 30 : (t == 5 && C.transient) ? 3 : 0;
   }
   if (C.pin_raw >= 0 && P.raw_slot[C.pin_raw] >= 0) vlist[P.raw_slot[C.pin_raw]].push_back(2);
   h.ndv = std::max(ndv, h.node_count);
@@ -1096,7 +1114,7 @@ Program make_program(const gpuklu_circuit& C, const gk::Plan& P) {
 // beff = (u0*1e-4*(EPSILON_OX/tox))*W/L (bsim/mod.rs:445, params.rs:10,
 // 460-462, evaluate.rs:318).
 void circuit_constants(int64_t ndev, const int32_t* type, const double* p,
-                       std::vector<double>& out) {
+                       std::vector<double>& out, double dt = 0.0) {
   const double eps_ox = 3.9 * 8.854e-12;
   for (int64_t d = 0; d < ndev; ++d) {
     const double* q = p + 6 * d;
@@ -1120,6 +1138,10 @@ void circuit_constants(int64_t ndev, const int32_t* type, const double* p,
         c[2] = beta * q[4] / q[5];
         break;
       }
+      case 5:  // C, and C/dt for the backward-Euler companion
+        c[0] = q[0];
+        c[1] = dt > 0.0 ? q[0] / dt : 0.0;
+        break;
       default: c[0] = q[0]; break;
     }
     out.insert(out.end(), c, c + 4);
@@ -1129,12 +1151,29 @@ void circuit_constants(int64_t ndev, const int32_t* type, const double* p,
 
 extern "C" {
 
-gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
-                                  const int64_t* node_counts, const int32_t* type,
-                                  const int32_t* nodes, const double* p, int64_t ninst,
-                                  const int64_t* inst_circ, const int64_t* inst_dev,
-                                  const double* inst_val, const double* x0,
-                                  const int64_t* x0_off, int64_t x0_len) {
+}  // extern "C"
+
+namespace {
+gk::NewtonCfg to_newton_cfg(const gpuklu_newton_config& cfg) {
+  gk::NewtonCfg c{};
+  c.max_iters = (int)cfg.max_iters;
+  c.gmin_steps = (int)cfg.gmin_steps;
+  c.abs_tol = cfg.abs_tol;
+  c.rel_tol = cfg.rel_tol;
+  c.gmin = cfg.gmin;
+  c.damping = cfg.damping;
+  c.damping_min = cfg.damping_min;
+  return c;
+}
+
+// Groups, programs, constants and launch classes of a batch. transient: the
+// circuits are compiled with their capacitors' backward-Euler companions
+// for step dt (pivots are chosen on the matrix with those conductances).
+gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* node_counts,
+                          const int32_t* type, const int32_t* nodes, const double* p,
+                          int64_t ninst, const int64_t* inst_circ, const int64_t* inst_dev,
+                          const double* inst_val, const double* x0, const int64_t* x0_off,
+                          int64_t x0_len, int transient, double dt) {
   auto B = std::make_unique<gpuklu_batch>();
   B->ncirc = ncirc;
   B->ninst = ninst;
@@ -1159,10 +1198,10 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
   for (int64_t c = 0; c < ncirc; ++c) {
     const int64_t d0 = dev_off[c], nd = dev_off[c + 1] - d0;
     circ_poff[c] = (long long)dparams.size();
-    circuit_constants(nd, type + d0, p + 6 * d0, dparams);
+    circuit_constants(nd, type + d0, p + 6 * d0, dparams, transient ? dt : 0.0);
     if (first[c] < 0) continue;
     gpuklu_circuit* C = gpuklu_compile_devices(node_counts[c], nd, type + d0, nodes + 4 * d0,
-                                               p + 6 * d0, 0);
+                                               p + 6 * d0, transient);
     if (!C) {
       gpuklu_destroy(H);
       return nullptr;
@@ -1178,8 +1217,8 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
     std::vector<double> ax(C->ai.size()), rhs(C->n);
     gpuklu_prepare(H, C->n);
     gpuklu_reset_pattern(H);
-    int st = gpuklu_stamp(H, C, xr.data(), (int64_t)xr.size(), 1e-12, 1.0, 0.0, nullptr, -1.0,
-                          ax.data(), rhs.data());
+    int st = gpuklu_stamp(H, C, xr.data(), (int64_t)xr.size(), 1e-12, 1.0, transient ? dt : 0.0,
+                          nullptr, 1.0, ax.data(), rhs.data());
     if (st == GPUKLU_OK)
       st = gpuklu_factor(H, C->ap.data(), (int64_t)C->ap.size(), C->ai.data(),
                          (int64_t)C->ai.size(), ax.data());
@@ -1409,7 +1448,180 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
     C->args.region = C->region;
     C->args.prog_ints = C->prog_ints;
   }
+  B->transient = transient;
+  B->dt = dt;
   return B.release();
+}
+}  // namespace
+
+extern "C" {
+
+gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
+                                  const int64_t* node_counts, const int32_t* type,
+                                  const int32_t* nodes, const double* p, int64_t ninst,
+                                  const int64_t* inst_circ, const int64_t* inst_dev,
+                                  const double* inst_val, const double* x0,
+                                  const int64_t* x0_off, int64_t x0_len) {
+  return batch_build(ncirc, dev_off, node_counts, type, nodes, p, ninst, inst_circ, inst_dev,
+                     inst_val, x0, x0_off, x0_len, 0, 0.0);
+}
+
+gpuklu_batch* gpuklu_tran_create(int64_t ncirc, const int64_t* dev_off,
+                                 const int64_t* node_counts, const int32_t* type,
+                                 const int32_t* nodes, const double* p, const double* x_init,
+                                 const int64_t* x_init_off, int64_t x_init_len, double dt,
+                                 int64_t steps, int64_t ckpt_every, const int64_t* probe,
+                                 double target) {
+  if (ncirc <= 0 || !(dt > 0.0) || steps <= 0 || ckpt_every <= 0 || !x_init || !x_init_off ||
+      !probe) {
+    fprintf(stderr, "gpuklu_tran_create: invalid arguments\n");
+    return nullptr;
+  }
+  for (int64_t i = 0; i < ncirc; ++i)
+    if (probe[i] < 0 || probe[i] >= node_counts[i] || x_init_off[i] < 0 ||
+        x_init_off[i] + node_counts[i] > x_init_len) {
+      fprintf(stderr, "gpuklu_tran_create: instance %ld: probe or initial state out of range\n",
+              (long)i);
+      return nullptr;
+    }
+  std::vector<int64_t> ic(ncirc);
+  for (int64_t i = 0; i < ncirc; ++i) ic[i] = i;
+  std::unique_ptr<gpuklu_batch> B(batch_build(ncirc, dev_off, node_counts, type, nodes, p, ncirc,
+                                              ic.data(), nullptr, nullptr, x_init, x_init_off,
+                                              x_init_len, 1, dt));
+  if (!B) return nullptr;
+  const int64_t ninst = ncirc;
+  B->steps = steps;
+  B->ckpt_every = ckpt_every;
+  const int64_t nck = steps / ckpt_every + 1;
+  std::vector<long long> ck_off(ninst), seg_off(ninst);
+  std::vector<i32> probe_h(ninst);
+  B->grad_off_h.assign(ninst, 0);
+  long long ck = 0, sg = 0, go = 0;
+  int region = 0, prog = 0;
+  for (int64_t i = 0; i < ninst; ++i) {
+    const gk::GroupHdr& h = B->groups[B->inst_group_h[i]];
+    region = std::max(region, 2 * h.node_count + 2 * h.n + h.ndv + h.nslots + h.noffd + h.ndev);
+    prog = std::max(prog, (4 * h.n + 2 * h.nslots + h.nupd + 3) & ~3);
+    ck_off[i] = ck;
+    ck += nck * h.node_count;
+    seg_off[i] = sg;
+    sg += (ckpt_every + 1) * h.node_count;
+    B->grad_off_h[i] = go;
+    go += h.ndev;
+    probe_h[i] = (i32)probe[i];
+  }
+  region = (region + 1) & ~1;
+  B->tran_region = region;
+  B->tran_prog = prog;
+  B->grad_len = go;
+  cudaStream_t s = B->stream;
+  cudaError_t e = B->d_inst_group.upload(B->inst_group_h, s);
+  if (e == cudaSuccess) e = B->d_probe.upload(probe_h, s);
+  if (e == cudaSuccess) e = B->d_ckpt_off.upload(ck_off, s);
+  if (e == cudaSuccess) e = B->d_seg_off.upload(seg_off, s);
+  if (e == cudaSuccess) e = B->d_grad_off.upload(B->grad_off_h, s);
+  if (e == cudaSuccess) e = B->d_loss.resize(ninst);
+  if (e == cudaSuccess) e = B->d_ckpt.resize(std::max<long long>(ck, 1));
+  if (e == cudaSuccess) e = B->d_seg.resize(std::max<long long>(sg, 1));
+  if (e == cudaSuccess) e = B->d_grad.resize(std::max<long long>(go, 1));
+  if (e == cudaSuccess) e = B->d_tcounter.resize(1);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "gpuklu_tran_create: %s\n", cudaGetErrorString(e));
+    return nullptr;
+  }
+  int regs = 0, bf = 0, bb = 0;
+  gk::tran_kernel_info(false, 1, region, prog, &regs, &bf);
+  gk::tran_kernel_info(true, 1, region, prog, &regs, &bb);
+  if (bf <= 0 || bb <= 0) {
+    fprintf(stderr, "gpuklu_tran_create: a circuit needs %d KB of shared memory\n",
+            (int)((region * 8 + prog * 4) / 1024));
+    return nullptr;
+  }
+  B->tran_grid_f = (int)std::min<int64_t>(ninst, (int64_t)sm_count() * bf);
+  B->tran_grid_b = (int)std::min<int64_t>(ninst, (int64_t)sm_count() * bb);
+  gk::BatchArgs& a = B->args;
+  a.ninst = (int)ninst;
+  a.inst_group = B->d_inst_group.p;
+  a.dt = dt;
+  a.inv_dt = 1.0 / dt;
+  a.steps = (int)steps;
+  a.ckpt_every = (int)ckpt_every;
+  a.probe = B->d_probe.p;
+  a.target = target;
+  a.loss = B->d_loss.p;
+  a.wave = nullptr;
+  a.ckpt = B->d_ckpt.p;
+  a.ckpt_off = B->d_ckpt_off.p;
+  a.seg = B->d_seg.p;
+  a.seg_off = B->d_seg_off.p;
+  a.grad = B->d_grad.p;
+  a.grad_off = B->d_grad_off.p;
+  a.region = region;
+  a.prog_ints = prog;
+  a.counter = B->d_tcounter.p;
+  return B.release();
+}
+
+int gpuklu_tran_forward(gpuklu_batch* b, const gpuklu_newton_config* cfg, double* loss_out,
+                        double* wave_out, int64_t* iters_out, int32_t* reason_out) {
+  if (!b || !cfg || !b->transient) return GPUKLU_INVALID_MATRIX;
+  gk::BatchArgs a = b->args;
+  a.cfg = to_newton_cfg(*cfg);
+  cudaStream_t s = b->stream;
+  cudaError_t e = cudaSuccess;
+  if (wave_out) {
+    e = b->d_wave.resize((size_t)b->ninst * (size_t)b->steps);
+    a.wave = b->d_wave.p;
+  }
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return b->fail(cuda_msg(e, "transient forward"));
+  gk::launch_tran_forward(a, b->tran_grid_f, 1, s);
+  const int64_t ni = b->ninst;
+  std::vector<i32> it(ni), rs(ni);
+  e = cudaGetLastError();
+  if (e == cudaSuccess && loss_out)
+    e = cudaMemcpyAsync(loss_out, b->d_loss.p, ni * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && wave_out)
+    e = cudaMemcpyAsync(wave_out, b->d_wave.p, (size_t)ni * b->steps * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(it.data(), b->d_iters_total.p, ni * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rs.data(), b->d_reason.p, ni * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return b->fail(cuda_msg(e, "transient forward"));
+  for (int64_t i = 0; i < ni; ++i) {
+    if (iters_out) iters_out[i] = it[i];
+    if (reason_out) reason_out[i] = rs[i];
+  }
+  b->tran_fwd_done = true;
+  return GPUKLU_OK;
+}
+
+int gpuklu_tran_backward(gpuklu_batch* b, const gpuklu_newton_config* cfg, double* grad_out,
+                         int64_t* iters_out) {
+  if (!b || !cfg || !b->transient) return GPUKLU_INVALID_MATRIX;
+  if (!b->tran_fwd_done) {
+    b->err = "gpuklu_tran_backward needs a completed gpuklu_tran_forward";
+    return GPUKLU_SOLVE_FAILED;
+  }
+  gk::BatchArgs a = b->args;
+  a.cfg = to_newton_cfg(*cfg);
+  cudaStream_t s = b->stream;
+  cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return b->fail(cuda_msg(e, "transient backward"));
+  gk::launch_tran_backward(a, b->tran_grid_b, 1, s);
+  const int64_t ni = b->ninst;
+  std::vector<i32> it(ni);
+  e = cudaGetLastError();
+  if (e == cudaSuccess && grad_out)
+    e = cudaMemcpyAsync(grad_out, b->d_grad.p, b->grad_len * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(it.data(), b->d_iters.p, ni * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return b->fail(cuda_msg(e, "transient backward"));
+  if (iters_out)
+    for (int64_t i = 0; i < ni; ++i) iters_out[i] = it[i];
+  return GPUKLU_OK;
 }
 
 void gpuklu_batch_destroy(gpuklu_batch* b) {
@@ -1422,14 +1634,7 @@ void gpuklu_batch_destroy(gpuklu_batch* b) {
 
 int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
   if (!b || !cfg) return GPUKLU_INVALID_MATRIX;
-  gk::NewtonCfg c{};
-  c.max_iters = (int)cfg->max_iters;
-  c.gmin_steps = (int)cfg->gmin_steps;
-  c.abs_tol = cfg->abs_tol;
-  c.rel_tol = cfg->rel_tol;
-  c.gmin = cfg->gmin;
-  c.damping = cfg->damping;
-  c.damping_min = cfg->damping_min;
+  const gk::NewtonCfg c = to_newton_cfg(*cfg);
   cudaStream_t s = b->stream;
   cudaMemsetAsync(b->d_gnext.p, 0, b->d_gnext.n * sizeof(unsigned), s);
   for (auto& C : b->classes) cudaMemsetAsync(C->d_counter.p, 0, sizeof(unsigned), s);

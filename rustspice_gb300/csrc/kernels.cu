@@ -31,6 +31,7 @@
 // CPU evaluation in the reference's order.
 #include <cstdio>
 
+#include "batch_common.cuh"
 #include "device.cuh"
 #include "kernels.cuh"
 
@@ -337,8 +338,10 @@ __device__ void mos_reference(const double* p, double vd, double vg, double vs, 
   ieq = ids_s - gm * (vg - vs) - gds * (vd - vs);
 }
 
-// Level-1 MOSFET with a self-consistent linearisation: drain current and its
-// partials with respect to (vg, vd, vs).
+// Level-1 MOSFET in the Shichman-Hodges form (the (1 + lambda vds) factor in
+// both regions, so the current is continuous where they meet) with a
+// self-consistent linearisation: drain current and its partials with respect
+// to (vg, vd, vs).
 __device__ void mos_consistent(const double* p, double vd, double vg, double vs, double& id,
                                double& ddg, double& ddd, double& dds, double gmin_dev) {
   const double lambda = 0.02;
@@ -354,10 +357,12 @@ __device__ void mos_consistent(const double* p, double vd, double vg, double vs,
     ids = 0.0;
     gm = 0.0;
     gds = gmin_dev;
-  } else if (vdse < vgse - vth) {
-    ids = beff * ((vgse - vth) * vdse - 0.5 * vdse * vdse);
-    gm = beff * vdse;
-    gds = fmax(beff * ((vgse - vth) - vdse), gmin_dev);
+  } else if (vdse < vgse - vth) {  // Shichman-Hodges: (1 + lambda vds) here too
+    const double k = 1.0 + lambda * vdse;
+    const double q = (vgse - vth) * vdse - 0.5 * vdse * vdse;
+    ids = beff * q * k;
+    gm = beff * vdse * k;
+    gds = fmax(beff * ((vgse - vth) - vdse) * k + lambda * beff * q, gmin_dev);
   } else {
     const double t = vgse - vth;
     ids = 0.5 * beff * (t * t) * (1.0 + lambda * vdse);
@@ -565,7 +570,9 @@ __global__ void k_param_grad(DCircuit C, const double* __restrict__ x, int xlen,
         sgn = pm ? -1.0 : 1.0;
       }
       double gm = 0.0;
-      if (vgs > vth) gm = vds < vgs - vth ? beff * vds : beff * (vgs - vth) * (1.0 + 0.02 * vds);
+      if (vgs > vth)
+        gm = vds < vgs - vth ? beff * vds * (C.type[d] == 6 ? 1.0 + 0.02 * vds : 1.0)
+                             : beff * (vgs - vth) * (1.0 + 0.02 * vds);
       // dvth/dVTO: |VTO| -> sign(VTO); the reference's PMOS uses -|VTO|
       double dvth = p[1] >= 0.0 ? 1.0 : -1.0;
       if (C.type[d] == 4 && pm) dvth = -dvth;
@@ -691,11 +698,9 @@ __global__ void k_rcond(DPlan P, const double* __restrict__ lu, double* out) {
 }
 
 // --------------------------------------------------------------- batched
-// One warp owns one circuit instance at a time and keeps all of its state in
-// shared memory: iterate x[nc], solve vector t[n], device value records
-// dv[ndv] and the LU values v[nslots+noffd]. Program arrays (the group's
-// symbolic plan) and circuit constants are read through the read-only path;
-// each iteration touches global memory only for them.
+// One warp owns M instances of one circuit program at a time and keeps all
+// of their state in shared memory (batch_common.cuh); each Newton iteration
+// touches global memory only for the program and the circuit constants.
 //   stamp     - lanes evaluate devices (strided) into their value records
 //   assemble  - lanes sum each LU slot's and each rhs row's contributions in
 //               stamping order (bit-identical to the reference's scatter)
@@ -704,169 +709,9 @@ __global__ void k_rcond(DPlan P, const double* __restrict__ lu, double* out) {
 //               substitution of the right-hand side is fused in
 //   backward  - U sweep, lanes over a column's U entries
 //   update    - convergence test, damping and iterate update
-__device__ __forceinline__ double contrib(const double* dv, int code) {
-  const int kind = code & 7, idx = code >> 3;
-  switch (kind) {
-    case 0: return dv[idx];
-    case 1: return -dv[idx];
-    case 2: return 1.0;
-    case 3: return -1.0;
-    default: return 0.0;
-  }
-}
-
-// Device value record (see eval): R [g]; V [value]; I [value]; D [g, ieq];
-// M [gds, gm, ieq]; MC [ddd, dds, ddg, ieq]. Circuit constants per device:
-// R [1/R]; V, I [value]; D [Is, vt, Is/vt]; M [is_pmos, vth0, beff];
-// MC [polarity, |vth0|, beff].
-__device__ __forceinline__ void eval_record(int type, const int* nd, const double* dp,
-                                            const double* X, int nc, double gmin, double* rec) {
-  auto xg = [&](int i) { return (i >= 0 && i < nc) ? X[i] : 0.0; };
-  switch (type) {
-    case 0:
-    case 1:
-    case 2:
-      rec[0] = dp[0];
-      break;
-    case 3: {  // crates/sim-core/src/stamp.rs:351-387
-      const double gf = gmin > 0.0 ? gmin : 1e-12;
-      const double vd = xg(nd[0]) - xg(nd[1]);
-      const double e = exp(vd / dp[1]);
-      const double id = dp[0] * (e - 1.0);
-      const double gd = dp[2] * e;
-      rec[0] = fmax(gd, gf);
-      rec[1] = id - gd * vd;
-      break;
-    }
-    case 4: {  // level 1 as the reference evaluates it (evaluate.rs:285-356)
-      const double lambda = 0.02, gdev = 1e-12;
-      const double gf = gmin > 0.0 ? gmin : 1e-12;
-      const bool pm = dp[0] != 0.0;
-      const double vd = xg(nd[0]), vg = xg(nd[1]), vs = xg(nd[2]);
-      double vdi = pm ? -vs : vd, vgi = pm ? -vg : vg, vsi = pm ? -vd : vs;
-      double vgs = vgi - vsi, vds = vdi - vsi;
-      if (vds < 0.0) {
-        vds = -vds;
-        vgs = vgi - vdi;
-      }
-      const double vth = pm ? -fabs(dp[1]) : fabs(dp[1]);
-      const double beff = dp[2];
-      double ids, gm, gds;
-      if (vgs <= vth) {
-        ids = 0.0;
-        gm = 0.0;
-        gds = gdev;
-      } else if (vds < vgs - vth) {
-        ids = beff * ((vgs - vth) * vds - 0.5 * vds * vds);
-        gm = beff * vds;
-        gds = fmax(beff * ((vgs - vth) - vds), gdev);
-      } else {
-        const double t = vgs - vth;
-        ids = 0.5 * beff * (t * t) * (1.0 + lambda * vds);
-        gm = beff * (vgs - vth) * (1.0 + lambda * vds);
-        gds = fmax(0.5 * beff * (t * t) * lambda, gdev);
-      }
-      const double ids_s = pm ? -ids : ids;
-      rec[0] = fmax(gds, gf);
-      rec[1] = gm;
-      rec[2] = ids_s - gm * (vg - vs) - gds * (vd - vs);
-      break;
-    }
-    case 6: {  // consistent level 1
-      const double lambda = 0.02, gdev = 1e-12;
-      const double pol = dp[0];
-      const double vd = xg(nd[0]), vg = xg(nd[1]), vs = xg(nd[2]);
-      const double vgs = pol * (vg - vs), vds = pol * (vd - vs);
-      const bool rev = vds < 0.0;
-      const double vgse = rev ? vgs - vds : vgs, vdse = rev ? -vds : vds;
-      const double vth = dp[1], beff = dp[2];
-      double ids, gm, gds;
-      if (vgse <= vth) {
-        ids = 0.0;
-        gm = 0.0;
-        gds = gdev;
-      } else if (vdse < vgse - vth) {
-        ids = beff * ((vgse - vth) * vdse - 0.5 * vdse * vdse);
-        gm = beff * vdse;
-        gds = fmax(beff * ((vgse - vth) - vdse), gdev);
-      } else {
-        const double t = vgse - vth;
-        ids = 0.5 * beff * (t * t) * (1.0 + lambda * vdse);
-        gm = beff * (vgse - vth) * (1.0 + lambda * vdse);
-        gds = fmax(0.5 * beff * (t * t) * lambda, gdev);
-      }
-      double id, ddg, ddd, dds;
-      if (!rev) {
-        id = pol * ids;
-        ddg = gm;
-        ddd = gds;
-        dds = -(gm + gds);
-      } else {
-        id = -pol * ids;
-        ddg = -gm;
-        ddd = gm + gds;
-        dds = -gds;
-      }
-      rec[0] = ddd;
-      rec[1] = dds;
-      rec[2] = ddg;
-      rec[3] = id - (ddg * vg + ddd * vd + dds * vs);
-      break;
-    }
-    default:
-      break;
-  }
-}
-
-// 1/d for the batched factorization: a single-precision seed built from d's
-// bits on the integer pipe, the hardware float reciprocal, and one FP64
-// Newton step (relative error about 1e-14). FP64 operations have a 64-cycle
-// dependent latency on this part, so this is about half the latency of the
-// correctly rounded reciprocal, which serves magnitudes outside the
-// single-precision range.
-__device__ __forceinline__ double fast_rcp(double d) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const int e = (int)((b >> 52) & 0x7ff);
-  if (e < 1023 - 120 || e > 1023 + 120) return __drcp_rn(d);
-  const unsigned fb = (unsigned)((b >> 32) & 0x80000000u) | ((unsigned)(e - 1023 + 127) << 23) |
-                      (unsigned)((b >> 29) & 0x7fffffu);
-  float rf;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(__uint_as_float(fb)));
-  const unsigned rb = __float_as_uint(rf);
-  const unsigned long long r64 =
-      ((unsigned long long)(rb & 0x80000000u) << 32) |
-      ((unsigned long long)(((rb >> 23) & 0xff) - 127 + 1023) << 52) |
-      ((unsigned long long)(rb & 0x7fffffu) << 29);
-  const double r = __longlong_as_double((long long)r64);
-  return fma(r, fma(-d, r, 1.0), r);
-}
-
-// Contribution lists longer than this are summed across the instance's
-// lanes instead of by one lane.
-constexpr int kHeavy = 12;
-
-__device__ __forceinline__ bool nonzero(double u) {
-  return (__double_as_longlong(u) << 1) != 0;
-}
-
-// The reference's pivot perturbation (native_klu.rs:1229-1231, :1345-1348)
-// on the bit pattern: integer compares instead of FP64 pipe compares.
-__device__ __forceinline__ double perturb_bits(double d, bool singleton) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const unsigned long long a = b & 0x7fffffffffffffffull;
-  if (singleton)
-    return a < (unsigned long long)__double_as_longlong(1e-300) ? 1e-14 : d;
-  if (a < (unsigned long long)__double_as_longlong(1e-14))
-    return (a == 0 || (b >> 63) == 0) ? 1e-14 : -1e-14;
-  return d;
-}
-
 // M instances per warp, 32/M lanes each; the M instances run the same
 // program (one group), so the warp's control flow is shared and every FP64
 // warp instruction of the sequential factor and solve serves M instances.
-// A block works on one group at a time and first stages the group's factor
-// and solve structure (per-column records, slot rows, update lists) in its
-// shared memory, so the sequential critical path reads only shared memory.
 template <int M>
 __global__ void k_batch_newton(BatchArgs A) {
   constexpr int LPI = 32 / M;
@@ -890,45 +735,12 @@ __global__ void k_batch_newton(BatchArgs A) {
     if (ti >= A.ntiles) return;
     const int g = A.tile_group[ti];
     const GroupHdr G = A.groups[g];
-    const int n = G.n, nc = G.node_count, nv = G.nslots + G.noffd;
-    // ---- stage the program: colrec[4n] = (s0, ds, s1, singleton), slot_row,
-    // upd_ptr, upd_dst
-    int4* const colrec = reinterpret_cast<int4*>(prog);
-    int* const srow = prog + 4 * n;
-    int* const uptr = srow + G.nslots;
-    int* const udst = uptr + G.nslots;
-    {
-      const int* cp = A.col_ptr + G.col_off;
-      const int* dsl = A.dslot + G.col_off;
-      const int* cs = A.col_single + G.col_off;
-      for (int k = lane; k < n; k += 32) colrec[k] = make_int4(cp[k], dsl[k], cp[k + 1], cs[k]);
-      const int* sr = A.slot_row + G.slot_off;
-      const int* up = A.upd_ptr + G.slot_off;
-      for (int q = lane; q < G.nslots; q += 32) {
-        srow[q] = sr[q];
-        uptr[q] = up[q];
-      }
-      const int* ud = A.upd_dst + G.upd_off;
-      for (int q = lane; q < G.nupd; q += 32) udst[q] = ud[q];
-    }
-    __syncwarp();
+    const bt::Prog P = bt::stage_program(A, G, prog, lane);
+    const int n = P.n, nc = P.nc;
     double* const X = region;
     double* const T = X + nc;
     double* const DV = T + n;
     double* const V = DV + G.ndv;
-    const int* dev_type = A.dev_type + G.dev_off;
-    const int* dev_nodes = A.dev_nodes + 4 * G.dev_off;
-    const int* dev_dv = A.dev_dv + G.dev_off;
-    const int* amap_ptr = A.amap_ptr + G.amap_off;
-    const int* amap_code = A.amap_code + G.amap_code_off;
-    const int* rmap_ptr = A.rmap_ptr + G.rmap_off;
-    const int* rmap_code = A.rmap_code + G.rmap_code_off;
-    const int* in_row = A.in_row + G.col_off;
-    const int* out_pos = A.out_pos + G.col_off;
-    const int* offd_ptr = A.offd_ptr + G.col_off;
-    const int* offd_col = A.offd_col + G.offd_off;
-    const int* bptr = A.block_ptr + G.blk_off;
-    const int* heavy = A.heavy + G.heavy_off;
 
     int inst = -1, it = 0, total = 0, gstep = 0, ov_dev = -1;
     bool exhausted = false;
@@ -964,110 +776,15 @@ __global__ void k_batch_newton(BatchArgs A) {
       if (!__any_sync(FULL, inst >= 0)) break;
       __syncwarp();
       const bool live = inst >= 0;
-      // ---- stamp
-      if (live) {
-        for (int d = sl; d < G.ndev; d += LPI) {
-          double dp[4];
-          const double* src = dparams + 4 * d;
-#pragma unroll
-          for (int k = 0; k < 4; ++k) dp[k] = __ldg(src + k);
-          if (d == ov_dev) dp[0] = ov_val;
-          double rec[4];
-          const int type = dev_type[d];
-          eval_record(type, dev_nodes + 4 * d, dp, X, nc, gmin, rec);
-          const int o = dev_dv[d];
-          const int nrec = type == 6 ? 4 : type == 4 ? 3 : type == 3 ? 2 : type == 5 ? 0 : 1;
-          for (int k = 0; k < nrec; ++k) DV[o + k] = rec[k];
-        }
-      }
+      if (live) bt::stamp_devices<LPI>(P, dparams, ov_dev, ov_val, X, X, gmin, 1e-12, false, DV, sl);
       __syncwarp();
-      // ---- assemble LU slots and the permuted right-hand side: short
-      // contribution lists one lane each, long ones (the ground and supply
-      // rows and columns) reduced across the instance's lanes
-      for (int v = sl; v < nv; v += LPI) {
-        const int t0 = amap_ptr[v], t1 = amap_ptr[v + 1];
-        if (t1 - t0 > kHeavy) continue;
-        double acc = 0.0;
-        for (int t = t0; t < t1; ++t) acc += contrib(DV, amap_code[t]);
-        V[v] = acc;
-      }
-      for (int i = sl; i < n; i += LPI) {
-        const int r = in_row[i];
-        const int t0 = rmap_ptr[r], t1 = rmap_ptr[r + 1];
-        if (t1 - t0 > kHeavy) continue;
-        double acc = 0.0;
-        for (int t = t0; t < t1; ++t) acc += contrib(DV, rmap_code[t]);
-        T[i] = acc;
-      }
-      for (int h = 0; h < G.nheavy; ++h) {
-        const int code = heavy[h];  // (index << 1) | is_row
-        const int idx = code >> 1;
-        const int* ptr = (code & 1) ? rmap_ptr : amap_ptr;
-        const int* cds = (code & 1) ? rmap_code : amap_code;
-        const int key = (code & 1) ? in_row[idx] : idx;
-        const int t0 = ptr[key], t1 = ptr[key + 1];
-        double acc = 0.0;
-        for (int t = t0 + sl; t < t1; t += LPI) acc += contrib(DV, cds[t]);
-#pragma unroll
-        for (int o = LPI / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
-        if (sl == 0) {
-          if (code & 1)
-            T[idx] = acc;
-          else
-            V[idx] = acc;
-        }
-      }
+      bt::assemble<LPI>(P, DV, V, T, sl);
       __syncwarp();
-      // ---- factor + forward substitution, then backward, block by block;
-      // V[dslot] holds the reciprocal of the (perturbed) pivot
-      for (int b = 0; b < G.nblocks; ++b) {
-        const int b0 = bptr[b], b1 = bptr[b + 1];
-        for (int i = b0 + sl; i < b1; i += LPI)
-          for (int e = offd_ptr[i]; e < offd_ptr[i + 1]; ++e)
-            T[i] = fma(-V[G.nslots + e], T[offd_col[e]], T[i]);
-        __syncwarp();
-        for (int k = b0; k < b1; ++k) {
-          const int4 ck = colrec[k];
-          for (int s = ck.x; s < ck.y; ++s) {
-            const double u = V[s];
-            if (nonzero(u)) {
-              const int4 cj = colrec[srow[s]];
-              const int q0 = cj.y + 1;
-              const int* dst = udst + uptr[s] - q0;
-              for (int qq = q0 + sl; qq < cj.z; qq += LPI) {
-                const int dd = dst[qq];
-                V[dd] = fma(-V[qq], u, V[dd]);
-              }
-            }
-            __syncwarp();
-          }
-          const double r = fast_rcp(perturb_bits(V[ck.y], ck.w != 0));
-          const double zk = T[k];
-          for (int qq = ck.y + 1 + sl; qq < ck.z; qq += LPI) {
-            const double l = V[qq] * r;
-            V[qq] = l;
-            const int row = srow[qq];
-            T[row] = fma(-l, zk, T[row]);
-          }
-          if (sl == 0) V[ck.y] = r;
-          __syncwarp();
-        }
-        for (int k = b1 - 1; k >= b0; --k) {
-          const int4 ck = colrec[k];
-          const double xk = T[k] * V[ck.y];
-          for (int s = ck.x + sl; s < ck.y; s += LPI) {
-            const int row = srow[s];
-            T[row] = fma(-V[s], xk, T[row]);
-          }
-          __syncwarp();
-          if (sl == 0) T[k] = xk;
-          __syncwarp();
-        }
-      }
+      bt::factor_solve<LPI>(P, V, T, sl);
       // ---- Newton update (crates/sim-core/src/newton.rs:93-107)
       bool conv = true, fin = true;
       for (int c = sl; c < nc; c += LPI) {
-        const double a = T[out_pos[c]];
+        const double a = T[P.out_pos[c]];
         const double dx = a - X[c];
         DV[c] = dx * dx;
         if (!(fabs(dx) <= cfg.abs_tol + cfg.rel_tol * fabs(a))) conv = false;
@@ -1085,7 +802,7 @@ __global__ void k_batch_newton(BatchArgs A) {
           rsn = 0;
           const long long xo = A.inst_x_off[inst];
           if (xo >= 0)
-            for (int c = sl; c < n; c += LPI) A.x_out[xo + c] = T[out_pos[c]];
+            for (int c = sl; c < n; c += LPI) A.x_out[xo + c] = T[P.out_pos[c]];
         } else {
           double ss = 0.0;  // norm2 of dx, reduced across the instance's lanes
           for (int c = sl; c < nc; c += LPI) ss += DV[c];
@@ -1094,7 +811,7 @@ __global__ void k_batch_newton(BatchArgs A) {
           const double dxn = sqrt(ss);
           if (dxn > prev && damp > cfg.damping_min) damp = fmax(damp * 0.5, cfg.damping_min);
           prev = dxn;
-          for (int c = sl; c < nc; c += LPI) X[c] = fma(damp, T[out_pos[c]] - X[c], X[c]);
+          for (int c = sl; c < nc; c += LPI) X[c] = fma(damp, T[P.out_pos[c]] - X[c], X[c]);
           if (nfin) {
             rsn = 1;
           } else if (it >= cfg.max_iters) {
@@ -1220,10 +937,11 @@ static void launch_m(const BatchArgs& a, int grid, int warps_per_block, cudaStre
   k_batch_newton<M><<<grid, 32 * warps_per_block, sm, s>>>(a);
 }
 
+// The tile counter and the per-group instance counters are reset by the
+// caller before the classes start (the classes share the group counter
+// array and run concurrently).
 void launch_batch_newton(const BatchArgs& a, int m, int grid, int warps_per_block,
                          cudaStream_t s) {
-  cudaMemsetAsync(a.counter, 0, sizeof(unsigned), s);
-  cudaMemsetAsync(a.gnext, 0, sizeof(unsigned) * (a.ngroups > 0 ? a.ngroups : 1), s);
   switch (m) {
     case 8: launch_m<8>(a, grid, warps_per_block, s); break;
     case 4: launch_m<4>(a, grid, warps_per_block, s); break;

@@ -94,6 +94,20 @@ struct BatchArgs {
   const long long* inst_x_off;
   double* x_out;
   int* status;
+  // transient (fixed-step backward Euler, one instance per circuit)
+  int ninst;
+  const int* inst_group;       // group of each instance
+  double dt, inv_dt, target;
+  int steps, ckpt_every;
+  const int* probe;            // per instance: the node of the loss
+  double* loss;                // per instance
+  double* wave;                // per instance x steps values of the probe node (or null)
+  double* ckpt;                // per instance: (steps / ckpt_every + 1) x node_count states
+  const long long* ckpt_off;
+  double* seg;                 // per instance: (ckpt_every + 1) x node_count states
+  const long long* seg_off;
+  double* grad;                // per instance: dL/dp[d][0] per device
+  const long long* grad_off;
 };
 
 // --------------------------------------------------------------- launches
@@ -121,6 +135,11 @@ double fp64_peak_tflops();
 void launch_batch_newton(const BatchArgs& a, int m, int grid, int warps_per_block,
                          cudaStream_t s);
 // Registers per thread and resident blocks per SM of the batched kernel.
+// Transient forward / adjoint over a batch: one warp per instance.
+void launch_tran_forward(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
+void launch_tran_backward(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
+void tran_kernel_info(bool backward, int warps_per_block, int region, int prog_ints, int* regs,
+                      int* blocks_per_sm);
 void batch_kernel_info(int m, int warps_per_block, int region, int prog_ints, int* regs,
                        int* blocks_per_sm);
 

@@ -32,7 +32,8 @@ SYMBOLS = [
     "gpuklu_circuit_set_params", "gpuklu_stamp", "gpuklu_newton_dc", "gpuklu_batch_create",
     "gpuklu_batch_destroy", "gpuklu_batch_run", "gpuklu_batch_results",
     "gpuklu_batch_update_inputs", "gpuklu_batch_last_error", "gpuklu_batch_info",
-    "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_fp64_peak_tflops", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free",
+    "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_tran_create", "gpuklu_tran_forward",
+    "gpuklu_tran_backward", "gpuklu_fp64_peak_tflops", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free",
 ]
 
 
@@ -99,6 +100,10 @@ def lib(build_if_missing: bool = True):
         "gpuklu_batch_info": (C.c_int, [_P, _P]),
         "gpuklu_batch_stream": (_P, [_P]),
         "gpuklu_batch_work": (C.c_int, [_P, _P, _P]),
+        "gpuklu_tran_create": (_P, [_I64, _P, _P, _P, _P, _P, _P, _P, _I64, _D, _I64, _I64, _P,
+                                    _D]),
+        "gpuklu_tran_forward": (C.c_int, [_P, _P, _P, _P, _P, _P]),
+        "gpuklu_tran_backward": (C.c_int, [_P, _P, _P, _P]),
         "gpuklu_fp64_peak_tflops": (_D, []),
         "gpuklu_solve_device_noalloc": (C.c_int, [_P, _P, _P]),
         "gpuklu_dc_backward": (C.c_int, [_P, _P, _P, _I64, _P, _D, _P, _P]),

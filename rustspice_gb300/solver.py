@@ -292,3 +292,65 @@ class Batch:
 
     def stream(self) -> int:
         return N.lib().gpuklu_batch_stream(self._h) or 0
+
+
+class TranBatch:
+    """Fixed-step backward-Euler transient of many circuits (one instance per
+    circuit) with the checkpointed adjoint of
+    L_i = sum_t (x_t[probe_i] - target)^2 with respect to every capacitance."""
+
+    def __init__(self, circuits, x_init, x_off, dt, steps, ckpt_every, probe, target):
+        self.circuits = circuits
+        n = len(circuits)
+        dev_off = np.zeros(n + 1, np.int64)
+        for i, c in enumerate(circuits):
+            dev_off[i + 1] = dev_off[i] + c.ndev
+        self.dev_off = dev_off
+        ncs = N.i64([c.node_count for c in circuits])
+        t = N.i32(np.concatenate([c.type for c in circuits]))
+        nd = N.i32(np.concatenate([c.nodes for c in circuits]))
+        p = N.f64(np.concatenate([c.p for c in circuits]))
+        xi, xo = N.f64(x_init), N.i64(x_off)
+        pr = N.i64(np.broadcast_to(np.asarray(probe, np.int64), (n,)).copy())
+        self.steps = int(steps)
+        self._h = N.lib().gpuklu_tran_create(n, N.ptr(dev_off), N.ptr(ncs), N.ptr(t), N.ptr(nd),
+                                             N.ptr(p), N.ptr(xi), N.ptr(xo), len(xi), dt, steps,
+                                             ckpt_every, N.ptr(pr), target)
+        if not self._h:
+            raise RuntimeError("gpuklu_tran_create failed")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().gpuklu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _err(self, st):
+        if st != N.OK:
+            raise SolverError(st, N.lib().gpuklu_batch_last_error(self._h).decode())
+
+    def forward(self, cfg: N.NewtonConfig, with_wave: bool = False):
+        """(loss, wave or None, iterations, reason) per instance."""
+        n = len(self.circuits)
+        loss = np.zeros(n)
+        wave = np.zeros((n, self.steps)) if with_wave else None
+        it = np.zeros(n, np.int64)
+        rs = np.zeros(n, np.int32)
+        self._err(N.lib().gpuklu_tran_forward(self._h, C.byref(cfg), N.ptr(loss),
+                                              N.ptr(wave) if with_wave else None, N.ptr(it),
+                                              N.ptr(rs)))
+        return loss, wave, it, rs
+
+    def backward(self, cfg: N.NewtonConfig):
+        """dL_i/dp[d][0] per device of every instance (list of arrays), and the
+        Newton iterations of the recomputation."""
+        g = np.zeros(int(self.dev_off[-1]))
+        it = np.zeros(len(self.circuits), np.int64)
+        self._err(N.lib().gpuklu_tran_backward(self._h, C.byref(cfg), N.ptr(g), N.ptr(it)))
+        return [g[self.dev_off[i]:self.dev_off[i + 1]] for i in range(len(self.circuits))], it
+
+    def stream(self) -> int:
+        return N.lib().gpuklu_batch_stream(self._h) or 0
+

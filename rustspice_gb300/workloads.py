@@ -74,3 +74,50 @@ def inverter_batch(nchains: int = 4096, nvin: int = 61, seed: int = 3,
 # converged iterate's residual is at the FP64 floor.
 TIGHT = dict(max_iters=100, abs_tol=1e-12, rel_tol=1e-10, gmin=1e-12, gmin_steps=0,
              source_steps=0, damping=1.0, damping_min=0.1)
+
+
+# ---------------------------------------------------------------- rings
+RING_DT = 1e-12         # backward-Euler step [s]
+RING_STEPS = 2000
+RING_CKPT = 50          # checkpoint interval of the adjoint
+RING_TARGET = 0.6       # loss target of ring node 0 [V]
+RING_PROBE = 2          # ring node 0 (node 1 is VDD)
+
+
+def ring_stages(count: int = 1024, seed: int = 11) -> np.ndarray:
+    """Uneven odd ring lengths in 11..101."""
+    return 2 * cz.Stream(seed, 13).integers(5, 50, count) + 1
+
+
+def ring_initial_state(c: cz.Circuit, vdd: float = 1.2) -> np.ndarray:
+    """Logic levels alternating around the ring, VDD on node 1. With an odd
+    length the first stage's input and output agree, which starts the
+    oscillation (the `.ic` of a ring oscillator)."""
+    stages = c.node_count - 2
+    x = np.zeros(c.node_count)
+    x[1] = vdd
+    for s in range(stages):
+        x[2 + s] = vdd if s % 2 == 0 else 0.0
+    return x
+
+
+@dataclasses.dataclass
+class RingBatch:
+    circuits: list
+    x_init: np.ndarray      # concatenated initial states
+    x_off: np.ndarray       # per instance offset into x_init
+
+    @property
+    def ninst(self) -> int:
+        return len(self.circuits)
+
+
+def ring_batch(count: int = 1024, seed: int = 5) -> RingBatch:
+    """1024 CMOS rings (level-1 card, 10 fF per node with +-10 % jitter), one
+    instance per ring."""
+    stages = ring_stages(count)
+    circuits = [cz.ring_oscillator(int(s), seed=seed, ring_id=i) for i, s in enumerate(stages)]
+    xs = [ring_initial_state(c) for c in circuits]
+    off = np.zeros(count, np.int64)
+    off[1:] = np.cumsum([len(x) for x in xs])[:-1]
+    return RingBatch(circuits, np.concatenate(xs), off)

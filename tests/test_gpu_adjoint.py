@@ -51,7 +51,8 @@ def _host_grads(c, x, lam):
             beff = p[d, 2] * 1e-4 * ((3.9 * 8.854e-12) / p[d, 3]) * p[d, 4] / p[d, 5]
             gm = 0.0
             if vgs > vth:
-                gm = beff * vds if vds < vgs - vth else beff * (vgs - vth) * (1 + 0.02 * vds)
+                gm = (beff * vds * (1 + 0.02 * vds) if vds < vgs - vth
+                      else beff * (vgs - vth) * (1 + 0.02 * vds))
             sgn = -pol if rev else pol
             did = sgn * (-gm) * (1.0 if p[d, 1] >= 0 else -1.0)
             out[d] = -(lam[dr] - lam[sr]) * did
