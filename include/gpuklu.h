@@ -232,6 +232,36 @@ int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out);
 int gpuklu_batch_work(const gpuklu_batch* b, int64_t* flops, int64_t* bytes);
 void* gpuklu_batch_stream(gpuklu_batch* b);
 
+/* ------------------------------------------ bordered block diagonal */
+/* The reference's BbdSolver (crates/sim-core/src/bbd_solver.rs:86-1095,
+ * bbd.rs:355-485) with a known partition (the Partitioner trait's result,
+ * bbd.rs:44-72): assignment[i] = block of node i, or -1 for the border.
+ * Nodes with an entry into another block are promoted to the border; a
+ * trivial decomposition or a border above n/2 falls back to one solver over
+ * the whole matrix (as the reference falls back to SparseLU). The diagonal
+ * blocks are factored together on the device, the Schur complement
+ * S = B_T - C B^-1 R is assembled and factored densely on the device (border
+ * up to 16384). gpuklu_bbd_factor/solve take host arrays in the original
+ * order (the LinearSolver factor/solve of solver.rs:141-166). */
+typedef struct gpuklu_bbd gpuklu_bbd;
+gpuklu_bbd* gpuklu_bbd_create(int64_t n, const int64_t* ap, int64_t ap_len, const int64_t* ai,
+                              int64_t ai_len, const int64_t* assignment, int64_t num_blocks);
+void gpuklu_bbd_destroy(gpuklu_bbd* b);
+const char* gpuklu_bbd_last_error(const gpuklu_bbd* b);
+/* out[0] blocks, out[1] border start, out[2] border size, out[3] fallback,
+ * out[4] Schur right-hand-side tiles, out[5] blocks the inner factorization
+ * found. */
+int gpuklu_bbd_info(const gpuklu_bbd* b, int64_t* out);
+/* perm[new] = original index (blocks in order, then the border). */
+int gpuklu_bbd_perm(const gpuklu_bbd* b, int64_t* perm);
+int gpuklu_bbd_factor(gpuklu_bbd* b, const double* ax);
+int gpuklu_bbd_solve(gpuklu_bbd* b, double* rhs, int64_t len);
+/* DC operating point of a compiled circuit whose pattern is the solver's,
+ * with the loop and outputs of gpuklu_newton_dc. */
+int gpuklu_bbd_newton_dc(gpuklu_bbd* b, gpuklu_circuit* c, const gpuklu_newton_config* cfg,
+                         const double* x0, double* x_out, int64_t x_cap, int64_t* x_len,
+                         int64_t* iters, int64_t* iters_total, int* reason);
+
 /* ------------------------------------------ batched transient + adjoint */
 /* Fixed-step backward-Euler transient of many circuits, one instance per
  * circuit, and the discrete adjoint of the loss

@@ -28,6 +28,25 @@ void* orc_solver_new(const char* kind, int64_t n) {
   return make_solver(kind, (size_t)n).release();
 }
 void orc_solver_free(void* h) { delete static_cast<LinearSolver*>(h); }
+
+// BbdSolver with a known partition: assignment[i] = block or -1 (border).
+void* orc_bbd_new(int64_t n, const int64_t* assignment, int64_t num_blocks) {
+  return static_cast<LinearSolver*>(
+      new BbdSolver((size_t)n, std::vector<int64_t>(assignment, assignment + n), (size_t)num_blocks));
+}
+// out[0..3] = num_blocks, border_start, border_size, uses_fallback; perm[n]
+int orc_bbd_info(void* h, int64_t* out, int64_t* perm) {
+  auto* b = dynamic_cast<BbdSolver*>(static_cast<LinearSolver*>(h));
+  if (!b) return -1;
+  const BbdDecomposition& d = b->decomposition();
+  out[0] = (int64_t)d.num_blocks;
+  out[1] = (int64_t)d.border_start;
+  out[2] = (int64_t)d.border_size;
+  out[3] = b->uses_fallback() ? 1 : 0;
+  if (perm)
+    for (size_t i = 0; i < d.perm.size(); ++i) perm[i] = (int64_t)d.perm[i];
+  return 0;
+}
 void orc_prepare(void* h, int64_t n) { static_cast<LinearSolver*>(h)->prepare((size_t)n); }
 const char* orc_name(void* h) { return static_cast<LinearSolver*>(h)->name(); }
 void orc_reset(void* h) { static_cast<LinearSolver*>(h)->reset_pattern(); }
@@ -160,6 +179,32 @@ int orc_dc_op(int64_t node_count, int64_t ndev, const int32_t* type,
   auto solver = make_solver(solver_kind, c.node_count);
   Vec x;
   NewtonResult r = dc_op(c, cfg, *solver, x, x0);
+  *x_len = (int64_t)x.size();
+  for (int64_t i = 0; i < x_cap && (size_t)i < x.size(); ++i) x_out[i] = x[(size_t)i];
+  *iters = (int64_t)r.iterations;
+  return r.reason;
+}
+
+// DC operating point through the BbdSolver with a known partition.
+int orc_dc_op_bbd(int64_t node_count, int64_t ndev, const int32_t* type, const int32_t* nodes,
+                  const double* p, const int64_t* assignment, int64_t num_blocks,
+                  int64_t max_iters, double abs_tol, double rel_tol, double gmin,
+                  int64_t gmin_steps, const double* x0, double* x_out, int64_t x_cap,
+                  int64_t* x_len, int64_t* iters) {
+  Circuit c = make_circuit(node_count, ndev, type, nodes, p);
+  NewtonConfig cfg;
+  cfg.max_iters = (size_t)max_iters;
+  cfg.abs_tol = abs_tol;
+  cfg.rel_tol = rel_tol;
+  cfg.gmin = gmin;
+  cfg.gmin_steps = (size_t)gmin_steps;
+  size_t naux = 0;
+  for (size_t d = 0; d < c.ndev(); ++d) naux += c.type[d] == DEV_V;
+  std::vector<int64_t> asg(assignment, assignment + node_count);
+  asg.resize(node_count + naux, -1);  // aux rows join the border
+  BbdSolver solver(node_count + naux, asg, (size_t)num_blocks);
+  Vec x;
+  NewtonResult r = dc_op(c, cfg, solver, x, x0);
   *x_len = (int64_t)x.size();
   for (int64_t i = 0; i < x_cap && (size_t)i < x.size(); ++i) x_out[i] = x[(size_t)i];
   *iters = (int64_t)r.iterations;

@@ -342,6 +342,65 @@ double residual_inf(const Circuit& c, const Vec& x, double gmin);
 
 std::unique_ptr<LinearSolver> make_solver(const std::string& kind, size_t n);
 
+// ---------------------------------------------------------------- BBD
+// bbd_decompose (crates/sim-core/src/bbd.rs:355-485) on a given partition
+// (the Partitioner trait's result, bbd.rs:44-72): assignment[i] = block id,
+// or -1 for the border. Nodes with an entry coupling them to another block
+// are promoted to the border in the reference's two passes; empty blocks
+// are dropped; perm[new] = old with the blocks first, then the border.
+struct BbdDecomposition {
+  size_t num_blocks = 0, border_start = 0, border_size = 0;
+  UVec perm, inv_perm, block_ptr;
+};
+BbdDecomposition bbd_decompose_known(size_t n, const i64* ap, const i64* ai,
+                                     const std::vector<int64_t>& assignment,
+                                     size_t num_blocks);
+
+// BbdSolver (crates/sim-core/src/bbd_solver.rs:86-1095): one SparseLU per
+// diagonal block; the Schur complement S = B_T - sum_k C_k B_k^-1 R_k built
+// column by column of R_k; dense partial-pivot LU for a border of at most 64
+// (singular below 1e-30), otherwise SparseLU on the structural Schur pattern;
+// a trivial decomposition or a border above half of n falls back to SparseLU.
+class BbdSolver : public LinearSolver {
+ public:
+  BbdSolver(size_t n, std::vector<int64_t> assignment, size_t num_blocks);
+  void prepare(size_t n) override;
+  int analyze(const IVec& ap, const IVec& ai) override;
+  int factor(const IVec& ap, const IVec& ai, const Vec& ax) override;
+  int solve(Vec& rhs) override;
+  void reset_pattern() override;
+  const char* name() const override { return "BBD"; }
+  const BbdDecomposition& decomposition() const { return dec_; }
+  bool uses_fallback() const { return fallback_ != nullptr; }
+
+ private:
+  struct Sparse {  // CSC with values in pattern order
+    size_t nrows = 0, ncols = 0;
+    UVec col_ptr, row_idx;
+    Vec values;
+  };
+  int analyze_bbd(const IVec& ap, const IVec& ai);
+  int factor_bbd(const IVec& ap, const IVec& ai, const Vec& ax);
+  int solve_bbd(Vec& rhs);
+  size_t n_;
+  std::vector<int64_t> assign_;
+  size_t nblk_target_;
+  BbdDecomposition dec_;
+  bool have_dec_ = false, analyzed_ = false, factored_ = false;
+  std::vector<SparseLuSolver> blocks_;
+  std::vector<Sparse> c_, r_;
+  Vec block_work_;
+  // Schur: dense (border <= 64) or sparse
+  bool dense_schur_ = true;
+  Vec bt_dense_, schur_dense_, schur_lu_;
+  UVec schur_piv_;
+  std::unique_ptr<SparseLuSolver> schur_sparse_;
+  IVec schur_ap_, schur_ai_;
+  Vec schur_ax_;
+  std::unique_ptr<SparseLuSolver> fallback_;
+  IVec last_ap_, last_ai_;
+};
+
 // ---------------------------------------------------------------- transient
 // Fixed-step backward Euler with the physical companion sign (the transient
 // the reference's engine would run with `.tran dt` and BE, crates/sim-core/

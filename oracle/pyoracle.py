@@ -30,6 +30,10 @@ def lib():
         L.orc_solver_new.restype = _P
         L.orc_solver_new.argtypes = [C.c_char_p, _I64]
         L.orc_solver_free.argtypes = [_P]
+        L.orc_bbd_new.restype = _P
+        L.orc_bbd_new.argtypes = [_I64, _P, _I64]
+        L.orc_bbd_info.restype = C.c_int
+        L.orc_bbd_info.argtypes = [_P, _P, _P]
         L.orc_prepare.argtypes = [_P, _I64]
         L.orc_name.restype = C.c_char_p
         L.orc_name.argtypes = [_P]
@@ -52,6 +56,9 @@ def lib():
         L.orc_dc_op.restype = C.c_int
         L.orc_dc_op.argtypes = [_I64, _I64, _P, _P, _P, C.c_char_p, _I64, _D, _D, _D,
                                 _I64, _I64, _P, _P, _I64, _P, _P]
+        L.orc_dc_op_bbd.restype = C.c_int
+        L.orc_dc_op_bbd.argtypes = [_I64, _I64, _P, _P, _P, _P, _I64, _I64, _D, _D, _D, _I64,
+                                    _P, _P, _I64, _P, _P]
         L.orc_tran.restype = C.c_int
         L.orc_tran.argtypes = [_I64, _I64, _P, _P, _P, C.c_char_p, _I64, _D, _D, _D, _D, _I64,
                                _P, _P, _P]
@@ -76,8 +83,12 @@ def _f64(a):
 class Solver:
     """One of the reference's LinearSolver implementations, restated."""
 
-    def __init__(self, kind: str, n: int):
-        self.h = lib().orc_solver_new(kind.encode(), n)
+    def __init__(self, kind: str, n: int, assignment=None, num_blocks: int = 0):
+        if kind == "bbd":
+            asg = _i64(assignment)
+            self.h = lib().orc_bbd_new(n, _ptr(asg), num_blocks)
+        else:
+            self.h = lib().orc_solver_new(kind.encode(), n)
         self.n = n
 
     def __del__(self):
@@ -118,6 +129,14 @@ class Solver:
         d = {k: int(v) for k, v in zip(keys, out)}
         d["rcond"] = rc.value
         return d
+
+    def bbd_info(self):
+        out = np.zeros(4, np.int64)
+        perm = np.zeros(max(self.n, 1), np.int64)
+        if lib().orc_bbd_info(self.h, _ptr(out), _ptr(perm)) != 0:
+            return None
+        return dict(num_blocks=int(out[0]), border_start=int(out[1]), border_size=int(out[2]),
+                    fallback=bool(out[3]), perm=perm[:self.n])
 
     def klu_pivots(self):
         cap = max(self.n, 1)
@@ -214,6 +233,22 @@ def tran_adjoint(c, states, dt, probe, target, gmin=1e-12):
     if r != 0:
         raise RuntimeError("singular Jacobian in the transient adjoint")
     return g
+
+
+def dc_op_bbd(c, assignment, num_blocks, max_iters=100, abs_tol=1e-6, rel_tol=1e-3,
+              gmin=1e-12, gmin_steps=0, x0=None):
+    """Engine DC operating point through the BbdSolver (known partition)."""
+    _, t, nd, p = _circ_arrays(c)
+    asg = _i64(assignment)
+    x0a = _f64(x0) if x0 is not None else None
+    x = np.zeros(c.n)
+    xl = C.c_int64()
+    it = C.c_int64()
+    r = lib().orc_dc_op_bbd(c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p), _ptr(asg),
+                            num_blocks, max_iters, abs_tol, rel_tol, gmin, gmin_steps,
+                            _ptr(x0a) if x0a is not None else None, _ptr(x), c.n, C.byref(xl),
+                            C.byref(it))
+    return REASONS[r], it.value, x[:xl.value]
 
 
 def residual(c, x, gmin=1e-12):

@@ -200,6 +200,64 @@ def mesh_dc(side: int = 32, ndiodes: int = 64, seed: int = 1) -> Circuit:
 
 
 # ---------------------------------------------------------------- inverters
+def bordered_meshes(nblocks: int = 64, nborder: int = 1024, side_lo: int = 30,
+                    side_hi: int = 50, ndiodes: int = 32, seed: int = 2):
+    """Bordered-block-diagonal DC case: ``nblocks`` square resistor meshes
+    (side uniform in [side_lo, side_hi], R log-uniform 100 ohm..10 kohm),
+    ``ndiodes`` diodes per mesh from seeded mesh nodes to ground, and
+    ``nborder`` border nodes, each tied by 4..8 resistors of 1 kohm to
+    seeded nodes of seeded meshes. The supply is a Norton source on border
+    node 0: 12 mA in parallel with 100 ohm to ground (1.2 V open circuit); a
+    current source keeps the border free of voltage-source rows, whose zero
+    diagonal the reference's no-pivot Schur factorisation cannot take.
+
+    A border node ties to a mesh node at most once, and the diodes of a mesh
+    sit on distinct nodes, so no block-border entry is duplicated (the
+    reference's Schur assembly keeps only the last of duplicated entries of
+    R, bbd_solver.rs:788, 867).
+
+    Returns (circuit, assignment, nblocks): assignment[i] is node i's mesh,
+    -1 for ground and the border nodes (the known partition).
+    """
+    rs = Stream(seed, 21)
+    sides = rs.integers(side_lo, side_hi, nblocks)
+    dev = _Dev()
+    first = 1
+    starts, sizes = [], []
+    for k in range(nblocks):
+        s = int(sides[k])
+        _mesh_resistors(dev, s, s, first, Stream(seed, 1000 + k))
+        dn = Stream(seed, 3000 + k).choice(s * s, ndiodes) + first
+        for a in dn:
+            dev.add(DEV_D, (int(a), 0), (1e-14, 1.0))
+        starts.append(first)
+        sizes.append(s * s)
+        first += s * s
+    b0 = first
+    ties = Stream(seed, 22)
+    nt = ties.integers(4, 8, nborder)
+    blk = Stream(seed, 23)
+    pos = Stream(seed, 24)
+    for j in range(nborder):
+        kk = blk.integers(0, nblocks - 1, int(nt[j]))
+        uu = pos.uniform(int(nt[j]))
+        seen = set()
+        for k, u in zip(kk, uu):
+            node = starts[int(k)] + int(u * sizes[int(k)])
+            if node in seen:  # one tie per (border node, mesh node): no duplicate entries
+                continue
+            seen.add(node)
+            dev.add(DEV_R, (b0 + j, node), (1000.0,))
+    dev.add(DEV_I, (0, b0), (12e-3,))
+    dev.add(DEV_R, (b0, 0), (100.0,))
+    nc = b0 + nborder
+    c = dev.build(nc, f"bbd{nblocks}_b{nborder}_s{seed}")
+    assignment = -np.ones(nc, np.int64)
+    for k in range(nblocks):
+        assignment[starts[k]:starts[k] + sizes[k]] = k
+    return c, assignment, nblocks
+
+
 def _mos(model: str) -> int:
     if model == "consistent":
         return DEV_MC

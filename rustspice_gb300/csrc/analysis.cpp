@@ -424,7 +424,11 @@ void block_csc(const Plan& p, const i64* ap, const i64* ai, int b,
 }
 }  // namespace
 
-std::string analyze(int n, const i64* ap, const i64* ai, int pivot_mode, Plan& p) {
+const char* const kTooLarge =
+    "the factorization's update lists exceed 2^31 entries (fill too large for this solver)";
+
+std::string analyze(int n, const i64* ap, const i64* ai, int pivot_mode, Plan& p,
+                    const std::vector<int>* given_blocks) {
   p = Plan();
   p.n = n;
   p.nnz_raw = ap[n];
@@ -436,7 +440,24 @@ std::string analyze(int n, const i64* ap, const i64* ai, int pivot_mode, Plan& p
   }
   BtfResult b;
   bool keep = false;
-  if (n >= 4 && !structurally_irreducible(n, ap, ai)) {
+  if (given_blocks) {  // caller's blocks in index order, identity row order
+    const std::vector<int>& g = *given_blocks;
+    if (g.size() < 2 || g.front() != 0 || g.back() != n) return "block boundaries do not cover n";
+    for (size_t k = 0; k + 1 < g.size(); ++k)
+      if (g[k + 1] <= g[k]) return "empty or decreasing block";
+    for (int c = 0, k = 0; c < n; ++c) {
+      while (c >= g[k + 1]) ++k;
+      for (i64 t = ap[c]; t < ap[c + 1]; ++t)
+        if (ai[t] < n && (ai[t] < g[k] || ai[t] >= g[k + 1])) return "entry outside the given blocks";
+    }
+    b.block_ptr = g;
+    b.nblocks = (int)g.size() - 1;
+    b.col_perm.resize(n);
+    b.row_inv.resize(n);
+    b.col_inv.resize(n);
+    for (int i = 0; i < n; ++i) b.col_perm[i] = b.row_inv[i] = b.col_inv[i] = i;
+    keep = b.nblocks >= 2;
+  } else if (n >= 4 && !structurally_irreducible(n, ap, ai)) {
     b = btf_decompose(n, ap, ai);
     keep = b.nblocks >= 2 && b.max_block < n;
   }
@@ -476,6 +497,7 @@ std::string analyze(int n, const i64* ap, const i64* ai, int pivot_mode, Plan& p
   p.row_inv = p.row_perm;
   p.pats = p.pats_orig;
   finalize_plan(p, ap, ai, p.pats);
+  if (p.too_large) return kTooLarge;
   return "";
 }
 
@@ -544,7 +566,16 @@ void finalize_plan(Plan& p, const i64* ap, const i64* ai, const std::vector<Patt
   p.upd_ptr.assign(ns + 1, 0);
   p.upd_dst.clear();
   p.flops_refactor = 0;
-  for (int k = 0; k < n; ++k) {
+  {  // one int32 destination per update: refuse fills whose list would not index
+    int64_t total = 0;
+    for (int k = 0; k < n; ++k)
+      for (int s = p.col_ptr[k]; s < p.dslot[k]; ++s) {
+        const int j = p.slot_row[s];
+        total += p.col_ptr[j + 1] - p.dslot[j] - 1;
+      }
+    p.too_large = total > (int64_t)0x7fffffff;
+  }
+  for (int k = 0; k < n && !p.too_large; ++k) {
     open_col(k);
     for (int s = p.col_ptr[k]; s < p.col_ptr[k + 1]; ++s) {
       p.upd_ptr[s] = (int)p.upd_dst.size();
@@ -690,6 +721,53 @@ void finalize_plan(Plan& p, const i64* ap, const i64* ai, const std::vector<Patt
     }
     p.pcol_ptr[kg + 1] = (int)p.pcol_raw.size();
   }
+}
+
+// ------------------------------------------------------------------ BBD
+BbdDecomp bbd_decompose(int n, const i64* ap, const i64* ai, const int64_t* assignment,
+                        int num_blocks) {
+  std::vector<int> asg(n);
+  for (int i = 0; i < n; ++i)
+    asg[i] = (assignment[i] < 0 || assignment[i] >= num_blocks) ? -1 : (int)assignment[i];
+  for (int col = 0; col < n; ++col) {  // bbd.rs:366-385
+    if (asg[col] < 0) continue;
+    for (i64 q = ap[col]; q < ap[col + 1]; ++q) {
+      const int row = (int)ai[q];
+      if (row < n && row != col && asg[row] >= 0 && asg[row] != asg[col]) {
+        asg[col] = -1;
+        break;
+      }
+    }
+  }
+  for (int col = 0; col < n; ++col)  // bbd.rs:391-407
+    for (i64 q = ap[col]; q < ap[col + 1]; ++q) {
+      const int row = (int)ai[q];
+      if (row < n && row != col && asg[row] >= 0 && asg[col] >= 0 && asg[col] != asg[row])
+        asg[row] = -1;
+    }
+  std::vector<std::vector<int>> blocks(std::max(num_blocks, 0));
+  std::vector<int> border;
+  for (int i = 0; i < n; ++i) (asg[i] < 0 ? border : blocks[asg[i]]).push_back(i);
+  BbdDecomp d;
+  for (auto& b : blocks) {
+    if (b.empty()) continue;
+    d.block_ptr.push_back((int)d.perm.size());
+    for (int i : b) {
+      d.perm.push_back(i);
+      d.block_of.push_back(d.num_blocks);
+    }
+    ++d.num_blocks;
+  }
+  d.block_ptr.push_back((int)d.perm.size());
+  d.border_start = (int)d.perm.size();
+  for (int i : border) {
+    d.perm.push_back(i);
+    d.block_of.push_back(-1);
+  }
+  d.border_size = n - d.border_start;
+  d.inv_perm.assign(n, 0);
+  for (int k = 0; k < n; ++k) d.inv_perm[d.perm[k]] = k;
+  return d;
 }
 
 }  // namespace gk

@@ -33,6 +33,18 @@ struct BtfResult {
 BtfResult btf_decompose(int n, const i64* ap, const i64* ai);
 bool structurally_irreducible(int n, const i64* ap, const i64* ai);
 
+// Bordered-block-diagonal decomposition of a given partition (the
+// reference's bbd_decompose, crates/sim-core/src/bbd.rs:355-485): nodes with
+// an entry to another block are promoted to the border (column pass, then
+// row pass), empty blocks are dropped, and perm[new] = old lists the blocks
+// in order, then the border. num_blocks <= 1 after dropping means trivial.
+struct BbdDecomp {
+  int num_blocks = 0, border_start = 0, border_size = 0;
+  std::vector<int> perm, inv_perm, block_ptr, block_of;  // block_of[new]: -1 border
+};
+BbdDecomp bbd_decompose(int n, const i64* ap, const i64* ai, const int64_t* assignment,
+                        int num_blocks);
+
 // Symbolic L/U pattern of an already permuted block, column by column.
 struct Pattern {
   std::vector<int> lp, li, up, ui;  // U columns end with the diagonal
@@ -69,6 +81,7 @@ struct Plan {
   // index), as NativeKLU's row_perm / row_perm_inv.
   std::vector<i32> row_perm, row_inv;  // [n], block-local values
   int pivot_mode = PIVOT_REFERENCE;
+  bool too_large = false;  // update lists beyond int32 indexing: not factorable here
   bool pivots_known = false;
   i64 swaps = 0;
 
@@ -118,7 +131,10 @@ struct Plan {
 // Builds the Plan for pattern (ap, ai) of dimension n: BTF kept under the
 // reference's rule (n >= 4, >= 2 blocks, largest block < n), AMD per block,
 // symbolic DFS. Pivots start as the identity.
-std::string analyze(int n, const i64* ap, const i64* ai, int pivot_mode, Plan& p);
+// given_blocks: boundaries of diagonal blocks the caller guarantees (no
+// entry outside them); they replace the BTF, with the identity row order.
+std::string analyze(int n, const i64* ap, const i64* ai, int pivot_mode, Plan& p,
+                    const std::vector<int>* given_blocks = nullptr);
 
 // Installs a pivot sequence (block-local row_perm for every position) found
 // by the first factorization and rebuilds what depends on it: in exact mode

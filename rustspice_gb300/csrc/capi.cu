@@ -338,6 +338,11 @@ struct gpuklu_handle {
   std::vector<i64> last_ap, last_ai;
   std::vector<i64> sym_ap, sym_ai;
   int sym_mode = -1;
+  // Set by an owner that knows the matrix (the BBD solver's block-diagonal
+  // part): diagonal blocks to use instead of the BTF, and no row exchanges in
+  // the first factorization (the reference's SparseLU keeps the diagonal).
+  std::vector<int> given_blocks;
+  bool no_swap = false;
   cudaStream_t stream = nullptr;
   DBuf<double> d_ax, d_lu, d_z, d_x, d_out, d_rhs, d_work, d_rc, d_rhs_c, d_xnew, d_newx,
       d_scratch2;
@@ -394,7 +399,8 @@ struct gpuklu_handle {
           std::equal(sym_ai.begin(), sym_ai.end(), ai))) {
       pd_sym_ok = piv_ok = false;
       sym_mode = -1;
-      std::string m = gk::analyze((int)n, ap, ai, pivot_mode, sym_plan);
+      std::string m = gk::analyze((int)n, ap, ai, pivot_mode, sym_plan,
+                                  given_blocks.empty() ? nullptr : &given_blocks);
       if (!m.empty()) return fail(GPUKLU_INVALID_MATRIX, m);
       sym_ap.assign(ap, ap + ap_len);
       sym_ai.assign(ai, ai + ai_len);
@@ -466,8 +472,8 @@ struct gpuklu_handle {
       return check_status("refactor");
     }
     // First factorization: the reference's pivot pass.
-    gk::launch_first_factor(pd_sym.dp, d_ax.p, d_lu.p, d_work.p, d_rperm.p, d_rinv.p, 0.001,
-                            d_status.p, stream);
+    gk::launch_first_factor(pd_sym.dp, d_ax.p, d_lu.p, d_work.p, d_rperm.p, d_rinv.p,
+                            no_swap ? 0.0 : 0.001, d_status.p, stream);
     std::vector<i32> rperm(n);
     cudaError_t e = cudaMemcpyAsync(rperm.data(), d_rperm.p, n * sizeof(i32),
                                     cudaMemcpyDeviceToHost, stream);
@@ -479,6 +485,12 @@ struct gpuklu_handle {
       piv_ok = false;
       plan = sym_plan;
       gk::set_pivots(plan, last_ap.data(), last_ai.data(), rperm);
+      if (plan.too_large) {
+        state = ANALYZED;
+        return fail(GPUKLU_INVALID_MATRIX,
+                    "the factorization's update lists exceed 2^31 entries "
+                    "(fill too large for this solver)");
+      }
       st = upload_plan();
       if (st) return st;
       piv_rperm.swap(rperm);
@@ -1726,6 +1738,518 @@ int gpuklu_batch_work(const gpuklu_batch* b, int64_t* flops, int64_t* bytes) {
 }
 
 void* gpuklu_batch_stream(gpuklu_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+}  // extern "C"
+
+// ====================================================================== BBD
+// Bordered-block-diagonal solver (the reference's BbdSolver with a known
+// partition, crates/sim-core/src/bbd_solver.rs): the diagonal blocks as one
+// block-diagonal matrix M on an inner handle, the border through the Schur
+// complement S = B_T - C M^-1 R, dense on the device.
+struct gpuklu_bbd {
+  int64_t n = 0;
+  std::vector<i64> ap, ai;
+  gk::BbdDecomp d;
+  bool fallback = false;
+  gpuklu_handle* M = nullptr;   // block-diagonal part, or the whole matrix on fallback
+  std::vector<i64> m_ap, m_ai;
+  std::vector<i32> m_raw;       // M raw entry -> raw entry of the full matrix
+  bool tiles_ready = false;
+  int ntiles = 0;
+  std::vector<i32> perm32;
+  DBuf<i32> d_m_raw, d_perm, d_tile_pos0, d_tile_size, d_tile_blk, d_init_ptr, d_init_code,
+      d_init_raw, d_bt_ptr, d_bt_row, d_bt_raw, d_yref_ptr, d_yref, d_c_ptr, d_c_row, d_c_pos,
+      d_c_raw, d_crow_ptr, d_crow_col, d_crow_raw, d_rrow_ptr, d_rrow_col, d_rrow_raw, d_bperm;
+  DBuf<long long> d_tile_off;
+  DBuf<double> d_ax, d_rhs, d_rhs_c, d_x, d_newx, d_y, d_S, d_xT, d_z;
+  DBuf<gk::NewtonState> d_nstate;
+  DBuf<int> d_status;
+  gk::BbdArgs args{};
+  std::string err;
+  ~gpuklu_bbd() {
+    if (M) gpuklu_destroy(M);
+  }
+  int fail(int code, const std::string& m) {
+    err = m;
+    return code;
+  }
+  cudaStream_t stream() const { return M->stream; }
+
+  // Tile, Schur and product index lists; they depend on M's pivots, so they
+  // are built after the first factorization.
+  int build_tiles() {
+    const gk::Plan& P = M->plan;
+    const int nm = d.border_start, bs = d.border_size;
+    std::vector<int> in_pos(nm), out_pos(nm);
+    for (int r = 0; r < nm; ++r) in_pos[r] = P.in_pos[r];
+    for (int c = 0; c < nm; ++c) out_pos[c] = P.out_pos[c];
+    const int nb = P.nblocks;
+    std::vector<int> pblk(nm);  // plan block of each M index (row or column)
+    for (int b = 0; b < nb; ++b)
+      for (int q = P.block_ptr[b]; q < P.block_ptr[b + 1]; ++q) pblk[q] = b;
+    // R entries by plan block: border column j, M row m, raw q (CSC order)
+    std::vector<std::vector<int>> jcols(nb);
+    std::vector<std::vector<std::pair<int, int>>> rent(nb);  // (pos offset, raw) per (j)
+    std::vector<std::vector<int>> rent_j(nb);
+    std::vector<std::vector<i32>> rrow(nm);  // per M row: (j, raw) pairs flattened
+    std::vector<i32> bt_ptr(bs + 1, 0), bt_row, bt_raw;
+    for (int j = 0; j < bs; ++j) {
+      const int oc = d.perm[d.border_start + j];
+      for (i64 q = ap[oc]; q < ap[oc + 1]; ++q) {
+        const int orow = (int)ai[q];
+        if (orow >= n) continue;
+        const int nr = d.inv_perm[orow];
+        if (nr >= d.border_start) {
+          bt_row.push_back(nr - d.border_start);
+          bt_raw.push_back((i32)q);
+        } else {
+          const int pos = in_pos[nr], b = pblk[pos];
+          if (jcols[b].empty() || jcols[b].back() != j) jcols[b].push_back(j);
+          rent[b].push_back({pos - P.block_ptr[b], (int)q});
+          rent_j[b].push_back((int)jcols[b].size() - 1);
+          rrow[nr].push_back(j);
+          rrow[nr].push_back((i32)q);
+        }
+      }
+      bt_ptr[j + 1] = (i32)bt_row.size();
+    }
+    // tiles of 32 border columns per plan block
+    std::vector<i32> tile_pos0, tile_size, tile_blk, init_ptr(1, 0), init_code, init_raw;
+    std::vector<long long> tile_off;
+    std::vector<std::vector<i32>> yref(bs);
+    long long off = 0;
+    for (int b = 0; b < nb; ++b) {
+      const int ncol = (int)jcols[b].size();
+      const int sz = P.block_ptr[b + 1] - P.block_ptr[b];
+      const int first_tile = (int)tile_pos0.size();
+      for (int t0 = 0; t0 < ncol; t0 += 32) {
+        tile_pos0.push_back(P.block_ptr[b]);
+        tile_size.push_back(sz);
+        tile_blk.push_back(b);
+        tile_off.push_back(off);
+        off += (long long)sz * 32;
+        const int t = (int)tile_pos0.size() - 1;
+        for (int l = 0; l < 32 && t0 + l < ncol; ++l) yref[jcols[b][t0 + l]].push_back((t << 5) | l);
+      }
+      (void)first_tile;
+      for (int t0 = 0; t0 < ncol; t0 += 32) {  // each tile's R entries, CSC order
+        for (size_t e = 0; e < rent[b].size(); ++e) {
+          const int k = rent_j[b][e];
+          if (k < t0 || k >= t0 + 32) continue;
+          init_code.push_back(rent[b][e].first * 32 + (k - t0));
+          init_raw.push_back(rent[b][e].second);
+        }
+        init_ptr.push_back((i32)init_code.size());
+      }
+    }
+    ntiles = (int)tile_pos0.size();
+    // C entries: block columns c with border rows, per plan block and per border row
+    std::vector<std::vector<i32>> cb(nb);    // per plan block: (row, pos, raw) triples
+    std::vector<std::vector<i32>> crow(bs);  // per border row: (c, raw)
+    for (int c = 0; c < nm; ++c) {
+      const int oc = d.perm[c];
+      const int pos = out_pos[c], b = pblk[pos];
+      for (i64 q = ap[oc]; q < ap[oc + 1]; ++q) {
+        const int orow = (int)ai[q];
+        if (orow >= n) continue;
+        const int nr = d.inv_perm[orow];
+        if (nr < d.border_start) continue;
+        const int r = nr - d.border_start;
+        cb[b].push_back(r);
+        cb[b].push_back(pos - P.block_ptr[b]);
+        cb[b].push_back((i32)q);
+        crow[r].push_back(c);
+        crow[r].push_back((i32)q);
+      }
+    }
+    // Elimination order of S: AMD on its structural pattern (B_T plus, for
+    // every block touching column j, the border rows of that block's C), the
+    // order the reference's sparse Schur factorisation uses
+    // (bbd_solver.rs:330-411 with sparse_lu.rs). It matters: the ground row
+    // couples to everything, and eliminated last it keeps the final pivots
+    // away from the near-singular constant mode of the conductance matrix.
+    std::vector<int> spos(bs), sinv(bs);
+    {
+      std::vector<std::vector<int>> crows(nb);
+      for (int b = 0; b < nb; ++b) {
+        std::vector<char> m(bs, 0);
+        for (size_t e = 0; e < cb[b].size(); e += 3)
+          if (!m[cb[b][e]]) {
+            m[cb[b][e]] = 1;
+            crows[b].push_back(cb[b][e]);
+          }
+      }
+      std::vector<i64> sap(bs + 1, 0), sai;
+      std::vector<int> mark(bs, -1);
+      for (int j = 0; j < bs; ++j) {
+        std::vector<int> rows;
+        for (int e = bt_ptr[j]; e < bt_ptr[j + 1]; ++e)
+          if (mark[bt_row[e]] != j) {
+            mark[bt_row[e]] = j;
+            rows.push_back(bt_row[e]);
+          }
+        for (i32 code : yref[j]) {
+          const int b = tile_blk[code >> 5];
+          for (int r : crows[b])
+            if (mark[r] != j) {
+              mark[r] = j;
+              rows.push_back(r);
+            }
+        }
+        std::sort(rows.begin(), rows.end());
+        for (int r : rows) sai.push_back(r);
+        sap[j + 1] = (i64)sai.size();
+      }
+      gk::amd_order(bs, sap.data(), sai.data(), spos, sinv);
+    }
+    for (auto& r : bt_row) r = spos[r];
+    std::vector<i32> yref_ptr(bs + 1, 0), yref_flat, bt_ptr_s(bs + 1, 0), bt_row_s, bt_raw_s;
+    for (int s2 = 0; s2 < bs; ++s2) {  // S columns in elimination order
+      const int j = sinv[s2];
+      yref_flat.insert(yref_flat.end(), yref[j].begin(), yref[j].end());
+      yref_ptr[s2 + 1] = (i32)yref_flat.size();
+      for (int e = bt_ptr[j]; e < bt_ptr[j + 1]; ++e) {
+        bt_row_s.push_back(bt_row[e]);
+        bt_raw_s.push_back(bt_raw[e]);
+      }
+      bt_ptr_s[s2 + 1] = (i32)bt_row_s.size();
+    }
+    bt_ptr.swap(bt_ptr_s);
+    bt_row.swap(bt_row_s);
+    bt_raw.swap(bt_raw_s);
+    std::vector<i32> bperm(bs);
+    for (int s2 = 0; s2 < bs; ++s2) bperm[s2] = d.perm[d.border_start + sinv[s2]];
+    std::vector<i32> c_ptr(nb + 1, 0), c_row, c_pos, c_raw;
+    for (int b = 0; b < nb; ++b) {
+      for (size_t e = 0; e < cb[b].size(); e += 3) {
+        c_row.push_back(spos[cb[b][e]]);
+        c_pos.push_back(cb[b][e + 1]);
+        c_raw.push_back(cb[b][e + 2]);
+      }
+      c_ptr[b + 1] = (i32)c_row.size();
+    }
+    std::vector<i32> crow_ptr(bs + 1, 0), crow_col, crow_raw;
+    for (int s2 = 0; s2 < bs; ++s2) {  // border rows in S order
+      const int r = sinv[s2];
+      for (size_t e = 0; e < crow[r].size(); e += 2) {
+        crow_col.push_back(crow[r][e]);
+        crow_raw.push_back(crow[r][e + 1]);
+      }
+      crow_ptr[s2 + 1] = (i32)crow_col.size();
+    }
+    std::vector<i32> rrow_ptr(nm + 1, 0), rrow_col, rrow_raw;
+    for (int m = 0; m < nm; ++m) {
+      for (size_t e = 0; e < rrow[m].size(); e += 2) {
+        rrow_col.push_back(spos[rrow[m][e]]);
+        rrow_raw.push_back(rrow[m][e + 1]);
+      }
+      rrow_ptr[m + 1] = (i32)rrow_col.size();
+    }
+    cudaStream_t s = stream();
+    cudaError_t e = cudaSuccess;
+#define UP(buf, vec) \
+  if (e == cudaSuccess) e = buf.upload(vec, s);
+    UP(d_tile_pos0, tile_pos0) UP(d_tile_size, tile_size) UP(d_tile_blk, tile_blk)
+    UP(d_tile_off, tile_off) UP(d_init_ptr, init_ptr) UP(d_init_code, init_code)
+    UP(d_init_raw, init_raw) UP(d_bt_ptr, bt_ptr) UP(d_bt_row, bt_row) UP(d_bt_raw, bt_raw)
+    UP(d_yref_ptr, yref_ptr) UP(d_yref, yref_flat) UP(d_c_ptr, c_ptr) UP(d_c_row, c_row)
+    UP(d_c_pos, c_pos) UP(d_c_raw, c_raw) UP(d_crow_ptr, crow_ptr) UP(d_crow_col, crow_col)
+    UP(d_crow_raw, crow_raw) UP(d_rrow_ptr, rrow_ptr) UP(d_rrow_col, rrow_col)
+    UP(d_rrow_raw, rrow_raw) UP(d_bperm, bperm)
+#undef UP
+    if (e == cudaSuccess) e = d_y.resize(std::max<long long>(off, 1));
+    if (e == cudaSuccess) e = d_S.resize(std::max<size_t>((size_t)bs * bs, 1));
+    if (e == cudaSuccess) e = d_xT.resize(std::max(bs, 1));
+    if (e == cudaSuccess) e = d_z.resize(std::max(nm, 1));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd tiles"));
+    gk::BbdArgs& a = args;
+    a.ntiles = ntiles;
+    a.bs = bs;
+    a.border_start = d.border_start;
+    a.tile_pos0 = d_tile_pos0.p;
+    a.tile_size = d_tile_size.p;
+    a.tile_off = d_tile_off.p;
+    a.tile_blk = d_tile_blk.p;
+    a.init_ptr = d_init_ptr.p;
+    a.init_code = d_init_code.p;
+    a.init_raw = d_init_raw.p;
+    a.bt_ptr = d_bt_ptr.p;
+    a.bt_row = d_bt_row.p;
+    a.bt_raw = d_bt_raw.p;
+    a.yref_ptr = d_yref_ptr.p;
+    a.yref = d_yref.p;
+    a.c_ptr = d_c_ptr.p;
+    a.c_row = d_c_row.p;
+    a.c_pos = d_c_pos.p;
+    a.c_raw = d_c_raw.p;
+    a.crow_ptr = d_crow_ptr.p;
+    a.crow_col = d_crow_col.p;
+    a.crow_raw = d_crow_raw.p;
+    a.rrow_ptr = d_rrow_ptr.p;
+    a.rrow_col = d_rrow_col.p;
+    a.rrow_raw = d_rrow_raw.p;
+    a.perm = d_perm.p;
+    a.bperm = d_bperm.p;
+    tiles_ready = true;
+    return GPUKLU_OK;
+  }
+
+  // Factor with the full matrix's values in d_ax.
+  int factor_device(bool sync) {
+    cudaStream_t s = stream();
+    if (fallback) {
+      cudaError_t e = cudaMemcpyAsync(M->d_ax.p, d_ax.p, ai.size() * 8, cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd factor"));
+      const bool first = M->state != gpuklu_handle::FACTORED;
+      int st = M->factor_on_device(sync || first);
+      if (st) return fail(st, M->err);
+      return GPUKLU_OK;
+    }
+    gk::launch_gather(M->d_ax.p, d_ax.p, d_m_raw.p, (int)m_raw.size(), s);
+    const bool first = M->state != gpuklu_handle::FACTORED;
+    int st = M->factor_on_device(sync || first);
+    if (st) return fail(st, M->err);
+    if (!tiles_ready) {
+      st = build_tiles();
+      if (st) return st;
+    }
+    gk::launch_bbd_ysolve(M->pd.dp, M->d_lu.p, d_ax.p, args, d_y.p, s);
+    gk::launch_bbd_schur(d_ax.p, args, d_y.p, d_S.p, s);
+    gk::launch_dense_lu(d_S.p, d.border_size, s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && sync) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd factor"));
+    if (sync) {
+      st = M->check_status("bbd factor");
+      if (st) return fail(st, M->err);
+    }
+    return GPUKLU_OK;
+  }
+
+  // x = A^-1 rhs, both full-length device arrays (original order).
+  int solve_device(const double* rhs, double* x) {
+    cudaStream_t s = stream();
+    if (fallback) {
+      cudaError_t e = cudaMemcpyAsync(M->d_rhs.p, rhs, n * 8, cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd solve"));
+      int st = M->solve_on_device(false, false);
+      if (st) return fail(st, M->err);
+      e = cudaMemcpyAsync(x, M->d_out.p, n * 8, cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd solve"));
+      return GPUKLU_OK;
+    }
+    const int nm = d.border_start;
+    gk::launch_gather(M->d_rhs.p, rhs, d_perm.p, nm, s);  // block rows
+    int st = M->solve_on_device(false, false);
+    if (st) return fail(st, M->err);
+    cudaMemcpyAsync(d_z.p, M->d_out.p, (size_t)nm * 8, cudaMemcpyDeviceToDevice, s);
+    gk::launch_bbd_border_rhs(d_ax.p, rhs, d_z.p, args, d_xT.p, s);
+    gk::launch_dense_lu_solve(d_S.p, d.border_size, d_xT.p, s);
+    gk::launch_bbd_rmatvec(d_ax.p, d_xT.p, args, M->d_rhs.p, s);
+    st = M->solve_on_device(false, false);
+    if (st) return fail(st, M->err);
+    gk::launch_bbd_combine(d_z.p, M->d_out.p, d_xT.p, args, x, s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd solve"));
+    return GPUKLU_OK;
+  }
+};
+
+extern "C" {
+
+gpuklu_bbd* gpuklu_bbd_create(int64_t n, const int64_t* ap, int64_t ap_len, const int64_t* ai,
+                              int64_t ai_len, const int64_t* assignment, int64_t num_blocks) {
+  if (n <= 0 || ap_len != n + 1 || ap[n] != ai_len || !assignment) {
+    fprintf(stderr, "gpuklu_bbd_create: invalid pattern\n");
+    return nullptr;
+  }
+  auto B = std::make_unique<gpuklu_bbd>();
+  B->n = n;
+  B->ap.assign(ap, ap + ap_len);
+  B->ai.assign(ai, ai + ai_len);
+  B->d = gk::bbd_decompose((int)n, ap, ai, assignment, (int)num_blocks);
+  const gk::BbdDecomp& d = B->d;
+  const double ratio = (double)d.border_size / (double)n;
+  B->fallback = d.num_blocks <= 1 || d.border_size == 0 || ratio > 0.5;  // bbd_solver.rs:418-431
+  if (!B->fallback && d.border_size > 16384) {
+    fprintf(stderr, "gpuklu_bbd_create: border of %d is above the dense limit 16384\n",
+            d.border_size);
+    return nullptr;
+  }
+  B->M = gpuklu_create(B->fallback ? n : d.border_start);
+  if (!B->M) return nullptr;
+  gpuklu_set_pivot_mode(B->M, GPUKLU_PIVOT_EXACT);
+  if (!B->fallback) {  // SparseLU per block (bbd_solver.rs:436-444): AMD, no row exchanges
+    gpuklu_set_pivot_mode(B->M, GPUKLU_PIVOT_REFERENCE);
+    B->M->given_blocks = d.block_ptr;
+    B->M->no_swap = true;
+  }
+  int st;
+  if (B->fallback) {
+    st = gpuklu_analyze(B->M, ap, ap_len, ai, ai_len);
+  } else {
+    const int nm = d.border_start;
+    B->m_ap.assign(nm + 1, 0);
+    for (int c = 0; c < nm; ++c) {
+      const int oc = d.perm[c];
+      for (i64 q = ap[oc]; q < ap[oc + 1]; ++q) {
+        const int orow = (int)ai[q];
+        if (orow >= n) continue;
+        const int nr = d.inv_perm[orow];
+        if (nr < nm && d.block_of[nr] == d.block_of[c]) {
+          B->m_ai.push_back(nr);
+          B->m_raw.push_back((i32)q);
+        }
+      }
+      B->m_ap[c + 1] = (i64)B->m_ai.size();
+    }
+    st = gpuklu_analyze(B->M, B->m_ap.data(), (int64_t)B->m_ap.size(), B->m_ai.data(),
+                        (int64_t)B->m_ai.size());
+  }
+  if (st != GPUKLU_OK) {
+    fprintf(stderr, "gpuklu_bbd_create: %s\n", B->M->err.c_str());
+    return nullptr;
+  }
+  cudaStream_t s = B->stream();
+  B->perm32.assign(d.perm.begin(), d.perm.end());
+  cudaError_t e = B->d_m_raw.upload(B->m_raw, s);
+  if (e == cudaSuccess) e = B->d_perm.upload(B->perm32, s);
+  if (e == cudaSuccess) e = B->d_ax.resize(std::max<int64_t>(ai_len, 1));
+  for (auto* b : {&B->d_rhs, &B->d_x, &B->d_newx})
+    if (e == cudaSuccess) e = b->resize(n);
+  if (e == cudaSuccess) e = B->d_nstate.resize(1);
+  if (e == cudaSuccess) e = B->d_status.resize(1);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B->d_status.p, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "gpuklu_bbd_create: %s\n", cudaGetErrorString(e));
+    return nullptr;
+  }
+  return B.release();
+}
+
+void gpuklu_bbd_destroy(gpuklu_bbd* b) { delete b; }
+
+const char* gpuklu_bbd_last_error(const gpuklu_bbd* b) { return b ? b->err.c_str() : ""; }
+
+int gpuklu_bbd_info(const gpuklu_bbd* b, int64_t* out) {
+  if (!b) return GPUKLU_INVALID_MATRIX;
+  out[0] = b->d.num_blocks;
+  out[1] = b->d.border_start;
+  out[2] = b->d.border_size;
+  out[3] = b->fallback ? 1 : 0;
+  out[4] = b->ntiles;
+  out[5] = b->M ? b->M->cur_plan().nblocks : 0;
+  return GPUKLU_OK;
+}
+
+int gpuklu_bbd_perm(const gpuklu_bbd* b, int64_t* perm) {
+  if (!b) return GPUKLU_INVALID_MATRIX;
+  for (int64_t i = 0; i < b->n; ++i) perm[i] = b->d.perm[i];
+  return GPUKLU_OK;
+}
+
+int gpuklu_bbd_factor(gpuklu_bbd* b, const double* ax) {
+  if (!b || !ax) return GPUKLU_INVALID_MATRIX;
+  cudaError_t e = cudaMemcpyAsync(b->d_ax.p, ax, b->ai.size() * 8, cudaMemcpyHostToDevice,
+                                  b->stream());
+  if (e != cudaSuccess) return b->fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd factor"));
+  return b->factor_device(true);
+}
+
+int gpuklu_bbd_solve(gpuklu_bbd* b, double* rhs, int64_t len) {
+  if (!b || !rhs || len != b->n) return GPUKLU_INVALID_MATRIX;
+  if (!b->fallback && !b->tiles_ready) return b->fail(GPUKLU_SOLVE_FAILED, "solve before factor");
+  cudaStream_t s = b->stream();
+  cudaError_t e = cudaMemcpyAsync(b->d_rhs.p, rhs, len * 8, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return b->fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd solve"));
+  int st = b->solve_device(b->d_rhs.p, b->d_x.p);
+  if (st) return st;
+  e = cudaMemcpyAsync(rhs, b->d_x.p, len * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return b->fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd solve"));
+  int stt = b->M->check_status("bbd solve");
+  return stt ? b->fail(stt, b->M->err) : GPUKLU_OK;
+}
+
+int gpuklu_bbd_newton_dc(gpuklu_bbd* b, gpuklu_circuit* c, const gpuklu_newton_config* cfg,
+                         const double* x0, double* x_out, int64_t x_cap, int64_t* x_len,
+                         int64_t* iters, int64_t* iters_total, int* reason) {
+  if (!b || !c || !cfg) return GPUKLU_INVALID_MATRIX;
+  if (c->n != b->n || c->ap != b->ap || c->ai != b->ai)
+    return b->fail(GPUKLU_INVALID_MATRIX, "the circuit's pattern differs from the solver's");
+  cudaStream_t s = b->stream();
+  const int nc = c->node_count, n = c->n;
+  cudaError_t e = b->d_rhs_c.resize(std::max(c->ncontrib, 1));
+  std::vector<double> xinit(n, 0.0);
+  if (x0) std::copy(x0, x0 + nc, xinit.begin());
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_newx.p, xinit.data(), n * 8, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return b->fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd newton"));
+  const gk::NewtonCfg ncfg = to_newton_cfg(*cfg);
+  const double gstart = std::max(cfg->gmin * 1e3, 1e-6);
+  int64_t total = 0, last = 0;
+  int rsn = 1;
+  bool conv = false, failed = false;
+  for (int64_t gi = 0; gi <= cfg->gmin_steps && !conv && !failed; ++gi) {
+    const double gmin = cfg->gmin_steps == 0
+                            ? cfg->gmin
+                            : gstart + (cfg->gmin - gstart) * ((double)gi / (double)cfg->gmin_steps);
+    for (int64_t si = 0; si <= cfg->source_steps && !conv && !failed; ++si) {
+      const double scale = cfg->source_steps == 0 ? 1.0 : (double)si / (double)cfg->source_steps;
+      gk::NewtonState ns{cfg->damping, DBL_MAX, 0.0, 0, 0};
+      e = cudaMemcpyAsync(b->d_nstate.p, &ns, sizeof(ns), cudaMemcpyHostToDevice, s);
+      if (e != cudaSuccess) return b->fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd newton"));
+      int64_t it = 0;
+      rsn = 1;
+      for (; it < cfg->max_iters; ++it) {
+        gk::launch_stamp(c->dc, b->d_newx.p, nc, gmin, scale, 0.0, nullptr, -1.0, b->d_ax.p,
+                         b->d_rhs_c.p, b->d_rhs.p, s);
+        int st = b->factor_device(false);
+        if (st == GPUKLU_OK) st = b->solve_device(b->d_rhs.p, b->d_x.p);
+        if (st != GPUKLU_OK) {
+          rsn = 2;
+          failed = true;
+          ++it;
+          break;
+        }
+        gk::launch_newton_update(nc, n, b->d_newx.p, b->d_x.p, b->d_nstate.p, ncfg,
+                                 b->d_status.p, s);
+        gk::NewtonState hs;
+        e = cudaMemcpyAsync(&hs, b->d_nstate.p, sizeof(hs), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return b->fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd newton"));
+        st = b->M->check_status("bbd iteration");
+        if (st) {
+          rsn = 2;
+          failed = true;
+          ++it;
+          break;
+        }
+        if (hs.converged) {
+          conv = true;
+          rsn = 0;
+          ++it;
+          break;
+        }
+      }
+      total += it;
+      last = it;
+    }
+  }
+  const int64_t len = conv ? n : nc;
+  std::vector<double> xh(n);
+  e = cudaMemcpyAsync(xh.data(), b->d_newx.p, n * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return b->fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd newton"));
+  for (int64_t i = 0; i < std::min(len, x_cap); ++i) x_out[i] = xh[i];
+  if (x_len) *x_len = len;
+  if (iters) *iters = last;
+  if (iters_total) *iters_total = total;
+  if (reason) *reason = rsn;
+  return GPUKLU_OK;
+}
 
 }  // extern "C"
 

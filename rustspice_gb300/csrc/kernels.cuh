@@ -110,6 +110,24 @@ struct BatchArgs {
   const long long* grad_off;
 };
 
+// Bordered-block-diagonal solver: the index lists its kernels read.
+struct BbdArgs {
+  int ntiles, bs, border_start;
+  const int* tile_pos0;        // first plan position of the tile's block
+  const int* tile_size;        // block size
+  const long long* tile_off;   // offset of the tile's [size][32] array
+  const int* tile_blk;         // plan block of the tile
+  const int *init_ptr, *init_code, *init_raw;  // R entries: (row offset * 32 + lane, raw)
+  // border indices below are Schur positions (the elimination order of S)
+  const int *bt_ptr, *bt_row, *bt_raw;         // B_T by Schur column
+  const int *yref_ptr, *yref;                  // per border column: (tile << 5 | lane)
+  const int *c_ptr, *c_row, *c_pos, *c_raw;    // C by plan block: (border row, row offset of Y, raw)
+  const int *crow_ptr, *crow_col, *crow_raw;   // C by border row: (block column, raw)
+  const int *rrow_ptr, *rrow_col, *rrow_raw;   // R by block row: (border column, raw)
+  const int* perm;                             // bordered order -> original index
+  const int* bperm;                            // Schur position -> original index
+};
+
 // --------------------------------------------------------------- launches
 void launch_first_factor(const DPlan& P, const double* ax, double* lu, double* work,
                          int* rperm, int* rinv, double tol, int* status, cudaStream_t s);
@@ -135,6 +153,21 @@ double fp64_peak_tflops();
 void launch_batch_newton(const BatchArgs& a, int m, int grid, int warps_per_block,
                          cudaStream_t s);
 // Registers per thread and resident blocks per SM of the batched kernel.
+// Bordered-block-diagonal solver pieces.
+void launch_bbd_ysolve(const DPlan& P, const double* lu, const double* ax, const BbdArgs& B,
+                       double* ybuf, cudaStream_t s);
+void launch_bbd_schur(const double* ax, const BbdArgs& B, const double* ybuf, double* S,
+                      cudaStream_t s);
+void launch_dense_lu(double* S, int bs, cudaStream_t s);
+void launch_dense_lu_solve(const double* S, int bs, double* x, cudaStream_t s);
+void launch_bbd_border_rhs(const double* ax, const double* rhs, const double* z,
+                           const BbdArgs& B, double* bb, cudaStream_t s);
+void launch_bbd_rmatvec(const double* ax, const double* xT, const BbdArgs& B, double* w,
+                        cudaStream_t s);
+void launch_gather(double* dst, const double* src, const int* idx, int n, cudaStream_t s);
+void launch_bbd_combine(const double* z, const double* w2, const double* xT, const BbdArgs& B,
+                        double* x, cudaStream_t s);
+
 // Transient forward / adjoint over a batch: one warp per instance.
 void launch_tran_forward(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
 void launch_tran_backward(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);

@@ -33,7 +33,8 @@ SYMBOLS = [
     "gpuklu_batch_destroy", "gpuklu_batch_run", "gpuklu_batch_results",
     "gpuklu_batch_update_inputs", "gpuklu_batch_last_error", "gpuklu_batch_info",
     "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_tran_create", "gpuklu_tran_forward",
-    "gpuklu_tran_backward", "gpuklu_fp64_peak_tflops", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free",
+    "gpuklu_tran_backward", "gpuklu_bbd_create", "gpuklu_bbd_destroy", "gpuklu_bbd_last_error",
+    "gpuklu_bbd_info", "gpuklu_bbd_perm", "gpuklu_bbd_factor", "gpuklu_bbd_solve", "gpuklu_bbd_newton_dc", "gpuklu_fp64_peak_tflops", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free",
 ]
 
 
@@ -104,6 +105,14 @@ def lib(build_if_missing: bool = True):
                                     _D]),
         "gpuklu_tran_forward": (C.c_int, [_P, _P, _P, _P, _P, _P]),
         "gpuklu_tran_backward": (C.c_int, [_P, _P, _P, _P]),
+        "gpuklu_bbd_create": (_P, [_I64, _P, _I64, _P, _I64, _P, _I64]),
+        "gpuklu_bbd_destroy": (None, [_P]),
+        "gpuklu_bbd_last_error": (C.c_char_p, [_P]),
+        "gpuklu_bbd_info": (C.c_int, [_P, _P]),
+        "gpuklu_bbd_perm": (C.c_int, [_P, _P]),
+        "gpuklu_bbd_factor": (C.c_int, [_P, _P]),
+        "gpuklu_bbd_solve": (C.c_int, [_P, _P, _I64]),
+        "gpuklu_bbd_newton_dc": (C.c_int, [_P, _P, _P, _P, _P, _I64, _P, _P, _P, _P]),
         "gpuklu_fp64_peak_tflops": (_D, []),
         "gpuklu_solve_device_noalloc": (C.c_int, [_P, _P, _P]),
         "gpuklu_dc_backward": (C.c_int, [_P, _P, _P, _I64, _P, _D, _P, _P]),

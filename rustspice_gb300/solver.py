@@ -354,3 +354,70 @@ class TranBatch:
     def stream(self) -> int:
         return N.lib().gpuklu_batch_stream(self._h) or 0
 
+
+class BbdSolver:
+    """The reference's BbdSolver with a known partition, on the GPU.
+
+    ``assignment[i]``: block of node i, -1 for the border. ``factor`` /
+    ``solve`` follow the LinearSolver calls (host arrays, original order);
+    ``newton_dc`` runs the device Newton loop of a compiled circuit whose
+    pattern is the solver's."""
+
+    def __init__(self, ap, ai, assignment, num_blocks):
+        ap, ai, asg = N.i64(ap), N.i64(ai), N.i64(assignment)
+        self.n = len(ap) - 1
+        self._h = N.lib().gpuklu_bbd_create(self.n, N.ptr(ap), len(ap), N.ptr(ai), len(ai),
+                                            N.ptr(asg), num_blocks)
+        if not self._h:
+            raise RuntimeError("gpuklu_bbd_create failed")
+        self.nnz = len(ai)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().gpuklu_bbd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, st):
+        if st != N.OK:
+            raise SolverError(st, N.lib().gpuklu_bbd_last_error(self._h).decode())
+
+    def info(self) -> dict:
+        out = np.zeros(6, np.int64)
+        self._check(N.lib().gpuklu_bbd_info(self._h, N.ptr(out)))
+        return dict(num_blocks=int(out[0]), border_start=int(out[1]), border_size=int(out[2]),
+                    fallback=bool(out[3]), tiles=int(out[4]), inner_blocks=int(out[5]))
+
+    def perm(self) -> np.ndarray:
+        p = np.zeros(self.n, np.int64)
+        self._check(N.lib().gpuklu_bbd_perm(self._h, N.ptr(p)))
+        return p
+
+    def factor(self, ax) -> None:
+        ax = N.f64(ax)
+        if len(ax) != self.nnz:
+            raise SolverError(N.INVALID_MATRIX, "ax and ai lengths differ")
+        self._check(N.lib().gpuklu_bbd_factor(self._h, N.ptr(ax)))
+
+    def solve(self, rhs: np.ndarray) -> None:
+        """Overwrites ``rhs`` (contiguous float64) with x."""
+        if not (isinstance(rhs, np.ndarray) and rhs.dtype == np.float64 and rhs.flags.c_contiguous):
+            raise TypeError("rhs must be a contiguous float64 numpy array")
+        self._check(N.lib().gpuklu_bbd_solve(self._h, N.ptr(rhs), len(rhs)))
+
+    def newton_dc(self, dc: "DeviceCircuit", cfg: N.NewtonConfig, x0=None) -> NewtonResult:
+        n = dc.n
+        x = np.zeros(n)
+        xl = C.c_int64()
+        it = C.c_int64()
+        itt = C.c_int64()
+        rs = C.c_int()
+        x0a = N.f64(x0) if x0 is not None else None
+        self._check(N.lib().gpuklu_bbd_newton_dc(self._h, dc.handle, C.byref(cfg),
+                                                 N.ptr(x0a) if x0a is not None else None,
+                                                 N.ptr(x), n, C.byref(xl), C.byref(it),
+                                                 C.byref(itt), C.byref(rs)))
+        return NewtonResult(rs.value == 0, it.value, itt.value, REASONS[rs.value], x[:xl.value])
+

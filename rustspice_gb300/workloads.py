@@ -121,3 +121,16 @@ def ring_batch(count: int = 1024, seed: int = 5) -> RingBatch:
     off = np.zeros(count, np.int64)
     off[1:] = np.cumsum([len(x) for x in xs])[:-1]
     return RingBatch(circuits, np.concatenate(xs), off)
+
+
+def bordered_nodeset(c: cz.Circuit, v: float = 0.55) -> np.ndarray:
+    """Initial iterate of the bordered-mesh case: every node but ground at
+    0.55 V, inside the diodes' conduction knee (a `.nodeset`). From the zero
+    start the first linear solve lifts the unloaded meshes to the supply
+    voltage and the unlimited diode exponentials (the reference evaluates
+    them at the raw iterate) stall Newton; the reference's source stepping
+    would not help, because its schedule starts at scale 0 and returns the
+    first converged step (crates/sim-core/src/newton.rs:164-179)."""
+    x = np.full(c.node_count, v)
+    x[0] = 0.0
+    return x

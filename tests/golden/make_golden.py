@@ -172,7 +172,26 @@ def kats():
                    nodes=[[1, 0, 0, 0], [1, 2, 0, 0], [2, 0, 0, 0]],
                    p=[[1.0, 0, 0, 0, 0, 0], [1e3, 0, 0, 0, 0, 0], [2e3, 0, 0, 0, 0, 0]],
                    expect={"1": 1.0, "2": 2.0 / 3.0}, tol=1e-6)
-    return dict(solve=out, refactor=refactor, rcond=rcond, stamps=stamps, divider=divider)
+    bbd = [  # bbd_solver.rs tests, with the partition each test's comment states
+        dict(name="bbd_block_diagonal", src="crates/sim-core/src/bbd_solver.rs:1173-1193",
+             ap=[0, 2, 4, 6, 8], ai=[0, 1, 0, 1, 2, 3, 2, 3],
+             ax=[2.0, 1.0, 1.0, 3.0, 4.0, 1.0, 1.0, 2.0], b=[7.0, 11.0, 17.0, 6.0],
+             assignment=[0, 0, 1, 1], nblocks=2, fallback=True),
+        dict(name="bbd_bordered_5", src="crates/sim-core/src/bbd_solver.rs:1231-1291",
+             ap=[0, 2, 5, 7, 10, 13], ai=[0, 1, 0, 1, 4, 2, 3, 2, 3, 4, 1, 3, 4],
+             ax=[4.0, 1.0, 1.0, 4.0, 1.0, 4.0, 1.0, 1.0, 4.0, 1.0, 1.0, 1.0, 3.0],
+             b=[5.0, 10.0, 5.0, 10.0, 8.0], assignment=[0, 0, 1, 1, -1], nblocks=2,
+             fallback=False),
+        dict(name="bbd_bordered_8", src="crates/sim-core/src/bbd_solver.rs:1294-1363",
+             ap=[0, 2, 5, 8, 10, 13, 16, 19, 22],
+             ai=[0, 1, 0, 1, 2, 1, 2, 6, 3, 4, 3, 4, 5, 4, 5, 7, 2, 6, 7, 5, 6, 7],
+             ax=[2.0, -1.0, -1.0, 2.0, -1.0, -1.0, 2.0, 1.0, 2.0, -1.0, -1.0, 2.0, -1.0, -1.0,
+                 2.0, 1.0, 1.0, 3.0, 0.5, 1.0, 0.5, 3.0],
+             b=[1.0, 2.0, 3.0, 1.0, 2.0, 3.0, 4.0, 4.0],
+             assignment=[0, 0, 0, 1, 1, 1, -1, -1], nblocks=2, fallback=False),
+    ]
+    return dict(solve=out, refactor=refactor, rcond=rcond, stamps=stamps, divider=divider,
+                bbd=bbd)
 
 
 def main(ref: str) -> None:
