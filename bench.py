@@ -47,6 +47,8 @@ def _args():
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="instances timed on the host cores (0: sized for ~15 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the single-circuit, adjoint, transient and bordered-block lines")
     return ap.parse_args()
 
 
@@ -185,6 +187,95 @@ def _ncu_traffic(iters_per_step):
     except (OSError, AttributeError, ValueError):
         return None, "no ncu summary"
     return per * iters_per_step, f"{os.path.relpath(path, ROOT)} ({per:.1f} B per iteration)"
+
+
+def secondary(with_cpu=True):
+    """The other workloads of the path, each timed once warm (CUDA-synchronised
+    wall clock around the public call): the 32x32 diode mesh with gmin
+    stepping, the 20k-node adjoint, the 1024-ring transient adjoint and the
+    64-mesh bordered-block-diagonal DC solve, with the oracle's time for the
+    same work on one host core where it is short."""
+    import torch
+    from oracle import pyoracle as po
+    from rustspice_gb300 import circuits as cz
+    from rustspice_gb300 import native as N
+    from rustspice_gb300 import workloads as wl
+    from rustspice_gb300.solver import (BbdSolver, DeviceCircuit, GpuKluSolver, TranBatch,
+                                        dc_backward, dc_forward, newton_dc)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    out = {}
+    ocfg = {k: wl.TIGHT[k] for k in ("max_iters", "abs_tol", "rel_tol", "gmin", "gmin_steps")}
+    # diode mesh, gmin stepping (one circuit, device-resident Newton)
+    c = cz.mesh_dc()
+    cfg = N.newton_config(**dict(wl.TIGHT, gmin_steps=10))
+    g = GpuKluSolver(1, pivot_mode=N.PIVOT_EXACT)
+    dc = DeviceCircuit(c)
+    newton_dc(g, dc, cfg)
+    r, t = timed(lambda: newton_dc(g, dc, cfg))
+    e = {"workload": "32x32 diode mesh, gmin stepping (10 steps)", "n": dc.n,
+         "newton_iterations": r.iterations_total, "gpu_ms": t * 1e3}
+    if with_cpu:
+        t0 = time.perf_counter()
+        ro = po.dc_op(c, "nativeklu_exact", **dict(ocfg, gmin_steps=10))
+        e["oracle_ms_1core"] = (time.perf_counter() - t0) * 1e3
+    out["mesh_dc"] = e
+    # DC adjoint of the 20k-node mesh with inverters
+    c = cz.mesh_with_inverters(120, 1000)
+    outs = cz.output_nodes(c, 256)
+    g = GpuKluSolver(1, pivot_mode=N.PIVOT_EXACT)
+    dc = DeviceCircuit(c)
+    cfg = N.newton_config(**wl.TIGHT)
+    f = dc_forward(g, dc, cfg)
+    f, t_f = timed(lambda: dc_forward(g, dc, cfg))
+    dl = np.zeros(dc.n)
+    dl[outs] = 2.0 * (f.x[outs] - 0.6)
+    dc_backward(g, dc, f.x, dl)
+    _, t_b = timed(lambda: dc_backward(g, dc, f.x, dl))
+    out["dc_adjoint"] = {"workload": "120x120 mesh + 1000 inverters, loss on 256 nodes",
+                         "n": dc.n, "forward_ms": t_f * 1e3, "newton_iterations": f.iterations,
+                         "backward_ms": t_b * 1e3, "backward_over_forward": t_b / t_f}
+    # transient adjoint of 1024 rings
+    B = wl.ring_batch(1024)
+    tb = TranBatch(B.circuits, B.x_init, B.x_off, wl.RING_DT, wl.RING_STEPS, wl.RING_CKPT,
+                   wl.RING_PROBE, wl.RING_TARGET)
+    cfg = N.newton_config(**wl.TIGHT)
+    tb.forward(cfg)
+    (loss, _, it, rs), t_f = timed(lambda: tb.forward(cfg))
+    _, t_b = timed(lambda: tb.backward(cfg))
+    out["transient_adjoint"] = {
+        "workload": "1024 CMOS rings (11-101 stages) x 2000 BE steps of 1 ps, checkpoint 50",
+        "forward_ms": t_f * 1e3, "backward_ms": t_b * 1e3, "backward_over_forward": t_b / t_f,
+        "newton_iterations_forward": int(it.sum()), "converged_fraction": float(np.mean(rs == 0))}
+    tb.close()
+    # bordered block diagonal
+    c, asg, nb = cz.bordered_meshes()
+    dc = DeviceCircuit(c)
+    ap, ai = dc.pattern()
+    bb = BbdSolver(ap, ai, asg, nb)
+    x0 = wl.bordered_nodeset(c)
+    cfg = N.newton_config(**wl.TIGHT)
+    bb.newton_dc(dc, cfg, x0=x0)
+    r, t = timed(lambda: bb.newton_dc(dc, cfg, x0=x0))
+    info = bb.info()
+    e = {"workload": "64 meshes (side 30-50) + 1024 border nodes, known partition",
+         "n": dc.n, "border": info["border_size"], "newton_iterations": r.iterations,
+         "gpu_ms_per_iteration": t * 1e3 / max(r.iterations, 1)}
+    if with_cpu:
+        ts = []
+        for k in (1, 3):  # the difference removes the analysis
+            t0 = time.perf_counter()
+            po.dc_op_bbd(c, asg, nb, x0=x0, **dict(ocfg, max_iters=k))
+            ts.append(time.perf_counter() - t0)
+        e["oracle_ms_per_iteration_1core"] = (ts[1] - ts[0]) * 1e3 / 2
+    out["bbd"] = e
+    return out
 
 
 def run_gpu(a):
@@ -328,6 +419,8 @@ def run_gpu(a):
     }
     if not a.no_cpu_baseline and rank == 0:
         line["cpu_baseline"] = cpu_baseline(B, a, cfg_dict=wl.TIGHT)
+    if not a.no_secondary and rank == 0:
+        line["secondary"] = secondary(with_cpu=not a.no_cpu_baseline)
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:
