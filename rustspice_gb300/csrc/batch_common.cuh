@@ -21,11 +21,14 @@ constexpr unsigned kFull = 0xffffffffu;
 // lanes instead of by one lane.
 constexpr int kHeavy = 12;
 
+// S: element stride of dv (1 in shared memory; 32 in a lane-interleaved
+// scratch, where element i of a lane's array sits at [i * 32])
+template <int S = 1>
 __device__ __forceinline__ double contrib(const double* dv, int code) {
   const int kind = code & 7, idx = code >> 3;
   switch (kind) {
-    case 0: return dv[idx];
-    case 1: return -dv[idx];
+    case 0: return dv[idx * S];
+    case 1: return -dv[idx * S];
     case 2: return 1.0;
     case 3: return -1.0;
     default: return 0.0;
@@ -38,10 +41,11 @@ __device__ __forceinline__ double contrib(const double* dv, int code) {
 // M [is_pmos, vth0, beff]; MC [polarity, |vth0|, beff]; C [C, C/dt].
 // gdev is the level-1 conductance floor (1e-12 as the reference has it; 0
 // for the exact Jacobian of the adjoint).
+template <int S = 1>
 __device__ __forceinline__ void eval_record(int type, const int* nd, const double* dp,
                                             const double* X, const double* XP, int nc,
                                             double gmin, double gdev, double* rec) {
-  auto xg = [&](int i) { return (i >= 0 && i < nc) ? X[i] : 0.0; };
+  auto xg = [&](int i) { return (i >= 0 && i < nc) ? X[i * S] : 0.0; };
   switch (type) {
     case 0:
     case 1:
@@ -94,8 +98,8 @@ __device__ __forceinline__ void eval_record(int type, const int* nd, const doubl
     }
     case 5: {  // backward-Euler capacitor companion, physical sign
       const double g = dp[1];
-      const double vp = ((nd[0] >= 0 && nd[0] < nc) ? XP[nd[0]] : 0.0) -
-                        ((nd[1] >= 0 && nd[1] < nc) ? XP[nd[1]] : 0.0);
+      const double vp = ((nd[0] >= 0 && nd[0] < nc) ? XP[nd[0] * S] : 0.0) -
+                        ((nd[1] >= 0 && nd[1] < nc) ? XP[nd[1] * S] : 0.0);
       rec[0] = g;
       rec[1] = g * vp;
       break;
@@ -199,6 +203,7 @@ struct Prog {
   const int* udst;     // staged: update destinations
   const int *dev_type, *dev_nodes, *dev_dv, *amap_ptr, *amap_code, *rmap_ptr, *rmap_code,
       *in_row, *out_pos, *offd_ptr, *offd_col, *bptr, *heavy;
+  const int *lvl_col, *lseg_ptr, *lseg;  // level schedule of the factorization
   int n, nc, nv, nslots, ndev, nblocks, nheavy;
 };
 
@@ -244,6 +249,9 @@ __device__ __forceinline__ Prog stage_program(const BatchArgs& A, const GroupHdr
   P.offd_col = A.offd_col + G.offd_off;
   P.bptr = A.block_ptr + G.blk_off;
   P.heavy = A.heavy + G.heavy_off;
+  P.lvl_col = A.lvl_col + G.col_off;
+  P.lseg_ptr = A.lseg_ptr + G.blk_off;
+  P.lseg = A.lseg + 3 * G.seg_off;
   P.n = n;
   P.nc = G.node_count;
   P.nslots = G.nslots;
@@ -317,12 +325,37 @@ __device__ __forceinline__ void assemble(const Prog& P, const double* DV, double
   }
 }
 
-// Factor + forward substitution, then backward substitution, block by block
+// Factor, forward substitution, backward substitution, block by block
 // (blocks in order; the BTF coupling lies below the diagonal blocks).
+// The factorization follows the program's level schedule: in a parallel
+// segment every lane factors whole columns of one level (each column reads
+// only finished columns and writes only its own slots, its U entries in
+// order), in a sequential segment (the rails) the lanes share each update.
 // Afterwards V[dslot] holds the reciprocal of the (perturbed) pivot and T
 // the permuted solution.
+__device__ __forceinline__ void factor_column(const Prog& P, double* V, int k) {
+  const int4 ck = P.colrec[k];
+  for (int s = ck.x; s < ck.y; ++s) {
+    const double u = V[s];
+    if (nonzero(u)) {
+      const int4 cj = P.colrec[P.srow[s]];
+      const int q0 = cj.y + 1;
+      const int* dst = P.udst + P.uptr[s] - q0;
+      for (int qq = q0; qq < cj.z; ++qq) {
+        const int dd = dst[qq];
+        V[dd] = fma(-V[qq], u, V[dd]);
+      }
+    }
+  }
+  const double r = fast_rcp(perturb_bits(V[ck.y], ck.w != 0));
+  for (int qq = ck.y + 1; qq < ck.z; ++qq) V[qq] = V[qq] * r;
+  V[ck.y] = r;
+}
+
+// Column by column, lanes over each update, forward substitution fused.
 template <int LPI>
-__device__ __forceinline__ void factor_solve(const Prog& P, double* V, double* T, int sl) {
+__device__ __forceinline__ void factor_solve_columns(const Prog& P, double* V, double* T,
+                                                     int sl) {
   for (int b = 0; b < P.nblocks; ++b) {
     const int b0 = P.bptr[b], b1 = P.bptr[b + 1];
     for (int i = b0 + sl; i < b1; i += LPI)
@@ -353,6 +386,70 @@ __device__ __forceinline__ void factor_solve(const Prog& P, double* V, double* T
         T[row] = fma(-l, zk, T[row]);
       }
       if (sl == 0) V[ck.y] = r;
+      __syncwarp();
+    }
+    for (int k = b1 - 1; k >= b0; --k) {
+      const int4 ck = P.colrec[k];
+      const double xk = T[k] * V[ck.y];
+      for (int s = ck.x + sl; s < ck.y; s += LPI) {
+        const int row = P.srow[s];
+        T[row] = fma(-V[s], xk, T[row]);
+      }
+      __syncwarp();
+      if (sl == 0) T[k] = xk;
+      __syncwarp();
+    }
+  }
+}
+
+template <int LPI>
+__device__ __forceinline__ void factor_solve(const Prog& P, double* V, double* T, int sl) {
+  if (P.lseg_ptr[P.nblocks] == 0) {  // no level schedule for this program
+    factor_solve_columns<LPI>(P, V, T, sl);
+    return;
+  }
+  for (int b = 0; b < P.nblocks; ++b) {
+    const int b0 = P.bptr[b], b1 = P.bptr[b + 1];
+    for (int i = b0 + sl; i < b1; i += LPI)
+      for (int e = P.offd_ptr[i]; e < P.offd_ptr[i + 1]; ++e)
+        T[i] = fma(-V[P.nslots + e], T[P.offd_col[e]], T[i]);
+    for (int g = P.lseg_ptr[b]; g < P.lseg_ptr[b + 1]; ++g) {
+      const int start = P.lseg[3 * g], end = P.lseg[3 * g + 1];
+      if (P.lseg[3 * g + 2] == 0) {
+        for (int idx = start + sl; idx < end; idx += LPI) factor_column(P, V, P.lvl_col[idx]);
+        __syncwarp();
+        continue;
+      }
+      for (int idx = start; idx < end; ++idx) {
+        const int k = P.lvl_col[idx];
+        const int4 ck = P.colrec[k];
+        for (int s = ck.x; s < ck.y; ++s) {
+          const double u = V[s];
+          if (nonzero(u)) {
+            const int4 cj = P.colrec[P.srow[s]];
+            const int q0 = cj.y + 1;
+            const int* dst = P.udst + P.uptr[s] - q0;
+            for (int qq = q0 + sl; qq < cj.z; qq += LPI) {
+              const int dd = dst[qq];
+              V[dd] = fma(-V[qq], u, V[dd]);
+            }
+          }
+          __syncwarp();
+        }
+        const double r = fast_rcp(perturb_bits(V[ck.y], ck.w != 0));
+        for (int qq = ck.y + 1 + sl; qq < ck.z; qq += LPI) V[qq] = V[qq] * r;
+        __syncwarp();
+        if (sl == 0) V[ck.y] = r;
+        __syncwarp();
+      }
+    }
+    for (int k = b0; k < b1; ++k) {  // L z = b, column order
+      const int4 ck = P.colrec[k];
+      const double zk = T[k];
+      for (int qq = ck.y + 1 + sl; qq < ck.z; qq += LPI) {
+        const int row = P.srow[qq];
+        T[row] = fma(-V[qq], zk, T[row]);
+      }
       __syncwarp();
     }
     for (int k = b1 - 1; k >= b0; --k) {

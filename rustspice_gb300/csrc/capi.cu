@@ -902,6 +902,7 @@ struct gpuklu_batch {
   DBuf<i32> d_order, d_dev_type, d_dev_nodes, d_dev_dv, d_amap_ptr, d_amap_code,
       d_rmap_ptr, d_rmap_code, d_col_ptr, d_dslot, d_col_single, d_in_row, d_out_pos,
       d_offd_ptr, d_slot_row, d_upd_ptr, d_upd_dst, d_offd_col, d_block_ptr, d_heavy, d_ov_dev,
+      d_lvl_col, d_lseg_ptr, d_lseg,
       d_iters,
       d_iters_total, d_reason, d_status;
   DBuf<double> d_dparams, d_ov_val, d_x0, d_xout;
@@ -918,8 +919,8 @@ struct gpuklu_batch {
   struct Class {
     int m = 1, region = 0, prog_ints = 0, grid = 0, warps_per_block = 1, regs = 0,
         blocks_per_sm = 0;
-    std::vector<i32> tiles;
-    DBuf<i32> d_tiles;
+    std::vector<i32> tiles, tiles2;  // tiles2: after the lane phase (parked instances)
+    DBuf<i32> d_tiles, d_tiles2;
     DBuf<unsigned> d_counter;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
@@ -928,6 +929,13 @@ struct gpuklu_batch {
   std::vector<std::unique_ptr<Class>> classes;
   cudaEvent_t start_ev = nullptr;
   gk::BatchArgs args{};
+  // lane-per-instance phase (k_batch_lanes) in front of the warp classes
+  bool lanes = false;
+  int lane_cap = 0, lane_grid = 0, lane_wpb = 4;
+  std::vector<i32> ltiles;
+  DBuf<i32> d_ltiles, d_cont_list, d_cont_it, d_cont_total, d_cont_gstep;
+  DBuf<unsigned> d_lcounter, d_cont_count, d_gnext2;
+  DBuf<double> d_scratch, d_cont_damp, d_cont_prev;
   // transient
   int transient = 0;
   double dt = 0.0;
@@ -962,7 +970,7 @@ struct Program {
   gk::GroupHdr h{};
   std::vector<i32> dev_type, dev_nodes, dev_dv, amap_ptr, amap_code, rmap_ptr, rmap_code,
       col_ptr, dslot, col_single, in_row, out_pos, offd_ptr, slot_row, upd_ptr, upd_dst,
-      offd_col, block_ptr, heavy;
+      offd_col, block_ptr, heavy, lvl_col, lseg_ptr, lseg;
   int64_t flops = 0, bytes = 0;
   std::string key() const {
     std::string k;
@@ -975,7 +983,8 @@ struct Program {
     k.append((const char*)hdr, sizeof(hdr));
     for (auto* v : {&dev_type, &dev_nodes, &dev_dv, &amap_ptr, &amap_code, &rmap_ptr,
                     &rmap_code, &col_ptr, &dslot, &col_single, &in_row, &out_pos, &offd_ptr,
-                    &slot_row, &upd_ptr, &upd_dst, &offd_col, &block_ptr, &heavy})
+                    &slot_row, &upd_ptr, &upd_dst, &offd_col, &block_ptr, &heavy, &lvl_col,
+                    &lseg_ptr, &lseg})
       app(*v);
     return k;
   }
@@ -1109,6 +1118,51 @@ Program make_program(const gpuklu_circuit& C, const gk::Plan& P) {
   g.upd_dst = P.upd_dst;
   g.offd_col = P.offd_col;
   g.block_ptr.assign(P.block_ptr.begin(), P.block_ptr.end());
+  // Level schedule of the factorization: column k depends on the columns of
+  // its U entries; columns of one level are independent, each writes only
+  // its own slots and performs its updates in the usual order, so lanes can
+  // take them in parallel with results identical to the column order.
+  // Columns with many U entries (the supply and ground rails) run as
+  // sequential segments, lanes spread over each update instead.
+  {
+    const int kHub = 16;
+    std::vector<int> lvl(P.n, 0);
+    g.lseg_ptr.push_back(0);
+    for (int b = 0; b < P.nblocks; ++b) {
+      const int b0 = P.block_ptr[b], b1 = P.block_ptr[b + 1];
+      int top = 0;
+      for (int k = b0; k < b1; ++k) {
+        int l = 0;
+        for (int s = P.col_ptr[k]; s < P.dslot[k]; ++s) l = std::max(l, lvl[P.slot_row[s]]);
+        lvl[k] = l + 1;
+        top = std::max(top, lvl[k]);
+      }
+      for (int l = 1; l <= top; ++l)
+        for (int hub = 0; hub < 2; ++hub) {
+          const int start = (int)g.lvl_col.size();
+          for (int k = b0; k < b1; ++k)
+            if (lvl[k] == l && ((P.dslot[k] - P.col_ptr[k] > kHub) == (hub == 1)))
+              g.lvl_col.push_back(k);
+          const int end = (int)g.lvl_col.size();
+          if (end > start) {
+            g.lseg.push_back(start);
+            g.lseg.push_back(end);
+            g.lseg.push_back(hub);
+          }
+        }
+      g.lseg_ptr.push_back((i32)g.lseg.size() / 3);
+    }
+    g.lvl_col.push_back(0);  // n+1 entries, parallel to the column arrays
+    // Pivoting can chain the columns (an inverter chain's threshold swaps
+    // leave one column per level); then the column-by-column path with lanes
+    // over each update is faster, and the schedule is dropped.
+    int levels = 0;
+    for (int k = 0; k < P.n; ++k) levels = std::max(levels, lvl[k]);
+    if ((int64_t)levels * 4 > P.n) {
+      g.lseg.clear();
+      std::fill(g.lseg_ptr.begin(), g.lseg_ptr.end(), 0);
+    }
+  }
   // FP64 operations of one Newton iteration: device evaluation, assembly
   // additions, refactorization, both substitutions, block coupling, update
   const int64_t nl = P.nnz_l, nu = P.nnz_u - P.n;
@@ -1260,7 +1314,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   const int ng = (int)progs.size();
   std::vector<i32> dev_type, dev_nodes, dev_dv, amap_ptr, amap_code, rmap_ptr, rmap_code,
       col_ptr, dslot, col_single, in_row, out_pos, offd_ptr, slot_row, upd_ptr, upd_dst,
-      offd_col, block_ptr, heavy;
+      offd_col, block_ptr, heavy, lvl_col, lseg_ptr, lseg;
   auto cat = [](std::vector<i32>& dst, const std::vector<i32>& src) {
     dst.insert(dst.end(), src.begin(), src.end());
   };
@@ -1280,6 +1334,8 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     h.heavy_off = (int)heavy.size();
     h.rmap_off = (int)rmap_ptr.size();
     h.rmap_code_off = (int)rmap_code.size();
+    h.seg_off = (int)lseg.size() / 3;
+    h.nseg = (int)pr.lseg.size() / 3;
     cat(dev_type, pr.dev_type);
     cat(dev_nodes, pr.dev_nodes);
     cat(dev_dv, pr.dev_dv);
@@ -1299,6 +1355,9 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     cat(offd_col, pr.offd_col);
     cat(block_ptr, pr.block_ptr);
     cat(heavy, pr.heavy);
+    cat(lvl_col, pr.lvl_col);
+    cat(lseg_ptr, pr.lseg_ptr);
+    cat(lseg, pr.lseg);
     B->groups.push_back(h);
     B->group_flops.push_back(pr.flops);
     B->group_bytes.push_back(pr.bytes);
@@ -1354,7 +1413,9 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       if (pick_m(gregion[g], prog) != C->m || h.inst_count == 0) continue;
       C->region = std::max(C->region, gregion[g]);
       C->prog_ints = std::max(C->prog_ints, prog);
-      for (int t = 0; t < (h.inst_count + C->m - 1) / C->m; ++t) C->tiles.push_back(g);
+      const int nt = (h.inst_count + C->m - 1) / C->m;
+      for (int t = 0; t < nt; ++t) C->tiles.push_back(g);
+      for (int t = 0; t < std::min(nt, 8); ++t) C->tiles2.push_back(g);
     }
     if (C->tiles.empty()) continue;
     gk::batch_kernel_info(C->m, C->warps_per_block, C->region, C->prog_ints, &C->regs,
@@ -1391,12 +1452,55 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   UP(d_col_single, col_single) UP(d_in_row, in_row) UP(d_out_pos, out_pos)
   UP(d_offd_ptr, offd_ptr) UP(d_slot_row, slot_row) UP(d_upd_ptr, upd_ptr)
   UP(d_upd_dst, upd_dst) UP(d_offd_col, offd_col) UP(d_block_ptr, block_ptr)
-  UP(d_heavy, heavy) UP(d_dparams, dparams) UP(d_p_off, poff) UP(d_ov_dev, ov_dev) UP(d_ov_val, ov_val)
+  UP(d_heavy, heavy) UP(d_lvl_col, lvl_col) UP(d_lseg_ptr, lseg_ptr) UP(d_lseg, lseg)
+  UP(d_dparams, dparams) UP(d_p_off, poff) UP(d_ov_dev, ov_dev) UP(d_ov_val, ov_val)
   UP(d_x0_off, x0o) UP(d_x_off, B->x_off)
 #undef UP
   for (auto& C : B->classes) {
     if (e == cudaSuccess) e = C->d_tiles.upload(C->tiles, s);
+    if (e == cudaSuccess) e = C->d_tiles2.upload(C->tiles2, s);
     if (e == cudaSuccess) e = C->d_counter.resize(1);
+  }
+  // Lane phase: every group split into tiles of about lane_target instances,
+  // most expensive programs first; a scratch of region x 32 doubles per warp.
+  {
+    const char* env = getenv("GPUKLU_BATCH_LANES");
+    B->lanes = !transient && !(env && env[0] == '0');
+    const char* ecap = getenv("GPUKLU_LANE_CAP");
+    B->lane_cap = ecap ? std::max(1, atoi(ecap)) : 6;
+    const char* etgt = getenv("GPUKLU_LANE_TARGET");
+    const int target = etgt ? std::max(32, atoi(etgt)) : 64;
+    long long lregion = 0;
+    for (int g : gorder) {
+      const gk::GroupHdr& h = B->groups[g];
+      if (h.inst_count == 0) continue;
+      const int nt = std::max(1, (h.inst_count + target - 1) / target);
+      for (int t = 0; t < nt; ++t) B->ltiles.push_back(g);
+      lregion = std::max<long long>(lregion, (long long)h.node_count + h.n + h.ndv + h.nslots +
+                                                 h.noffd + 4LL * h.ndev);
+    }
+    if (B->lanes && !B->ltiles.empty()) {
+      int regs = 0, bps = 0;
+      gk::lanes_kernel_info(B->lane_wpb, &regs, &bps);
+      const long long warps_max = (long long)sm_count() * std::max(bps, 1) * B->lane_wpb;
+      const long long warps = std::min<long long>(warps_max, (long long)B->ltiles.size());
+      B->lane_grid = (int)((warps + B->lane_wpb - 1) / B->lane_wpb);
+      const long long stride = lregion * 32;
+      if (e == cudaSuccess)
+        e = B->d_scratch.resize((size_t)B->lane_grid * B->lane_wpb * (size_t)stride);
+      if (e == cudaSuccess) e = B->d_ltiles.upload(B->ltiles, s);
+      if (e == cudaSuccess) e = B->d_lcounter.resize(1);
+      if (e == cudaSuccess) e = B->d_cont_list.resize(std::max<int64_t>(ninst, 1));
+      for (auto* b : {&B->d_cont_it, &B->d_cont_total, &B->d_cont_gstep})
+        if (e == cudaSuccess) e = b->resize(std::max<int64_t>(ninst, 1));
+      for (auto* b : {&B->d_cont_damp, &B->d_cont_prev})
+        if (e == cudaSuccess) e = b->resize(std::max<int64_t>(ninst, 1));
+      if (e == cudaSuccess) e = B->d_cont_count.resize(std::max(ngr, 1));
+      if (e == cudaSuccess) e = B->d_gnext2.resize(std::max(ngr, 1));
+      B->args.warp_stride = stride;
+    } else {
+      B->lanes = false;
+    }
   }
   if (e == cudaSuccess) {
     std::vector<double> x0v;
@@ -1439,6 +1543,9 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   a.offd_col = B->d_offd_col.p;
   a.block_ptr = B->d_block_ptr.p;
   a.heavy = B->d_heavy.p;
+  a.lvl_col = B->d_lvl_col.p;
+  a.lseg_ptr = B->d_lseg_ptr.p;
+  a.lseg = B->d_lseg.p;
   a.inst_p_off = B->d_p_off.p;
   a.dparams = B->d_dparams.p;
   a.inst_ov_dev = B->d_ov_dev.p;
@@ -1451,6 +1558,22 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   a.inst_x_off = B->d_x_off.p;
   a.x_out = B->d_xout.p;
   a.status = B->d_status.p;
+  if (B->lanes) {
+    a.scratch = B->d_scratch.p;
+    a.warp_stride = B->args.warp_stride;
+    a.ltile_group = B->d_ltiles.p;
+    a.nltiles = (int)B->ltiles.size();
+    a.lcounter = B->d_lcounter.p;
+    a.cap = B->lane_cap;
+    a.cont_list = B->d_cont_list.p;
+    a.cont_count = B->d_cont_count.p;
+    a.gnext2 = B->d_gnext2.p;
+    a.cont_it = B->d_cont_it.p;
+    a.cont_total = B->d_cont_total.p;
+    a.cont_gstep = B->d_cont_gstep.p;
+    a.cont_damp = B->d_cont_damp.p;
+    a.cont_prev = B->d_cont_prev.p;
+  }
   B->args = a;
   for (auto& C : B->classes) {
     C->args = a;
@@ -1650,11 +1773,25 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
   cudaStream_t s = b->stream;
   cudaMemsetAsync(b->d_gnext.p, 0, b->d_gnext.n * sizeof(unsigned), s);
   for (auto& C : b->classes) cudaMemsetAsync(C->d_counter.p, 0, sizeof(unsigned), s);
+  if (b->lanes) {  // phase 1: lane per instance, then the warp classes take the parked ones
+    cudaMemsetAsync(b->d_lcounter.p, 0, sizeof(unsigned), s);
+    cudaMemsetAsync(b->d_cont_count.p, 0, b->d_cont_count.n * sizeof(unsigned), s);
+    cudaMemsetAsync(b->d_gnext2.p, 0, b->d_gnext2.n * sizeof(unsigned), s);
+    gk::BatchArgs la = b->args;
+    la.cfg = c;
+    gk::launch_batch_lanes(la, b->lane_grid, b->lane_wpb, s);
+  }
   cudaEventRecord(b->start_ev, s);
   for (auto& C : b->classes) {  // largest programs first, all classes concurrent
     cudaStreamWaitEvent(C->stream, b->start_ev, 0);
     C->args.cfg = c;
-    gk::launch_batch_newton(C->args, C->m, C->grid, C->warps_per_block, C->stream);
+    gk::BatchArgs ca = C->args;
+    if (b->lanes) {
+      ca.cont_mode = 1;
+      ca.tile_group = C->d_tiles2.p;
+      ca.ntiles = (int)C->tiles2.size();
+    }
+    gk::launch_batch_newton(ca, C->m, C->grid, C->warps_per_block, C->stream);
     cudaEventRecord(C->done, C->stream);
     cudaStreamWaitEvent(s, C->done, 0);
   }
@@ -1715,7 +1852,7 @@ int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out) {
   if (!b) return GPUKLU_INVALID_MATRIX;
   for (int q = 0; q < 8; ++q) out[q] = 0;
   out[2] = (int64_t)b->groups.size();
-  out[6] = (int64_t)b->classes.size();
+  out[6] = (int64_t)b->classes.size() + (b->lanes ? 1 : 0);
   for (auto& C : b->classes) {  // the largest class (first) describes the launch
     out[0] += C->grid;
     if (out[1] == 0) {

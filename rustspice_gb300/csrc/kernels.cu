@@ -752,22 +752,37 @@ __global__ void k_batch_newton(BatchArgs A) {
       const unsigned want = __ballot_sync(FULL, need) & leaders;
       if (want) {
         const int first_lane = __ffs(want) - 1;
+        unsigned* const ctr = A.cont_mode ? &A.gnext2[g] : &A.gnext[g];
         int base = 0;
-        if (lane == first_lane) base = (int)atomicAdd(&A.gnext[g], (unsigned)__popc(want));
+        if (lane == first_lane) base = (int)atomicAdd(ctr, (unsigned)__popc(want));
         base = __shfl_sync(FULL, base, first_lane);
         if (need) {
           const int k = base + __popc(want & ((1u << lead) - 1));
-          if (k < G.inst_count) {
-            inst = A.order[G.inst_begin + k];
+          const int count = A.cont_mode ? (int)A.cont_count[g] : G.inst_count;
+          if (k < count) {
+            inst = A.cont_mode ? A.cont_list[G.inst_begin + k] : A.order[G.inst_begin + k];
             dparams = A.dparams + A.inst_p_off[inst];
             ov_dev = A.inst_ov_dev[inst];
             ov_val = A.inst_ov_val[inst];
-            const long long xo = A.inst_x0_off[inst];
-            for (int i = sl; i < nc; i += LPI) X[i] = xo >= 0 ? A.x0[xo + i] : 0.0;
-            it = total = gstep = 0;
-            damp = cfg.damping;
-            prev = 1.7976931348623157e308;
-            gmin = cfg.gmin_steps == 0 ? cfg.gmin : gstart;
+            if (A.cont_mode) {  // resume where the lane phase parked it
+              const long long xo = A.inst_x_off[inst];
+              for (int i = sl; i < nc; i += LPI) X[i] = A.x_out[xo + i];
+              it = A.cont_it[inst];
+              total = A.cont_total[inst];
+              gstep = A.cont_gstep[inst];
+              damp = A.cont_damp[inst];
+              prev = A.cont_prev[inst];
+              gmin = cfg.gmin_steps == 0
+                         ? cfg.gmin
+                         : gstart + (cfg.gmin - gstart) * ((double)gstep / (double)cfg.gmin_steps);
+            } else {
+              const long long xo = A.inst_x0_off[inst];
+              for (int i = sl; i < nc; i += LPI) X[i] = xo >= 0 ? A.x0[xo + i] : 0.0;
+              it = total = gstep = 0;
+              damp = cfg.damping;
+              prev = 1.7976931348623157e308;
+              gmin = cfg.gmin_steps == 0 ? cfg.gmin : gstart;
+            }
           } else {
             exhausted = true;
           }

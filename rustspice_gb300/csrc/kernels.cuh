@@ -60,6 +60,9 @@ struct GroupHdr {
   int inst_begin;  // range of the group's instances in the order array
   int inst_count;
   int cost;        // scheduling weight (FP64 operations of one Newton iteration)
+  int seg_off;     // factor schedule: segments (start, end, sequential) per block,
+  int nseg;        //   block b's at lseg_ptr[b]..lseg_ptr[b+1] (lseg_ptr at blk_off);
+                   //   the columns in schedule order sit at col_off in lvl_col
 };
 
 // Contribution codes of the batched stamp: (index << 3) | kind with kind
@@ -81,6 +84,7 @@ struct BatchArgs {
   const int *col_ptr, *dslot, *col_single, *in_row, *out_pos, *offd_ptr, *slot_row,
       *upd_ptr, *upd_dst, *offd_col, *block_ptr;
   const int* heavy;  // (value index << 1) or (position << 1 | 1), per group
+  const int *lvl_col, *lseg_ptr, *lseg;  // level-scheduled factor (see GroupHdr)
   const long long* inst_p_off;  // offset of the instance's circuit constants (4 per device)
   const double* dparams;
   const int* inst_ov_dev;
@@ -108,6 +112,19 @@ struct BatchArgs {
   const long long* seg_off;
   double* grad;                // per instance: dL/dp[d][0] per device
   const long long* grad_off;
+  // lane-per-instance phase of the batched DC run, and its continuation
+  double* scratch;             // per warp: lane-interleaved state, warp_stride doubles
+  long long warp_stride;
+  const int* ltile_group;      // lane-phase tiles: group of each
+  int nltiles;
+  unsigned* lcounter;
+  int cap;                     // Newton iterations per instance in the lane phase (0: all)
+  int cont_mode;               // warp kernel: take the instances the lane phase left
+  int* cont_list;              // per group at inst_begin: the instances left
+  unsigned* cont_count;        // per group
+  unsigned* gnext2;            // per group: next entry of cont_list to hand out
+  int *cont_it, *cont_total, *cont_gstep;
+  double *cont_damp, *cont_prev;  // the iterate itself waits in x_out
 };
 
 // Bordered-block-diagonal solver: the index lists its kernels read.
@@ -153,6 +170,10 @@ double fp64_peak_tflops();
 void launch_batch_newton(const BatchArgs& a, int m, int grid, int warps_per_block,
                          cudaStream_t s);
 // Registers per thread and resident blocks per SM of the batched kernel.
+// Lane-per-instance batched Newton (phase 1 of gpuklu_batch_run).
+void launch_batch_lanes(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
+void lanes_kernel_info(int warps_per_block, int* regs, int* blocks_per_sm);
+
 // Bordered-block-diagonal solver pieces.
 void launch_bbd_ysolve(const DPlan& P, const double* lu, const double* ax, const BbdArgs& B,
                        double* ybuf, cudaStream_t s);
