@@ -207,10 +207,11 @@ struct Prog {
   int n, nc, nv, nslots, ndev, nblocks, nheavy;
 };
 
-// Stages the group's factor and solve structure into the warp's shared
-// memory and returns the program view.
+// Stages the group's factor and solve structure into shared memory and
+// returns the program view: by one warp (tid = lane, nthr = 32) or by the
+// whole block (block = true; every thread of the block calls it).
 __device__ __forceinline__ Prog stage_program(const BatchArgs& A, const GroupHdr& G, int* prog,
-                                              int lane) {
+                                              int lane, int nthr = 32, bool block = false) {
   Prog P;
   const int n = G.n;
   int4* const colrec = reinterpret_cast<int4*>(prog);
@@ -221,17 +222,20 @@ __device__ __forceinline__ Prog stage_program(const BatchArgs& A, const GroupHdr
     const int* cp = A.col_ptr + G.col_off;
     const int* dsl = A.dslot + G.col_off;
     const int* cs = A.col_single + G.col_off;
-    for (int k = lane; k < n; k += 32) colrec[k] = make_int4(cp[k], dsl[k], cp[k + 1], cs[k]);
+    for (int k = lane; k < n; k += nthr) colrec[k] = make_int4(cp[k], dsl[k], cp[k + 1], cs[k]);
     const int* sr = A.slot_row + G.slot_off;
     const int* up = A.upd_ptr + G.slot_off;
-    for (int q = lane; q < G.nslots; q += 32) {
+    for (int q = lane; q < G.nslots; q += nthr) {
       srow[q] = sr[q];
       uptr[q] = up[q];
     }
     const int* ud = A.upd_dst + G.upd_off;
-    for (int q = lane; q < G.nupd; q += 32) udst[q] = ud[q];
+    for (int q = lane; q < G.nupd; q += nthr) udst[q] = ud[q];
   }
-  __syncwarp();
+  if (block)
+    __syncthreads();
+  else
+    __syncwarp();
   P.colrec = colrec;
   P.srow = srow;
   P.uptr = uptr;

@@ -919,6 +919,9 @@ struct gpuklu_batch {
   struct Class {
     int m = 1, region = 0, prog_ints = 0, grid = 0, warps_per_block = 1, regs = 0,
         blocks_per_sm = 0;
+    // continuation phase: warps of a block share one staged program
+    int grid2 = 0, wpb2 = 1;
+    bool shared2 = false;
     std::vector<i32> tiles, tiles2;  // tiles2: after the lane phase (parked instances)
     DBuf<i32> d_tiles, d_tiles2;
     DBuf<unsigned> d_counter;
@@ -1415,7 +1418,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       C->prog_ints = std::max(C->prog_ints, prog);
       const int nt = (h.inst_count + C->m - 1) / C->m;
       for (int t = 0; t < nt; ++t) C->tiles.push_back(g);
-      for (int t = 0; t < std::min(nt, 8); ++t) C->tiles2.push_back(g);
+      for (int t = 0; t < std::min(nt, 2); ++t) C->tiles2.push_back(g);
     }
     if (C->tiles.empty()) continue;
     gk::batch_kernel_info(C->m, C->warps_per_block, C->region, C->prog_ints, &C->regs,
@@ -1426,6 +1429,21 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       return nullptr;
     }
     C->grid = std::min<int>(sm_count() * C->blocks_per_sm, (int)C->tiles.size());
+    {  // the largest block of warps sharing one program that fits shared memory
+      const size_t cap = 227 * 1024, prog = (size_t)C->prog_ints * 4;
+      const size_t per = (size_t)C->region * 8 * C->m;
+      int w = prog < cap ? (int)std::min<size_t>(8, (cap - prog) / per) : 0;
+      int r2 = 0, b2 = 0;
+      if (w >= 2) gk::batch_kernel_info(C->m, w, C->region, C->prog_ints, &r2, &b2, true);
+      if (w >= 2 && b2 > 0 && w * b2 > C->blocks_per_sm * C->warps_per_block) {
+        C->shared2 = true;
+        C->wpb2 = w;
+        C->grid2 = sm_count() * b2;
+      } else {
+        C->grid2 = C->grid;
+        C->wpb2 = C->warps_per_block;
+      }
+    }
     if (cudaStreamCreateWithFlags(&C->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&C->done, cudaEventDisableTiming) != cudaSuccess)
       return nullptr;
@@ -1790,8 +1808,10 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
       ca.cont_mode = 1;
       ca.tile_group = C->d_tiles2.p;
       ca.ntiles = (int)C->tiles2.size();
+      gk::launch_batch_newton(ca, C->m, C->grid2, C->wpb2, C->stream, C->shared2);
+    } else {
+      gk::launch_batch_newton(ca, C->m, C->grid, C->warps_per_block, C->stream);
     }
-    gk::launch_batch_newton(ca, C->m, C->grid, C->warps_per_block, C->stream);
     cudaEventRecord(C->done, C->stream);
     cudaStreamWaitEvent(s, C->done, 0);
   }

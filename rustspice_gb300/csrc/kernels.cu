@@ -712,30 +712,43 @@ __global__ void k_rcond(DPlan P, const double* __restrict__ lu, double* out) {
 // M instances per warp, 32/M lanes each; the M instances run the same
 // program (one group), so the warp's control flow is shared and every FP64
 // warp instruction of the sequential factor and solve serves M instances.
-template <int M>
+// SHARED: the warps of a block work on one group at a time and share one
+// staged program (more instances per SM when the program is large); the
+// block moves to its next tile when every warp has run out of instances.
+template <int M, bool SHARED>
 __global__ void k_batch_newton(BatchArgs A) {
   constexpr int LPI = 32 / M;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31;
+  __shared__ int s_tile;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / LPI, sl = lane % LPI, lead = sub * LPI;
   const unsigned leaders =
       M == 1 ? 1u : (M == 2 ? 0x00010001u : (M == 4 ? 0x01010101u : 0x11111111u));
-  // per-warp slice: the staged program, then M instance regions
+  // per-warp slice (the staged program, then M instance regions), or one
+  // program for the block followed by every warp's regions
   unsigned char* const slice =
-      smem_raw + (size_t)(threadIdx.x >> 5) * ((size_t)A.prog_ints * 4 + (size_t)M * A.region * 8);
+      SHARED ? smem_raw
+             : smem_raw + (size_t)warp * ((size_t)A.prog_ints * 4 + (size_t)M * A.region * 8);
   int* const prog = reinterpret_cast<int*>(slice);
   double* const region = reinterpret_cast<double*>(slice + (size_t)A.prog_ints * 4) +
-                         (size_t)sub * A.region;
+                         (size_t)((SHARED ? warp * M : 0) + sub) * A.region;
   const NewtonCfg cfg = A.cfg;
   const double gstart = fmax(cfg.gmin * 1e3, 1e-6);
   while (true) {
     int ti = 0;
-    if (lane == 0) ti = (int)atomicAdd(A.counter, 1u);
-    ti = __shfl_sync(FULL, ti, 0);
+    if (SHARED) {
+      if (threadIdx.x == 0) s_tile = (int)atomicAdd(A.counter, 1u);
+      __syncthreads();
+      ti = s_tile;
+    } else {
+      if (lane == 0) ti = (int)atomicAdd(A.counter, 1u);
+      ti = __shfl_sync(FULL, ti, 0);
+    }
     if (ti >= A.ntiles) return;
     const int g = A.tile_group[ti];
     const GroupHdr G = A.groups[g];
-    const bt::Prog P = bt::stage_program(A, G, prog, lane);
+    const bt::Prog P = SHARED ? bt::stage_program(A, G, prog, threadIdx.x, blockDim.x, true)
+                              : bt::stage_program(A, G, prog, lane);
     const int n = P.n, nc = P.nc;
     double* const X = region;
     double* const T = X + nc;
@@ -857,7 +870,10 @@ __global__ void k_batch_newton(BatchArgs A) {
       }
       __syncwarp();
     }
-    __syncwarp();  // done with this group's staged program
+    if (SHARED)
+      __syncthreads();  // every warp is done with the block's staged program
+    else
+      __syncwarp();  // done with this group's staged program
   }
 }
 
@@ -941,49 +957,72 @@ double fp64_peak_tflops() {
   return flops / (best * 1e-3) / 1e12;
 }
 
-template <int M>
+template <int M, bool SHARED>
 static size_t smem_bytes(const BatchArgs& a, int warps_per_block) {
+  if (SHARED)
+    return (size_t)a.prog_ints * 4 + (size_t)a.region * M * sizeof(double) * warps_per_block;
   return ((size_t)a.prog_ints * 4 + (size_t)a.region * M * sizeof(double)) * warps_per_block;
 }
 
-template <int M>
+template <int M, bool SHARED>
 static void launch_m(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s) {
-  const size_t sm = smem_bytes<M>(a, warps_per_block);
-  k_batch_newton<M><<<grid, 32 * warps_per_block, sm, s>>>(a);
+  const size_t sm = smem_bytes<M, SHARED>(a, warps_per_block);
+  k_batch_newton<M, SHARED><<<grid, 32 * warps_per_block, sm, s>>>(a);
 }
 
 // The tile counter and the per-group instance counters are reset by the
 // caller before the classes start (the classes share the group counter
 // array and run concurrently).
 void launch_batch_newton(const BatchArgs& a, int m, int grid, int warps_per_block,
-                         cudaStream_t s) {
+                         cudaStream_t s, bool shared) {
+  if (shared) {
+    switch (m) {
+      case 8: launch_m<8, true>(a, grid, warps_per_block, s); break;
+      case 4: launch_m<4, true>(a, grid, warps_per_block, s); break;
+      case 2: launch_m<2, true>(a, grid, warps_per_block, s); break;
+      default: launch_m<1, true>(a, grid, warps_per_block, s); break;
+    }
+    return;
+  }
   switch (m) {
-    case 8: launch_m<8>(a, grid, warps_per_block, s); break;
-    case 4: launch_m<4>(a, grid, warps_per_block, s); break;
-    case 2: launch_m<2>(a, grid, warps_per_block, s); break;
-    default: launch_m<1>(a, grid, warps_per_block, s); break;
+    case 8: launch_m<8, false>(a, grid, warps_per_block, s); break;
+    case 4: launch_m<4, false>(a, grid, warps_per_block, s); break;
+    case 2: launch_m<2, false>(a, grid, warps_per_block, s); break;
+    default: launch_m<1, false>(a, grid, warps_per_block, s); break;
   }
 }
 
-template <int M>
+template <int M, bool SHARED>
 static void info_m(int warps_per_block, int region, int prog_ints, int* regs,
                    int* blocks_per_sm) {
   cudaFuncAttributes fa{};
-  cudaFuncGetAttributes(&fa, k_batch_newton<M>);
+  cudaFuncGetAttributes(&fa, k_batch_newton<M, SHARED>);
   *regs = fa.numRegs;
-  const size_t sm = ((size_t)prog_ints * 4 + (size_t)region * M * sizeof(double)) * warps_per_block;
-  cudaFuncSetAttribute(k_batch_newton<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch_newton<M>,
+  const size_t per = (size_t)region * M * sizeof(double);
+  const size_t sm = SHARED ? (size_t)prog_ints * 4 + per * warps_per_block
+                           : ((size_t)prog_ints * 4 + per) * warps_per_block;
+  cudaFuncSetAttribute(k_batch_newton<M, SHARED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sm);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch_newton<M, SHARED>,
                                                 32 * warps_per_block, sm);
 }
 
 void batch_kernel_info(int m, int warps_per_block, int region, int prog_ints, int* regs,
-                       int* blocks_per_sm) {
+                       int* blocks_per_sm, bool shared) {
+  if (shared) {
+    switch (m) {
+      case 8: info_m<8, true>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+      case 4: info_m<4, true>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+      case 2: info_m<2, true>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+      default: info_m<1, true>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+    }
+    return;
+  }
   switch (m) {
-    case 8: info_m<8>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
-    case 4: info_m<4>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
-    case 2: info_m<2>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
-    default: info_m<1>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+    case 8: info_m<8, false>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+    case 4: info_m<4, false>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+    case 2: info_m<2, false>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+    default: info_m<1, false>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
   }
 }
 

@@ -167,8 +167,9 @@ void launch_rcond(const DPlan& P, const double* lu, double* out2, cudaStream_t s
 // Measured FP64 fused multiply-add throughput of the current device [TFLOP/s].
 double fp64_peak_tflops();
 // m: instances per warp (1, 2 or 4); region: shared doubles per instance.
+// shared: the warps of a block share one staged program (one group at a time)
 void launch_batch_newton(const BatchArgs& a, int m, int grid, int warps_per_block,
-                         cudaStream_t s);
+                         cudaStream_t s, bool shared = false);
 // Registers per thread and resident blocks per SM of the batched kernel.
 // Lane-per-instance batched Newton (phase 1 of gpuklu_batch_run).
 void launch_batch_lanes(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
@@ -195,6 +196,6 @@ void launch_tran_backward(const BatchArgs& a, int grid, int warps_per_block, cud
 void tran_kernel_info(bool backward, int warps_per_block, int region, int prog_ints, int* regs,
                       int* blocks_per_sm);
 void batch_kernel_info(int m, int warps_per_block, int region, int prog_ints, int* regs,
-                       int* blocks_per_sm);
+                       int* blocks_per_sm, bool shared = false);
 
 }  // namespace gk
