@@ -368,15 +368,35 @@ __device__ __forceinline__ void factor_solve_columns(const Prog& P, double* V, d
     __syncwarp();
     for (int k = b0; k < b1; ++k) {
       const int4 ck = P.colrec[k];
+      // The update structure of U entry s (its L column, this lane's first
+      // destination) does not depend on values: it is loaded one entry
+      // ahead, so its latency overlaps the previous update and its warp
+      // synchronisation.
+      int4 cj = make_int4(0, 0, 0, 0);
+      int dbase = 0, dd0 = 0;
+      if (ck.x < ck.y) {
+        cj = P.colrec[P.srow[ck.x]];
+        dbase = P.uptr[ck.x] - (cj.y + 1);
+        if (cj.y + 1 + sl < cj.z) dd0 = P.udst[dbase + cj.y + 1 + sl];
+      }
       for (int s = ck.x; s < ck.y; ++s) {
+        const int4 cur = cj;
+        const int cbase = dbase, cdd0 = dd0;
+        if (s + 1 < ck.y) {
+          cj = P.colrec[P.srow[s + 1]];
+          dbase = P.uptr[s + 1] - (cj.y + 1);
+          if (cj.y + 1 + sl < cj.z) dd0 = P.udst[dbase + cj.y + 1 + sl];
+        }
         const double u = V[s];
         if (nonzero(u)) {
-          const int4 cj = P.colrec[P.srow[s]];
-          const int q0 = cj.y + 1;
-          const int* dst = P.udst + P.uptr[s] - q0;
-          for (int qq = q0 + sl; qq < cj.z; qq += LPI) {
-            const int dd = dst[qq];
-            V[dd] = fma(-V[qq], u, V[dd]);
+          const int q0 = cur.y + 1;
+          int qq = q0 + sl;
+          if (qq < cur.z) {
+            V[cdd0] = fma(-V[qq], u, V[cdd0]);
+            for (qq += LPI; qq < cur.z; qq += LPI) {
+              const int dd = P.udst[cbase + qq];
+              V[dd] = fma(-V[qq], u, V[dd]);
+            }
           }
         }
         __syncwarp();
