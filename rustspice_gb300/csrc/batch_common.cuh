@@ -199,8 +199,9 @@ __device__ __forceinline__ double perturb_bits(double d, bool singleton) {
 struct Prog {
   const int4* colrec;  // staged: (s0, dslot, s1, singleton) per column
   const int* srow;     // staged: slot rows
-  const int* uptr;     // staged: update-list offsets per slot
-  const int* udst;     // staged: update destinations
+  const int* uptr;     // update-list offsets per slot (staged when leveled)
+  const int* udst;     // update destinations (staged when leveled)
+  int* map;            // per instance: row -> slot of the column being factored
   const int *dev_type, *dev_nodes, *dev_dv, *amap_ptr, *amap_code, *rmap_ptr, *rmap_code,
       *in_row, *out_pos, *offd_ptr, *offd_col, *bptr, *heavy;
   const int *lvl_col, *lseg_ptr, *lseg;  // level schedule of the factorization
@@ -216,21 +217,21 @@ __device__ __forceinline__ Prog stage_program(const BatchArgs& A, const GroupHdr
   const int n = G.n;
   int4* const colrec = reinterpret_cast<int4*>(prog);
   int* const srow = prog + 4 * n;
-  int* const uptr = srow + G.nslots;
-  int* const udst = uptr + G.nslots;
   {
     const int* cp = A.col_ptr + G.col_off;
     const int* dsl = A.dslot + G.col_off;
     const int* cs = A.col_single + G.col_off;
     for (int k = lane; k < n; k += nthr) colrec[k] = make_int4(cp[k], dsl[k], cp[k + 1], cs[k]);
     const int* sr = A.slot_row + G.slot_off;
-    const int* up = A.upd_ptr + G.slot_off;
-    for (int q = lane; q < G.nslots; q += nthr) {
-      srow[q] = sr[q];
-      uptr[q] = up[q];
+    for (int q = lane; q < G.nslots; q += nthr) srow[q] = sr[q];
+    if (G.nseg > 0) {  // the level path reads the update lists per lane: stage them too
+      int* const uptr = srow + G.nslots;
+      int* const udst = uptr + G.nslots;
+      const int* up = A.upd_ptr + G.slot_off;
+      for (int q = lane; q < G.nslots; q += nthr) uptr[q] = up[q];
+      const int* ud = A.upd_dst + G.upd_off;
+      for (int q = lane; q < G.nupd; q += nthr) udst[q] = ud[q];
     }
-    const int* ud = A.upd_dst + G.upd_off;
-    for (int q = lane; q < G.nupd; q += nthr) udst[q] = ud[q];
   }
   if (block)
     __syncthreads();
@@ -238,8 +239,9 @@ __device__ __forceinline__ Prog stage_program(const BatchArgs& A, const GroupHdr
     __syncwarp();
   P.colrec = colrec;
   P.srow = srow;
-  P.uptr = uptr;
-  P.udst = udst;
+  P.uptr = G.nseg > 0 ? srow + G.nslots : A.upd_ptr + G.slot_off;
+  P.udst = G.nseg > 0 ? srow + 2 * G.nslots : A.upd_dst + G.upd_off;
+  P.map = nullptr;
   P.dev_type = A.dev_type + G.dev_off;
   P.dev_nodes = A.dev_nodes + 4 * G.dev_off;
   P.dev_dv = A.dev_dv + G.dev_off;
@@ -366,26 +368,28 @@ __device__ __forceinline__ void factor_solve_columns(const Prog& P, double* V, d
       for (int e = P.offd_ptr[i]; e < P.offd_ptr[i + 1]; ++e)
         T[i] = fma(-V[P.nslots + e], T[P.offd_col[e]], T[i]);
     __syncwarp();
+    int* const map = P.map;
     for (int k = b0; k < b1; ++k) {
       const int4 ck = P.colrec[k];
+      // destination slots of this column's updates: row -> slot
+      for (int q = ck.x + sl; q < ck.z; q += LPI) map[P.srow[q]] = q;
+      __syncwarp();
       // The update structure of U entry s (its L column, this lane's first
       // destination) does not depend on values: it is loaded one entry
       // ahead, so its latency overlaps the previous update and its warp
       // synchronisation.
       int4 cj = make_int4(0, 0, 0, 0);
-      int dbase = 0, dd0 = 0;
+      int dd0 = 0;
       if (ck.x < ck.y) {
         cj = P.colrec[P.srow[ck.x]];
-        dbase = P.uptr[ck.x] - (cj.y + 1);
-        if (cj.y + 1 + sl < cj.z) dd0 = P.udst[dbase + cj.y + 1 + sl];
+        if (cj.y + 1 + sl < cj.z) dd0 = map[P.srow[cj.y + 1 + sl]];
       }
       for (int s = ck.x; s < ck.y; ++s) {
         const int4 cur = cj;
-        const int cbase = dbase, cdd0 = dd0;
+        const int cdd0 = dd0;
         if (s + 1 < ck.y) {
           cj = P.colrec[P.srow[s + 1]];
-          dbase = P.uptr[s + 1] - (cj.y + 1);
-          if (cj.y + 1 + sl < cj.z) dd0 = P.udst[dbase + cj.y + 1 + sl];
+          if (cj.y + 1 + sl < cj.z) dd0 = map[P.srow[cj.y + 1 + sl]];
         }
         const double u = V[s];
         if (nonzero(u)) {
@@ -394,7 +398,7 @@ __device__ __forceinline__ void factor_solve_columns(const Prog& P, double* V, d
           if (qq < cur.z) {
             V[cdd0] = fma(-V[qq], u, V[cdd0]);
             for (qq += LPI; qq < cur.z; qq += LPI) {
-              const int dd = P.udst[cbase + qq];
+              const int dd = map[P.srow[qq]];
               V[dd] = fma(-V[qq], u, V[dd]);
             }
           }

@@ -922,8 +922,10 @@ struct gpuklu_batch {
     // continuation phase: warps of a block share one staged program
     int grid2 = 0, wpb2 = 1;
     bool shared2 = false;
-    std::vector<i32> tiles, tiles2;  // tiles2: after the lane phase (parked instances)
-    DBuf<i32> d_tiles, d_tiles2;
+    // after the lane phase (parked instances): tiles2 for blocks sharing a
+    // program, tiles3 for one warp per tile
+    std::vector<i32> tiles, tiles2, tiles3;
+    DBuf<i32> d_tiles, d_tiles2, d_tiles3;
     DBuf<unsigned> d_counter;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
@@ -1382,7 +1384,8 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     B->groups[g].inst_count = (int)members[g].size();
     order.insert(order.end(), members[g].begin(), members[g].end());
     const gk::GroupHdr& h = B->groups[g];
-    gregion[g] = (h.node_count + h.n + h.ndv + h.nslots + h.noffd + 1) & ~1;
+    // state doubles, then the row -> slot map (n ints)
+    gregion[g] = (h.node_count + h.n + h.ndv + h.nslots + h.noffd + (h.n + 1) / 2 + 2) & ~1;
   }
   (void)region;
   B->x_off.assign(ninst, 0);
@@ -1412,13 +1415,15 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     C->m = mclass[ci];
     for (int g : gorder) {
       const gk::GroupHdr& h = B->groups[g];
-      const int prog = (4 * h.n + 2 * h.nslots + h.nupd + 3) & ~3;
+      // column records, slot rows (and the update lists for leveled programs)
+      const int prog = (4 * h.n + h.nslots + (h.nseg > 0 ? h.nslots + h.nupd : 0) + 3) & ~3;
       if (pick_m(gregion[g], prog) != C->m || h.inst_count == 0) continue;
       C->region = std::max(C->region, gregion[g]);
       C->prog_ints = std::max(C->prog_ints, prog);
       const int nt = (h.inst_count + C->m - 1) / C->m;
       for (int t = 0; t < nt; ++t) C->tiles.push_back(g);
       for (int t = 0; t < std::min(nt, 2); ++t) C->tiles2.push_back(g);
+      for (int t = 0; t < std::min(nt, 12); ++t) C->tiles3.push_back(g);
     }
     if (C->tiles.empty()) continue;
     gk::batch_kernel_info(C->m, C->warps_per_block, C->region, C->prog_ints, &C->regs,
@@ -1434,6 +1439,8 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       const size_t per = (size_t)C->region * 8 * C->m;
       int w = prog < cap ? (int)std::min<size_t>(8, (cap - prog) / per) : 0;
       int r2 = 0, b2 = 0;
+      const char* esh = getenv("GPUKLU_SHARED_PROGRAM");
+      if (esh && esh[0] == '0') w = 0;
       if (w >= 2) gk::batch_kernel_info(C->m, w, C->region, C->prog_ints, &r2, &b2, true);
       if (w >= 2 && b2 > 0 && w * b2 > C->blocks_per_sm * C->warps_per_block) {
         C->shared2 = true;
@@ -1477,6 +1484,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   for (auto& C : B->classes) {
     if (e == cudaSuccess) e = C->d_tiles.upload(C->tiles, s);
     if (e == cudaSuccess) e = C->d_tiles2.upload(C->tiles2, s);
+    if (e == cudaSuccess) e = C->d_tiles3.upload(C->tiles3, s);
     if (e == cudaSuccess) e = C->d_counter.resize(1);
   }
   // Lane phase: every group split into tiles of about lane_target instances,
@@ -1654,8 +1662,9 @@ gpuklu_batch* gpuklu_tran_create(int64_t ncirc, const int64_t* dev_off,
   int region = 0, prog = 0;
   for (int64_t i = 0; i < ninst; ++i) {
     const gk::GroupHdr& h = B->groups[B->inst_group_h[i]];
-    region = std::max(region, 2 * h.node_count + 2 * h.n + h.ndv + h.nslots + h.noffd + h.ndev);
-    prog = std::max(prog, (4 * h.n + 2 * h.nslots + h.nupd + 3) & ~3);
+    region = std::max(region, 2 * h.node_count + 2 * h.n + h.ndv + h.nslots + h.noffd + h.ndev +
+                                  (h.n + 1) / 2 + 1);
+    prog = std::max(prog, (4 * h.n + h.nslots + (h.nseg > 0 ? h.nslots + h.nupd : 0) + 3) & ~3);
     ck_off[i] = ck;
     ck += nck * h.node_count;
     seg_off[i] = sg;
@@ -1806,8 +1815,8 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
     gk::BatchArgs ca = C->args;
     if (b->lanes) {
       ca.cont_mode = 1;
-      ca.tile_group = C->d_tiles2.p;
-      ca.ntiles = (int)C->tiles2.size();
+      ca.tile_group = C->shared2 ? C->d_tiles2.p : C->d_tiles3.p;
+      ca.ntiles = (int)(C->shared2 ? C->tiles2.size() : C->tiles3.size());
       gk::launch_batch_newton(ca, C->m, C->grid2, C->wpb2, C->stream, C->shared2);
     } else {
       gk::launch_batch_newton(ca, C->m, C->grid, C->warps_per_block, C->stream);

@@ -747,13 +747,14 @@ __global__ void k_batch_newton(BatchArgs A) {
     if (ti >= A.ntiles) return;
     const int g = A.tile_group[ti];
     const GroupHdr G = A.groups[g];
-    const bt::Prog P = SHARED ? bt::stage_program(A, G, prog, threadIdx.x, blockDim.x, true)
-                              : bt::stage_program(A, G, prog, lane);
+    bt::Prog P = SHARED ? bt::stage_program(A, G, prog, threadIdx.x, blockDim.x, true)
+                        : bt::stage_program(A, G, prog, lane);
     const int n = P.n, nc = P.nc;
     double* const X = region;
     double* const T = X + nc;
     double* const DV = T + n;
     double* const V = DV + G.ndv;
+    P.map = reinterpret_cast<int*>(V + G.nslots + G.noffd);
 
     int inst = -1, it = 0, total = 0, gstep = 0, ov_dev = -1;
     bool exhausted = false;

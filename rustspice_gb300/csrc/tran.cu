@@ -97,13 +97,14 @@ __global__ void k_tran_fwd(BatchArgs A) {
     const int inst = next_instance(A, lane);
     if (inst >= A.ninst) return;
     const GroupHdr G = A.groups[A.inst_group[inst]];
-    const bt::Prog P = bt::stage_program(A, G, S.prog, lane);
+    bt::Prog P = bt::stage_program(A, G, S.prog, lane);
     const int nc = P.nc, n = P.n;
     double* const X = S.region;
     double* const XP = X + nc;
     double* const T = XP + nc;
     double* const DV = T + n;
     double* const V = DV + G.ndv;
+    P.map = reinterpret_cast<int*>(V + P.nv);
     const double* dparams = A.dparams + A.inst_p_off[inst];
     copy_vec(X, A.x0 + A.inst_x0_off[inst], nc, sl);
     double* ck = A.ckpt + A.ckpt_off[inst];
@@ -143,7 +144,7 @@ __global__ void k_tran_bwd(BatchArgs A) {
     const int inst = next_instance(A, lane);
     if (inst >= A.ninst) return;
     const GroupHdr G = A.groups[A.inst_group[inst]];
-    const bt::Prog P = bt::stage_program(A, G, S.prog, lane);
+    bt::Prog P = bt::stage_program(A, G, S.prog, lane);
     const int nc = P.nc, n = P.n, ndev = P.ndev;
     double* const X = S.region;
     double* const XP = X + nc;
@@ -152,6 +153,7 @@ __global__ void k_tran_bwd(BatchArgs A) {
     double* const V = DV + G.ndv;
     double* const LAM = V + P.nv;  // lambda_{t+1}, original row order
     double* const GR = LAM + n;    // dL/dC per device
+    P.map = reinterpret_cast<int*>(GR + ndev);
     const double* dparams = A.dparams + A.inst_p_off[inst];
     const double* ck = A.ckpt + A.ckpt_off[inst];
     double* const seg = A.seg + A.seg_off[inst];
