@@ -902,7 +902,7 @@ struct gpuklu_batch {
   DBuf<i32> d_order, d_dev_type, d_dev_nodes, d_dev_dv, d_amap_ptr, d_amap_code,
       d_rmap_ptr, d_rmap_code, d_col_ptr, d_dslot, d_col_single, d_in_row, d_out_pos,
       d_offd_ptr, d_slot_row, d_upd_ptr, d_upd_dst, d_offd_col, d_block_ptr, d_heavy, d_ov_dev,
-      d_lvl_col, d_lseg_ptr, d_lseg,
+      d_lvl_col, d_lseg_ptr, d_lseg, d_amap4, d_rmap4, d_lng,
       d_iters,
       d_iters_total, d_reason, d_status;
   DBuf<double> d_dparams, d_ov_val, d_x0, d_xout;
@@ -975,7 +975,7 @@ struct Program {
   gk::GroupHdr h{};
   std::vector<i32> dev_type, dev_nodes, dev_dv, amap_ptr, amap_code, rmap_ptr, rmap_code,
       col_ptr, dslot, col_single, in_row, out_pos, offd_ptr, slot_row, upd_ptr, upd_dst,
-      offd_col, block_ptr, heavy, lvl_col, lseg_ptr, lseg;
+      offd_col, block_ptr, heavy, lvl_col, lseg_ptr, lseg, amap4, rmap4, lng;
   int64_t flops = 0, bytes = 0;
   std::string key() const {
     std::string k;
@@ -989,7 +989,7 @@ struct Program {
     for (auto* v : {&dev_type, &dev_nodes, &dev_dv, &amap_ptr, &amap_code, &rmap_ptr,
                     &rmap_code, &col_ptr, &dslot, &col_single, &in_row, &out_pos, &offd_ptr,
                     &slot_row, &upd_ptr, &upd_dst, &offd_col, &block_ptr, &heavy, &lvl_col,
-                    &lseg_ptr, &lseg})
+                    &lseg_ptr, &lseg, &amap4, &rmap4, &lng})
       app(*v);
     return k;
   }
@@ -1120,6 +1120,28 @@ Program make_program(const gpuklu_circuit& C, const gk::Plan& P) {
     if (g.rmap_ptr[r + 1] - g.rmap_ptr[r] > 12) g.heavy.push_back((i << 1) | 1);
   }
   h.nheavy = (int)g.heavy.size();
+  // Four codes per value slot and per permuted rhs row, padded with +0.0
+  // (x + 0.0 == x); longer lists are listed in lng and summed by the loop.
+  g.amap4.assign((size_t)4 * nv, 4);
+  g.rmap4.assign((size_t)4 * P.n, 4);
+  for (int v = 0; v < nv; ++v) {
+    const int t0 = g.amap_ptr[v], t1 = g.amap_ptr[v + 1];
+    if (t1 - t0 > 4) {
+      g.lng.push_back(v << 1);
+      continue;
+    }
+    for (int t = t0; t < t1; ++t) g.amap4[(size_t)4 * v + (t - t0)] = g.amap_code[t];
+  }
+  for (int i = 0; i < P.n; ++i) {
+    const int r = g.in_row[i];
+    const int t0 = g.rmap_ptr[r], t1 = g.rmap_ptr[r + 1];
+    if (t1 - t0 > 4) {
+      g.lng.push_back((i << 1) | 1);
+      continue;
+    }
+    for (int t = t0; t < t1; ++t) g.rmap4[(size_t)4 * i + (t - t0)] = g.rmap_code[t];
+  }
+  h.nlng = (int)g.lng.size();
   g.upd_dst = P.upd_dst;
   g.offd_col = P.offd_col;
   g.block_ptr.assign(P.block_ptr.begin(), P.block_ptr.end());
@@ -1319,7 +1341,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   const int ng = (int)progs.size();
   std::vector<i32> dev_type, dev_nodes, dev_dv, amap_ptr, amap_code, rmap_ptr, rmap_code,
       col_ptr, dslot, col_single, in_row, out_pos, offd_ptr, slot_row, upd_ptr, upd_dst,
-      offd_col, block_ptr, heavy, lvl_col, lseg_ptr, lseg;
+      offd_col, block_ptr, heavy, lvl_col, lseg_ptr, lseg, amap4, rmap4, lng;
   auto cat = [](std::vector<i32>& dst, const std::vector<i32>& src) {
     dst.insert(dst.end(), src.begin(), src.end());
   };
@@ -1341,6 +1363,9 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     h.rmap_code_off = (int)rmap_code.size();
     h.seg_off = (int)lseg.size() / 3;
     h.nseg = (int)pr.lseg.size() / 3;
+    h.amap4_off = (int)amap4.size();
+    h.rmap4_off = (int)rmap4.size();
+    h.lng_off = (int)lng.size();
     cat(dev_type, pr.dev_type);
     cat(dev_nodes, pr.dev_nodes);
     cat(dev_dv, pr.dev_dv);
@@ -1363,6 +1388,9 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     cat(lvl_col, pr.lvl_col);
     cat(lseg_ptr, pr.lseg_ptr);
     cat(lseg, pr.lseg);
+    cat(amap4, pr.amap4);
+    cat(rmap4, pr.rmap4);
+    cat(lng, pr.lng);
     B->groups.push_back(h);
     B->group_flops.push_back(pr.flops);
     B->group_bytes.push_back(pr.bytes);
@@ -1478,6 +1506,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   UP(d_offd_ptr, offd_ptr) UP(d_slot_row, slot_row) UP(d_upd_ptr, upd_ptr)
   UP(d_upd_dst, upd_dst) UP(d_offd_col, offd_col) UP(d_block_ptr, block_ptr)
   UP(d_heavy, heavy) UP(d_lvl_col, lvl_col) UP(d_lseg_ptr, lseg_ptr) UP(d_lseg, lseg)
+  UP(d_amap4, amap4) UP(d_rmap4, rmap4) UP(d_lng, lng)
   UP(d_dparams, dparams) UP(d_p_off, poff) UP(d_ov_dev, ov_dev) UP(d_ov_val, ov_val)
   UP(d_x0_off, x0o) UP(d_x_off, B->x_off)
 #undef UP
@@ -1572,6 +1601,9 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   a.lvl_col = B->d_lvl_col.p;
   a.lseg_ptr = B->d_lseg_ptr.p;
   a.lseg = B->d_lseg.p;
+  a.amap4 = B->d_amap4.p;
+  a.rmap4 = B->d_rmap4.p;
+  a.lng = B->d_lng.p;
   a.inst_p_off = B->d_p_off.p;
   a.dparams = B->d_dparams.p;
   a.inst_ov_dev = B->d_ov_dev.p;

@@ -60,6 +60,8 @@ struct GroupHdr {
   int inst_begin;  // range of the group's instances in the order array
   int inst_count;
   int cost;        // scheduling weight (FP64 operations of one Newton iteration)
+  int amap4_off, rmap4_off;  // four padded codes per value slot / permuted row
+  int lng_off, nlng;         // slots and rows with longer lists: (index << 1) | is_row
   int seg_off;     // factor schedule: segments (start, end, sequential) per block,
   int nseg;        //   block b's at lseg_ptr[b]..lseg_ptr[b+1] (lseg_ptr at blk_off);
                    //   the columns in schedule order sit at col_off in lvl_col
@@ -85,6 +87,7 @@ struct BatchArgs {
       *upd_ptr, *upd_dst, *offd_col, *block_ptr;
   const int* heavy;  // (value index << 1) or (position << 1 | 1), per group
   const int *lvl_col, *lseg_ptr, *lseg;  // level-scheduled factor (see GroupHdr)
+  const int *amap4, *rmap4, *lng;        // padded contribution codes (see GroupHdr)
   const long long* inst_p_off;  // offset of the instance's circuit constants (4 per device)
   const double* dparams;
   const int* inst_ov_dev;

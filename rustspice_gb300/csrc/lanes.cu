@@ -58,11 +58,15 @@ __global__ void k_batch_lanes(BatchArgs A) {
     const int* upd_dst = A.upd_dst + G.upd_off;
     const int* offd_col = A.offd_col + G.offd_off;
     const int* bptr = A.block_ptr + G.blk_off;
-    double* const X = W;
-    double* const T = X + (long long)nc * 32;
-    double* const DV = T + (long long)n * 32;
-    double* const V = DV + (long long)G.ndv * 32;
-    double* const K = V + (long long)nv * 32;  // 4 constants per device
+    // disjoint views of the scratch (restrict: loads may pass earlier stores)
+    double* __restrict__ const X = W;
+    double* __restrict__ const T = X + (long long)nc * 32;
+    double* __restrict__ const DV = T + (long long)n * 32;
+    double* __restrict__ const V = DV + (long long)G.ndv * 32;
+    double* __restrict__ const K = V + (long long)nv * 32;  // 4 constants per device
+    const int* amap4 = A.amap4 + G.amap4_off;
+    const int* rmap4 = A.rmap4 + G.rmap4_off;
+    const int* lng = A.lng + G.lng_off;
 #define AT(base, i) (base)[(long long)(i) * 32]
 
     int inst = -1, it = 0, total = 0, gstep = 0, nphase = 0;
@@ -100,6 +104,7 @@ __global__ void k_batch_lanes(BatchArgs A) {
       const bool live = inst >= 0;
       if (!__any_sync(kAllLanes, live)) break;
       // ---- device evaluation into the value records
+#pragma unroll 2
       for (int d = 0; d < ndev; ++d) {
         const int type = dev_type[d];
         const int nd[4] = {dev_nodes[4 * d], dev_nodes[4 * d + 1], dev_nodes[4 * d + 2],
@@ -113,17 +118,34 @@ __global__ void k_batch_lanes(BatchArgs A) {
         const int nrec = bt::record_len(type, false);
         for (int q = 0; q < nrec; ++q) AT(DV, o + q) = rec[q];
       }
-      // ---- assembly, in stamping order per slot and per row
+      // ---- assembly, in stamping order per slot and per row: four padded
+      // codes each (the loads of a slot issue together), longer lists after
+#pragma unroll 2
       for (int v = 0; v < nv; ++v) {
-        double acc = 0.0;
-        for (int t = amap_ptr[v]; t < amap_ptr[v + 1]; ++t) acc += bt::contrib<32>(DV, amap_code[t]);
-        AT(V, v) = acc;
+        const int4 c4 = *reinterpret_cast<const int4*>(amap4 + 4 * v);
+        const double a0 = bt::contrib<32>(DV, c4.x), a1 = bt::contrib<32>(DV, c4.y);
+        const double a2 = bt::contrib<32>(DV, c4.z), a3 = bt::contrib<32>(DV, c4.w);
+        AT(V, v) = (((0.0 + a0) + a1) + a2) + a3;
       }
+#pragma unroll 2
       for (int i = 0; i < n; ++i) {
-        const int r = in_row[i];
+        const int4 c4 = *reinterpret_cast<const int4*>(rmap4 + 4 * i);
+        const double a0 = bt::contrib<32>(DV, c4.x), a1 = bt::contrib<32>(DV, c4.y);
+        const double a2 = bt::contrib<32>(DV, c4.z), a3 = bt::contrib<32>(DV, c4.w);
+        AT(T, i) = (((0.0 + a0) + a1) + a2) + a3;
+      }
+      for (int h = 0; h < G.nlng; ++h) {
+        const int code = lng[h];
+        const int idx = code >> 1;
         double acc = 0.0;
-        for (int t = rmap_ptr[r]; t < rmap_ptr[r + 1]; ++t) acc += bt::contrib<32>(DV, rmap_code[t]);
-        AT(T, i) = acc;
+        if (code & 1) {
+          const int r = in_row[idx];
+          for (int t = rmap_ptr[r]; t < rmap_ptr[r + 1]; ++t) acc += bt::contrib<32>(DV, rmap_code[t]);
+          AT(T, idx) = acc;
+        } else {
+          for (int t = amap_ptr[idx]; t < amap_ptr[idx + 1]; ++t) acc += bt::contrib<32>(DV, amap_code[t]);
+          AT(V, idx) = acc;
+        }
       }
       // ---- factor + forward substitution, backward substitution, per block
       for (int b = 0; b < G.nblocks; ++b) {

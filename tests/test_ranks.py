@@ -19,10 +19,17 @@ def _rank_main(rank, world, port, q):
     dist.destroy_process_group()
 
 
+def _free_port():
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
 def test_two_ranks_gloo():
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    port = 29500 + os.getpid() % 1000
+    port = _free_port()
     ps = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
     for p in ps:
         p.start()
