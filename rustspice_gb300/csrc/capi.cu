@@ -80,14 +80,79 @@ std::vector<i32> make_tasks(const gk::Plan& p, bool transpose) {
   return t;
 }
 
+// Chunked schedule of the one-block solve (k_solve_cta): per BTF block in
+// solve order, the coupling rows, the forward sweep and the backward sweep,
+// cut so that the slots each chunk needs are contiguous and at most
+// gk::kSolveChunk long; consecutive pieces share a chunk while their slots fit.
+void make_cta_solve(const gk::Plan& p, std::vector<i32>& chunk, std::vector<i32>& op) {
+  chunk.clear();
+  op.clear();
+  struct Piece {
+    int code, a, b, lo, hi;  // slot range [lo, hi), empty when lo == hi
+  };
+  std::vector<Piece> ps;
+  const bool fwd = p.offd_lower;
+  for (int bb = 0; bb < p.nblocks; ++bb) {
+    const int b = fwd ? bb : p.nblocks - 1 - bb;
+    const int b0 = p.block_ptr[b], b1 = p.block_ptr[b + 1];
+    if (p.offd_ptr[b1] > p.offd_ptr[b0]) ps.push_back({0, b0, b1, 0, 0});
+    std::vector<std::pair<int, int>> cut;  // column pieces
+    for (int a = b0; a < b1;) {
+      int e = a + 1;
+      while (e < b1 && p.col_ptr[e + 1] - p.col_ptr[a] <= gk::kSolveChunk) ++e;
+      cut.push_back({a, e});
+      a = e;
+    }
+    for (auto& c : cut) {
+      const int lo = p.col_ptr[c.first], hi = p.col_ptr[c.second];
+      const bool direct = hi - lo > gk::kSolveChunk;
+      ps.push_back({1 | (direct ? 4 : 0), c.first, c.second, direct ? 0 : lo, direct ? 0 : hi});
+    }
+    for (auto it = cut.rbegin(); it != cut.rend(); ++it) {
+      const int lo = p.col_ptr[it->first], hi = p.col_ptr[it->second];
+      const bool direct = hi - lo > gk::kSolveChunk;
+      ps.push_back({2 | (direct ? 4 : 0), it->first, it->second, direct ? 0 : lo,
+                    direct ? 0 : hi});
+    }
+  }
+  int lo = 0, hi = 0, o0 = 0;
+  auto close = [&]() {
+    const int o1 = (int)(op.size() / 3);
+    if (o1 > o0) chunk.insert(chunk.end(), {lo, hi, o0, o1});
+    o0 = o1;
+    lo = hi = 0;
+  };
+  for (const Piece& q : ps) {
+    if (q.lo < q.hi) {
+      const bool empty = lo == hi;
+      const int nlo = empty ? q.lo : std::min(lo, q.lo), nhi = empty ? q.hi : std::max(hi, q.hi);
+      const bool joins = empty || (q.lo <= hi && q.hi >= lo);
+      if (!joins || nhi - nlo > gk::kSolveChunk) {
+        close();
+        lo = q.lo;
+        hi = q.hi;
+      } else {
+        lo = nlo;
+        hi = nhi;
+      }
+    } else if (q.code & 4) {
+      close();  // a direct piece runs alone, with nothing loaded
+    }
+    op.insert(op.end(), {q.code, q.a, q.b});
+    if (q.code & 4) close();
+  }
+  close();
+}
+
 // Device copy of a Plan.
 struct PlanDev {
   DBuf<i32> col_ptr, dslot, slot_row, upd_ptr, upd_dst, col_single, amap_ptr, amap_idx,
       offd_ptr, offd_col, offd_raw, offdT_ptr, offdT_row, offdT_raw, lrow_ptr, lrow_col,
       lrow_slot, urow_ptr, urow_col,
       urow_slot, in_row, out_col, pcol_ptr, pcol_raw, pcol_q, pos_block, block_ptr, task,
-      ttask;
+      ttask, cs_chunk, cs_op;
   gk::DPlan dp{}, dpt{};
+  int64_t updates = 0;  // multiply-subtract pairs of one refactorization
 
   cudaError_t upload(const gk::Plan& p, cudaStream_t s) {
     std::vector<i32> h_in_row(p.n), h_out_col(p.n), bp(p.block_ptr.begin(), p.block_ptr.end());
@@ -109,8 +174,17 @@ struct PlanDev {
     std::vector<i32> t = make_tasks(p, false), tt = make_tasks(p, true);
     if (e == cudaSuccess) e = task.upload(t, s);
     if (e == cudaSuccess) e = ttask.upload(tt, s);
+    std::vector<i32> hc, ho;
+    make_cta_solve(p, hc, ho);
+    if (e == cudaSuccess) e = cs_chunk.upload(hc, s);
+    if (e == cudaSuccess) e = cs_op.upload(ho, s);
+    updates = (int64_t)p.upd_dst.size();
     gk::DPlan d{};
     d.n = p.n;
+    d.noffd = p.offd_ptr.empty() ? 0 : p.offd_ptr.back();
+    d.cs_nchunk = (int)(hc.size() / 4);
+    d.cs_chunk = cs_chunk.p;
+    d.cs_op = cs_op.p;
     d.nslots = p.nslots();
     d.nblocks = p.nblocks;
     d.ntask = (int)t.size();
@@ -351,6 +425,12 @@ struct gpuklu_handle {
   DBuf<gk::NewtonState> d_nstate;
   unsigned epoch = 0, sepoch = 0;
   int64_t factor_count = 0, refactor_count = 0;
+  bool cta_ref = false, cta_sol = false;  // one-block refactor / solve for this plan
+  // Plans with up to this many multiply-subtract pairs refactor in one block.
+  // FP64 issue on one SM (a warp instruction per 16 cycles) bounds that
+  // kernel: the 32x32 diode mesh (273k pairs) already refactors faster over
+  // the whole grid, despite the grid kernel's dependency hops through L2.
+  static constexpr int64_t kOneBlockUpdates = 1 << 16;
   double rcond = 0.0;
   bool rcond_valid = false;
   std::string err;
@@ -383,6 +463,11 @@ struct gpuklu_handle {
     cudaError_t e = pd.upload(plan, stream);
     if (e == cudaSuccess) e = d_lu.resize(std::max(plan.nslots(), 1));
     if (e != cudaSuccess) return cuda_fail(e, "upload plan");
+    // one-block refactor and solve for small factorizations (GPUKLU_ONE_BLOCK=0: off)
+    const char* ob = getenv("GPUKLU_ONE_BLOCK");
+    const bool allow = !(ob && ob[0] == '0');
+    cta_ref = allow && pd.updates <= kOneBlockUpdates && gk::refactor_cta_fits(pd.dp);
+    cta_sol = allow && gk::solve_cta_fits(pd.dp);
     return GPUKLU_OK;
   }
 
@@ -461,18 +546,29 @@ struct gpuklu_handle {
   }
 
   // Factor with the values already in d_ax.
+  void refactor_launch() {
+    if (cta_ref) {
+      gk::launch_refactor_cta(pd.dp, d_ax.p, d_lu.p, d_status.p, stream);
+      return;
+    }
+    unsigned ep = next_epoch(epoch, d_flags);
+    gk::launch_refactor(pd.dp, d_ax.p, d_lu.p, d_flags.p, ep, d_counter.p, d_status.p,
+                        grid_cols, stream);
+  }
+
   int factor_on_device(bool sync) {
     rcond_valid = false;
     if (state == FACTORED) {
-      unsigned ep = next_epoch(epoch, d_flags);
-      gk::launch_refactor(pd.dp, d_ax.p, d_lu.p, d_flags.p, ep, d_counter.p, d_status.p,
-                          grid_cols, stream);
+      refactor_launch();
       ++refactor_count;
       if (!sync) return GPUKLU_OK;
       return check_status("refactor");
     }
     // First factorization: the reference's pivot pass.
-    gk::launch_first_factor(pd_sym.dp, d_ax.p, d_lu.p, d_work.p, d_rperm.p, d_rinv.p,
+    int maxblk = 0;
+    for (int b = 0; b < sym_plan.nblocks; ++b)
+      maxblk = std::max(maxblk, sym_plan.block_ptr[b + 1] - sym_plan.block_ptr[b]);
+    gk::launch_first_factor(pd_sym.dp, maxblk, d_ax.p, d_lu.p, d_work.p, d_rperm.p, d_rinv.p,
                             no_swap ? 0.0 : 0.001, d_status.p, stream);
     std::vector<i32> rperm(n);
     cudaError_t e = cudaMemcpyAsync(rperm.data(), d_rperm.p, n * sizeof(i32),
@@ -496,11 +592,7 @@ struct gpuklu_handle {
       piv_rperm.swap(rperm);
       piv_ok = true;
     }
-    if (pivot_mode == GPUKLU_PIVOT_EXACT) {  // refactor the exact pattern
-      unsigned ep = next_epoch(epoch, d_flags);
-      gk::launch_refactor(pd.dp, d_ax.p, d_lu.p, d_flags.p, ep, d_counter.p, d_status.p,
-                          grid_cols, stream);
-    }
+    if (pivot_mode == GPUKLU_PIVOT_EXACT) refactor_launch();  // the exact pattern
     ++factor_count;
     state = FACTORED;
     return check_status("factor");
@@ -508,6 +600,11 @@ struct gpuklu_handle {
 
   // Solve with rhs in d_rhs; result in d_out (original column order).
   int solve_on_device(bool transpose, bool sync) {
+    if (cta_sol && !transpose) {
+      gk::launch_solve_cta(pd.dp, d_rhs.p, d_ax.p, d_lu.p, d_out.p, stream);
+      if (!sync) return GPUKLU_OK;
+      return check_status("solve");
+    }
     unsigned ep = sepoch + 1;
     if (ep == 0) ep = 1;
     sepoch = ep;
@@ -814,11 +911,13 @@ int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_co
         gk::launch_newton_update(nc, n, h->d_newx.p, h->d_out.p, h->d_nstate.p, nc_,
                                  h->d_status.p, h->stream);
         gk::NewtonState hs;
+        int dst = 0;
         e = cudaMemcpyAsync(&hs, h->d_nstate.p, sizeof(hs), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(&dst, h->d_status.p, sizeof(int), cudaMemcpyDeviceToHost,
+                              h->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
         if (e != cudaSuccess) return h->cuda_fail(e, "newton step");
-        int dst = 0;
-        cudaMemcpy(&dst, h->d_status.p, sizeof(int), cudaMemcpyDeviceToHost);
         if (dst == GPUKLU_DEVICE_TIMEOUT) {
           cudaMemset(h->d_status.p, 0, sizeof(int));
           h->err = "device dependency wait timed out";
@@ -2551,6 +2650,11 @@ int64_t gpuklu_plan_array(const gpuklu_plan* P, const char* name, int64_t* out, 
     return (int64_t)v.size();
   };
   if (k == "info") return put(P->info);
+  if (k == "cs_chunk" || k == "cs_op") {  // the one-block solve's schedule
+    std::vector<i32> hc, ho;
+    make_cta_solve(p, hc, ho);
+    return put(k == "cs_chunk" ? hc : ho);
+  }
 #define ARR(nm) \
   if (k == #nm) return put(p.nm);
   ARR(col_ptr) ARR(dslot) ARR(slot_row) ARR(upd_ptr) ARR(upd_dst) ARR(amap_ptr) ARR(amap_idx)

@@ -29,6 +29,7 @@
 // contraction, so every product is rounded before it is added exactly as in
 // the reference; the factor and solve results are bit-identical to a scalar
 // CPU evaluation in the reference's order.
+#include <algorithm>
 #include <cstdio>
 
 #include "batch_common.cuh"
@@ -131,6 +132,193 @@ __global__ void k_first_factor(DPlan P, const double* __restrict__ ax, double* l
     __syncwarp();
   }
   (void)status;
+}
+
+// The same first factorization with the working column, the block's row
+// inverse and the operands of each column's updates in shared memory. The
+// operations and their order are those of k_first_factor (and therefore the
+// reference's); only where the operands sit differs. Per column:
+//   1. A(:,k) is loaded by all lanes and lane 0 adds it into the working
+//      column in CSC order;
+//   2. the U entries are taken in chunks of 32: for each, the L column it
+//      updates with (rows and values, all of them final) is copied into
+//      shared memory by cp.async, every lane issuing its copies at once, and
+//      the updates then run in order out of shared memory;
+//   3. the threshold pivot search, the swap and the scaling follow.
+// Shared layout: work[maxblk] f64, bl[cap] f64, rinv[maxblk] i32, br[cap]
+// i32, kpat[kcap] i32, then the chunk table.
+constexpr int kPatCap = 1024;
+
+__device__ __forceinline__ void cp_async4(void* sdst, const void* gsrc) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+__global__ void k_first_factor_s(DPlan P, const double* __restrict__ ax, double* lu,
+                                 int* rperm, int* rinv, double tol, int maxblk, int cap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* const work = reinterpret_cast<double*>(smem_raw);
+  double* const bl = work + maxblk;
+  int* const srinv = reinterpret_cast<int*>(bl + cap);
+  int* const br = srinv + maxblk;
+  int* const kpat = br + cap;
+  int* const soff = kpat + kPatCap;  // [33]
+  int* const sq0 = soff + 33;        // [32]
+  int* const sj = sq0 + 32;          // [32]
+  const int lane = threadIdx.x;
+  const int n = P.n;
+  for (int i = lane; i < n; i += 32) rperm[i] = i - P.block_ptr[P.pos_block[i]];
+  for (int i = lane; i < maxblk; i += 32) work[i] = 0.0;
+  for (int b = 0; b < P.nblocks; ++b) {
+    const int b0 = P.block_ptr[b], b1 = P.block_ptr[b + 1];
+    for (int i = lane; i < b1 - b0; i += 32) srinv[i] = i;
+    __syncwarp();
+    for (int k = b0; k < b1; ++k) {
+      const int s0 = P.col_ptr[k], ds = P.dslot[k], s1 = P.col_ptr[k + 1];
+      const int t0 = P.pcol_ptr[k], t1 = P.pcol_ptr[k + 1];
+      if (P.col_single[k]) {
+        double d = 0.0;
+        for (int tc = t0; tc < t1; tc += 32) {
+          const double v = tc + lane < t1 ? ax[P.pcol_raw[tc + lane]] : 0.0;
+          const int cnt = min(32, t1 - tc);
+          for (int i = 0; i < cnt; ++i) d += __shfl_sync(FULL, v, i);
+        }
+        if (lane == 0) lu[ds] = perturb(d, true);
+        continue;
+      }
+      const bool staged = s1 - s0 <= kPatCap;
+      if (staged)
+        for (int s = s0 + lane; s < s1; s += 32) cp_async4(&kpat[s - s0], &P.slot_row[s]);
+      // 1. A(:,k), duplicates added in CSC order
+      for (int tc = t0; tc < t1; tc += 32) {
+        int q = 0;
+        double v = 0.0;
+        if (tc + lane < t1) {
+          q = P.pcol_q[tc + lane];
+          v = ax[P.pcol_raw[tc + lane]];
+        }
+        const int cnt = min(32, t1 - tc);
+        for (int i = 0; i < cnt; ++i) {
+          const int qi = __shfl_sync(FULL, q, i);
+          const double vi = __shfl_sync(FULL, v, i);
+          if (lane == 0) work[srinv[qi]] += vi;
+        }
+      }
+      cp_async_wait_all();
+      __syncwarp();
+      auto row = [&](int s) { return staged ? kpat[s - s0] : P.slot_row[s]; };
+      // 2. updates by the U entries, in order
+      for (int sc = s0; sc < ds; sc += 32) {
+        const int cnt = min(32, ds - sc);
+        int j = 0, q0 = 0, len = 0;
+        if (lane < cnt) {
+          j = row(sc + lane);
+          q0 = P.dslot[j] + 1;
+          len = P.col_ptr[j + 1] - q0;
+        }
+        int incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(FULL, incl, o);
+          if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(FULL, incl, 31);
+        if (total <= cap) {
+          soff[lane] = incl - len;
+          sq0[lane] = q0;
+          sj[lane] = j;
+          if (lane == 31) soff[32] = total;
+          __syncwarp();
+          int si = 0;
+          for (int e = lane; e < total; e += 32) {
+            while (soff[si + 1] <= e) ++si;
+            const int q = sq0[si] + (e - soff[si]);
+            cp_async4(&br[e], &P.slot_row[q]);
+            cp_async8(&bl[e], &lu[q]);
+          }
+          cp_async_wait_all();
+          __syncwarp();
+          for (int i = 0; i < cnt; ++i) {
+            const double u = work[sj[i] - b0];
+            if (u != 0.0) {
+              const int e1 = soff[i + 1];
+              for (int e = soff[i] + lane; e < e1; e += 32) {
+                const int r = br[e] - b0;
+                work[r] = work[r] - bl[e] * u;
+              }
+            }
+            __syncwarp();
+          }
+        } else {  // a chunk larger than the buffer: its operands straight from memory
+          for (int i = 0; i < cnt; ++i) {
+            const int ji = __shfl_sync(FULL, j, i);
+            const int qa = __shfl_sync(FULL, q0, i);
+            const int qb = qa + __shfl_sync(FULL, len, i);
+            const double u = work[ji - b0];
+            if (u != 0.0)
+              for (int q = qa + lane; q < qb; q += 32) {
+                const int r = P.slot_row[q] - b0;
+                work[r] = work[r] - lu[q] * u;
+              }
+            __syncwarp();
+          }
+        }
+      }
+      // 3. threshold pivot search inside the symbolic pattern: the first row
+      // with the largest magnitude wins; the diagonal wins ties
+      const double dabs = fabs(work[k - b0]);
+      double best = -1.0;
+      int bidx = 0x7fffffff;
+      for (int q = ds + 1 + lane; q < s1; q += 32) {
+        const double v = fabs(work[row(q) - b0]);
+        if (v > best) {
+          best = v;
+          bidx = q;
+        }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        const double ov = __shfl_down_sync(FULL, best, off);
+        const int oi = __shfl_down_sync(FULL, bidx, off);
+        if (ov > best || (ov == best && oi < bidx)) {
+          best = ov;
+          bidx = oi;
+        }
+      }
+      best = __shfl_sync(FULL, best, 0);
+      bidx = __shfl_sync(FULL, bidx, 0);
+      if (lane == 0 && bidx != 0x7fffffff && best > dabs && dabs < tol * best) {
+        const int mr = row(bidx);
+        const double tmp = work[k - b0];
+        work[k - b0] = work[mr - b0];
+        work[mr - b0] = tmp;
+        const int ok = rperm[k], om = rperm[mr];
+        rperm[k] = om;
+        rperm[mr] = ok;
+        srinv[ok] = mr - b0;
+        srinv[om] = k - b0;
+      }
+      __syncwarp();
+      for (int s = s0 + lane; s < ds; s += 32) lu[s] = work[row(s) - b0];
+      const double diag = perturb(work[k - b0], false);
+      if (lane == 0) lu[ds] = diag;
+      for (int q = ds + 1 + lane; q < s1; q += 32) lu[q] = work[row(q) - b0] / diag;
+      __syncwarp();
+      for (int t = t0 + lane; t < t1; t += 32) work[srinv[P.pcol_q[t]]] = 0.0;
+      for (int q = s0 + lane; q < s1; q += 32) work[row(q) - b0] = 0.0;
+      __syncwarp();
+      if (lane == 0) work[k - b0] = 0.0;
+      __syncwarp();
+    }
+    for (int i = lane; i < b1 - b0; i += 32) rinv[b0 + i] = srinv[i];
+    __syncwarp();
+  }
 }
 
 // --------------------------------------------------------------- refactor
@@ -301,6 +489,221 @@ __global__ void k_tsolve(DPlan P, const double* __restrict__ g, const double* __
       }
     }
   }
+}
+
+// --------------------------------------------------------------- one-block factor and solve
+// For factorizations small enough that one SM does their arithmetic faster
+// than the dependency hops of the grid-wide kernels cost, the refactor and
+// the solve run in one thread block, where a hop is a shared-memory flag (or
+// a warp barrier) instead of a round trip through L2.
+
+__device__ __forceinline__ unsigned ld_acquire_cta(const unsigned* p) {
+  unsigned v;
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ld.acquire.cta.shared::cta.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_cta(unsigned* p, unsigned v) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("st.release.cta.shared::cta.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+
+// k_refactor in one block, with the factor itself in shared memory: the
+// column code is k_refactor's (same operations, same order); the completion
+// flags also live in shared memory, so a warp waiting for a column sees it
+// finish within a few hundred cycles. The static metadata of the U entries is
+// fetched in a pipeline - the row two entries ahead, the L range and update
+// list one entry ahead, the first update destinations before the wait - so a
+// step costs shared-memory latency only. All warps of the block are resident
+// and a warp only waits for columns handed out before its own, so the warp
+// holding the lowest unfinished column always proceeds. Shared: lu[nslots]
+// f64, done[n] u32.
+__global__ void __launch_bounds__(1024) k_refactor_cta(DPlan P, const double* __restrict__ ax,
+                                                       double* lu_out, int* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* const lu = reinterpret_cast<double*>(smem_raw);
+  unsigned* const sdone = reinterpret_cast<unsigned*>(lu + P.nslots);
+  __shared__ unsigned snext;
+  const int lane = threadIdx.x & 31;
+  const int n = P.n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sdone[i] = 0u;
+  if (threadIdx.x == 0) snext = 0u;
+  __syncthreads();
+  bool failed = false;
+  while (!failed) {
+    int k = 0;
+    if (lane == 0) k = (int)atomicAdd(&snext, 1u);
+    k = __shfl_sync(FULL, k, 0);
+    if (k >= n) break;
+    const int s0 = P.col_ptr[k], ds = P.dslot[k], s1 = P.col_ptr[k + 1];
+    for (int s = s0 + lane; s < s1; s += 32) {
+      double v = 0.0;
+      for (int t = P.amap_ptr[s]; t < P.amap_ptr[s + 1]; ++t) v += ax[P.amap_idx[t]];
+      lu[s] = v;
+    }
+    int j0 = s0 < ds ? P.slot_row[s0] : 0;
+    int j1 = s0 + 1 < ds ? P.slot_row[s0 + 1] : 0;
+    int qa = 0, qb = 0, up = 0;
+    if (s0 < ds) {
+      qa = P.dslot[j0] + 1;
+      qb = P.col_ptr[j0 + 1];
+      up = P.upd_ptr[s0];
+    }
+    __syncwarp();
+    for (int s = s0; s < ds; ++s) {
+      int nqa = 0, nqb = 0, nup = 0, j2 = 0;
+      if (s + 1 < ds) {
+        nqa = P.dslot[j1] + 1;
+        nqb = P.col_ptr[j1 + 1];
+        nup = P.upd_ptr[s + 1];
+      }
+      if (s + 2 < ds) j2 = P.slot_row[s + 2];
+      const int q = qa + lane;
+      const int d0 = q < qb ? P.upd_dst[up + lane] : 0;
+      int ok = 1;
+      if (lane == 0) {
+        unsigned spins = 0;
+        while (ld_acquire_cta(&sdone[j0]) == 0u) {
+          if (++spins > kSpinLimit) {
+            atomicCAS(status, DS_OK, DS_TIMEOUT);
+            ok = 0;
+            break;
+          }
+          if ((spins & 63u) == 0 && *(volatile int*)status != DS_OK) {
+            ok = 0;
+            break;
+          }
+          __nanosleep(20);
+        }
+      }
+      if (!__shfl_sync(FULL, ok, 0)) {
+        failed = true;
+        break;
+      }
+      const double u = lu[s];
+      if (u != 0.0) {
+        if (q < qb) lu[d0] = lu[d0] - lu[q] * u;
+        for (int qq = q + 32; qq < qb; qq += 32) {
+          const int d = P.upd_dst[up + qq - qa];
+          lu[d] = lu[d] - lu[qq] * u;
+        }
+      }
+      __syncwarp();
+      j0 = j1;
+      j1 = j2;
+      qa = nqa;
+      qb = nqb;
+      up = nup;
+    }
+    if (failed) break;
+    const double diag = perturb(lu[ds], P.col_single[k] != 0);
+    for (int q = ds + 1 + lane; q < s1; q += 32) lu[q] = lu[q] / diag;
+    if (lane == 0) lu[ds] = diag;
+    __syncwarp();
+    __threadfence_block();
+    if (lane == 0) st_release_cta(&sdone[k], 1u);
+  }
+  __syncthreads();
+  for (int s = threadIdx.x; s < P.nslots; s += blockDim.x) lu_out[s] = lu[s];
+}
+
+// The solve of k_solve in one block, column by column: the forward sweep
+// takes the L columns in ascending order and subtracts l(r,j) x(j) from each
+// row r below, the backward sweep the U columns in descending order, so every
+// row receives its terms in the order of its row lists (L ascending, U
+// descending) - the reference's order - and the results are those of k_solve
+// bit for bit. The block coupling of a BTF block is subtracted, row by row in
+// its list order, before the block's first column.
+//
+// Warp 0 does the arithmetic; the other warps copy the factor's slots (rows
+// and values) chunk by chunk into a double buffer ahead of it. The host cuts
+// the sweeps into chunks of contiguous slots (CtaSolve in capi.cu):
+//   chunk c: cs_chunk[4c..4c+3] = slot_lo, slot_hi, op_lo, op_hi
+//   op o:    cs_op[3o..3o+2]    = kind | direct << 2, a, b
+// kind 0: coupling of rows [a, b); 1: forward over columns [a, b); 2:
+// backward over columns [a, b); direct: a column larger than a chunk, read
+// from memory. Shared: w[n] f64, 2 x chunk values f64, then (i32) 2 x chunk
+// rows, col_ptr[n+1], dslot[n], offd_ptr[n+1] (when there is coupling).
+__global__ void __launch_bounds__(256) k_solve_cta(DPlan P, const double* __restrict__ rhs,
+                                                   const double* __restrict__ ax,
+                                                   const double* __restrict__ lu, double* out,
+                                                   int chunk) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = P.n, tid = threadIdx.x, lane = tid & 31;
+  const bool coupled = P.noffd > 0;
+  double* const w = reinterpret_cast<double*>(smem_raw);
+  double* const bval = w + n;
+  int* const brow = reinterpret_cast<int*>(bval + 2 * chunk);
+  int* const scp = brow + 2 * chunk;
+  int* const sds = scp + n + 1;
+  int* const sop = sds + n;
+  for (int i = tid; i <= n; i += blockDim.x) {
+    cp_async4(&scp[i], &P.col_ptr[i]);
+    if (i < n) cp_async4(&sds[i], &P.dslot[i]);
+    if (coupled) cp_async4(&sop[i], &P.offd_ptr[i]);
+  }
+  for (int i = tid; i < n; i += blockDim.x) w[i] = rhs[P.in_row[i]];
+  cp_async_wait_all();
+  const int nchunk = P.cs_nchunk;
+  const int nprod = blockDim.x - 32;
+  auto load = [&](int c) {
+    const int lo = P.cs_chunk[4 * c], hi = P.cs_chunk[4 * c + 1];
+    double* const bv = bval + (c & 1) * chunk;
+    int* const br = brow + (c & 1) * chunk;
+    for (int s = lo + tid - 32; s < hi; s += nprod) {  // all copies in flight at once
+      cp_async8(&bv[s - lo], &lu[s]);
+      cp_async4(&br[s - lo], &P.slot_row[s]);
+    }
+    cp_async_wait_all();
+  };
+  if (tid >= 32 && nchunk > 0) load(0);
+  __syncthreads();
+  for (int c = 0; c < nchunk; ++c) {
+    if (tid >= 32) {
+      if (c + 1 < nchunk) load(c + 1);
+    } else {
+      const int lo = P.cs_chunk[4 * c], o0 = P.cs_chunk[4 * c + 2], o1 = P.cs_chunk[4 * c + 3];
+      const double* const bv = bval + (c & 1) * chunk - lo;  // indexed by slot
+      const int* const br = brow + (c & 1) * chunk - lo;
+      for (int o = o0; o < o1; ++o) {
+        const int code = P.cs_op[3 * o], a = P.cs_op[3 * o + 1], b = P.cs_op[3 * o + 2];
+        const bool direct = (code & 4) != 0;
+        const double* const V = direct ? lu : bv;
+        const int* const R = direct ? P.slot_row : br;
+        if ((code & 3) == 0) {  // coupling to the blocks solved before
+          for (int i = a + lane; i < b; i += 32) {
+            double v = w[i];
+            for (int e = sop[i]; e < sop[i + 1]; ++e) v = v - ax[P.offd_raw[e]] * w[P.offd_col[e]];
+            w[i] = v;
+          }
+        } else if ((code & 3) == 1) {  // forward: L columns ascending
+          for (int j = a; j < b; ++j) {
+            const double xj = w[j];
+            const int q1 = scp[j + 1];
+            for (int q = sds[j] + 1 + lane; q < q1; q += 32) {
+              const int r = R[q];
+              w[r] = w[r] - V[q] * xj;
+            }
+            __syncwarp();
+          }
+        } else {  // backward: U columns descending
+          for (int j = b - 1; j >= a; --j) {
+            const int ds = sds[j];
+            const double xj = w[j] / V[ds];
+            for (int q = scp[j] + lane; q < ds; q += 32) {
+              const int r = R[q];
+              w[r] = w[r] - V[q] * xj;
+            }
+            __syncwarp();
+            if (lane == 0) w[j] = xj;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < n; i += blockDim.x) out[P.out_col[i]] = w[i];
 }
 
 // --------------------------------------------------------------- devices
@@ -881,8 +1284,22 @@ __global__ void k_batch_newton(BatchArgs A) {
 }  // namespace
 
 // ------------------------------------------------------------------ launches
-void launch_first_factor(const DPlan& P, const double* ax, double* lu, double* work,
-                         int* rperm, int* rinv, double tol, int* status, cudaStream_t s) {
+void launch_first_factor(const DPlan& P, int maxblk, const double* ax, double* lu,
+                         double* work, int* rperm, int* rinv, double tol, int* status,
+                         cudaStream_t s) {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t fixed = (size_t)12 * maxblk + 4 * (size_t)(kPatCap + 33 + 32 + 32) + 16;
+  int cap = 4096;
+  while (cap > 256 && fixed + (size_t)12 * cap > (size_t)optin) cap >>= 1;
+  const size_t bytes = fixed + (size_t)12 * cap;
+  if (maxblk > 0 && bytes <= (size_t)optin) {
+    cudaFuncSetAttribute(k_first_factor_s, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)bytes);
+    k_first_factor_s<<<1, 32, bytes, s>>>(P, ax, lu, rperm, rinv, tol, maxblk, cap);
+    return;
+  }
   k_first_factor<<<1, 32, 0, s>>>(P, ax, lu, work, rperm, rinv, tol, status);
 }
 
@@ -891,6 +1308,48 @@ void launch_refactor(const DPlan& P, const double* ax, double* lu, unsigned* fla
                      cudaStream_t s) {
   cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
   k_refactor<<<grid, 128, 0, s>>>(P, ax, lu, flags, epoch, counter, status);
+}
+
+namespace {
+size_t refactor_cta_bytes(const DPlan& P) {
+  return (size_t)8 * P.nslots + (size_t)4 * P.n + 16;
+}
+int smem_optin() {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return optin;
+}
+}  // namespace
+
+bool refactor_cta_fits(const DPlan& P) {
+  return P.n > 0 && refactor_cta_bytes(P) + 64 <= (size_t)smem_optin();
+}
+
+void launch_refactor_cta(const DPlan& P, const double* ax, double* lu, int* status,
+                         cudaStream_t s) {
+  const size_t bytes = refactor_cta_bytes(P);
+  cudaFuncSetAttribute(k_refactor_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k_refactor_cta<<<1, 1024, bytes, s>>>(P, ax, lu, status);
+}
+
+namespace {
+size_t solve_cta_bytes(const DPlan& P) {
+  return (size_t)8 * P.n + (size_t)24 * kSolveChunk + (size_t)4 * (2 * (size_t)P.n + 1) +
+         (P.noffd > 0 ? (size_t)4 * (P.n + 1) : 0) + 16;
+}
+}  // namespace
+
+bool solve_cta_fits(const DPlan& P) {
+  return P.n > 0 && solve_cta_bytes(P) <= (size_t)smem_optin();
+}
+
+void launch_solve_cta(const DPlan& P, const double* rhs, const double* ax, const double* lu,
+                      double* out, cudaStream_t s) {
+  const size_t bytes = solve_cta_bytes(P);
+  if (bytes > 48 * 1024)
+    cudaFuncSetAttribute(k_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k_solve_cta<<<1, 256, bytes, s>>>(P, rhs, ax, lu, out, kSolveChunk);
 }
 
 void launch_solve(const DPlan& P, const double* rhs, const double* ax, const double* lu,

@@ -16,6 +16,9 @@ struct DPlan {
   const int *in_row, *out_col;  // position -> original row / original column
   const int *pcol_ptr, *pcol_raw, *pcol_q, *pos_block, *block_ptr;
   const int *task;              // solve order: (position << 1) | is_upper
+  int noffd;                    // block-coupling entries
+  int cs_nchunk;                // one-block solve schedule (k_solve_cta)
+  const int *cs_chunk, *cs_op;
 };
 
 // Device form of a compiled circuit (device list + stamp-to-slot map).
@@ -149,11 +152,25 @@ struct BbdArgs {
 };
 
 // --------------------------------------------------------------- launches
-void launch_first_factor(const DPlan& P, const double* ax, double* lu, double* work,
-                         int* rperm, int* rinv, double tol, int* status, cudaStream_t s);
+// maxblk: the largest diagonal block; blocks up to about 14k rows run with the
+// working column in shared memory.
+void launch_first_factor(const DPlan& P, int maxblk, const double* ax, double* lu,
+                         double* work, int* rperm, int* rinv, double tol, int* status,
+                         cudaStream_t s);
 void launch_refactor(const DPlan& P, const double* ax, double* lu, unsigned* flags,
                      unsigned epoch, unsigned* counter, int* status, int grid,
                      cudaStream_t s);
+// Slots per chunk of the one-block solve's schedule.
+constexpr int kSolveChunk = 2048;
+// One-block variants for small factorizations; *_cta_fits says whether the
+// kernel's shared-memory working set (the whole factor, for the refactor)
+// fits one block.
+bool refactor_cta_fits(const DPlan& P);
+void launch_refactor_cta(const DPlan& P, const double* ax, double* lu, int* status,
+                         cudaStream_t s);
+bool solve_cta_fits(const DPlan& P);
+void launch_solve_cta(const DPlan& P, const double* rhs, const double* ax, const double* lu,
+                      double* out, cudaStream_t s);
 void launch_solve(const DPlan& P, const double* rhs, const double* ax, const double* lu,
                   double* z, double* x, double* out, unsigned* zflag, unsigned* xflag,
                   unsigned epoch, unsigned* counter, int* status, int grid, bool transpose,

@@ -126,6 +126,65 @@ def solve(P: native.Plan, ax, lu, rhs):
     return out
 
 
+SOLVE_CHUNK = 2048  # slots per chunk of the one-block solve (kSolveChunk)
+
+
+def solve_one_block(P: native.Plan, ax, lu, rhs):
+    """The one-block solve's column sweeps over its chunk schedule, with the
+    double buffer's index arithmetic checked: every slot an op reads lies in
+    its chunk's range, and no chunk is longer than the buffer."""
+    n = P.n
+    in_row = np.zeros(n, np.int64)
+    in_row[P.in_pos] = np.arange(n)
+    w = np.asarray(rhs, np.float64)[in_row].copy()
+    ch, op = P.cs_chunk.reshape(-1, 4), P.cs_op.reshape(-1, 3)
+    assert ch.shape[0] > 0 and ch[0, 2] == 0 and ch[-1, 3] == op.shape[0]
+    for c in range(ch.shape[0]):
+        lo, hi, o0, o1 = (int(v) for v in ch[c])
+        assert 0 <= lo <= hi <= P.nslots and hi - lo <= SOLVE_CHUNK
+        if c + 1 < ch.shape[0]:
+            assert ch[c + 1, 2] == o1
+        buf_v = lu[lo:hi]
+        buf_r = P.slot_row[lo:hi]
+
+        def at(q, direct):
+            if direct:
+                return lu[q], P.slot_row[q]
+            assert lo <= q < hi
+            return buf_v[q - lo], buf_r[q - lo]
+
+        for o in range(o0, o1):
+            code, a, b = (int(v) for v in op[o])
+            direct = bool(code & 4)
+            assert 0 <= a < b <= n
+            if code & 3 == 0:
+                for i in range(a, b):
+                    v = w[i]
+                    for e in range(P.offd_ptr[i], P.offd_ptr[i + 1]):
+                        v = v - ax[P.offd_raw[e]] * w[P.offd_col[e]]
+                    w[i] = v
+            elif code & 3 == 1:
+                for j in range(a, b):
+                    xj = w[j]
+                    for q in range(P.dslot[j] + 1, P.col_ptr[j + 1]):
+                        val, r = at(q, direct)
+                        assert j < r < n
+                        w[r] = w[r] - val * xj
+            else:
+                for j in range(b - 1, a - 1, -1):
+                    ds = P.dslot[j]
+                    dv, _ = at(ds, direct)
+                    xj = w[j] / dv
+                    for q in range(P.col_ptr[j], ds):
+                        val, r = at(q, direct)
+                        assert 0 <= r < j
+                        w[r] = w[r] - val * xj
+                    w[j] = xj
+    out = np.zeros(n)
+    out[:] = w[P.out_pos]
+    return out
+
+
 class EmulatedSolver:
     """LinearSolver call sequence over the emulated kernels."""
 

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as po
-from plan_emulator import EmulatedSolver
+from plan_emulator import SOLVE_CHUNK, EmulatedSolver, solve_one_block
 from rustspice_gb300 import circuits as cz
 from rustspice_gb300 import native as N
 
@@ -62,6 +62,8 @@ def test_plan_emulation_bit_exact(sysm, mode, kind):
         assert st == 0
         xe = es.solve(rhs)
         assert np.array_equal(xe, xo), np.max(np.abs(xe - xo))
+        xb = solve_one_block(es.plan, es.ax, es.lu, rhs)  # column sweeps, chunked
+        assert np.array_equal(xb, xo), np.max(np.abs(xb - xo))
     st = s.klu_stats()
     assert es.plan.nblocks == st["nblocks"]
     if mode == N.PIVOT_REFERENCE:  # the pattern of the pivot-free symbolic pass
@@ -74,3 +76,61 @@ def test_mesh_dimensions():
     c = cz.mesh_dc()
     n, ap, ai, ax, rhs = po.mna(c, np.zeros(c.node_count))
     assert n == 1026 and len(ai) == 8201
+
+
+def _star(n, seed):
+    """A hub coupled to every other node: after ordering the hub's column holds
+    n slots, more than one chunk of the one-block solve."""
+    rng = np.random.default_rng(seed)
+    cols = []
+    for c in range(n):
+        if c == 0:
+            rows = list(range(n))
+        else:
+            rows = [0, c]
+        cols.append(rows)
+    ap = np.zeros(n + 1, np.int64)
+    ap[1:] = np.cumsum([len(r) for r in cols])
+    ai = np.concatenate([np.array(r, np.int64) for r in cols])
+    ax = np.where(np.repeat(np.arange(n), [len(r) for r in cols]) == ai,
+                  float(n) + rng.uniform(1, 2, len(ai)), rng.uniform(-1, 1, len(ai)))
+    return ap, ai, ax, rng.uniform(-1, 1, n)
+
+
+@pytest.mark.parametrize("mode,kind", MODES, ids=["reference", "exact"])
+def test_one_block_solve_direct_column(mode, kind):
+    """A column longer than a chunk is read straight from memory; the result
+    stays the oracle's bit for bit."""
+    n = SOLVE_CHUNK + 300
+    ap, ai, ax, rhs = _star(n, 5)
+    es = EmulatedSolver(mode)
+    es.factor(n, ap, ai, ax)
+    op = es.plan.cs_op.reshape(-1, 3)
+    assert np.any(op[:, 0] & 4), "expected a direct piece"
+    s = po.Solver(kind, n)
+    s.prepare(n)
+    assert s.analyze(ap, ai) == 0
+    assert s.factor(ap, ai, ax) == 0
+    st, xo = s.solve(rhs)
+    assert st == 0
+    xb = solve_one_block(es.plan, es.ax, es.lu, rhs)
+    assert np.array_equal(xb, xo)
+
+
+def test_one_block_schedule_mesh():
+    """The 32x32 diode mesh's schedule: several chunks, each within the
+    buffer, and the sweeps bit-identical to the oracle's solve."""
+    c = cz.mesh_dc()
+    x = np.random.default_rng(4).uniform(0, 1.2, c.node_count)
+    n, ap, ai, ax, rhs = po.mna(c, x)
+    es = EmulatedSolver(N.PIVOT_EXACT)
+    es.factor(n, ap, ai, ax)
+    ch = es.plan.cs_chunk.reshape(-1, 4)
+    assert ch.shape[0] > 4 and np.all(ch[:, 1] - ch[:, 0] <= SOLVE_CHUNK)
+    s = po.Solver("nativeklu_exact", n)
+    s.prepare(n)
+    assert s.analyze(ap, ai) == 0
+    assert s.factor(ap, ai, ax) == 0
+    st, xo = s.solve(rhs)
+    assert st == 0
+    assert np.array_equal(solve_one_block(es.plan, es.ax, es.lu, rhs), xo)
