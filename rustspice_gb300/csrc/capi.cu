@@ -1019,7 +1019,7 @@ struct gpuklu_batch {
     int m = 1, region = 0, prog_ints = 0, grid = 0, warps_per_block = 1, regs = 0,
         blocks_per_sm = 0;
     // continuation phase: warps of a block share one staged program
-    int grid2 = 0, wpb2 = 1;
+    int grid2 = 0, wpb2 = 1, shared_bytes = 0;
     bool shared2 = false;
     // after the lane phase (parked instances): tiles2 for blocks sharing a
     // program, tiles3 for one warp per tile
@@ -1031,6 +1031,9 @@ struct gpuklu_batch {
     gk::BatchArgs args{};
   };
   std::vector<std::unique_ptr<Class>> classes;
+  // warps of a block that shares one program: up to this many, as the
+  // group's program and instance regions fit the block's shared memory
+  static constexpr int kSharedWarpsMax = 16;
   cudaEvent_t start_ev = nullptr;
   gk::BatchArgs args{};
   // lane-per-instance phase (k_batch_lanes) in front of the warp classes
@@ -1537,14 +1540,21 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     return region <= 1152 ? 4 : (region <= 2304 ? 2 : 1);
   };
   const int mclass[4] = {1, 2, 4, 8};
+  for (int g = 0; g < ngr; ++g) {
+    gk::GroupHdr& h = B->groups[g];
+    h.region = gregion[g];
+    // column records, slot rows (and the update lists for leveled programs)
+    h.prog = (4 * h.n + h.nslots + (h.nseg > 0 ? h.nslots + h.nupd : 0) + 3) & ~3;
+  }
   for (int ci = 0; ci < 4; ++ci) {
     auto C = std::make_unique<gpuklu_batch::Class>();
     C->m = mclass[ci];
+    std::vector<int> members;
     for (int g : gorder) {
       const gk::GroupHdr& h = B->groups[g];
-      // column records, slot rows (and the update lists for leveled programs)
-      const int prog = (4 * h.n + h.nslots + (h.nseg > 0 ? h.nslots + h.nupd : 0) + 3) & ~3;
+      const int prog = h.prog;
       if (pick_m(gregion[g], prog) != C->m || h.inst_count == 0) continue;
+      members.push_back(g);
       C->region = std::max(C->region, gregion[g]);
       C->prog_ints = std::max(C->prog_ints, prog);
       const int nt = (h.inst_count + C->m - 1) / C->m;
@@ -1561,14 +1571,32 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       return nullptr;
     }
     C->grid = std::min<int>(sm_count() * C->blocks_per_sm, (int)C->tiles.size());
-    {  // the largest block of warps sharing one program that fits shared memory
-      const size_t cap = 227 * 1024, prog = (size_t)C->prog_ints * 4;
-      const size_t per = (size_t)C->region * 8 * C->m;
-      int w = prog < cap ? (int)std::min<size_t>(8, (cap - prog) / per) : 0;
+    {  // a block of warps sharing one program: each group fills the shared
+       // memory with as many instance regions as fit beside its program
+      const size_t cap = 227 * 1024;
+      int wmin = 1 << 30, w = 0;
+      std::vector<int> fit;
+      for (int g : members) {
+        const gk::GroupHdr& h = B->groups[g];
+        const size_t prog = (size_t)h.prog * 4, per = (size_t)h.region * 8 * C->m;
+        const int f = prog < cap ? (int)((cap - prog) / per) : 0;
+        fit.push_back(f);
+        wmin = std::min(wmin, f);
+        w = std::max(w, f);
+      }
+      w = std::min(w, gpuklu_batch::kSharedWarpsMax);
+      size_t bytes = 0;
+      for (size_t q = 0; q < members.size(); ++q) {
+        const gk::GroupHdr& h = B->groups[members[q]];
+        bytes = std::max(bytes, (size_t)h.prog * 4 +
+                                    (size_t)std::min(w, fit[q]) * h.region * 8 * C->m);
+      }
       int r2 = 0, b2 = 0;
       const char* esh = getenv("GPUKLU_SHARED_PROGRAM");
-      if (esh && esh[0] == '0') w = 0;
-      if (w >= 2) gk::batch_kernel_info(C->m, w, C->region, C->prog_ints, &r2, &b2, true);
+      if ((esh && esh[0] == '0') || wmin < 2) w = 0;
+      if (w >= 2)
+        gk::batch_kernel_info(C->m, w, C->region, C->prog_ints, &r2, &b2, true, bytes);
+      C->shared_bytes = (int)bytes;
       if (w >= 2 && b2 > 0 && w * b2 > C->blocks_per_sm * C->warps_per_block) {
         C->shared2 = true;
         C->wpb2 = w;
@@ -1623,7 +1651,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     const char* ecap = getenv("GPUKLU_LANE_CAP");
     B->lane_cap = ecap ? std::max(1, atoi(ecap)) : 6;
     const char* etgt = getenv("GPUKLU_LANE_TARGET");
-    const int target = etgt ? std::max(32, atoi(etgt)) : 64;
+    const int target = etgt ? std::max(32, atoi(etgt)) : 32;
     long long lregion = 0;
     for (int g : gorder) {
       const gk::GroupHdr& h = B->groups[g];
@@ -1739,6 +1767,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     C->args.counter = C->d_counter.p;
     C->args.region = C->region;
     C->args.prog_ints = C->prog_ints;
+    C->args.shared_bytes = C->shared_bytes;
   }
   B->transient = transient;
   B->dt = dt;
@@ -2595,6 +2624,12 @@ extern "C" int gpuklu_solve_device_noalloc(gpuklu_handle* h, const double* d_rhs
                    "gpuklu_solve_device_noalloc: n = " + std::to_string(h->n) +
                        " exceeds GPUKLU_NOALLOC_MAX_N = " +
                        std::to_string(GPUKLU_NOALLOC_MAX_N));
+  if (h->cta_sol) {  // the one-block solve keeps its vectors in shared memory
+    gk::launch_solve_cta(h->pd.dp, d_rhs, h->d_ax.p, h->d_lu.p, d_x, h->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return h->cuda_fail(e, "noalloc solve launch");
+    return h->check_status("solve_device_noalloc");
+  }
   unsigned char* base = nullptr;
   cudaError_t e = noalloc_scratch(&base);
   if (e != cudaSuccess) return h->cuda_fail(e, "noalloc scratch address");

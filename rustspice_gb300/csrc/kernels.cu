@@ -1118,6 +1118,10 @@ __global__ void k_rcond(DPlan P, const double* __restrict__ lu, double* out) {
 // SHARED: the warps of a block work on one group at a time and share one
 // staged program (more instances per SM when the program is large); the
 // block moves to its next tile when every warp has run out of instances.
+// The block's shared memory is carved per group: as many warps as the
+// group's own program and instance regions fit take instances, the others
+// sit the tile out, so groups smaller than the largest of their class keep
+// more instances resident.
 template <int M, bool SHARED>
 __global__ void k_batch_newton(BatchArgs A) {
   constexpr int LPI = 32 / M;
@@ -1133,8 +1137,6 @@ __global__ void k_batch_newton(BatchArgs A) {
       SHARED ? smem_raw
              : smem_raw + (size_t)warp * ((size_t)A.prog_ints * 4 + (size_t)M * A.region * 8);
   int* const prog = reinterpret_cast<int*>(slice);
-  double* const region = reinterpret_cast<double*>(slice + (size_t)A.prog_ints * 4) +
-                         (size_t)((SHARED ? warp * M : 0) + sub) * A.region;
   const NewtonCfg cfg = A.cfg;
   const double gstart = fmax(cfg.gmin * 1e3, 1e-6);
   while (true) {
@@ -1150,6 +1152,12 @@ __global__ void k_batch_newton(BatchArgs A) {
     if (ti >= A.ntiles) return;
     const int g = A.tile_group[ti];
     const GroupHdr G = A.groups[g];
+    const int pg = SHARED ? G.prog : A.prog_ints;
+    const int rg = SHARED ? G.region : A.region;
+    const int active =
+        SHARED ? min((int)(blockDim.x >> 5), (A.shared_bytes - pg * 4) / (rg * 8 * M)) : 1;
+    double* const region = reinterpret_cast<double*>(slice + (size_t)pg * 4) +
+                           (size_t)((SHARED ? warp * M : 0) + sub) * rg;
     bt::Prog P = SHARED ? bt::stage_program(A, G, prog, threadIdx.x, blockDim.x, true)
                         : bt::stage_program(A, G, prog, lane);
     const int n = P.n, nc = P.nc;
@@ -1160,7 +1168,7 @@ __global__ void k_batch_newton(BatchArgs A) {
     P.map = reinterpret_cast<int*>(V + G.nslots + G.noffd);
 
     int inst = -1, it = 0, total = 0, gstep = 0, ov_dev = -1;
-    bool exhausted = false;
+    bool exhausted = warp >= active;  // no room for this warp's instances in this group
     double damp = 0.0, prev = 0.0, gmin = 0.0, ov_val = 0.0;
     const double* dparams = nullptr;
     while (true) {
@@ -1419,8 +1427,7 @@ double fp64_peak_tflops() {
 
 template <int M, bool SHARED>
 static size_t smem_bytes(const BatchArgs& a, int warps_per_block) {
-  if (SHARED)
-    return (size_t)a.prog_ints * 4 + (size_t)a.region * M * sizeof(double) * warps_per_block;
+  if (SHARED) return (size_t)a.shared_bytes;
   return ((size_t)a.prog_ints * 4 + (size_t)a.region * M * sizeof(double)) * warps_per_block;
 }
 
@@ -1454,13 +1461,12 @@ void launch_batch_newton(const BatchArgs& a, int m, int grid, int warps_per_bloc
 
 template <int M, bool SHARED>
 static void info_m(int warps_per_block, int region, int prog_ints, int* regs,
-                   int* blocks_per_sm) {
+                   int* blocks_per_sm, size_t shared_bytes) {
   cudaFuncAttributes fa{};
   cudaFuncGetAttributes(&fa, k_batch_newton<M, SHARED>);
   *regs = fa.numRegs;
   const size_t per = (size_t)region * M * sizeof(double);
-  const size_t sm = SHARED ? (size_t)prog_ints * 4 + per * warps_per_block
-                           : ((size_t)prog_ints * 4 + per) * warps_per_block;
+  const size_t sm = SHARED ? shared_bytes : ((size_t)prog_ints * 4 + per) * warps_per_block;
   cudaFuncSetAttribute(k_batch_newton<M, SHARED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sm);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch_newton<M, SHARED>,
@@ -1468,21 +1474,24 @@ static void info_m(int warps_per_block, int region, int prog_ints, int* regs,
 }
 
 void batch_kernel_info(int m, int warps_per_block, int region, int prog_ints, int* regs,
-                       int* blocks_per_sm, bool shared) {
+                       int* blocks_per_sm, bool shared, size_t shared_bytes) {
+  auto run = [&](auto fn) {
+    fn(warps_per_block, region, prog_ints, regs, blocks_per_sm, shared_bytes);
+  };
   if (shared) {
     switch (m) {
-      case 8: info_m<8, true>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
-      case 4: info_m<4, true>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
-      case 2: info_m<2, true>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
-      default: info_m<1, true>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+      case 8: run(info_m<8, true>); break;
+      case 4: run(info_m<4, true>); break;
+      case 2: run(info_m<2, true>); break;
+      default: run(info_m<1, true>); break;
     }
     return;
   }
   switch (m) {
-    case 8: info_m<8, false>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
-    case 4: info_m<4, false>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
-    case 2: info_m<2, false>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
-    default: info_m<1, false>(warps_per_block, region, prog_ints, regs, blocks_per_sm); break;
+    case 8: run(info_m<8, false>); break;
+    case 4: run(info_m<4, false>); break;
+    case 2: run(info_m<2, false>); break;
+    default: run(info_m<1, false>); break;
   }
 }
 

@@ -68,6 +68,8 @@ struct GroupHdr {
   int seg_off;     // factor schedule: segments (start, end, sequential) per block,
   int nseg;        //   block b's at lseg_ptr[b]..lseg_ptr[b+1] (lseg_ptr at blk_off);
                    //   the columns in schedule order sit at col_off in lvl_col
+  int region;      // shared-memory doubles of one instance of this program
+  int prog;        // ints of the staged program (a multiple of 4)
 };
 
 // Contribution codes of the batched stamp: (index << 3) | kind with kind
@@ -100,6 +102,7 @@ struct BatchArgs {
   NewtonCfg cfg;
   int region;     // shared-memory doubles per instance
   int prog_ints;  // shared-memory ints of the staged program (largest group)
+  int shared_bytes;  // dynamic shared memory of a launch whose warps share a program
   int *iters, *iters_total, *reason;
   const long long* inst_x_off;
   double* x_out;
@@ -215,7 +218,8 @@ void launch_tran_forward(const BatchArgs& a, int grid, int warps_per_block, cuda
 void launch_tran_backward(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
 void tran_kernel_info(bool backward, int warps_per_block, int region, int prog_ints, int* regs,
                       int* blocks_per_sm);
+// shared: the warps share one program and the block holds shared_bytes.
 void batch_kernel_info(int m, int warps_per_block, int region, int prog_ints, int* regs,
-                       int* blocks_per_sm, bool shared = false);
+                       int* blocks_per_sm, bool shared = false, size_t shared_bytes = 0);
 
 }  // namespace gk

@@ -25,6 +25,14 @@ KATS = json.load(open(os.path.join(GOLD, "kats.json")))
 MODES = [(N.PIVOT_REFERENCE, "nativeklu"), (N.PIVOT_EXACT, "nativeklu_exact")]
 
 
+@pytest.fixture(params=["one_block", "grid"])
+def kernels(request, monkeypatch):
+    """Small factorizations refactor and solve in one thread block; "grid"
+    switches that off so the grid-wide flag kernels run the same systems."""
+    monkeypatch.setenv("GPUKLU_ONE_BLOCK", "1" if request.param == "one_block" else "0")
+    return request.param
+
+
 def _gpu_solve(g, ap, ai, ax, b):
     g.factor(ap, ai, ax)
     x = np.ascontiguousarray(b, np.float64).copy()
@@ -43,7 +51,7 @@ def _oracle_solve(kind, ap, ai, ax, b):
 
 
 @pytest.mark.parametrize("mode,kind", MODES, ids=["reference", "exact"])
-def test_kats(mode, kind):
+def test_kats(mode, kind, kernels):
     for k in KATS["solve"]:
         n = len(k["ap"]) - 1
         g = GpuKluSolver(n, pivot_mode=mode)
@@ -75,7 +83,7 @@ def test_refactor_counters_and_rcond():
 
 @pytest.mark.parametrize("mode,kind", MODES, ids=["reference", "exact"])
 @pytest.mark.parametrize("name", ["adder_dcop_01", "circuit_1", "rajat01"])
-def test_matrix_market_bit_exact(name, mode, kind):
+def test_matrix_market_bit_exact(name, mode, kind, kernels):
     z = np.load(os.path.join(GOLD, f"mtx_{name}.npz"))
     ap, ai, ax, rhs = z["ap"].astype(np.int64), z["ai"].astype(np.int64), z["ax"], z["rhs"]
     n = len(ap) - 1
@@ -127,3 +135,22 @@ def test_divider_and_began_newton():
     r = newton_dc(g, DeviceCircuit(div), N.newton_config(**cfg))
     for node, v in d["expect"].items():
         assert abs(r.x[int(node)] - v) < d["tol"]
+
+
+@pytest.mark.parametrize("mode,kind", MODES, ids=["reference", "exact"])
+def test_mesh_solve_both_kernel_sets(mode, kind, kernels):
+    """The 32x32 diode mesh (a dense 300-row separator at the end of its
+    ordering; the one-block solve streams it in 13 chunks per sweep) solves
+    bit for bit like the oracle with either kernel set, across a refactor."""
+    c = cz.mesh_dc()
+    n, ap, ai, ax, rhs = po.mna(c, np.random.default_rng(11).uniform(0, 0.8, c.node_count))
+    g = GpuKluSolver(n, pivot_mode=mode)
+    s = po.Solver(kind, n)
+    s.prepare(n)
+    ax2 = ax * (1.0 + 1e-3 * np.random.default_rng(2).standard_normal(len(ax)))
+    for a in (ax, ax2):
+        x = _gpu_solve(g, ap, ai, a, rhs)
+        assert s.factor(ap, ai, a) == 0
+        st, xo = s.solve(rhs)
+        assert np.array_equal(x, xo), np.max(np.abs(x - xo))
+    g.close()

@@ -31,7 +31,9 @@ def _system():
     return dc.n, ap, ai, ax, rhs
 
 
-def test_noalloc_solve_matches_solve():
+@pytest.mark.parametrize("one_block", ["1", "0"], ids=["one_block", "grid"])
+def test_noalloc_solve_matches_solve(one_block, monkeypatch):
+    monkeypatch.setenv("GPUKLU_ONE_BLOCK", one_block)
     import torch
     from rustspice_gb300 import native as N
     from rustspice_gb300.solver import GpuKluSolver
