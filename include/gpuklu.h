@@ -209,11 +209,14 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
                                   const double* inst_val, const double* x0,
                                   const int64_t* x0_off, int64_t x0_len);
 void gpuklu_batch_destroy(gpuklu_batch* b);
-/* Runs every instance's Newton loop on the device (one kernel launch). */
+/* Runs every instance's Newton loop on the device: a lane-per-instance
+ * kernel for the first iterations, then the warp kernels for the instances
+ * still iterating. */
 int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg);
 /* Results: per instance iterations (final run), total iterations, exit
  * reason, and x (n of its circuit values, at x_out + x_off[i]; x_off may be
- * NULL to skip). */
+ * NULL to skip). When x_off is the batch's own layout (consecutive
+ * instances, n values each) x arrives in one copy, a DMA into pinned x_out. */
 int gpuklu_batch_results(gpuklu_batch* b, int64_t* iters, int64_t* iters_total, int32_t* reason,
                          double* x_out, const int64_t* x_off);
 /* Host->device copy of new per-instance values and initial iterates

@@ -1535,9 +1535,18 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   // instances per warp by per-instance shared memory: small programs put
   // four instances in a warp, medium two, large one (more resident warps
   // hide more FP64 latency than wider packing saves)
-  auto pick_m = [](int region, int prog) {
+  // Behind the lane phase the warp kernels only run the instances it parked,
+  // mostly long non-converging runs: there one instance per warp, with the
+  // block's shared memory carved per group, beats packing (measured on the
+  // inverter chains: 140 ms against 161 ms per batch). Without the lane
+  // phase small programs pack four or two instances per warp.
+  const char* elanes = getenv("GPUKLU_BATCH_LANES");
+  const bool lanes_on = !transient && !(elanes && elanes[0] == '0');
+  int t4 = lanes_on ? 0 : 1152, t2 = lanes_on ? 0 : 2304;
+  if (const char* epm = getenv("GPUKLU_PICK_M")) sscanf(epm, "%d,%d", &t4, &t2);
+  auto pick_m = [t4, t2](int region, int prog) {
     (void)prog;
-    return region <= 1152 ? 4 : (region <= 2304 ? 2 : 1);
+    return region <= t4 ? 4 : (region <= t2 ? 2 : 1);
   };
   const int mclass[4] = {1, 2, 4, 8};
   for (int g = 0; g < ngr; ++g) {
@@ -1646,8 +1655,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   // Lane phase: every group split into tiles of about lane_target instances,
   // most expensive programs first; a scratch of region x 32 doubles per warp.
   {
-    const char* env = getenv("GPUKLU_BATCH_LANES");
-    B->lanes = !transient && !(env && env[0] == '0');
+    B->lanes = lanes_on;
     const char* ecap = getenv("GPUKLU_LANE_CAP");
     B->lane_cap = ecap ? std::max(1, atoi(ecap)) : 6;
     const char* etgt = getenv("GPUKLU_LANE_TARGET");
@@ -2001,7 +2009,13 @@ int gpuklu_batch_results(gpuklu_batch* b, int64_t* iters, int64_t* iters_total, 
     e = cudaMemcpyAsync(itt.data(), b->d_iters_total.p, ni * 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(rs.data(), b->d_reason.p, ni * 4, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess && x_out && b->xout_len) {
+  // the caller's layout is the batch's own (the usual case): one copy straight
+  // into x_out, a DMA when x_out is pinned
+  bool direct = x_out && x_off && b->xout_len;
+  for (int64_t i = 0; direct && i < ni; ++i) direct = x_off[i] == b->x_off[i];
+  if (e == cudaSuccess && direct) {
+    e = cudaMemcpyAsync(x_out, b->d_xout.p, b->xout_len * 8, cudaMemcpyDeviceToHost, s);
+  } else if (e == cudaSuccess && x_out && x_off && b->xout_len) {
     xo.resize(b->xout_len);
     e = cudaMemcpyAsync(xo.data(), b->d_xout.p, b->xout_len * 8, cudaMemcpyDeviceToHost, s);
   }
@@ -2012,7 +2026,7 @@ int gpuklu_batch_results(gpuklu_batch* b, int64_t* iters, int64_t* iters_total, 
     if (iters_total) iters_total[i] = itt[i];
     if (reason) reason[i] = rs[i];
   }
-  if (x_out && x_off) {
+  if (x_out && x_off && !direct) {
     for (int64_t i = 0; i < ni; ++i) {
       const long long a = b->x_off[i];
       const long long len = (i + 1 < ni ? b->x_off[i + 1] : b->xout_len) - a;

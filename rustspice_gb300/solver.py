@@ -264,11 +264,21 @@ class Batch:
         if st != N.OK:
             raise SolverError(st, N.lib().gpuklu_batch_last_error(self._h).decode())
 
-    def results(self, with_x: bool = True):
+    def results(self, with_x: bool = True, x_out: np.ndarray = None):
+        """Iterations, total iterations, exit reasons and (with_x) the
+        solutions, concatenated per instance. x_out: a float64 buffer of
+        x_len values to fill instead of a new array (pinned memory makes
+        the copy a DMA)."""
         it = np.zeros(self.ninst, np.int64)
         itt = np.zeros(self.ninst, np.int64)
         rs = np.zeros(self.ninst, np.int32)
-        x = np.zeros(self.x_len) if with_x else None
+        if with_x and x_out is not None:
+            if not (x_out.dtype == np.float64 and x_out.flags.c_contiguous
+                    and len(x_out) >= self.x_len):
+                raise TypeError("x_out must be a contiguous float64 array of x_len values")
+            x = x_out
+        else:
+            x = np.zeros(self.x_len) if with_x else None
         st = N.lib().gpuklu_batch_results(self._h, N.ptr(it), N.ptr(itt), N.ptr(rs),
                                           N.ptr(x) if with_x else None,
                                           N.ptr(self.x_off) if with_x else None)
