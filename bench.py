@@ -175,18 +175,22 @@ def _residual_sample(B, bt, rs, count=64):
     return worst
 
 
-def _ncu_traffic(iters_per_step):
-    """DRAM bytes of one batch run, scaled from the committed ncu summary of
-    k_batch_newton (dram__bytes_read.sum + dram__bytes_write.sum over all size
-    classes of a smaller batch, per Newton iteration)."""
-    path = os.path.join(ROOT, "profiles", "k_batch_newton_inverter_chains.txt")
+PROFILE = os.path.join(ROOT, "profiles", "batch_kernels_inverter_chains.txt")
+
+
+def _ncu_traffic(kernel, iters):
+    """DRAM bytes of one launch of `kernel` that runs `iters` Newton
+    iterations, scaled from the committed ncu summary (dram__bytes_read.sum +
+    dram__bytes_write.sum of one launch on a 2048-chain batch, per iteration
+    that launch ran)."""
     try:
-        with open(path) as f:
-            m = re.search(r"^dram_bytes_per_newton_iteration:\s*([0-9.eE+-]+)", f.read(), re.M)
+        with open(PROFILE) as f:
+            m = re.search(r"^dram_bytes_per_iteration %s:\s*([0-9.eE+-]+)" % re.escape(kernel),
+                          f.read(), re.M)
         per = float(m.group(1))
     except (OSError, AttributeError, ValueError):
         return None, "no ncu summary"
-    return per * iters_per_step, f"{os.path.relpath(path, ROOT)} ({per:.1f} B per iteration)"
+    return per * iters, f"{os.path.relpath(PROFILE, ROOT)} ({per:.1f} B per iteration)"
 
 
 def secondary(with_cpu=True):
@@ -346,6 +350,13 @@ def run_gpu(a):
             it2, itt2, rs2, x2 = bt.results(with_x=True, x_out=xout_h.numpy())
             e2e_ms.append((time.perf_counter() - t1) * 1e3)
         e2e_step = ranks.max_over_ranks(float(np.median(e2e_ms)), dev)
+
+        # per-kernel device time (CUDA events the library records on its
+        # launching streams around the lane kernel and the warp kernels)
+        phases = []
+        for _ in range(max(3, a.steps)):
+            step()
+            phases.append(bt.phase_ms())
         h2d = val_h.numel() * 8 + x0_h.numel() * 8
         d2h = len(x2) * 8 + 3 * 8 * len(it2)
     conv = float(np.mean(rs == 0))
@@ -355,13 +366,29 @@ def run_gpu(a):
     # stamped at x by the device and evaluated on the host, normwise relative
     resid = _residual_sample(B, bt, rs)
 
-    # roofline
+    # roofline of the dominant kernel: its share of the algorithmic bytes
+    # (iterations an instance runs in the lane kernel: min(total, cap); the
+    # rest in the warp kernel) over its own event-timed duration
     hbm_peak, peak_src = _measured_peaks()
     per_key = _alg_bytes_per_iter(B.circuits)
     keys = [(B.circuits[c].ndev, B.circuits[c].node_count) for c in B.inst_circ]
-    alg_bytes = float(sum(per_key[k] * t for k, t in zip(keys, itt)))
-    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
-    traffic, traffic_src = _ncu_traffic(iters_per_step)
+    b_inst = np.array([per_key[k] for k in keys], np.float64)
+    alg_bytes = float(np.sum(b_inst * itt))
+    cap = phases[0]["lane_cap"]
+    lane_it = np.minimum(itt, cap) if cap > 0 else np.zeros_like(itt)
+    kern = {}
+    for name, ms_k, its in (("k_batch_lanes", "lanes_ms", lane_it),
+                            ("k_batch_newton", "warps_ms", itt - lane_it)):
+        t_ms = float(np.median([p[ms_k] for p in phases]))
+        kb = float(np.sum(b_inst * its))
+        tr, tr_src = _ncu_traffic(name, int(its.sum()))
+        kern[name] = {"ms_per_launch": t_ms, "newton_iterations": int(its.sum()),
+                      "algorithmic_bytes_per_launch": kb,
+                      "achieved_gbs": kb / (t_ms * 1e-3) / 1e9 if t_ms > 0 else None,
+                      "dram_bytes_per_launch": tr, "traffic_source": tr_src}
+    dom = max(kern, key=lambda k: kern[k]["ms_per_launch"])
+    achieved = kern[dom]["achieved_gbs"]
+    traffic, traffic_src = kern[dom]["dram_bytes_per_launch"], kern[dom]["traffic_source"]
     flops, _ = bt.work()
     fp64 = float(np.sum(flops.astype(np.float64) * itt))
     fp64_tflops = fp64 / (ms_step * 1e-3) / 1e12
@@ -406,11 +433,11 @@ def run_gpu(a):
         "one_at_a_time": {"value": one_at_a_time, "unit": UNIT,
                           "how": "GpuKluSolver newton_dc, one instance at a time, 24 sampled",
                           "batched_over_one_at_a_time": value / one_at_a_time},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": traffic,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                      "traffic_source": traffic_src,
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                     "algorithmic_bytes_per_step": alg_bytes},
+                     "algorithmic_bytes_per_step": alg_bytes, "kernels": kern},
         "roofline_fp64": {"achieved": fp64_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
                           "frac": fp64_tflops / fp64_peak if fp64_peak else None,
                           "peak_source": "measured DFMA microbenchmark (gpuklu_fp64_peak_tflops)",

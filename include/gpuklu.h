@@ -228,12 +228,18 @@ const char* gpuklu_batch_last_error(const gpuklu_batch* b);
  * block, out[2] program groups, out[3] shared-memory bytes per warp,
  * out[4] registers per thread, out[5] resident blocks per SM (out[1], out[3..5]
  * describe the largest class), out[6] kernel launches per gpuklu_batch_run
- * (one per size class), out[7] reserved (0). */
+ * (the lane kernel and one per size class), out[7] reserved (0). */
 int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out);
 /* Work of one Newton iteration of every instance: FP64 operations and the
  * value bytes it moves through on-chip memory (arrays of ninst). */
 int gpuklu_batch_work(const gpuklu_batch* b, int64_t* flops, int64_t* bytes);
 void* gpuklu_batch_stream(gpuklu_batch* b);
+/* Device time of the last gpuklu_batch_run (waits for it), from CUDA events
+ * on the launching streams: out[0] the lane-per-instance kernel [ms], out[1]
+ * the warp kernels that finish the instances it parked [ms], out[2] the
+ * iterations an instance runs in the lane kernel before it is parked (0: no
+ * lane phase). */
+int gpuklu_batch_phase_ms(gpuklu_batch* b, double* out);
 
 /* ------------------------------------------ bordered block diagonal */
 /* The reference's BbdSolver (crates/sim-core/src/bbd_solver.rs:86-1095,

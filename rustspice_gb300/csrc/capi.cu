@@ -1035,6 +1035,9 @@ struct gpuklu_batch {
   // group's program and instance regions fit the block's shared memory
   static constexpr int kSharedWarpsMax = 16;
   cudaEvent_t start_ev = nullptr;
+  // timing events of the last run: before the lane kernel, after it, after
+  // the warp kernels joined back
+  cudaEvent_t ph_ev[3] = {nullptr, nullptr, nullptr};
   gk::BatchArgs args{};
   // lane-per-instance phase (k_batch_lanes) in front of the warp classes
   bool lanes = false;
@@ -1062,6 +1065,8 @@ struct gpuklu_batch {
       if (c->done) cudaEventDestroy(c->done);
     }
     if (start_ev) cudaEventDestroy(start_ev);
+    for (auto& ev : ph_ev)
+      if (ev) cudaEventDestroy(ev);
   }
 
   int fail(const std::string& m) {
@@ -1568,10 +1573,15 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       C->prog_ints = std::max(C->prog_ints, prog);
       const int nt = (h.inst_count + C->m - 1) / C->m;
       for (int t = 0; t < nt; ++t) C->tiles.push_back(g);
-      for (int t = 0; t < std::min(nt, 2); ++t) C->tiles2.push_back(g);
       for (int t = 0; t < std::min(nt, 12); ++t) C->tiles3.push_back(g);
     }
     if (C->tiles.empty()) continue;
+    {  // shared-program tiles: `per` consecutive ones per group
+      const char* ept = getenv("GPUKLU_SHARED_TILES");
+      const int per = std::max(1, ept ? atoi(ept) : 2);
+      for (int g : members)
+        for (int t = 0; t < per; ++t) C->tiles2.push_back(g);
+    }
     gk::batch_kernel_info(C->m, C->warps_per_block, C->region, C->prog_ints, &C->regs,
                           &C->blocks_per_sm);
     if (C->blocks_per_sm <= 0) {
@@ -1582,7 +1592,9 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     C->grid = std::min<int>(sm_count() * C->blocks_per_sm, (int)C->tiles.size());
     {  // a block of warps sharing one program: each group fills the shared
        // memory with as many instance regions as fit beside its program
-      const size_t cap = 227 * 1024;
+      const char* enb = getenv("GPUKLU_SHARED_BLOCKS");  // blocks per SM
+      const int nb = std::max(1, std::min(4, enb ? atoi(enb) : 1));
+      const size_t cap = (size_t)228 * 1024 / nb - 1024;
       int wmin = 1 << 30, w = 0;
       std::vector<int> fit;
       for (int g : members) {
@@ -1593,7 +1605,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
         wmin = std::min(wmin, f);
         w = std::max(w, f);
       }
-      w = std::min(w, gpuklu_batch::kSharedWarpsMax);
+      w = std::min(w, gpuklu_batch::kSharedWarpsMax / nb);
       size_t bytes = 0;
       for (size_t q = 0; q < members.size(); ++q) {
         const gk::GroupHdr& h = B->groups[members[q]];
@@ -1602,7 +1614,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       }
       int r2 = 0, b2 = 0;
       const char* esh = getenv("GPUKLU_SHARED_PROGRAM");
-      if ((esh && esh[0] == '0') || wmin < 2) w = 0;
+      if ((esh && esh[0] == '0') || wmin < (nb > 1 ? 1 : 2)) w = 0;
       if (w >= 2)
         gk::batch_kernel_info(C->m, w, C->region, C->prog_ints, &r2, &b2, true, bytes);
       C->shared_bytes = (int)bytes;
@@ -1621,6 +1633,8 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     B->classes.push_back(std::move(C));
   }
   if (cudaEventCreateWithFlags(&B->start_ev, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+  for (auto& ev : B->ph_ev)
+    if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
   cudaStream_t s = B->stream;
   cudaError_t e = cudaSuccess;
   std::vector<i32> ov_dev(ninst);
@@ -1672,6 +1686,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     if (B->lanes && !B->ltiles.empty()) {
       int regs = 0, bps = 0;
       gk::lanes_kernel_info(B->lane_wpb, &regs, &bps);
+      if (const char* eb = getenv("GPUKLU_LANE_BPS")) bps = std::max(1, std::min(bps, atoi(eb)));
       const long long warps_max = (long long)sm_count() * std::max(bps, 1) * B->lane_wpb;
       const long long warps = std::min<long long>(warps_max, (long long)B->ltiles.size());
       B->lane_grid = (int)((warps + B->lane_wpb - 1) / B->lane_wpb);
@@ -1972,10 +1987,14 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
     cudaMemsetAsync(b->d_lcounter.p, 0, sizeof(unsigned), s);
     cudaMemsetAsync(b->d_cont_count.p, 0, b->d_cont_count.n * sizeof(unsigned), s);
     cudaMemsetAsync(b->d_gnext2.p, 0, b->d_gnext2.n * sizeof(unsigned), s);
+  }
+  cudaEventRecord(b->ph_ev[0], s);
+  if (b->lanes) {
     gk::BatchArgs la = b->args;
     la.cfg = c;
     gk::launch_batch_lanes(la, b->lane_grid, b->lane_wpb, s);
   }
+  cudaEventRecord(b->ph_ev[1], s);
   cudaEventRecord(b->start_ev, s);
   for (auto& C : b->classes) {  // largest programs first, all classes concurrent
     cudaStreamWaitEvent(C->stream, b->start_ev, 0);
@@ -1992,8 +2011,22 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
     cudaEventRecord(C->done, C->stream);
     cudaStreamWaitEvent(s, C->done, 0);
   }
+  cudaEventRecord(b->ph_ev[2], s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return b->fail(cuda_msg(e, "batch launch"));
+  return GPUKLU_OK;
+}
+
+int gpuklu_batch_phase_ms(gpuklu_batch* b, double* out) {
+  if (!b || !out) return GPUKLU_INVALID_MATRIX;
+  cudaError_t e = cudaEventSynchronize(b->ph_ev[2]);
+  float a = 0.f, w = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&a, b->ph_ev[0], b->ph_ev[1]);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&w, b->ph_ev[1], b->ph_ev[2]);
+  if (e != cudaSuccess) return b->fail(cuda_msg(e, "batch phase timing"));
+  out[0] = a;
+  out[1] = w;
+  out[2] = b->lanes ? b->lane_cap : 0;
   return GPUKLU_OK;
 }
 

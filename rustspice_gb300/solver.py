@@ -303,6 +303,16 @@ class Batch:
     def stream(self) -> int:
         return N.lib().gpuklu_batch_stream(self._h) or 0
 
+    def phase_ms(self) -> dict:
+        """Device time of the last run by kernel (CUDA events; waits for the
+        run): the lane-per-instance kernel, the warp kernels after it, and
+        the lane kernel's iteration cap."""
+        out = np.zeros(3)
+        st = N.lib().gpuklu_batch_phase_ms(self._h, N.ptr(out))
+        if st != N.OK:
+            raise SolverError(st, N.lib().gpuklu_batch_last_error(self._h).decode())
+        return {"lanes_ms": float(out[0]), "warps_ms": float(out[1]), "lane_cap": int(out[2])}
+
 
 class TranBatch:
     """Fixed-step backward-Euler transient of many circuits (one instance per
