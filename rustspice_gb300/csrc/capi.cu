@@ -1576,12 +1576,10 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       for (int t = 0; t < std::min(nt, 12); ++t) C->tiles3.push_back(g);
     }
     if (C->tiles.empty()) continue;
-    {  // shared-program tiles: `per` consecutive ones per group
-      const char* ept = getenv("GPUKLU_SHARED_TILES");
-      const int per = std::max(1, ept ? atoi(ept) : 2);
-      for (int g : members)
-        for (int t = 0; t < per; ++t) C->tiles2.push_back(g);
-    }
+    // shared-program tiles: two consecutive ones per group (measured best
+    // against one, three, four, eight, and round-robin orders)
+    for (int g : members)
+      for (int t = 0; t < 2; ++t) C->tiles2.push_back(g);
     gk::batch_kernel_info(C->m, C->warps_per_block, C->region, C->prog_ints, &C->regs,
                           &C->blocks_per_sm);
     if (C->blocks_per_sm <= 0) {
@@ -1592,9 +1590,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     C->grid = std::min<int>(sm_count() * C->blocks_per_sm, (int)C->tiles.size());
     {  // a block of warps sharing one program: each group fills the shared
        // memory with as many instance regions as fit beside its program
-      const char* enb = getenv("GPUKLU_SHARED_BLOCKS");  // blocks per SM
-      const int nb = std::max(1, std::min(4, enb ? atoi(enb) : 1));
-      const size_t cap = (size_t)228 * 1024 / nb - 1024;
+      const size_t cap = 227 * 1024;
       int wmin = 1 << 30, w = 0;
       std::vector<int> fit;
       for (int g : members) {
@@ -1605,7 +1601,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
         wmin = std::min(wmin, f);
         w = std::max(w, f);
       }
-      w = std::min(w, gpuklu_batch::kSharedWarpsMax / nb);
+      w = std::min(w, gpuklu_batch::kSharedWarpsMax);
       size_t bytes = 0;
       for (size_t q = 0; q < members.size(); ++q) {
         const gk::GroupHdr& h = B->groups[members[q]];
@@ -1614,7 +1610,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       }
       int r2 = 0, b2 = 0;
       const char* esh = getenv("GPUKLU_SHARED_PROGRAM");
-      if ((esh && esh[0] == '0') || wmin < (nb > 1 ? 1 : 2)) w = 0;
+      if ((esh && esh[0] == '0') || wmin < 2) w = 0;
       if (w >= 2)
         gk::batch_kernel_info(C->m, w, C->region, C->prog_ints, &r2, &b2, true, bytes);
       C->shared_bytes = (int)bytes;
@@ -1686,7 +1682,6 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     if (B->lanes && !B->ltiles.empty()) {
       int regs = 0, bps = 0;
       gk::lanes_kernel_info(B->lane_wpb, &regs, &bps);
-      if (const char* eb = getenv("GPUKLU_LANE_BPS")) bps = std::max(1, std::min(bps, atoi(eb)));
       const long long warps_max = (long long)sm_count() * std::max(bps, 1) * B->lane_wpb;
       const long long warps = std::min<long long>(warps_max, (long long)B->ltiles.size());
       B->lane_grid = (int)((warps + B->lane_wpb - 1) / B->lane_wpb);
