@@ -140,10 +140,11 @@ __global__ void k_first_factor(DPlan P, const double* __restrict__ ax, double* l
 // reference's); only where the operands sit differs. Per column:
 //   1. A(:,k) is loaded by all lanes and lane 0 adds it into the working
 //      column in CSC order;
-//   2. the U entries are taken in chunks of 32: for each, the L column it
-//      updates with (rows and values, all of them final) is copied into
-//      shared memory by cp.async, every lane issuing its copies at once, and
-//      the updates then run in order out of shared memory;
+//   2. the U entries are taken in chunks of 32, and a chunk in runs whose
+//      L columns (rows and values, all of them final) fit the buffer: a run's
+//      operands are copied into shared memory by cp.async, every lane issuing
+//      its copies at once, and its updates then run in order out of shared
+//      memory;
 //   3. the threshold pivot search, the swap and the scaling follow.
 // Shared layout: work[maxblk] f64, bl[cap] f64, rinv[maxblk] i32, br[cap]
 // i32, kpat[kcap] i32, then the chunk table.
@@ -230,38 +231,40 @@ __global__ void k_first_factor_s(DPlan P, const double* __restrict__ ax, double*
           if (lane >= o) incl += v;
         }
         const int total = __shfl_sync(FULL, incl, 31);
-        if (total <= cap) {
-          soff[lane] = incl - len;
-          sq0[lane] = q0;
-          sj[lane] = j;
-          if (lane == 31) soff[32] = total;
-          __syncwarp();
-          int si = 0;
-          for (int e = lane; e < total; e += 32) {
-            while (soff[si + 1] <= e) ++si;
-            const int q = sq0[si] + (e - soff[si]);
-            cp_async4(&br[e], &P.slot_row[q]);
-            cp_async8(&bl[e], &lu[q]);
-          }
-          cp_async_wait_all();
-          __syncwarp();
-          for (int i = 0; i < cnt; ++i) {
-            const double u = work[sj[i] - b0];
-            if (u != 0.0) {
-              const int e1 = soff[i + 1];
-              for (int e = soff[i] + lane; e < e1; e += 32) {
-                const int r = br[e] - b0;
-                work[r] = work[r] - bl[e] * u;
-              }
+        soff[lane] = incl - len;
+        sq0[lane] = q0;
+        sj[lane] = j;
+        if (lane == 31) soff[32] = total;
+        __syncwarp();
+        // runs of consecutive U entries whose operands fit the buffer
+        for (int i0 = 0; i0 < cnt;) {
+          int i1 = i0 + 1;
+          while (i1 < cnt && soff[i1 + 1] - soff[i0] <= cap) ++i1;
+          const int e0 = soff[i0], e1 = soff[i1];
+          if (e1 - e0 <= cap) {
+            int si = i0;
+            for (int e = e0 + lane; e < e1; e += 32) {
+              while (soff[si + 1] <= e) ++si;
+              const int q = sq0[si] + (e - soff[si]);
+              cp_async4(&br[e - e0], &P.slot_row[q]);
+              cp_async8(&bl[e - e0], &lu[q]);
             }
+            cp_async_wait_all();
             __syncwarp();
-          }
-        } else {  // a chunk larger than the buffer: its operands straight from memory
-          for (int i = 0; i < cnt; ++i) {
-            const int ji = __shfl_sync(FULL, j, i);
-            const int qa = __shfl_sync(FULL, q0, i);
-            const int qb = qa + __shfl_sync(FULL, len, i);
-            const double u = work[ji - b0];
+            for (int i = i0; i < i1; ++i) {
+              const double u = work[sj[i] - b0];
+              if (u != 0.0) {
+                const int ea = soff[i] - e0, eb = soff[i + 1] - e0;
+                for (int e = ea + lane; e < eb; e += 32) {
+                  const int r = br[e] - b0;
+                  work[r] = work[r] - bl[e] * u;
+                }
+              }
+              __syncwarp();
+            }
+          } else {  // one L column longer than the buffer: straight from memory
+            const double u = work[sj[i0] - b0];
+            const int qa = sq0[i0], qb = qa + (e1 - e0);
             if (u != 0.0)
               for (int q = qa + lane; q < qb; q += 32) {
                 const int r = P.slot_row[q] - b0;
@@ -269,6 +272,7 @@ __global__ void k_first_factor_s(DPlan P, const double* __restrict__ ax, double*
               }
             __syncwarp();
           }
+          i0 = i1;
         }
       }
       // 3. threshold pivot search inside the symbolic pattern: the first row
@@ -322,10 +326,20 @@ __global__ void k_first_factor_s(DPlan P, const double* __restrict__ ax, double*
 }
 
 // --------------------------------------------------------------- refactor
+// A warp's column lives in shared memory while it is updated (columns of up
+// to kColBuf slots; longer ones stay in memory). The U entries are taken in
+// chunks of 32: one acquire per entry, all lanes at once, finds the columns
+// already final; those need no further wait, and the L column of the next
+// entry (its first 32 values and destinations) is loaded while the current
+// one is applied. The operations and their order are the reference's.
+constexpr int kColBuf = 768;
+
 __global__ void k_refactor(DPlan P, const double* __restrict__ ax, double* lu,
                            unsigned* flags, unsigned epoch, unsigned* counter,
                            int* status) {
+  extern __shared__ double scol[];
   const int lane = threadIdx.x & 31;
+  double* const cbuf = scol + (threadIdx.x >> 5) * kColBuf;
   const int n = P.n;
   while (true) {
     int k = 0;
@@ -333,32 +347,81 @@ __global__ void k_refactor(DPlan P, const double* __restrict__ ax, double* lu,
     k = __shfl_sync(FULL, k, 0);
     if (k >= n) return;
     const int s0 = P.col_ptr[k], ds = P.dslot[k], s1 = P.col_ptr[k + 1];
+    const bool staged = s1 - s0 <= kColBuf;
+    double* const C = staged ? cbuf - s0 : lu;  // the column, indexed by slot
     // A(:,k) into the column's slots; duplicates summed in CSC order
     for (int s = s0 + lane; s < s1; s += 32) {
       double v = 0.0;
       for (int t = P.amap_ptr[s]; t < P.amap_ptr[s + 1]; ++t) v += ax[P.amap_idx[t]];
-      lu[s] = v;
+      C[s] = v;
     }
     __syncwarp();
-    for (int s = s0; s < ds; ++s) {
-      const int j = P.slot_row[s];
-      int ok = 1;
-      if (lane == 0) ok = wait_flag(&flags[j], epoch, status);
-      ok = __shfl_sync(FULL, ok, 0);
-      if (!ok) return;
-      const double u = ld_cg(&lu[s]);
-      if (u != 0.0) {
-        const int q0 = P.dslot[j] + 1, q1 = P.col_ptr[j + 1];
-        const int* dst = P.upd_dst + P.upd_ptr[s] - q0;
-        for (int q = q0 + lane; q < q1; q += 32) {
-          const int d = dst[q];
-          lu[d] = ld_cg(&lu[d]) - ld_cg(&lu[q]) * u;
-        }
+    for (int sc = s0; sc < ds; sc += 32) {
+      const int cnt = min(32, ds - sc);
+      int jl = 0;
+      bool rdy = true;
+      if (lane < cnt) {
+        jl = P.slot_row[sc + lane];
+        rdy = ld_acquire(&flags[jl]) == epoch;
       }
-      __syncwarp();
+      const unsigned ready = __ballot_sync(FULL, rdy);
+      __syncwarp();  // orders every lane's later loads after the acquires
+      int j = 0, qa = 0, qb = 0, d0 = 0;
+      const int* dst = nullptr;
+      double v0 = 0.0;
+      auto fetch = [&](int i) {
+        j = __shfl_sync(FULL, jl, i);
+        qa = P.dslot[j] + 1;
+        qb = P.col_ptr[j + 1];
+        dst = P.upd_dst + P.upd_ptr[sc + i] - qa;
+        v0 = 0.0;
+        d0 = 0;
+        const int q = qa + lane;
+        if (q < qb && ((ready >> i) & 1u)) {
+          v0 = ld_cg(&lu[q]);
+          d0 = dst[q];
+        }
+      };
+      fetch(0);
+      for (int i = 0; i < cnt; ++i) {
+        const int s = sc + i, cqa = qa, cqb = qb;
+        const int* const cdst = dst;
+        int cd0 = d0;
+        double cv0 = v0;
+        const int cj = j;
+        if (i + 1 < cnt) fetch(i + 1);  // independent of this entry's update
+        if (!((ready >> i) & 1u)) {
+          int ok = 1;
+          if (lane == 0) ok = wait_flag(&flags[cj], epoch, status);
+          if (!__shfl_sync(FULL, ok, 0)) return;
+          __syncwarp();
+          const int q = cqa + lane;
+          if (q < cqb) {
+            cv0 = ld_cg(&lu[q]);
+            cd0 = cdst[q];
+          }
+        }
+        const double u = staged ? C[s] : ld_cg(&lu[s]);
+        if (u != 0.0) {
+          int q = cqa + lane;
+          if (q < cqb) {
+            const double c = staged ? C[cd0] : ld_cg(&lu[cd0]);
+            C[cd0] = c - cv0 * u;
+          }
+          for (q += 32; q < cqb; q += 32) {
+            const int d = cdst[q];
+            const double c = staged ? C[d] : ld_cg(&lu[d]);
+            C[d] = c - ld_cg(&lu[q]) * u;
+          }
+        }
+        __syncwarp();
+      }
     }
-    const double diag = perturb(ld_cg(&lu[ds]), P.col_single[k] != 0);
-    for (int q = ds + 1 + lane; q < s1; q += 32) lu[q] = ld_cg(&lu[q]) / diag;
+    const double diag = perturb(staged ? C[ds] : ld_cg(&lu[ds]), P.col_single[k] != 0);
+    for (int q = ds + 1 + lane; q < s1; q += 32)
+      lu[q] = (staged ? C[q] : ld_cg(&lu[q])) / diag;
+    if (staged)
+      for (int q = s0 + lane; q < ds; q += 32) lu[q] = C[q];
     if (lane == 0) lu[ds] = diag;
     __syncwarp();
     __threadfence();
@@ -1315,7 +1378,8 @@ void launch_refactor(const DPlan& P, const double* ax, double* lu, unsigned* fla
                      unsigned epoch, unsigned* counter, int* status, int grid,
                      cudaStream_t s) {
   cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
-  k_refactor<<<grid, 128, 0, s>>>(P, ax, lu, flags, epoch, counter, status);
+  k_refactor<<<grid, 128, 4 * kColBuf * sizeof(double), s>>>(P, ax, lu, flags, epoch, counter,
+                                                             status);
 }
 
 namespace {
