@@ -14,8 +14,8 @@ enum DevStatus : int {
 };
 
 // Upper bound on polls of a dependency flag before a kernel gives up, sets
-// DS_TIMEOUT and returns. With the back-off below this is well under a
-// second of waiting.
+// DS_TIMEOUT and returns. With the back-off below this is a few seconds of
+// waiting at most.
 constexpr unsigned kSpinLimit = 1u << 22;
 
 // Arithmetic without contraction: every product is rounded before it is
@@ -45,7 +45,7 @@ __device__ __forceinline__ bool wait_flag(const unsigned* flag, unsigned epoch, 
       return false;
     }
     if ((spins & 63u) == 0 && *(volatile int*)status != DS_OK) return false;
-    __nanosleep(spins < 64 ? 32 : 256);
+    if (spins > 16) __nanosleep(spins < 256 ? 32 : 256);  // a poll is an L2 round trip
   }
   return true;
 }

@@ -636,7 +636,7 @@ __global__ void __launch_bounds__(1024) k_refactor_cta(DPlan P, const double* __
             ok = 0;
             break;
           }
-          __nanosleep(20);
+          if (spins > 256) __nanosleep(20);  // shared-memory polls first
         }
       }
       if (!__shfl_sync(FULL, ok, 0)) {
