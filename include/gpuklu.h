@@ -154,7 +154,8 @@ int gpuklu_circuit_pattern(const gpuklu_circuit* c, int64_t* ap, int64_t* ai);
 int gpuklu_circuit_set_params(gpuklu_circuit* c, const double* p);
 /* Stamps the circuit at x on the device and copies the raw CSC values and
  * the right-hand side back (tests and callers that bring their own solver).
- * cap_v: per-device previous capacitor voltage (transient), may be NULL. */
+ * cap_v: per-device previous capacitor voltage (transient; ndev values), may
+ * be NULL. */
 int gpuklu_stamp(gpuklu_handle* h, gpuklu_circuit* c, const double* x, int64_t xlen,
                  double gmin, double source_scale, double dt, const double* cap_v,
                  double be_sign, double* ax_out, double* rhs_out);

@@ -176,6 +176,8 @@ def mna(c, x, gmin=1e-12, scale=1.0, dt=0.0, cap_v=None, be_sign=-1.0, gdev=1e-1
     _, t, nd, p = _circ_arrays(c)
     x = _f64(x)
     cv = _f64(cap_v) if cap_v is not None else None
+    if cv is not None and len(cv) != c.ndev:  # one previous voltage per device
+        raise ValueError(f"cap_v has {len(cv)} values, the circuit {c.ndev} devices")
     h = lib().orc_mna(c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p), _ptr(x), len(x),
                       gmin, scale, dt, _ptr(cv) if cv is not None else None, be_sign, gdev)
     n = C.c_int64()

@@ -730,36 +730,71 @@ __global__ void __launch_bounds__(256) k_solve_cta(DPlan P, const double* __rest
       const int* const br = brow + (c & 1) * chunk - lo;
       for (int o = o0; o < o1; ++o) {
         const int code = P.cs_op[3 * o], a = P.cs_op[3 * o + 1], b = P.cs_op[3 * o + 2];
-        const bool direct = (code & 4) != 0;
-        const double* const V = direct ? lu : bv;
-        const int* const R = direct ? P.slot_row : br;
+        // forward: L columns ascending. The next column's range is read, and
+        // this column's first rows and values are loaded, before the value
+        // of x(j) is: only the subtraction waits for the previous column.
+        auto fwd = [&](const auto* V, const auto* R) {
+          int q0 = sds[a] + 1, q1 = scp[a + 1];
+          for (int j = a; j < b; ++j) {
+            const int cq0 = q0, cq1 = q1;
+            if (j + 1 < b) {
+              q0 = sds[j + 1] + 1;
+              q1 = scp[j + 2];
+            }
+            const int q = cq0 + lane;
+            int r = 0;
+            double v = 0.0;
+            if (q < cq1) {
+              r = R[q];
+              v = V[q];
+            }
+            const double xj = w[j];
+            if (q < cq1) w[r] = w[r] - v * xj;
+            for (int qq = q + 32; qq < cq1; qq += 32) {
+              const int rr = R[qq];
+              w[rr] = w[rr] - V[qq] * xj;
+            }
+            __syncwarp();
+          }
+        };
+        // backward: U columns descending
+        auto bwd = [&](const auto* V, const auto* R) {
+          for (int j = b - 1; j >= a; --j) {
+            const int ds = sds[j], q = scp[j] + lane;
+            int r = 0;
+            double v = 0.0;
+            if (q < ds) {
+              r = R[q];
+              v = V[q];
+            }
+            const double xj = w[j] / V[ds];
+            if (q < ds) w[r] = w[r] - v * xj;
+            for (int qq = q + 32; qq < ds; qq += 32) {
+              const int rr = R[qq];
+              w[rr] = w[rr] - V[qq] * xj;
+            }
+            __syncwarp();
+            if (lane == 0) w[j] = xj;
+          }
+        };
+        // separate instantiations keep the buffered sweeps on shared-memory
+        // loads (a pointer that may be either space would make them generic)
         if ((code & 3) == 0) {  // coupling to the blocks solved before
           for (int i = a + lane; i < b; i += 32) {
             double v = w[i];
             for (int e = sop[i]; e < sop[i + 1]; ++e) v = v - ax[P.offd_raw[e]] * w[P.offd_col[e]];
             w[i] = v;
           }
-        } else if ((code & 3) == 1) {  // forward: L columns ascending
-          for (int j = a; j < b; ++j) {
-            const double xj = w[j];
-            const int q1 = scp[j + 1];
-            for (int q = sds[j] + 1 + lane; q < q1; q += 32) {
-              const int r = R[q];
-              w[r] = w[r] - V[q] * xj;
-            }
-            __syncwarp();
-          }
-        } else {  // backward: U columns descending
-          for (int j = b - 1; j >= a; --j) {
-            const int ds = sds[j];
-            const double xj = w[j] / V[ds];
-            for (int q = scp[j] + lane; q < ds; q += 32) {
-              const int r = R[q];
-              w[r] = w[r] - V[q] * xj;
-            }
-            __syncwarp();
-            if (lane == 0) w[j] = xj;
-          }
+        } else if ((code & 3) == 1) {
+          if (code & 4)
+            fwd(lu, P.slot_row);
+          else
+            fwd(bv, br);
+        } else {
+          if (code & 4)
+            bwd(lu, P.slot_row);
+          else
+            bwd(bv, br);
         }
         __syncwarp();
       }

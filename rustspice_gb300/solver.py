@@ -152,6 +152,8 @@ class DeviceCircuit:
         ax = np.zeros(self.nnz_raw)
         rhs = np.zeros(self.n)
         cv = N.f64(cap_v) if cap_v is not None else None
+        if cv is not None and len(cv) != self.circuit.ndev:  # one previous voltage per device
+            raise ValueError(f"cap_v has {len(cv)} values, the circuit {self.circuit.ndev} devices")
         st = N.lib().gpuklu_stamp(solver.handle, self._h, N.ptr(x), len(x), gmin, source_scale,
                                   dt, N.ptr(cv) if cv is not None else None, be_sign,
                                   N.ptr(ax), N.ptr(rhs))

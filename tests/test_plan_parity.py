@@ -34,7 +34,7 @@ def _systems():
         x = np.random.default_rng(seed).uniform(0, 1.2, c.node_count)
         transient = name.startswith("ring")
         n, ap, ai, ax, rhs = po.mna(c, x, dt=1e-12 if transient else 0.0,
-                                    cap_v=np.zeros(c.node_count) if transient else None)
+                                    cap_v=np.zeros(c.ndev) if transient else None)
         out.append((name, ap, ai, ax, rhs))
     z = np.load(os.path.join(GOLD, "mtx_adder_dcop_01.npz"))
     out.append(("adder_dcop_01", z["ap"].astype(np.int64), z["ai"].astype(np.int64), z["ax"],
