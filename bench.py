@@ -49,6 +49,8 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the single-circuit, adjoint, transient and bordered-block lines")
+    ap.add_argument("--only", choices=SECONDARY,
+                    help="run just this one of the other workloads (one JSON line, no batch)")
     return ap.parse_args()
 
 
@@ -193,19 +195,18 @@ def _ncu_traffic(kernel, iters):
     return per * iters, f"{os.path.relpath(PROFILE, ROOT)} ({per:.1f} B per iteration)"
 
 
-def secondary(with_cpu=True):
+SECONDARY = ("mesh_dc", "dc_adjoint", "transient_adjoint", "bbd")
+
+
+def secondary(with_cpu=True, parts=SECONDARY):
     """The other workloads of the path, each timed once warm (CUDA-synchronised
     wall clock around the public call): the 32x32 diode mesh with gmin
     stepping, the 20k-node adjoint, the 1024-ring transient adjoint and the
     64-mesh bordered-block-diagonal DC solve, with the oracle's time for the
-    same work on one host core where it is short."""
+    same work on one host core where it is short. `parts` selects among
+    them."""
     import torch
-    from oracle import pyoracle as po
-    from rustspice_gb300 import circuits as cz
-    from rustspice_gb300 import native as N
     from rustspice_gb300 import workloads as wl
-    from rustspice_gb300.solver import (BbdSolver, DeviceCircuit, GpuKluSolver, TranBatch,
-                                        dc_backward, dc_forward, newton_dc)
 
     def timed(fn):
         torch.cuda.synchronize()
@@ -216,7 +217,24 @@ def secondary(with_cpu=True):
 
     out = {}
     ocfg = {k: wl.TIGHT[k] for k in ("max_iters", "abs_tol", "rel_tol", "gmin", "gmin_steps")}
-    # diode mesh, gmin stepping (one circuit, device-resident Newton)
+    if "mesh_dc" in parts:
+        _mesh_dc(out, with_cpu, timed, ocfg)
+    if "dc_adjoint" in parts:
+        _dc_adjoint(out, timed)
+    if "transient_adjoint" in parts:
+        _transient_adjoint(out, timed)
+    if "bbd" in parts:
+        _bbd(out, with_cpu, timed, ocfg)
+    return out
+
+
+def _mesh_dc(out, with_cpu, timed, ocfg):
+    """Diode mesh, gmin stepping (one circuit, device-resident Newton)."""
+    from oracle import pyoracle as po
+    from rustspice_gb300 import circuits as cz
+    from rustspice_gb300 import native as N
+    from rustspice_gb300 import workloads as wl
+    from rustspice_gb300.solver import DeviceCircuit, GpuKluSolver, newton_dc
     c = cz.mesh_dc()
     cfg = N.newton_config(**dict(wl.TIGHT, gmin_steps=10))
     g = GpuKluSolver(1, pivot_mode=N.PIVOT_EXACT)
@@ -230,7 +248,14 @@ def secondary(with_cpu=True):
         ro = po.dc_op(c, "nativeklu_exact", **dict(ocfg, gmin_steps=10))
         e["oracle_ms_1core"] = (time.perf_counter() - t0) * 1e3
     out["mesh_dc"] = e
-    # DC adjoint of the 20k-node mesh with inverters
+
+
+def _dc_adjoint(out, timed):
+    """DC adjoint of the 20k-node mesh with inverters."""
+    from rustspice_gb300 import circuits as cz
+    from rustspice_gb300 import native as N
+    from rustspice_gb300 import workloads as wl
+    from rustspice_gb300.solver import DeviceCircuit, GpuKluSolver, dc_backward, dc_forward
     c = cz.mesh_with_inverters(120, 1000)
     outs = cz.output_nodes(c, 256)
     g = GpuKluSolver(1, pivot_mode=N.PIVOT_EXACT)
@@ -245,7 +270,13 @@ def secondary(with_cpu=True):
     out["dc_adjoint"] = {"workload": "120x120 mesh + 1000 inverters, loss on 256 nodes",
                          "n": dc.n, "forward_ms": t_f * 1e3, "newton_iterations": f.iterations,
                          "backward_ms": t_b * 1e3, "backward_over_forward": t_b / t_f}
-    # transient adjoint of 1024 rings
+
+
+def _transient_adjoint(out, timed):
+    """Transient adjoint of 1024 rings."""
+    from rustspice_gb300 import native as N
+    from rustspice_gb300 import workloads as wl
+    from rustspice_gb300.solver import TranBatch
     B = wl.ring_batch(1024)
     tb = TranBatch(B.circuits, B.x_init, B.x_off, wl.RING_DT, wl.RING_STEPS, wl.RING_CKPT,
                    wl.RING_PROBE, wl.RING_TARGET)
@@ -258,7 +289,15 @@ def secondary(with_cpu=True):
         "forward_ms": t_f * 1e3, "backward_ms": t_b * 1e3, "backward_over_forward": t_b / t_f,
         "newton_iterations_forward": int(it.sum()), "converged_fraction": float(np.mean(rs == 0))}
     tb.close()
-    # bordered block diagonal
+
+
+def _bbd(out, with_cpu, timed, ocfg):
+    """Bordered block diagonal DC solve."""
+    from oracle import pyoracle as po
+    from rustspice_gb300 import circuits as cz
+    from rustspice_gb300 import native as N
+    from rustspice_gb300 import workloads as wl
+    from rustspice_gb300.solver import BbdSolver, DeviceCircuit
     c, asg, nb = cz.bordered_meshes()
     dc = DeviceCircuit(c)
     ap, ai = dc.pattern()
@@ -279,7 +318,6 @@ def secondary(with_cpu=True):
             ts.append(time.perf_counter() - t0)
         e["oracle_ms_per_iteration_1core"] = (ts[1] - ts[0]) * 1e3 / 2
     out["bbd"] = e
-    return out
 
 
 def run_gpu(a):
@@ -533,7 +571,11 @@ def run_reference(a):
 
 if __name__ == "__main__":
     args = _args()
-    if args.impl == "reference":
+    if args.only:
+        print(json.dumps({"only": args.only,
+                          "secondary": secondary(with_cpu=not args.no_cpu_baseline,
+                                                 parts=(args.only,))}))
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
