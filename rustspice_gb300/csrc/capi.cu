@@ -70,6 +70,24 @@ int sm_count() {
 std::vector<i32> make_tasks(const gk::Plan& p, bool transpose) {
   std::vector<i32> t;
   t.reserve(2 * p.n);
+  const bool coupled = !p.offd_ptr.empty() && p.offd_ptr.back() > 0;
+  if (!coupled && p.nblocks > 1) {
+    // Independent blocks: their tasks interleave (row r of every block, then
+    // row r+1, ...; all forward tasks before the backward ones), so the warps
+    // that hold the handed-out tasks work on every block at once. Each task
+    // still comes after everything it waits for.
+    int longest = 0;
+    for (int b = 0; b < p.nblocks; ++b)
+      longest = std::max(longest, p.block_ptr[b + 1] - p.block_ptr[b]);
+    for (int r = 0; r < longest; ++r)
+      for (int b = 0; b < p.nblocks; ++b)
+        if (p.block_ptr[b] + r < p.block_ptr[b + 1]) t.push_back((p.block_ptr[b] + r) << 1);
+    for (int r = 0; r < longest; ++r)
+      for (int b = 0; b < p.nblocks; ++b)
+        if (p.block_ptr[b + 1] - 1 - r >= p.block_ptr[b])
+          t.push_back(((p.block_ptr[b + 1] - 1 - r) << 1) | 1);
+    return t;
+  }
   const bool fwd = transpose ? !p.offd_lower : p.offd_lower;
   for (int bb = 0; bb < p.nblocks; ++bb) {
     int b = fwd ? bb : p.nblocks - 1 - bb;
