@@ -37,29 +37,61 @@ __global__ void k_bbd_ysolve(DPlan P, const double* __restrict__ lu,
   if (lane == 0)  // R entries in CSC order (duplicates add in that order)
     for (int e = B.init_ptr[t]; e < B.init_ptr[t + 1]; ++e) Y[B.init_code[e]] += ax[B.init_raw[e]];
   __syncwarp();
-  for (int i = 0; i < sz; ++i) {  // L, unit diagonal
-    const int pos = b0 + i;
-    double v = Y[(long long)i * 32 + lane], w = 0.0;
-    const int e0 = P.lrow_ptr[pos], e1 = P.lrow_ptr[pos + 1];
-    int e = e0;
-    for (; e + 1 < e1; e += 2) {
-      v = fma(-lu[P.lrow_slot[e]], Y[(long long)(P.lrow_col[e] - b0) * 32 + lane], v);
-      w = fma(-lu[P.lrow_slot[e + 1]], Y[(long long)(P.lrow_col[e + 1] - b0) * 32 + lane], w);
+  // One row's dot product over its entries [e0, e1): the indices of eight
+  // entries load together, then their factor values and Y values, so a row
+  // costs two memory round trips per eight entries; the next row's range is
+  // read one row ahead.
+  auto row_dot = [&](const int* slot, const int* col, int e0, int e1, double v) {
+    double w = 0.0;
+    for (int e = e0; e < e1; e += 8) {
+      int sl[8], cl[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (e + u < e1) {
+          sl[u] = slot[e + u];
+          cl[u] = col[e + u];
+        }
+      double lv[8], yv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (e + u < e1) {
+          lv[u] = lu[sl[u]];
+          yv[u] = Y[(long long)(cl[u] - b0) * 32 + lane];
+        }
+#pragma unroll
+      for (int u = 0; u < 8; u += 2) {
+        if (e + u < e1) v = fma(-lv[u], yv[u], v);
+        if (e + u + 1 < e1) w = fma(-lv[u + 1], yv[u + 1], w);
+      }
     }
-    if (e < e1) v = fma(-lu[P.lrow_slot[e]], Y[(long long)(P.lrow_col[e] - b0) * 32 + lane], v);
-    Y[(long long)i * 32 + lane] = v + w;
+    return v + w;
+  };
+  {  // L, unit diagonal
+    int e0 = P.lrow_ptr[b0], e1 = P.lrow_ptr[b0 + 1];
+    for (int i = 0; i < sz; ++i) {
+      const int ce0 = e0, ce1 = e1;
+      if (i + 1 < sz) {
+        e0 = e1;
+        e1 = P.lrow_ptr[b0 + i + 2];
+      }
+      Y[(long long)i * 32 + lane] =
+          row_dot(P.lrow_slot, P.lrow_col, ce0, ce1, Y[(long long)i * 32 + lane]);
+    }
   }
-  for (int i = sz - 1; i >= 0; --i) {  // U
-    const int pos = b0 + i;
-    double v = Y[(long long)i * 32 + lane], w = 0.0;
-    const int e0 = P.urow_ptr[pos], e1 = P.urow_ptr[pos + 1];
-    int e = e0;
-    for (; e + 1 < e1; e += 2) {
-      v = fma(-lu[P.urow_slot[e]], Y[(long long)(P.urow_col[e] - b0) * 32 + lane], v);
-      w = fma(-lu[P.urow_slot[e + 1]], Y[(long long)(P.urow_col[e + 1] - b0) * 32 + lane], w);
+  {  // U
+    int e0 = P.urow_ptr[b0 + sz - 1], e1 = P.urow_ptr[b0 + sz];
+    double dg = lu[P.dslot[b0 + sz - 1]];
+    for (int i = sz - 1; i >= 0; --i) {
+      const int ce0 = e0, ce1 = e1;
+      const double cdg = dg;
+      if (i > 0) {
+        e1 = e0;
+        e0 = P.urow_ptr[b0 + i - 1];
+        dg = lu[P.dslot[b0 + i - 1]];
+      }
+      Y[(long long)i * 32 + lane] =
+          row_dot(P.urow_slot, P.urow_col, ce0, ce1, Y[(long long)i * 32 + lane]) / cdg;
     }
-    if (e < e1) v = fma(-lu[P.urow_slot[e]], Y[(long long)(P.urow_col[e] - b0) * 32 + lane], v);
-    Y[(long long)i * 32 + lane] = (v + w) / lu[P.dslot[pos]];
   }
 }
 
