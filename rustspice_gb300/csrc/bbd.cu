@@ -119,29 +119,76 @@ __global__ void k_bbd_schur(const double* __restrict__ ax, BbdArgs B,
 }
 
 // Panel factorisation of columns [k0, k0+nb) over rows k0..bs-1.
-__global__ void k_dlu_panel(double* S, int bs, int k0, int nb) {
-  for (int c = k0; c < k0 + nb; ++c) {
-    __syncthreads();
-    const double d = perturb_tiny(S[(long long)c * bs + c]);
-    __syncthreads();
-    if (threadIdx.x == 0) S[(long long)c * bs + c] = d;
-    for (int r = c + 1 + threadIdx.x; r < bs; r += blockDim.x) {
-      const double l = S[(long long)c * bs + r] / d;
-      S[(long long)c * bs + r] = l;
-      for (int c2 = c + 1; c2 < k0 + nb; ++c2)
-        S[(long long)c2 * bs + r] = fma(-l, S[(long long)c2 * bs + c], S[(long long)c2 * bs + r]);
+// Panel factorization of columns [k0, k0+nb) in two launches: k_dlu_diag
+// factors the nb x nb diagonal block in place (shared memory, one lane per
+// row, columns in order); k_dlu_panel then eliminates every row below it
+// against that block's U, one thread per row, column by column. Every element
+// sees the operations of a column-by-column panel in the same order, so the
+// factor is the same bit for bit.
+__global__ void k_dlu_diag(double* S, int bs, int k0, int nb) {
+  __shared__ double D[32][33];  // D[r][c] = S(k0 + r, k0 + c)
+  const int r = threadIdx.x;
+  for (int c = 0; c < nb; ++c)
+    if (r < nb) D[r][c] = S[(long long)(k0 + c) * bs + k0 + r];
+  __syncwarp();
+  for (int c = 0; c < nb; ++c) {
+    const double d = perturb_tiny(D[c][c]);
+    __syncwarp();
+    if (r == c) D[c][c] = d;
+    if (r > c && r < nb) {
+      const double l = D[r][c] / d;
+      D[r][c] = l;
+      for (int c2 = c + 1; c2 < nb; ++c2) D[r][c2] = fma(-l, D[c][c2], D[r][c2]);
     }
+    __syncwarp();
   }
+  for (int c = 0; c < nb; ++c)
+    if (r < nb) S[(long long)(k0 + c) * bs + k0 + r] = D[r][c];
 }
 
-// U12 = L11^-1 A12 for the rows of the panel, one thread per column.
+__global__ void __launch_bounds__(256) k_dlu_panel(double* S, int bs, int k0, int nb) {
+  __shared__ double D[32][33];  // the factored diagonal block
+  for (int q = threadIdx.x; q < nb * nb; q += blockDim.x) {
+    const int c = q / nb, r = q % nb;
+    D[r][c] = S[(long long)(k0 + c) * bs + k0 + r];
+  }
+  __syncthreads();
+  const int r = k0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= bs) return;
+  double a[32];
+#pragma unroll
+  for (int c = 0; c < 32; ++c)
+    if (c < nb) a[c] = S[(long long)(k0 + c) * bs + r];
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    if (c < nb) {
+      const double l = a[c] / D[c][c];
+      a[c] = l;
+#pragma unroll
+      for (int c2 = c + 1; c2 < 32; ++c2)
+        if (c2 < nb) a[c2] = fma(-l, D[c][c2], a[c2]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 32; ++c)
+    if (c < nb) S[(long long)(k0 + c) * bs + r] = a[c];
+}
+
+// U12 = L11^-1 A12 for the rows of the panel, one thread per column, L11 in
+// shared memory.
 __global__ void k_dlu_trsm(double* S, int bs, int k0, int nb) {
+  __shared__ double L[32][33];  // L[i][m] = S(k0 + i, k0 + m)
+  for (int q = threadIdx.x; q < nb * nb; q += blockDim.x) {
+    const int m = q / nb, i = q % nb;
+    L[i][m] = S[(long long)(k0 + m) * bs + k0 + i];
+  }
+  __syncthreads();
   const int j = k0 + nb + blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= bs) return;
   double* const col = S + (long long)j * bs;
   for (int i = 1; i < nb; ++i) {
     double v = col[k0 + i];
-    for (int m = 0; m < i; ++m) v = fma(-S[(long long)(k0 + m) * bs + k0 + i], col[k0 + m], v);
+    for (int m = 0; m < i; ++m) v = fma(-L[i][m], col[k0 + m], v);
     col[k0 + i] = v;
   }
 }
@@ -253,9 +300,10 @@ void launch_dense_lu(double* S, int bs, cudaStream_t s) {
   const int nb = 32;
   for (int k0 = 0; k0 < bs; k0 += nb) {
     const int w = bs - k0 < nb ? bs - k0 : nb;
-    k_dlu_panel<<<1, 512, 0, s>>>(S, bs, k0, w);
     const int rest = bs - k0 - w;
+    k_dlu_diag<<<1, 32, 0, s>>>(S, bs, k0, w);
     if (rest <= 0) break;
+    k_dlu_panel<<<cdiv(rest, 256), 256, 0, s>>>(S, bs, k0, w);
     k_dlu_trsm<<<cdiv(rest, 128), 128, 0, s>>>(S, bs, k0, w);
     dim3 g(cdiv(rest, 64), cdiv(rest, 64));
     k_dlu_update<<<g, 256, 0, s>>>(S, bs, k0, w);
