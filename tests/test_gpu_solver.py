@@ -180,3 +180,43 @@ def test_batch_matches_oracle():
         xg = x[bt.x_off[i]:bt.x_off[i] + n]
         xo = x_o[i, :n]
         assert np.max(np.abs(xg - xo)) <= 1e-10 * max(1.0, np.max(np.abs(xo))), i
+
+
+@pytest.mark.parametrize("lanes", ["1", "0"], ids=["two_phase", "warp_only"])
+def test_batch_results_pinned_and_phase_times(lanes, monkeypatch):
+    """The results land in a caller's pinned buffer exactly as in a new array,
+    both batch schedules (the lane kernel with the warp kernel behind it, and
+    the warp kernels alone) give the same operating points within 1e-10, and
+    the per-kernel device times of a run are reported."""
+    import torch
+    monkeypatch.setenv("GPUKLU_BATCH_LANES", lanes)
+    B = wl.inverter_batch(6, 21, seed=5)
+    bt = Batch(B.circuits, B.inst_circ, B.inst_dev, B.inst_val, B.x0, B.x0_off)
+    cfg = N.newton_config(**wl.TIGHT)
+    bt.run(cfg)
+    it, itt, rs, x = bt.results()
+    pinned = torch.empty(bt.x_len, dtype=torch.float64).pin_memory()
+    it2, itt2, rs2, x2 = bt.results(x_out=pinned.numpy())
+    assert np.array_equal(x, x2) and np.array_equal(itt, itt2) and np.array_equal(rs, rs2)
+    ph = bt.phase_ms()
+    assert ph["warps_ms"] >= 0.0 and ph["lanes_ms"] >= 0.0
+    if lanes == "1":
+        assert ph["lane_cap"] > 0 and ph["lanes_ms"] > 0.0
+    else:
+        assert ph["lane_cap"] == 0
+    # the other schedule on the same batch
+    monkeypatch.setenv("GPUKLU_BATCH_LANES", "0" if lanes == "1" else "1")
+    bt2 = Batch(B.circuits, B.inst_circ, B.inst_dev, B.inst_val, B.x0, B.x0_off)
+    bt2.run(cfg)
+    _, itt3, rs3, x3 = bt2.results()
+    # the two schedules round differently (one instance per lane or per warp):
+    # iteration counts may differ where a step lands on the tolerance
+    assert np.mean(rs == rs3) >= 0.98
+    conv = (rs == 0) & (rs3 == 0)
+    assert np.mean(itt[conv] == itt3[conv]) >= 0.98
+    for i in np.flatnonzero(conv):
+        n = B.circuits[B.inst_circ[i]].n
+        a, b = x[bt.x_off[i]:bt.x_off[i] + n], x3[bt.x_off[i]:bt.x_off[i] + n]
+        assert np.max(np.abs(a - b)) <= 1e-10 * max(1.0, np.max(np.abs(a)))
+    with pytest.raises(TypeError):
+        bt.results(x_out=np.zeros(3))
