@@ -220,9 +220,9 @@ def secondary(with_cpu=True, parts=SECONDARY):
     if "mesh_dc" in parts:
         _mesh_dc(out, with_cpu, timed, ocfg)
     if "dc_adjoint" in parts:
-        _dc_adjoint(out, timed)
+        _dc_adjoint(out, timed, with_cpu, ocfg)
     if "transient_adjoint" in parts:
-        _transient_adjoint(out, timed)
+        _transient_adjoint(out, timed, with_cpu)
     if "bbd" in parts:
         _bbd(out, with_cpu, timed, ocfg)
     return out
@@ -250,8 +250,9 @@ def _mesh_dc(out, with_cpu, timed, ocfg):
     out["mesh_dc"] = e
 
 
-def _dc_adjoint(out, timed):
-    """DC adjoint of the 20k-node mesh with inverters."""
+def _dc_adjoint(out, timed, with_cpu, ocfg):
+    """DC adjoint of the 20k-node mesh with inverters; the oracle's forward
+    (the reference's Newton loop with NativeKLU) on one host core beside it."""
     from rustspice_gb300 import circuits as cz
     from rustspice_gb300 import native as N
     from rustspice_gb300 import workloads as wl
@@ -270,10 +271,17 @@ def _dc_adjoint(out, timed):
     out["dc_adjoint"] = {"workload": "120x120 mesh + 1000 inverters, loss on 256 nodes",
                          "n": dc.n, "forward_ms": t_f * 1e3, "newton_iterations": f.iterations,
                          "backward_ms": t_b * 1e3, "backward_over_forward": t_b / t_f}
+    if with_cpu:
+        from oracle import pyoracle as po
+        t0 = time.perf_counter()
+        po.dc_op(c, "nativeklu_exact", **ocfg)
+        out["dc_adjoint"]["oracle_forward_ms_1core"] = (time.perf_counter() - t0) * 1e3
 
 
-def _transient_adjoint(out, timed):
-    """Transient adjoint of 1024 rings."""
+def _transient_adjoint(out, timed, with_cpu):
+    """Transient adjoint of 1024 rings; beside it the oracle's backward-Euler
+    forward run (the reference's transient Newton loop with NativeKLU) on one
+    host core, timed on 16 rings and scaled to the 1024."""
     from rustspice_gb300 import native as N
     from rustspice_gb300 import workloads as wl
     from rustspice_gb300.solver import TranBatch
@@ -289,6 +297,17 @@ def _transient_adjoint(out, timed):
         "forward_ms": t_f * 1e3, "backward_ms": t_b * 1e3, "backward_over_forward": t_b / t_f,
         "newton_iterations_forward": int(it.sum()), "converged_fraction": float(np.mean(rs == 0))}
     tb.close()
+    if with_cpu:
+        from oracle import pyoracle as po
+        sample = np.random.default_rng(2).choice(len(B.circuits), 16, replace=False)
+        t0 = time.perf_counter()
+        for i in sample:
+            c = B.circuits[i]
+            po.tran(c, B.x_init[B.x_off[i]:B.x_off[i] + c.node_count], wl.RING_DT,
+                    wl.RING_STEPS)
+        per = (time.perf_counter() - t0) / len(sample)
+        out["transient_adjoint"]["oracle_forward_ms_1core_est"] = per * len(B.circuits) * 1e3
+        out["transient_adjoint"]["oracle_sample"] = "16 rings (seed 2), scaled to 1024"
 
 
 def _bbd(out, with_cpu, timed, ocfg):
