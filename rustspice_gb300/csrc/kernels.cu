@@ -3,32 +3,40 @@
 //  * first_factor  - the reference's first numeric factorization with its
 //                    threshold pivot rule (crates/sim-core/src/native_klu.rs:
 //                    1194-1382), one warp walking the columns in order; it
-//                    discovers the pivot sequence.
+//                    discovers the pivot sequence. k_first_factor_s keeps the
+//                    working column and each column's update operands in
+//                    shared memory; k_first_factor is the fallback for blocks
+//                    too large for that.
 //  * refactor      - left-looking refactorization with frozen pivots. Warps
 //                    take columns in increasing order from an atomic counter
 //                    and wait on per-column completion flags of exactly the
 //                    columns they depend on (the U pattern), so independent
-//                    columns run concurrently without level barriers.
+//                    columns run concurrently without level barriers; a
+//                    warp's column sits in shared memory while it is updated.
+//                    k_refactor_cta is the same in one block, for small plans.
 //  * solve         - the forward (L) and backward (U) substitutions and the
-//                    BTF block coupling, one warp per row task, also driven by
-//                    per-row flags; the transpose variant solves A^T y = g.
+//                    BTF block coupling. k_solve_cta sweeps the columns in one
+//                    block (solution vector in shared memory); k_solve runs
+//                    one warp per row task driven by per-row flags (large
+//                    plans); k_tsolve solves A^T y = g for the adjoint.
 //  * stamp         - one thread per device instance writes its conductances
 //                    into the raw CSC slots given by the stamp-to-slot map and
 //                    its currents into per-contribution slots; a second pass
 //                    sums the right-hand side row by row in stamping order.
 //  * newton_update - convergence test, damping and the iterate update of
 //                    crates/sim-core/src/newton.rs:93-107, 187-201.
-//  * batch_newton  - thousands of independent circuits: each lane of a warp
-//                    owns one circuit instance and runs stamp, refactor, solve
-//                    and update for its whole Newton loop; the 32 lanes of a
-//                    warp share one circuit program, so every load of the
-//                    program is a broadcast and every value access is one
-//                    coalesced 256-byte transaction.
+//  * batch_newton  - batched Newton over many circuit instances, one warp per
+//                    instance (or 2, 4 per warp for small programs) with the
+//                    instance's whole state in shared memory; behind the lane
+//                    kernel (lanes.cu) it finishes the instances still
+//                    iterating.
 //
-// All floating-point work is FP64 and compiled without multiply-add
-// contraction, so every product is rounded before it is added exactly as in
-// the reference; the factor and solve results are bit-identical to a scalar
-// CPU evaluation in the reference's order.
+// All floating-point work of the single-circuit kernels is FP64 and compiled
+// without multiply-add contraction, so every product is rounded before it is
+// added exactly as in the reference; their factor and solve results are
+// bit-identical to a scalar CPU evaluation in the reference's order. The
+// batched kernels use fused multiply-adds and agree with the oracle within
+// the Newton tolerance.
 #include <algorithm>
 #include <cstdio>
 
