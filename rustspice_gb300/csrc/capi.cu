@@ -2750,6 +2750,7 @@ int64_t gpuklu_plan_array(const gpuklu_plan* P, const char* name, int64_t* out, 
     make_cta_solve(p, hc, ho);
     return put(k == "cs_chunk" ? hc : ho);
   }
+  if (k == "task" || k == "ttask") return put(make_tasks(p, k == "ttask"));  // grid solve order
 #define ARR(nm) \
   if (k == #nm) return put(p.nm);
   ARR(col_ptr) ARR(dslot) ARR(slot_row) ARR(upd_ptr) ARR(upd_dst) ARR(amap_ptr) ARR(amap_idx)

@@ -134,3 +134,56 @@ def test_one_block_schedule_mesh():
     st, xo = s.solve(rhs)
     assert st == 0
     assert np.array_equal(solve_one_block(es.plan, es.ax, es.lu, rhs), xo)
+
+
+def _block_diagonal(nblocks, seed):
+    """Independent meshes side by side: a factor with no block coupling."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    mats = []
+    for _ in range(nblocks):
+        m = int(rng.integers(3, 9))
+        g = sp.random(m * m, m * m, density=0.05, random_state=int(rng.integers(1 << 30)))
+        a = (g + g.T + sp.eye(m * m) * (m * m)).tocsc()
+        mats.append(a)
+    a = sp.block_diag(mats).tocsc()
+    a.sort_indices()
+    return a.shape[0], a.indptr.astype(np.int64), a.indices.astype(np.int64), a.data
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_grid_solve_task_order(seed):
+    """Every task of the grid solve comes after the tasks it waits for (the
+    dependency-flag kernels rely on it to finish), also when the tasks of
+    independent blocks interleave."""
+    n, ap, ai, ax = _block_diagonal(6, seed)
+    for mode in (N.PIVOT_REFERENCE, N.PIVOT_EXACT):
+        P = N.Plan(n, ap, ai, mode)
+        assert P.nblocks > 1
+        for name in ("task", "ttask"):
+            t = getattr(P, name)
+            assert len(t) == 2 * n and sorted(t) == list(range(2 * n))
+            pos = np.empty(2 * n, np.int64)
+            pos[t] = np.arange(2 * n)
+            fwd, bwd = pos[0::2], pos[1::2]  # by plan position
+            assert np.all(bwd > fwd)
+            lower = name == "task"
+            for i in range(n):
+                if lower:  # L row i needs z of its columns; U row i needs x of its columns
+                    deps_f = P.lrow_col[P.lrow_ptr[i]:P.lrow_ptr[i + 1]]
+                    deps_b = P.urow_col[P.urow_ptr[i]:P.urow_ptr[i + 1]]
+                else:  # transpose: U column i, then L column i
+                    s0, ds, s1 = P.col_ptr[i], P.dslot[i], P.col_ptr[i + 1]
+                    deps_f = P.slot_row[s0:ds]
+                    deps_b = P.slot_row[ds + 1:s1]
+                assert np.all(fwd[deps_f] < fwd[i])
+                assert np.all(bwd[deps_b] < bwd[i])
+        # and the interleaved order still solves bit for bit like the oracle
+        es = EmulatedSolver(mode)
+        es.factor(n, ap, ai, ax)
+        rhs = np.random.default_rng(seed).standard_normal(n)
+        s = po.Solver("nativeklu" if mode == N.PIVOT_REFERENCE else "nativeklu_exact", n)
+        s.prepare(n)
+        assert s.analyze(ap, ai) == 0 and s.factor(ap, ai, ax) == 0
+        st, xo = s.solve(rhs)
+        assert st == 0 and np.array_equal(es.solve(rhs), xo)
