@@ -1,0 +1,296 @@
+"""SPICE netlists of the R/V/I/D/M/C subset into the device-list Circuit.
+
+A deck becomes the flat device list the stamp compiler takes (``Circuit`` in
+circuits.py), with the reference's reading of every field, so a user deck
+runs on ``DeviceCircuit`` / ``newton_dc`` / ``Batch`` as the reference engine
+would run it:
+
+* lines (crates/sim-core/src/netlist.rs:150-190): surrounding blanks are
+  trimmed; ``*`` starts a comment; ``+`` continues the previous statement
+  (joined with one space); a first token beginning with ``.`` is a control,
+  any other a device named by its first letter;
+* tokens (netlist.rs:322-370): ``key=value`` tokens are parameters (a token
+  holding both ``=`` and ``,`` splits at top-level commas; a leading ``(`` and
+  a trailing ``)`` around a parameter are dropped), the rest positional;
+* device fields (netlist.rs:400-460): R, C, V, I take two nodes and a
+  value, the token after a ``DC`` keyword when there is one; D takes two
+  nodes and a model; M four nodes and a model, or three and a model with the
+  bulk on ground;
+* numbers (netlist.rs:1635-1660): one trailing ``f p n u m k g t`` scales by
+  1e-15 ... 1e12 and ``meg`` by 1e6, case-insensitive;
+* nodes (circuit.rs:31-57, netlist.rs:934-1100): ``0`` is ground (id 0),
+  other names take ids in order of first use, ``.ic`` nodes before device
+  nodes (controls are read first), names compared as written;
+* models and parameters (netlist.rs:940-960, 1120-1135): ``.model name type
+  params``, names and keys lower-cased; a device's parameters are its
+  model's, overridden by its own;
+* diode (crates/sim-core/src/stamp.rs:351-387): Is from ``is`` (1e-14), N
+  from ``n`` or ``nj`` (1.0);
+* MOSFET (stamp.rs:389-420, crates/sim-devices/src/bsim/mod.rs:83-200,
+  params.rs:303-462): the level from ``level`` (49 when absent); PMOS only if
+  parameter ``type`` contains ``pmos`` or equals ``p``, or a ``pmos`` key
+  exists -- the model card's own type word does not count; vth0 from
+  ``vth0``/``vto``/``vth`` (0.7, PMOS -0.7), u0 from ``u0``/``uo`` (500, PMOS
+  150), tox from ``tox`` (1.5e-8), W and L from ``w``/``l`` (1e-6).
+  Only level 1 is on this path; other levels raise ``NetlistError``;
+* ``.option`` keys (crates/sim-core/src/engine.rs:987-999): ``itl1`` max
+  iterations (100), ``vntol`` absolute (1e-6), ``reltol`` relative (1e-3),
+  ``gmin`` (1e-12).
+
+Subcircuits, includes, parameters expressions and the other device kinds are
+outside this path and raise ``NetlistError``.
+"""
+from __future__ import annotations
+
+import dataclasses
+import re
+
+import numpy as np
+
+from .circuits import (DEV_C, DEV_D, DEV_I, DEV_M, DEV_R, DEV_V, NPARAM, TOX, Circuit)
+
+
+class NetlistError(ValueError):
+    """A deck outside the subset this path runs (or a malformed line)."""
+
+
+_SCALE = {"f": 1e-15, "p": 1e-12, "n": 1e-9, "u": 1e-6, "m": 1e-3, "k": 1e3, "g": 1e9,
+          "t": 1e12}
+_FLOAT = re.compile(r"^[+-]?(\d+\.?\d*([eE][+-]?\d+)?|\.\d+([eE][+-]?\d+)?|inf|infinity|nan)$",
+                    re.I)
+
+
+def parse_number(token: str):
+    """A number with an optional SI suffix, or None."""
+    t = token.strip().lower()
+    mult = 1.0
+    if t.endswith("meg"):
+        t, mult = t[:-3], 1e6
+    elif t and t[-1] in _SCALE:
+        t, mult = t[:-1], _SCALE[t[-1]]
+    if not _FLOAT.match(t):
+        return None
+    return float(t) * mult
+
+
+def _split_top_commas(s: str):
+    out, depth, start = [], 0, 0
+    for i, ch in enumerate(s):
+        if ch == "(":
+            depth += 1
+        elif ch == ")":
+            depth = max(0, depth - 1)
+        elif ch == "," and depth == 0:
+            out.append(s[start:i])
+            start = i + 1
+    if start < len(s):
+        out.append(s[start:])
+    return out
+
+
+def _args_params(tokens):
+    args, params = [], []
+    for tok in tokens:
+        parts = _split_top_commas(tok) if ("=" in tok and "," in tok) else [tok]
+        for raw in parts:
+            part = raw.strip()
+            if not part:
+                continue
+            if part.startswith("(") and "=" in part:
+                part = part[1:]
+            if part.endswith(")") and "=" in part and "(" not in part[part.index("=") + 1:]:
+                part = part[:-1]
+            if not part:
+                continue
+            if "=" in part:
+                k, v = part.split("=", 1)
+                params.append((k, v))
+            else:
+                args.append(part)
+    return args, params
+
+
+@dataclasses.dataclass
+class Statement:
+    line: int
+    control: str = ""          # ".model", ".op", ... (lower-case) for a control
+    name: str = ""             # device name for a device line
+    kind: str = ""             # device letter, upper-case
+    args: list = dataclasses.field(default_factory=list)
+    params: list = dataclasses.field(default_factory=list)
+
+
+def parse(text: str):
+    """Statements of a deck and the errors the reader recorded (line, text)."""
+    stmts, errors, pending, pending_line = [], [], "", 0
+
+    def flush(line_text, line_no):
+        toks = line_text.split()
+        if not toks:
+            return
+        first = toks[0]
+        args, params = _args_params(toks[1:])
+        if first.startswith("."):
+            stmts.append(Statement(line_no, control=first.lower(), args=args, params=params))
+            return
+        kind = first[0].upper()
+        if kind not in "RCLVIDMEGFHX":
+            errors.append((line_no, f"unknown device type: {first}"))
+            return
+        stmts.append(Statement(line_no, name=first, kind=kind, args=args, params=params))
+
+    lines = text.splitlines()
+    for no, raw in enumerate(lines, 1):
+        s = raw.strip()
+        if not s or s.startswith("*"):
+            continue
+        if s.startswith("+"):
+            if not pending:
+                errors.append((no, "continuation line has no preceding line"))
+                continue
+            pending += " " + s.lstrip("+").strip()
+            continue
+        if pending:
+            flush(pending, pending_line)
+        pending, pending_line = s, no
+    if pending:
+        flush(pending, pending_line)
+    return stmts, errors
+
+
+@dataclasses.dataclass
+class Deck:
+    circuit: Circuit
+    node_names: list           # node id -> name
+    device_names: list         # device index -> instance name
+    options: dict              # lower-case option -> value string
+    initial: dict              # node id -> .ic voltage
+    analyses: list             # control commands seen (".op", ".dc", ...)
+
+    def newton_options(self) -> dict:
+        """The Newton settings the reference derives from the options."""
+        def num(key, default):
+            v = self.options.get(key)
+            x = parse_number(v) if v is not None else None
+            return default if x is None else x
+        return {"max_iters": int(num("itl1", 100)), "abs_tol": num("vntol", 1e-6),
+                "rel_tol": num("reltol", 1e-3), "gmin": num("gmin", 1e-12)}
+
+    def transient_x0(self) -> np.ndarray:
+        """A transient's starting point: zeros with the .ic voltages
+        (crates/sim-core/src/engine.rs:340-348; the DC operating point starts
+        from zeros)."""
+        x = np.zeros(self.circuit.node_count)
+        for k, v in self.initial.items():
+            x[k] = v
+        return x
+
+
+def _pnum(params: dict, keys, default):
+    for k in keys:
+        if k in params:
+            x = parse_number(params[k])
+            if x is not None:
+                return x
+    return default
+
+
+def compile_deck(text: str, name: str = "") -> Deck:
+    """A deck of R, V, I, D, level-1 M and C into a Circuit."""
+    stmts, errors = parse(text)
+    if errors:
+        raise NetlistError("; ".join(f"line {n}: {m}" for n, m in errors))
+    names = {"0": 0}
+    order = ["0"]
+
+    def node(s):
+        if s not in names:
+            names[s] = len(order)
+            order.append(s)
+        return names[s]
+
+    models, options, initial, analyses = {}, {}, {}, []
+    for st in stmts:  # controls first (as the reference builds the circuit)
+        if not st.control:
+            continue
+        if st.control == ".model":
+            if len(st.args) < 2:
+                raise NetlistError(f"line {st.line}: model statement missing name/type")
+            models[st.args[0].lower()] = {k.lower(): v for k, v in st.params}
+        elif st.control == ".option" or st.control == ".options":
+            for k, v in st.params:
+                options[k.lower()] = v
+            for a in st.args:
+                options[a.lower()] = "true"
+        elif st.control == ".ic":
+            for k, v in st.params:
+                key = k.strip().lower()
+                x = parse_number(v)
+                if key.startswith("v(") and key.endswith(")") and x is not None:
+                    initial[node(key[2:-1].strip())] = x
+        elif st.control in (".subckt", ".include", ".inc", ".lib", ".param"):
+            raise NetlistError(f"line {st.line}: {st.control} is outside this path")
+        elif st.control in (".op", ".dc", ".tran", ".ac"):
+            analyses.append(st.control)
+    t, nd, p, dev_names = [], [], [], []
+    for st in stmts:
+        if st.control:
+            continue
+        prm = {}
+        a = st.args
+        if st.kind in "RCVI":
+            if len(a) < 3:
+                raise NetlistError(f"line {st.line}: {st.name} needs two nodes and a value")
+            val = a[3] if (a[2].lower() == "dc" and len(a) >= 4) else a[2]
+            v = parse_number(val)
+            if v is None:
+                raise NetlistError(f"line {st.line}: {st.name} has no numeric value")
+            kind = {"R": DEV_R, "C": DEV_C, "V": DEV_V, "I": DEV_I}[st.kind]
+            nodes, params = (node(a[0]), node(a[1])), (v,)
+        elif st.kind in "DM":
+            if st.kind == "D":
+                if len(a) < 3:
+                    raise NetlistError(f"line {st.line}: {st.name} needs two nodes and a model")
+                terms, model = a[:2], a[2]
+            elif len(a) >= 5:
+                terms, model = a[:4], a[4]
+            elif len(a) == 4:  # drain gate source model: the bulk is ground
+                terms, model = a[:3] + ["0"], a[3]
+            else:
+                raise NetlistError(f"line {st.line}: {st.name} needs its nodes and a model")
+            nodes = tuple(node(x) for x in terms)
+            prm.update(models.get(model.lower(), {}))
+            prm.update({k.lower(): v for k, v in st.params})
+            if st.kind == "D":
+                kind = DEV_D
+                params = (_pnum(prm, ["is"], 1e-14), _pnum(prm, ["n", "nj"], 1.0))
+            else:
+                level = int(_pnum(prm, ["level"], 49.0))
+                if level != 1:
+                    raise NetlistError(f"line {st.line}: {st.name} is a level-{level} MOSFET;"
+                                       " this path evaluates level 1")
+                if "type" in prm:
+                    tl = prm["type"].lower()
+                    pmos = "pmos" in tl or tl == "p"
+                else:
+                    pmos = "pmos" in prm
+                kind = DEV_M
+                params = (1.0 if pmos else 0.0,
+                          _pnum(prm, ["vth0", "vto", "vth"], -0.7 if pmos else 0.7),
+                          _pnum(prm, ["u0", "uo"], 150.0 if pmos else 500.0),
+                          _pnum(prm, ["tox"], TOX),
+                          _pnum(prm, ["w"], 1e-6), _pnum(prm, ["l"], 1e-6))
+        else:
+            raise NetlistError(f"line {st.line}: device {st.name} ({st.kind}) is outside this path")
+        t.append(kind)
+        nd.append(tuple(nodes) + (0,) * (4 - len(nodes)))
+        p.append(tuple(params) + (0.0,) * (NPARAM - len(params)))
+        dev_names.append(st.name)
+    c = Circuit(len(order), np.asarray(t, np.int32), np.asarray(nd, np.int32).reshape(-1, 4),
+                np.asarray(p, np.float64).reshape(-1, NPARAM), name)
+    return Deck(c, order, dev_names, options, initial, analyses or [".op"])
+
+
+def load(path: str) -> Deck:
+    with open(path) as f:
+        return compile_deck(f.read(), name=path)

@@ -220,3 +220,33 @@ def test_batch_results_pinned_and_phase_times(lanes, monkeypatch):
         assert np.max(np.abs(a - b)) <= 1e-10 * max(1.0, np.max(np.abs(a)))
     with pytest.raises(TypeError):
         bt.results(x_out=np.zeros(3))
+
+
+def test_netlist_deck_on_the_device():
+    """A deck read by the netlist compiler runs on the device Newton path with
+    the oracle's iterations and solution (the deck's own .option settings)."""
+    from rustspice_gb300 import netlist as nl
+    deck = nl.compile_deck("""* two resistor-loaded NMOS stages beside a diode ladder
+VDD vdd 0 DC 1.8
+VIN in 0 DC 0.9
+RL1 vdd mid 20k
+MN1 mid in 0 0 nch W=2u L=1u
+RL2 vdd out 20k
+MN2 out mid 0 0 nch W=2u L=1u
+V1 a 0 DC 1.0
+R1 a b 1k
+D1 b 0 dx
+R2 b c 2k
+D2 c 0 dx
+.model nch nmos level=1 vto=0.45 u0=400
+.model dx d is=1e-14
+.option reltol=1e-10 vntol=1e-12 itl1=200
+.op
+.end
+""")
+    opts = deck.newton_options()
+    r_o, it_o, x_o = po.dc_op(deck.circuit, "nativeklu_exact", **opts)
+    g = GpuKluSolver(1, pivot_mode=N.PIVOT_EXACT)
+    res = newton_dc(g, DeviceCircuit(deck.circuit), N.newton_config(**opts))
+    assert r_o == "converged" and res.converged and res.iterations == it_o
+    assert np.max(np.abs(res.x - x_o)) <= 1e-10 * max(1.0, np.max(np.abs(x_o)))
