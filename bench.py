@@ -195,7 +195,7 @@ def _ncu_traffic(kernel, iters):
     return per * iters, f"{os.path.relpath(PROFILE, ROOT)} ({per:.1f} B per iteration)"
 
 
-SECONDARY = ("mesh_dc", "dc_adjoint", "transient_adjoint", "bbd")
+SECONDARY = ("mesh_dc", "dc_adjoint", "transient_adjoint", "bbd", "ac_sweep")
 
 
 def secondary(with_cpu=True, parts=SECONDARY):
@@ -225,7 +225,38 @@ def secondary(with_cpu=True, parts=SECONDARY):
         _transient_adjoint(out, timed, with_cpu)
     if "bbd" in parts:
         _bbd(out, with_cpu, timed, ocfg)
+    if "ac_sweep" in parts:
+        _ac(out, with_cpu, timed)
     return out
+
+
+def _ac(out, with_cpu, timed):
+    """AC sweep of a 100-section RC ladder (n = 103), 500 points per decade
+    from 1 Hz to 1 GHz; the oracle's dense complex LU timed on 64 of the
+    points on one host core and scaled."""
+    from oracle import pyoracle as po
+    from rustspice_gb300 import netlist as nl
+    from rustspice_gb300.solver import DeviceCircuit, GpuKluSolver, ac_sweep, frequency_sweep
+    rng = np.random.default_rng(3)
+    lines = ["V1 n0 0 DC 0 AC 1 30"]
+    for k in range(100):
+        lines.append(f"R{k} n{k} n{k + 1} {rng.uniform(100, 1000):.6g}")
+        lines.append(f"C{k} n{k + 1} 0 {rng.uniform(1e-12, 1e-9):.6g}")
+    c = nl.compile_deck("\n".join(lines) + "\n").circuit
+    f = frequency_sweep("dec", 500, 1.0, 1e9)
+    g = GpuKluSolver(1)
+    dc = DeviceCircuit(c)
+    x0 = np.zeros(c.n)
+    ac_sweep(g, dc, x0, f)
+    _, t = timed(lambda: ac_sweep(g, dc, x0, f))
+    e = {"workload": "100-section RC ladder, 4501 frequencies (dec 500, 1 Hz - 1 GHz)",
+         "n": c.n, "frequencies": len(f), "gpu_ms": t * 1e3}
+    if with_cpu:
+        sample = f[::max(1, len(f) // 64)][:64]
+        t0 = time.perf_counter()
+        po.ac_sweep(c, x0, sample)
+        e["oracle_ms_1core_est"] = (time.perf_counter() - t0) / len(sample) * len(f) * 1e3
+    out["ac_sweep"] = e
 
 
 def _mesh_dc(out, with_cpu, timed, ocfg):

@@ -181,6 +181,20 @@ int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_co
                      const double* x0, double* x_out, int64_t x_cap, int64_t* x_len,
                      int64_t* iters, int64_t* iters_total, int* reason);
 
+/* AC small-signal sweep at a DC solution: the reference's .ac
+ * (crates/sim-core/src/engine.rs:829-930) with its AC stamps (stamp.rs:
+ * 1525-1747) and dense complex LU with partial pivoting (complex_solver.rs:
+ * 28-144), every frequency point solved at once on the device. V and I
+ * sources carry the AC magnitude in p[1] and the phase [deg] in p[2]. x_dc:
+ * the operating point (node voltages at least); freqs: nf frequencies [Hz];
+ * out_re / out_im: nf x n values (n = node_count + one aux per V source, row
+ * 0 the ground); *n_out = n. n above GPUKLU_AC_MAX_N gives
+ * GPUKLU_INVALID_MATRIX, a pivot below 1e-30 GPUKLU_SINGULAR. */
+#define GPUKLU_AC_MAX_N 112
+int gpuklu_ac_sweep(gpuklu_handle* h, gpuklu_circuit* c, const double* x_dc, int64_t xlen,
+                    const double* freqs, int64_t nf, double* out_re, double* out_im,
+                    int64_t* n_out);
+
 /* Adjoint of a DC operating point (no counterpart in the reference). At the
  * converged x (xlen values, node voltages first) it stamps and factors the
  * exact Jacobian A(x) on the device (the consistent level-1 model without its

@@ -230,6 +230,24 @@ int orc_tran(int64_t node_count, int64_t ndev, const int32_t* type, const int32_
   return r;
 }
 
+// AC sweep (ac_sweep): out_re/out_im hold nf x cap values; *n_out = n.
+int orc_ac_sweep(int64_t node_count, int64_t ndev, const int32_t* type, const int32_t* nodes,
+                 const double* p, const double* xdc, int64_t xlen, const double* freqs,
+                 int64_t nf, double* out_re, double* out_im, int64_t cap, int64_t* n_out) {
+  Circuit c = make_circuit(node_count, ndev, type, nodes, p);
+  std::vector<double> re, im;
+  size_t n = 0;
+  int r = ac_sweep(c, Vec(xdc, xdc + xlen), Vec(freqs, freqs + nf), re, im, n);
+  *n_out = (int64_t)n;
+  if (r != 0 || (int64_t)n > cap) return r != 0 ? r : 2;
+  for (int64_t f = 0; f < nf; ++f)
+    for (size_t i = 0; i < n; ++i) {
+      out_re[f * cap + (int64_t)i] = re[(size_t)f * n + i];
+      out_im[f * cap + (int64_t)i] = im[(size_t)f * n + i];
+    }
+  return 0;
+}
+
 // Discrete adjoint of orc_tran's loss (tran_adjoint); grad has ndev entries.
 int orc_tran_adjoint(int64_t node_count, int64_t ndev, const int32_t* type,
                      const int32_t* nodes, const double* p, double dt, int64_t steps,

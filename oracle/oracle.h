@@ -304,6 +304,14 @@ MosJ eval_level1_consistent(double vth0, double u0, double tox, double w,
                             double l, double vd, double vg, double vs,
                             bool is_pmos, double gdev = 1e-12);
 
+// AC small-signal sweep at a DC solution (crates/sim-core/src/engine.rs:
+// 829-930 with the AC stamps and the dense complex LU; ac.cpp). V and I
+// sources carry the AC magnitude in p[1] and the phase [deg] in p[2]. out_re
+// and out_im get freqs.size() x n values; returns 0, or 1 on a pivot below
+// 1e-30.
+int ac_sweep(const Circuit& c, const Vec& xdc, const Vec& freqs, std::vector<double>& out_re,
+             std::vector<double>& out_im, size_t& n_out);
+
 // ---------------------------------------------------------------- Newton
 // crates/sim-core/src/newton.rs:1-265
 struct NewtonConfig {

@@ -62,6 +62,8 @@ def lib():
         L.orc_tran.restype = C.c_int
         L.orc_tran.argtypes = [_I64, _I64, _P, _P, _P, C.c_char_p, _I64, _D, _D, _D, _D, _I64,
                                _P, _P, _P]
+        L.orc_ac_sweep.restype = C.c_int
+        L.orc_ac_sweep.argtypes = [_I64, _I64, _P, _P, _P, _P, _I64, _P, _I64, _P, _P, _I64, _P]
         L.orc_tran_adjoint.restype = C.c_int
         L.orc_tran_adjoint.argtypes = [_I64, _I64, _P, _P, _P, _D, _I64, _P, _I64, _D, _D, _P]
         L.orc_residual.restype = _D
@@ -222,6 +224,24 @@ def tran(c, x_init, dt, steps, solver="nativeklu_exact", max_iters=100, abs_tol=
                        max_iters, abs_tol, rel_tol, gmin, dt, steps, _ptr(xi), _ptr(st),
                        C.byref(it))
     return r, it.value, st.reshape(steps + 1, c.node_count)
+
+
+def ac_sweep(c, x_dc, freqs):
+    """AC solutions at a DC point: complex array [len(freqs), n] (n = nodes
+    plus one aux per V source). V and I carry the AC magnitude in p[:, 1]
+    and the phase in degrees in p[:, 2]."""
+    _, t, nd, p = _circ_arrays(c)
+    xd = _f64(x_dc)
+    fr = _f64(freqs)
+    cap = c.n
+    re = np.zeros(len(fr) * cap)
+    im = np.zeros(len(fr) * cap)
+    n = C.c_int64()
+    r = lib().orc_ac_sweep(c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p), _ptr(xd), len(xd),
+                           _ptr(fr), len(fr), _ptr(re), _ptr(im), cap, C.byref(n))
+    if r != 0:
+        raise RuntimeError("singular AC system" if r == 1 else "AC system larger than expected")
+    return (re + 1j * im).reshape(len(fr), cap)[:, :n.value]
 
 
 def tran_adjoint(c, states, dt, probe, target, gmin=1e-12):

@@ -872,6 +872,128 @@ int gpuklu_stamp(gpuklu_handle* h, gpuklu_circuit* c, const double* x, int64_t x
   return GPUKLU_OK;
 }
 
+int gpuklu_ac_sweep(gpuklu_handle* h, gpuklu_circuit* c, const double* x_dc, int64_t xlen,
+                    const double* freqs, int64_t nf, double* out_re, double* out_im,
+                    int64_t* n_out) {
+  if (!h || !c || !x_dc || !freqs || !out_re || !out_im || nf < 0) return GPUKLU_INVALID_MATRIX;
+  const int n = c->n, nc = c->node_count;
+  if (n_out) *n_out = n;
+  if (n > GPUKLU_AC_MAX_N)
+    return h->fail(GPUKLU_INVALID_MATRIX, "gpuklu_ac_sweep: n = " + std::to_string(n) +
+                                              " exceeds GPUKLU_AC_MAX_N = " +
+                                              std::to_string(GPUKLU_AC_MAX_N));
+  if (nf == 0) return GPUKLU_OK;
+  // Cells of Y(w): the DC stamp's raw entries off the ground row in CSC order
+  // (duplicates add in that order), then the capacitor terms in insertion
+  // order (stamp.rs:1545-1564); row 0 becomes the identity row.
+  std::vector<int> cell_of((size_t)n * n, -1), crow, ccol;
+  std::vector<std::vector<int>> re_l, im_l;
+  auto cell = [&](int r, int col) {
+    int& id = cell_of[(size_t)r * n + col];
+    if (id < 0) {
+      id = (int)crow.size();
+      crow.push_back(r);
+      ccol.push_back(col);
+      re_l.emplace_back();
+      im_l.emplace_back();
+    }
+    return id;
+  };
+  for (int col = 0; col < n; ++col)
+    for (i64 t = c->ap[col]; t < c->ap[col + 1]; ++t)
+      if (c->ai[t] != 0) re_l[cell((int)c->ai[t], col)].push_back((int)t);
+  std::vector<double> cap(std::max(c->ndev, 1), 0.0);
+  std::vector<double> rhs(2 * (size_t)n, 0.0);
+  int aux = nc;
+  for (int d = 0; d < c->ndev; ++d) {
+    const int a = c->nodes[4 * d], b = c->nodes[4 * d + 1];
+    const double* p = &c->p[6 * (size_t)d];
+    if (c->type[d] == 5) {  // capacitor
+      cap[d] = p[0];
+      const int rr[4] = {a, b, a, b}, cc[4] = {a, b, b, a}, ng[4] = {0, 0, 1, 1};
+      for (int q = 0; q < 4; ++q)
+        if (rr[q] != 0) im_l[cell(rr[q], cc[q])].push_back((d << 1) | ng[q]);
+    } else if (c->type[d] == 1 || c->type[d] == 2) {  // V (its aux row) or I: the AC phasor
+      const double t = p[2] * 3.141592653589793 / 180.0;
+      const double pre = p[1] * std::cos(t), pim = p[1] * std::sin(t);
+      auto add = [&](int i, double re, double im) {
+        if (i >= 0 && i < n) {
+          rhs[2 * i] = rhs[2 * i] + re;
+          rhs[2 * i + 1] = rhs[2 * i + 1] + im;
+        }
+      };
+      if (c->type[d] == 1) {
+        add(aux++, pre, pim);
+      } else {
+        add(a, -pre, -pim);
+        add(b, pre, pim);
+      }
+    }
+  }
+  const int ncell = (int)crow.size();
+  std::vector<i32> re_ptr(1, 0), re_idx, im_ptr(1, 0), im_code;
+  for (int q = 0; q < ncell; ++q) {
+    re_idx.insert(re_idx.end(), re_l[q].begin(), re_l[q].end());
+    re_ptr.push_back((i32)re_idx.size());
+    im_code.insert(im_code.end(), im_l[q].begin(), im_l[q].end());
+    im_ptr.push_back((i32)im_code.size());
+  }
+  cudaStream_t s = h->stream;
+  DBuf<i32> d_crow, d_ccol, d_re_ptr, d_re_idx, d_im_ptr, d_im_code, d_status;
+  DBuf<double> d_cap, d_rhs, d_freqs, d_re, d_im, dx, dax, drc, drhs;
+  cudaError_t e = cudaSuccess;
+#define UP(buf, vec) \
+  if (e == cudaSuccess) e = buf.upload(vec, s);
+  std::vector<i32> vrow(crow.begin(), crow.end()), vcol(ccol.begin(), ccol.end());
+  std::vector<double> vfreq(freqs, freqs + nf), vx(x_dc, x_dc + std::max<int64_t>(xlen, 0));
+  UP(d_crow, vrow) UP(d_ccol, vcol) UP(d_re_ptr, re_ptr) UP(d_re_idx, re_idx) UP(d_im_ptr, im_ptr)
+  UP(d_im_code, im_code) UP(d_cap, cap) UP(d_rhs, rhs) UP(d_freqs, vfreq)
+#undef UP
+  if (e == cudaSuccess) e = d_re.resize((size_t)nf * n);
+  if (e == cudaSuccess) e = d_im.resize((size_t)nf * n);
+  if (e == cudaSuccess) e = d_status.resize(1);
+  if (e == cudaSuccess) e = dx.resize(std::max<int64_t>(xlen, 1));
+  if (e == cudaSuccess) e = dax.resize(std::max<size_t>(c->ai.size(), 1));
+  if (e == cudaSuccess) e = drc.resize(std::max(c->ncontrib, 1));
+  if (e == cudaSuccess) e = drhs.resize(n);
+  if (e == cudaSuccess && xlen > 0)
+    e = cudaMemcpyAsync(dx.p, vx.data(), xlen * sizeof(double), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_status.p, 0, sizeof(int), s);
+  if (e != cudaSuccess) return h->cuda_fail(e, "ac upload");
+  // G: the DC stamp at the operating point (the AC stamps of R, V, D and M
+  // are the DC stamp's matrix entries there, stamp.rs:1525-1747)
+  gk::launch_stamp(c->dc, dx.p, (int)std::min<int64_t>(xlen, nc), 1e-12, 1.0, 0.0, nullptr, -1.0,
+                   dax.p, drc.p, drhs.p, s, 1e-12);
+  gk::AcArgs a{};
+  a.n = n;
+  a.ncell = ncell;
+  a.cell_row = d_crow.p;
+  a.cell_col = d_ccol.p;
+  a.re_ptr = d_re_ptr.p;
+  a.re_idx = d_re_idx.p;
+  a.im_ptr = d_im_ptr.p;
+  a.im_code = d_im_code.p;
+  a.cap = d_cap.p;
+  a.ax = dax.p;
+  a.rhs = d_rhs.p;
+  a.freqs = d_freqs.p;
+  a.out_re = d_re.p;
+  a.out_im = d_im.p;
+  a.status = d_status.p;
+  gk::launch_ac_dense(a, (int)nf, s);
+  int st = 0;
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out_re, d_re.p, (size_t)nf * n * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out_im, d_im.p, (size_t)nf * n * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&st, d_status.p, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return h->cuda_fail(e, "ac sweep");
+  if (st) return h->fail(GPUKLU_SINGULAR, "ac sweep: a pivot below 1e-30");
+  return GPUKLU_OK;
+}
+
 int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_config* cfg,
                      const double* x0, double* x_out, int64_t x_cap, int64_t* x_len,
                      int64_t* iters, int64_t* iters_total, int* reason) {

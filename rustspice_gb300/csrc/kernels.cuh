@@ -154,6 +154,20 @@ struct BbdArgs {
   const int* bperm;                            // Schur position -> original index
 };
 
+// AC sweep: the dense cells of Y(w) = G + jwC and the per-frequency solve.
+struct AcArgs {
+  int n, ncell;
+  const int *cell_row, *cell_col;   // cell -> (row, column); row 0 is the ground row
+  const int *re_ptr, *re_idx;       // per cell: raw CSC entries of the DC stamp, in order
+  const int *im_ptr, *im_code;      // per cell: (capacitor device << 1) | negated, in order
+  const double* cap;                // capacitance per device
+  const double* ax;                 // the DC stamp at the operating point (raw CSC)
+  const double* rhs;                // 2 n: the AC sources (re, im), row 0 unused
+  const double* freqs;
+  double *out_re, *out_im;          // nf x n
+  int* status;                      // 1: a pivot below 1e-30
+};
+
 // --------------------------------------------------------------- launches
 // maxblk: the largest diagonal block; blocks up to about 14k rows run with the
 // working column in shared memory.
@@ -212,6 +226,10 @@ void launch_bbd_rmatvec(const double* ax, const double* xT, const BbdArgs& B, do
 void launch_gather(double* dst, const double* src, const int* idx, int n, cudaStream_t s);
 void launch_bbd_combine(const double* z, const double* w2, const double* xT, const BbdArgs& B,
                         double* x, cudaStream_t s);
+
+// One thread block per frequency; shared memory ac_smem_bytes(n, 256).
+size_t ac_smem_bytes(int n, int threads);
+void launch_ac_dense(const AcArgs& a, int nf, cudaStream_t s);
 
 // Transient forward / adjoint over a batch: one warp per instance.
 void launch_tran_forward(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);

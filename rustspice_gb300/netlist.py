@@ -12,10 +12,12 @@ would run it:
 * tokens (netlist.rs:322-370): ``key=value`` tokens are parameters (a token
   holding both ``=`` and ``,`` splits at top-level commas; a leading ``(`` and
   a trailing ``)`` around a parameter are dropped), the rest positional;
-* device fields (netlist.rs:400-460): R, C, V, I take two nodes and a
-  value, the token after a ``DC`` keyword when there is one; D takes two
-  nodes and a model; M four nodes and a model, or three and a model with the
-  bulk on ground;
+* device fields (netlist.rs:400-460, 1454-1476): R, C, V, I take two nodes
+  and a value, the token after a ``DC`` keyword when there is one (a source
+  without a DC value, which the reference leaves out of its DC system, is
+  refused); V and I carry the magnitude and phase after an ``AC`` keyword
+  (p[1], p[2]; 0 when absent); D takes two nodes and a model; M four nodes
+  and a model, or three and a model with the bulk on ground;
 * numbers (netlist.rs:1635-1660): one trailing ``f p n u m k g t`` scales by
   1e-15 ... 1e12 and ``meg`` by 1e6, case-insensitive;
 * nodes (circuit.rs:31-57, netlist.rs:934-1100): ``0`` is ground (id 0),
@@ -244,9 +246,16 @@ def compile_deck(text: str, name: str = "") -> Deck:
             val = a[3] if (a[2].lower() == "dc" and len(a) >= 4) else a[2]
             v = parse_number(val)
             if v is None:
-                raise NetlistError(f"line {st.line}: {st.name} has no numeric value")
+                raise NetlistError(f"line {st.line}: {st.name} has no numeric (DC) value")
             kind = {"R": DEV_R, "C": DEV_C, "V": DEV_V, "I": DEV_I}[st.kind]
             nodes, params = (node(a[0]), node(a[1])), (v,)
+            if st.kind in "VI":  # AC magnitude and phase after an AC keyword (netlist.rs:1454-1476)
+                up = [x.upper() for x in a]
+                if "AC" in up:
+                    k = up.index("AC")
+                    mag = parse_number(a[k + 1]) if k + 1 < len(a) else None
+                    ph = parse_number(a[k + 2]) if k + 2 < len(a) else None
+                    params = (v, 0.0 if mag is None else mag, 0.0 if ph is None else ph)
         elif st.kind in "DM":
             if st.kind == "D":
                 if len(a) < 3:

@@ -190,6 +190,39 @@ def newton_dc(solver: GpuKluSolver, dc: DeviceCircuit, cfg: N.NewtonConfig,
     return NewtonResult(rs.value == 0, it.value, itt.value, REASONS[rs.value], x[:xl.value])
 
 
+def ac_sweep(solver: GpuKluSolver, dc: DeviceCircuit, x_dc, freqs) -> np.ndarray:
+    """AC small-signal solutions at the operating point x_dc for every
+    frequency (the reference's .ac): complex array [len(freqs), n]. V and I
+    sources carry the AC magnitude in p[:, 1] and the phase [deg] in p[:, 2]."""
+    x = N.f64(x_dc)
+    fr = N.f64(freqs)
+    re = np.zeros(len(fr) * dc.n)
+    im = np.zeros(len(fr) * dc.n)
+    n = C.c_int64()
+    solver._check(N.lib().gpuklu_ac_sweep(solver.handle, dc.handle, N.ptr(x), len(x), N.ptr(fr),
+                                          len(fr), N.ptr(re), N.ptr(im), C.byref(n)))
+    return (re + 1j * im).reshape(len(fr), dc.n)
+
+
+def frequency_sweep(kind: str, points: int, fstart: float, fstop: float) -> np.ndarray:
+    """The reference's .ac frequency list (crates/sim-core/src/engine.rs:
+    1002-1042): "dec" and "oct" points per decade / octave, "lin" points."""
+    import math
+    kind = kind.lower()
+    if kind == "oct":
+        octaves = math.log2(fstop / fstart)
+        total = int(math.ceil(octaves * points)) + 1
+        return np.array([fstart * 2.0 ** ((i * octaves) / max(total - 1, 1))
+                         for i in range(total)])
+    if kind == "lin":
+        step = (fstop - fstart) / max(points - 1, 1)
+        return np.array([fstart + i * step for i in range(points)])
+    ls, lt = math.log10(fstart), math.log10(fstop)
+    dec = lt - ls
+    total = int(math.ceil(dec * points)) + 1
+    return np.array([10.0 ** (ls + (i * dec) / max(total - 1, 1)) for i in range(total)])
+
+
 def dc_forward(solver: GpuKluSolver, dc: DeviceCircuit, cfg: N.NewtonConfig,
                x0=None) -> NewtonResult:
     """Forward half of the DC operating-point function pair (newton_dc)."""
