@@ -273,7 +273,8 @@ def _mesh_dc(out, with_cpu, timed, ocfg):
     newton_dc(g, dc, cfg)
     r, t = timed(lambda: newton_dc(g, dc, cfg))
     e = {"workload": "32x32 diode mesh, gmin stepping (10 steps)", "n": dc.n,
-         "newton_iterations": r.iterations_total, "gpu_ms": t * 1e3}
+         "newton_iterations": r.iterations_total, "gpu_ms": t * 1e3,
+         "pivot_passes": g.pivot_passes()}
     if with_cpu:
         t0 = time.perf_counter()
         ro = po.dc_op(c, "nativeklu_exact", **dict(ocfg, gmin_steps=10))
@@ -301,6 +302,7 @@ def _dc_adjoint(out, timed, with_cpu, ocfg):
     _, t_b = timed(lambda: dc_backward(g, dc, f.x, dl))
     out["dc_adjoint"] = {"workload": "120x120 mesh + 1000 inverters, loss on 256 nodes",
                          "n": dc.n, "forward_ms": t_f * 1e3, "newton_iterations": f.iterations,
+                         "pivot_passes": g.pivot_passes(),
                          "backward_ms": t_b * 1e3, "backward_over_forward": t_b / t_f}
     if with_cpu:
         from oracle import pyoracle as po

@@ -94,6 +94,14 @@ int gpuklu_set_pivot_mode(gpuklu_handle* h, int mode);
 int gpuklu_get_stats(gpuklu_handle* h, gpuklu_stats* out);
 /* Text of the last error on this handle ("" if none). */
 const char* gpuklu_last_error(const gpuklu_handle* h);
+/* Refactorizations the last first factorization ran to find the pivot
+ * sequence of native_klu.rs:1194-1382 (the pivot pass restated as
+ * refactorizations that check the threshold rule on every column); 0 when
+ * the sequential one-warp pivot pass ran instead (below 512 rows, more than 8
+ * passes needed, or GPUKLU_PIVOT_PASS=sequential; GPUKLU_PIVOT_PASS=refactor
+ * takes the refactorizations at every size). Both give the same pivots and
+ * factor. */
+int64_t gpuklu_pivot_pass_count(const gpuklu_handle* h);
 /* factor/solve with values already in device memory (the device-stamp path):
  * d_ax has the cached pattern's nnz values, d_rhs has n values. */
 int gpuklu_factor_device(gpuklu_handle* h, const double* d_ax);

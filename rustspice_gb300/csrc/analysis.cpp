@@ -530,6 +530,40 @@ void set_pivots(Plan& p, const i64* ap, const i64* ai, const std::vector<i32>& r
   finalize_plan(p, ap, ai, p.pats);
 }
 
+void pivot_pass_amap(const Plan& p, const std::vector<int>& cand_row, std::vector<i32>& amap_ptr,
+                     std::vector<i32>& amap_idx, std::vector<i32>& row_perm) {
+  const int n = p.n, ns = p.nslots();
+  row_perm.assign(n, 0);
+  std::vector<int> rinv(n), where(n, -1), slot_of(p.pcol_raw.size(), -1);
+  for (int b = 0; b < p.nblocks; ++b)
+    for (int i = p.block_ptr[b]; i < p.block_ptr[b + 1]; ++i)
+      row_perm[i] = rinv[i] = i - p.block_ptr[b];
+  amap_ptr.assign(ns + 1, 0);
+  for (int k = 0; k < n; ++k) {
+    const int b0 = p.block_ptr[p.pos_block[k]];
+    for (int s = p.col_ptr[k]; s < p.col_ptr[k + 1]; ++s) where[p.slot_row[s]] = s;
+    for (int t = p.pcol_ptr[k]; t < p.pcol_ptr[k + 1]; ++t) {
+      const int s = where[b0 + rinv[b0 + p.pcol_q[t]]];
+      slot_of[t] = s;
+      if (s >= 0) ++amap_ptr[s + 1];
+    }
+    for (int s = p.col_ptr[k]; s < p.col_ptr[k + 1]; ++s) where[p.slot_row[s]] = -1;
+    const int mr = cand_row[k];
+    if (mr >= 0 && mr != k) {
+      const int ok = row_perm[k], om = row_perm[mr];
+      row_perm[k] = om;
+      row_perm[mr] = ok;
+      rinv[b0 + ok] = mr - b0;
+      rinv[b0 + om] = k - b0;
+    }
+  }
+  for (int s = 0; s < ns; ++s) amap_ptr[s + 1] += amap_ptr[s];
+  amap_idx.assign(amap_ptr[ns], 0);
+  std::vector<int> fill(amap_ptr.begin(), amap_ptr.end() - 1);
+  for (size_t t = 0; t < slot_of.size(); ++t)
+    if (slot_of[t] >= 0) amap_idx[fill[slot_of[t]]++] = p.pcol_raw[t];
+}
+
 void finalize_plan(Plan& p, const i64* ap, const i64* ai, const std::vector<Pattern>& pats) {
   const int n = p.n;
   p.col_ptr.assign(n + 1, 0);

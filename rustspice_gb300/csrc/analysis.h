@@ -142,6 +142,16 @@ std::string analyze(int n, const i64* ap, const i64* ai, int pivot_mode, Plan& p
 // entry -> slot map and the solve permutations.
 void set_pivots(Plan& p, const i64* ap, const i64* ai, const std::vector<i32>& row_perm);
 
+// The A scatter of the first factorization for a candidate pivot sequence,
+// as slot lists for the refactorization: column k adds its raw entries (in
+// the pivot pass's order) at the row positions that the candidate's swaps of
+// earlier columns give them; entries landing outside the column's pivot-free
+// pattern are left out (the pass adds them at working positions it never
+// reads). cand_row[k]: the row position swapped into pivot k, or -1. Also
+// returns the block-local row_perm the candidate produces.
+void pivot_pass_amap(const Plan& p, const std::vector<int>& cand_row, std::vector<i32>& amap_ptr,
+                     std::vector<i32>& amap_idx, std::vector<i32>& row_perm);
+
 // Rebuilds slot maps, update lists, row views and permutations from the
 // current per-block patterns and pivots.
 void finalize_plan(Plan& p, const i64* ap, const i64* ai,

@@ -449,6 +449,15 @@ struct gpuklu_handle {
   // kernel: the 32x32 diode mesh (273k pairs) already refactors faster over
   // the whole grid, despite the grid kernel's dependency hops through L2.
   static constexpr int64_t kOneBlockUpdates = 1 << 16;
+  // The first factorization's pivot pass on the refactorization kernels:
+  // buffers, the pass limit before the sequential kernel takes over, and the
+  // passes the last first factorization ran (0: the sequential kernel).
+  static constexpr int kMaxPivotPasses = 8;
+  // Below this many rows the sequential pass costs about as much as one
+  // refactorization plus its host round trip, so it runs directly.
+  static constexpr int64_t kPivotPassMinN = 512;
+  DBuf<int> d_cand, d_want, d_pamap_ptr, d_pamap_idx;
+  int64_t pivot_passes = 0;
   double rcond = 0.0;
   bool rcond_valid = false;
   std::string err;
@@ -574,6 +583,77 @@ struct gpuklu_handle {
                         grid_cols, stream);
   }
 
+  // The first factorization's pivot pass run as refactorizations of the
+  // pivot-free pattern (PivotCheck). Each pass refactors with a candidate
+  // pivot sequence - at first none - and reads back every column's own
+  // choice; from the first column that disagrees on, the choices become the
+  // next candidate. The columns before that one are final (a column's values
+  // depend only on earlier columns), so each pass settles at least one more
+  // column, and a pass that agrees everywhere has computed exactly what the
+  // sequential pass computes: its pivots, and its factor in d_lu. settled
+  // stays false when kMaxPivotPasses were not enough.
+  int pivot_pass(std::vector<i32>& rperm, bool& settled) {
+    settled = false;
+    const gk::Plan& P = sym_plan;
+    const int nn = P.n;
+    if (nn == 0) {
+      rperm.clear();
+      settled = true;
+      return GPUKLU_OK;
+    }
+    std::vector<int> cand(nn, -1), cand_row(nn, -1), want(nn, -1);
+    std::vector<i32> aptr, aidx;
+    cudaError_t e = d_cand.resize(nn);
+    if (e == cudaSuccess) e = d_want.resize(nn);
+    if (e != cudaSuccess) return cuda_fail(e, "pivot pass buffers");
+    const char* ob = getenv("GPUKLU_ONE_BLOCK");
+    const bool one_block = !(ob && ob[0] == '0') && pd_sym.updates <= kOneBlockUpdates &&
+                           gk::refactor_cta_fits(pd_sym.dp);
+    gk::PivotCheck pc;
+    pc.cand = d_cand.p;
+    pc.want = d_want.p;
+    pc.tol = no_swap ? 0.0 : 0.001;
+    for (int pass = 0; pass < kMaxPivotPasses; ++pass) {
+      gk::pivot_pass_amap(P, cand_row, aptr, aidx, rperm);
+      e = d_pamap_ptr.upload(aptr, stream);
+      if (e == cudaSuccess) e = d_pamap_idx.upload(aidx, stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_cand.p, cand.data(), nn * sizeof(int), cudaMemcpyHostToDevice,
+                            stream);
+      if (e != cudaSuccess) return cuda_fail(e, "pivot pass upload");
+      gk::DPlan dp = pd_sym.dp;
+      dp.amap_ptr = d_pamap_ptr.p;
+      dp.amap_idx = d_pamap_idx.p;
+      if (one_block) {
+        gk::launch_refactor_cta(dp, d_ax.p, d_lu.p, d_status.p, stream, pc);
+      } else {
+        unsigned ep = next_epoch(epoch, d_flags);
+        gk::launch_refactor(dp, d_ax.p, d_lu.p, d_flags.p, ep, d_counter.p, d_status.p,
+                            grid_cols, stream, pc);
+      }
+      e = cudaMemcpyAsync(want.data(), d_want.p, nn * sizeof(int), cudaMemcpyDeviceToHost,
+                          stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+      if (e != cudaSuccess) return cuda_fail(e, "pivot pass");
+      const int st = check_status("pivot pass");
+      if (st) return st;
+      ++pivot_passes;
+      int k1 = 0;
+      while (k1 < nn && want[k1] == cand[k1]) ++k1;
+      if (k1 == nn) {
+        settled = true;
+        return GPUKLU_OK;
+      }
+      for (int k = k1; k < nn; ++k) {
+        const int w = want[k];
+        const bool ok = w > P.dslot[k] && w < P.col_ptr[k + 1];  // an L slot of column k
+        cand[k] = ok ? w : -1;
+        cand_row[k] = ok ? P.slot_row[w] : -1;
+      }
+    }
+    return GPUKLU_OK;
+  }
+
   int factor_on_device(bool sync) {
     rcond_valid = false;
     if (state == FACTORED) {
@@ -582,17 +662,33 @@ struct gpuklu_handle {
       if (!sync) return GPUKLU_OK;
       return check_status("refactor");
     }
-    // First factorization: the reference's pivot pass.
-    int maxblk = 0;
-    for (int b = 0; b < sym_plan.nblocks; ++b)
-      maxblk = std::max(maxblk, sym_plan.block_ptr[b + 1] - sym_plan.block_ptr[b]);
-    gk::launch_first_factor(pd_sym.dp, maxblk, d_ax.p, d_lu.p, d_work.p, d_rperm.p, d_rinv.p,
-                            no_swap ? 0.0 : 0.001, d_status.p, stream);
+    // First factorization: the reference's pivot pass, as refactorizations
+    // from kPivotPassMinN rows on, else (or when those do not settle) the
+    // sequential one-warp kernel. GPUKLU_PIVOT_PASS=refactor / sequential
+    // picks one for every size.
     std::vector<i32> rperm(n);
-    cudaError_t e = cudaMemcpyAsync(rperm.data(), d_rperm.p, n * sizeof(i32),
-                                    cudaMemcpyDeviceToHost, stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-    if (e != cudaSuccess) return cuda_fail(e, "first factor");
+    bool settled = false;
+    pivot_passes = 0;
+    const char* pp = getenv("GPUKLU_PIVOT_PASS");
+    const bool seq = pp && std::strcmp(pp, "sequential") == 0;
+    const bool ref = pp && std::strcmp(pp, "refactor") == 0;
+    if (!seq && (ref || n >= kPivotPassMinN)) {
+      const int st = pivot_pass(rperm, settled);
+      if (st) return st;
+    }
+    if (!settled) {
+      pivot_passes = 0;
+      rperm.assign(n, 0);
+      int maxblk = 0;
+      for (int b = 0; b < sym_plan.nblocks; ++b)
+        maxblk = std::max(maxblk, sym_plan.block_ptr[b + 1] - sym_plan.block_ptr[b]);
+      gk::launch_first_factor(pd_sym.dp, maxblk, d_ax.p, d_lu.p, d_work.p, d_rperm.p,
+                              d_rinv.p, no_swap ? 0.0 : 0.001, d_status.p, stream);
+      cudaError_t e = cudaMemcpyAsync(rperm.data(), d_rperm.p, n * sizeof(i32),
+                                      cudaMemcpyDeviceToHost, stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+      if (e != cudaSuccess) return cuda_fail(e, "first factor");
+    }
     int st = check_status("first factor");
     if (st) return st;
     if (!(piv_ok && rperm == piv_rperm)) {
@@ -783,6 +879,8 @@ int gpuklu_get_stats(gpuklu_handle* h, gpuklu_stats* out) {
   out->rcond = h->state == gpuklu_handle::FACTORED ? h->rcond : 0.0;
   return GPUKLU_OK;
 }
+
+int64_t gpuklu_pivot_pass_count(const gpuklu_handle* h) { return h ? h->pivot_passes : 0; }
 
 const char* gpuklu_last_error(const gpuklu_handle* h) { return h ? h->err.c_str() : ""; }
 

@@ -342,9 +342,50 @@ __global__ void k_first_factor_s(DPlan P, const double* __restrict__ ax, double*
 // one is applied. The operations and their order are the reference's.
 constexpr int kColBuf = 768;
 
+// Pivot-pass mode of the refactorization (PivotCheck): the first
+// factorization's threshold rule on column k's finished values - the first L
+// slot of largest magnitude takes the pivot when it beats the diagonal and
+// the diagonal is below tol times it - written to want[k]; then the
+// candidate's row is swapped into the pivot. get(q) / put(q, v) access the
+// column by slot.
+template <class Get, class Put>
+__device__ __forceinline__ void pivot_check(const PivotCheck& pc, int k, int ds, int s1,
+                                            bool single, Get get, Put put) {
+  const int lane = threadIdx.x & 31;
+  double best = -1.0;
+  int bq = 0x7fffffff;
+  if (!single)
+    for (int q = ds + 1 + lane; q < s1; q += 32) {
+      const double v = fabs(get(q));
+      if (v > best) {
+        best = v;
+        bq = q;
+      }
+    }
+  for (int off = 16; off > 0; off >>= 1) {
+    const double ov = __shfl_down_sync(FULL, best, off);
+    const int oq = __shfl_down_sync(FULL, bq, off);
+    if (ov > best || (ov == best && oq < bq)) {
+      best = ov;
+      bq = oq;
+    }
+  }
+  if (lane == 0) {
+    const double dabs = fabs(get(ds));
+    pc.want[k] = (!single && bq != 0x7fffffff && best > dabs && dabs < pc.tol * best) ? bq : -1;
+    const int c = pc.cand[k];
+    if (c > ds && c < s1) {
+      const double t = get(ds);
+      put(ds, get(c));
+      put(c, t);
+    }
+  }
+  __syncwarp();
+}
+
 __global__ void k_refactor(DPlan P, const double* __restrict__ ax, double* lu,
                            unsigned* flags, unsigned epoch, unsigned* counter,
-                           int* status) {
+                           int* status, PivotCheck pc) {
   extern __shared__ double scol[];
   const int lane = threadIdx.x & 31;
   double* const cbuf = scol + (threadIdx.x >> 5) * kColBuf;
@@ -425,6 +466,11 @@ __global__ void k_refactor(DPlan P, const double* __restrict__ ax, double* lu,
         __syncwarp();
       }
     }
+    if (pc.want != nullptr)
+      pivot_check(
+          pc, k, ds, s1, P.col_single[k] != 0,
+          [&](int q) { return staged ? C[q] : ld_cg(&lu[q]); },
+          [&](int q, double v) { C[q] = v; });
     const double diag = perturb(staged ? C[ds] : ld_cg(&lu[ds]), P.col_single[k] != 0);
     for (int q = ds + 1 + lane; q < s1; q += 32)
       lu[q] = (staged ? C[q] : ld_cg(&lu[q])) / diag;
@@ -590,7 +636,8 @@ __device__ __forceinline__ void st_release_cta(unsigned* p, unsigned v) {
 // holding the lowest unfinished column always proceeds. Shared: lu[nslots]
 // f64, done[n] u32.
 __global__ void __launch_bounds__(1024) k_refactor_cta(DPlan P, const double* __restrict__ ax,
-                                                       double* lu_out, int* status) {
+                                                       double* lu_out, int* status,
+                                                       PivotCheck pc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* const lu = reinterpret_cast<double*>(smem_raw);
   unsigned* const sdone = reinterpret_cast<unsigned*>(lu + P.nslots);
@@ -667,6 +714,10 @@ __global__ void __launch_bounds__(1024) k_refactor_cta(DPlan P, const double* __
       up = nup;
     }
     if (failed) break;
+    if (pc.want != nullptr)
+      pivot_check(
+          pc, k, ds, s1, P.col_single[k] != 0, [&](int q) { return lu[q]; },
+          [&](int q, double v) { lu[q] = v; });
     const double diag = perturb(lu[ds], P.col_single[k] != 0);
     for (int q = ds + 1 + lane; q < s1; q += 32) lu[q] = lu[q] / diag;
     if (lane == 0) lu[ds] = diag;
@@ -1419,10 +1470,10 @@ void launch_first_factor(const DPlan& P, int maxblk, const double* ax, double* l
 
 void launch_refactor(const DPlan& P, const double* ax, double* lu, unsigned* flags,
                      unsigned epoch, unsigned* counter, int* status, int grid,
-                     cudaStream_t s) {
+                     cudaStream_t s, const PivotCheck& pc) {
   cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
   k_refactor<<<grid, 128, 4 * kColBuf * sizeof(double), s>>>(P, ax, lu, flags, epoch, counter,
-                                                             status);
+                                                             status, pc);
 }
 
 namespace {
@@ -1442,10 +1493,10 @@ bool refactor_cta_fits(const DPlan& P) {
 }
 
 void launch_refactor_cta(const DPlan& P, const double* ax, double* lu, int* status,
-                         cudaStream_t s) {
+                         cudaStream_t s, const PivotCheck& pc) {
   const size_t bytes = refactor_cta_bytes(P);
   cudaFuncSetAttribute(k_refactor_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  k_refactor_cta<<<1, 1024, bytes, s>>>(P, ax, lu, status);
+  k_refactor_cta<<<1, 1024, bytes, s>>>(P, ax, lu, status, pc);
 }
 
 namespace {

@@ -174,9 +174,23 @@ struct AcArgs {
 void launch_first_factor(const DPlan& P, int maxblk, const double* ax, double* lu,
                          double* work, int* rperm, int* rinv, double tol, int* status,
                          cudaStream_t s);
+// The refactorization in its pivot-pass mode (want == nullptr: off). Before
+// column k is scaled, the first factorization's threshold rule is applied to
+// the column's finished values and its choice written to want[k] (the L slot
+// of the row that takes the pivot, or -1 for the diagonal); then the row of
+// the candidate slot cand[k] (-1: none) is swapped into the pivot. Run over
+// the pivot-free pattern with the A scatter of the candidate's row order, it
+// computes what the first factorization computes wherever its earlier
+// choices are the candidate's, so want[] confirms the candidate up to the
+// first column that disagrees.
+struct PivotCheck {
+  const int* cand = nullptr;
+  int* want = nullptr;
+  double tol = 0.0;
+};
 void launch_refactor(const DPlan& P, const double* ax, double* lu, unsigned* flags,
                      unsigned epoch, unsigned* counter, int* status, int grid,
-                     cudaStream_t s);
+                     cudaStream_t s, const PivotCheck& pc = PivotCheck());
 // Slots per chunk of the one-block solve's schedule.
 constexpr int kSolveChunk = 2048;
 // One-block variants for small factorizations; *_cta_fits says whether the
@@ -184,7 +198,7 @@ constexpr int kSolveChunk = 2048;
 // fits one block.
 bool refactor_cta_fits(const DPlan& P);
 void launch_refactor_cta(const DPlan& P, const double* ax, double* lu, int* status,
-                         cudaStream_t s);
+                         cudaStream_t s, const PivotCheck& pc = PivotCheck());
 bool solve_cta_fits(const DPlan& P);
 void launch_solve_cta(const DPlan& P, const double* rhs, const double* ax, const double* lu,
                       double* out, cudaStream_t s);

@@ -106,6 +106,11 @@ class GpuKluSolver:
         self._check(N.lib().gpuklu_get_stats(self._h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in N.Stats._fields_}
 
+    def pivot_passes(self) -> int:
+        """Refactorizations the last first factorization used to find its
+        pivots (0: the sequential pivot pass ran)."""
+        return int(N.lib().gpuklu_pivot_pass_count(self._h))
+
 
 class DeviceCircuit:
     """A circuit compiled into its stamp-to-slot map on the device."""

@@ -74,6 +74,95 @@ def first_factor(P: native.Plan, ax, tol=0.001):
     return lu, rperm
 
 
+def staged_amap(P: native.Plan, swaps):
+    """Raw entries summed into each slot when column k scatters A(:,k)
+    through the row order the pivot pass has reached at column k: the swaps
+    {column: row position} of earlier columns applied to the identity.
+    Entries that land outside the column's pattern are dropped (the pivot
+    pass adds them to working positions it never reads)."""
+    n = P.n
+    b0s = P.block_ptr[P.pos_block]
+    rperm = (np.arange(n) - b0s).astype(np.int64)
+    rinv = rperm.copy()
+    lists = [[] for _ in range(P.nslots)]
+    for k in range(n):
+        b0 = b0s[k]
+        where = {int(P.slot_row[s]): s for s in range(P.col_ptr[k], P.col_ptr[k + 1])}
+        for t in range(P.pcol_ptr[k], P.pcol_ptr[k + 1]):
+            s = where.get(int(b0 + rinv[b0 + P.pcol_q[t]]))
+            if s is not None:
+                lists[s].append(int(P.pcol_raw[t]))
+        if k in swaps:
+            mr = swaps[k]
+            ok, om = rperm[k], rperm[mr]
+            rperm[k], rperm[mr] = om, ok
+            rinv[b0 + ok] = mr - b0
+            rinv[b0 + om] = k - b0
+    return lists, rperm
+
+
+def staged_refactor(P: native.Plan, ax, lists, cand, tol):
+    """The refactorization kernel in its pivot-pass mode: before scaling
+    column k it applies the pass's threshold rule to the column's finished
+    values, writes the choice to want[k] (an L slot, or -1 for the diagonal)
+    and swaps the candidate's row (cand[k], an L slot or -1) into the
+    pivot."""
+    lu = np.zeros(P.nslots)
+    want = np.full(P.n, -1, np.int64)
+    for k in range(P.n):
+        s0, ds, s1 = P.col_ptr[k], P.dslot[k], P.col_ptr[k + 1]
+        for s in range(s0, s1):
+            v = 0.0
+            for t in lists[s]:
+                v += ax[t]
+            lu[s] = v
+        for s in range(s0, ds):
+            j = P.slot_row[s]
+            u = lu[s]
+            if u != 0.0:
+                q0 = P.dslot[j] + 1
+                for q in range(q0, P.col_ptr[j + 1]):
+                    d = P.upd_dst[P.upd_ptr[s] + q - q0]
+                    lu[d] = lu[d] - lu[q] * u
+        if not P.col_single[k]:
+            dabs = abs(lu[ds])
+            best, bq = -1.0, -1
+            for q in range(ds + 1, s1):
+                v = abs(lu[q])
+                if v > best:
+                    best, bq = v, q
+            if bq >= 0 and best > dabs and dabs < tol * best:
+                want[k] = bq
+            c = cand[k]
+            if c >= 0:
+                lu[ds], lu[c] = lu[c], lu[ds]
+        diag = _perturb(lu[ds], bool(P.col_single[k]))
+        lu[ds] = diag
+        for q in range(ds + 1, s1):
+            lu[q] = lu[q] / diag
+    return lu, want
+
+
+def staged_first_factor(P: native.Plan, ax, tol=0.001, max_passes=8):
+    """The pivot pass as the host runs it on the device: refactorizations of
+    the pivot-free pattern with a candidate pivot sequence (at first none);
+    from the first column whose choice disagrees with the candidate on, the
+    choices become the next candidate, until a pass agrees everywhere.
+    Returns (lu, rperm, passes), or None when max_passes did not settle it
+    (the sequential pass runs then)."""
+    n = P.n
+    cand = np.full(n, -1, np.int64)
+    for p in range(max_passes):
+        rows = {k: int(P.slot_row[c]) for k, c in enumerate(cand) if c >= 0}
+        lists, rperm = staged_amap(P, rows)
+        lu, want = staged_refactor(P, ax, lists, cand, tol)
+        bad = np.nonzero(want != cand)[0]
+        if len(bad) == 0:
+            return lu, rperm, p + 1
+        cand[bad[0]:] = want[bad[0]:]
+    return None
+
+
 def refactor(P: native.Plan, ax):
     lu = np.zeros(P.nslots)
     for k in range(P.n):

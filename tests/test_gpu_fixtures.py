@@ -51,6 +51,33 @@ def _oracle_solve(kind, ap, ai, ax, b):
 
 
 @pytest.mark.parametrize("mode,kind", MODES, ids=["reference", "exact"])
+def test_pivot_pass_refactorizations(mode, kind, kernels, monkeypatch):
+    """The first factorization's pivot pass run as checked refactorizations
+    (the default) and as the sequential one-warp kernel give the same
+    pivots and factor: solutions equal bit for bit and equal to the
+    oracle's, the same swap count, and the number of passes the CPU
+    restatement of the host loop predicts."""
+    from plan_emulator import staged_first_factor
+    from test_plan_parity import PIVOT_SYSTEMS
+    for name, ap, ai, ax in PIVOT_SYSTEMS:
+        n = len(ap) - 1
+        b = np.random.default_rng(n).uniform(-1, 1, n)
+        r = staged_first_factor(N.Plan(n, ap, ai, mode), ax)
+        expect = r[2] if r is not None else 0
+        got = {}
+        for pp in ("refactor", "sequential"):
+            monkeypatch.setenv("GPUKLU_PIVOT_PASS", pp)
+            g = GpuKluSolver(n, pivot_mode=mode)
+            x = _gpu_solve(g, ap, ai, ax, b)
+            got[pp] = (x, g.stats()["pivot_swaps"], g.pivot_passes())
+        _, xo = _oracle_solve(kind, ap, ai, ax, b)
+        assert np.array_equal(got["refactor"][0], got["sequential"][0]), name
+        assert np.array_equal(got["refactor"][0], xo), name
+        assert got["refactor"][1] == got["sequential"][1], name
+        assert got["sequential"][2] == 0 and got["refactor"][2] == expect, (name, got["refactor"][2])
+
+
+@pytest.mark.parametrize("mode,kind", MODES, ids=["reference", "exact"])
 def test_kats(mode, kind, kernels):
     for k in KATS["solve"]:
         n = len(k["ap"]) - 1

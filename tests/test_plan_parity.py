@@ -14,7 +14,8 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as po
-from plan_emulator import SOLVE_CHUNK, EmulatedSolver, solve_one_block
+from plan_emulator import (SOLVE_CHUNK, EmulatedSolver, first_factor, solve_one_block,
+                            staged_first_factor)
 from rustspice_gb300 import circuits as cz
 from rustspice_gb300 import native as N
 
@@ -68,6 +69,49 @@ def test_plan_emulation_bit_exact(sysm, mode, kind):
     assert es.plan.nblocks == st["nblocks"]
     if mode == N.PIVOT_REFERENCE:  # the pattern of the pivot-free symbolic pass
         assert es.plan.nnz_l == st["nnz_l"]
+
+
+def _weak_diagonal(n, seed):
+    """Random sparse matrix whose diagonal is often far below its column:
+    the threshold rule exchanges many rows, in chains."""
+    rng = np.random.default_rng(seed)
+    a = (rng.random((n, n)) < 0.12) * rng.uniform(-1, 1, (n, n))
+    d = rng.uniform(-1, 1, n) * np.where(rng.random(n) < 0.4, 1e-5, 1.0)
+    a[np.arange(n), np.arange(n)] = d
+    ap = np.zeros(n + 1, np.int64)
+    ai, ax = [], []
+    for c in range(n):
+        r = np.nonzero(a[:, c])[0]
+        ai.extend(r)
+        ax.extend(a[r, c])
+        ap[c + 1] = len(ai)
+    return ap, np.array(ai, np.int64), np.array(ax)
+
+
+PIVOT_SYSTEMS = [(s[0], s[1], s[2], s[3]) for s in SYSTEMS] + [
+    (f"weak_diag_{seed}", *_weak_diagonal(60, seed)) for seed in range(4)]
+
+
+@pytest.mark.parametrize("mode", [N.PIVOT_REFERENCE, N.PIVOT_EXACT], ids=["reference", "exact"])
+@pytest.mark.parametrize("sysm", PIVOT_SYSTEMS, ids=[s[0] for s in PIVOT_SYSTEMS])
+def test_pivot_pass_as_refactorizations(sysm, mode):
+    """The first factorization's pivot pass restated as refactorizations of
+    the pivot-free pattern that check the threshold rule on every column (the
+    host loop and the refactor kernel's pivot-pass mode) gives the sequential
+    pass's pivots and factor bit for bit, with and without row exchanges."""
+    name, ap, ai, ax = sysm
+    n = len(ap) - 1
+    P = N.Plan(n, ap, ai, mode)
+    for a in (ax, ax * (1.0 + 0.1 * np.random.default_rng(7).standard_normal(len(ax)))):
+        lu, rperm = first_factor(P, a)
+        r = staged_first_factor(P, a, max_passes=n + 1)
+        assert r is not None
+        lu2, rperm2, passes = r
+        assert np.array_equal(rperm2, rperm)
+        assert np.array_equal(lu2, lu), np.max(np.abs(lu2 - lu))
+        assert passes <= n + 1
+        swaps = int(np.sum(rperm != np.arange(n) - P.block_ptr[P.pos_block]))
+        assert (passes == 1) == (swaps == 0)
 
 
 def test_mesh_dimensions():
