@@ -458,6 +458,11 @@ struct gpuklu_handle {
   static constexpr int64_t kPivotPassMinN = 512;
   DBuf<int> d_cand, d_want, d_pamap_ptr, d_pamap_idx;
   int64_t pivot_passes = 0;
+  // The candidate the last settled pass ended with (per column an L slot or
+  // -1), kept with the analysis: the next first factorization of the same
+  // pattern starts from it and, if the pivots did not change, settles in one
+  // pass.
+  std::vector<int> piv_cand;
   double rcond = 0.0;
   bool rcond_valid = false;
   std::string err;
@@ -510,6 +515,7 @@ struct gpuklu_handle {
           (int64_t)sym_ai.size() == ai_len && std::equal(sym_ap.begin(), sym_ap.end(), ap) &&
           std::equal(sym_ai.begin(), sym_ai.end(), ai))) {
       pd_sym_ok = piv_ok = false;
+      piv_cand.clear();
       sym_mode = -1;
       std::string m = gk::analyze((int)n, ap, ai, pivot_mode, sym_plan,
                                   given_blocks.empty() ? nullptr : &given_blocks);
@@ -585,7 +591,8 @@ struct gpuklu_handle {
 
   // The first factorization's pivot pass run as refactorizations of the
   // pivot-free pattern (PivotCheck). Each pass refactors with a candidate
-  // pivot sequence - at first none - and reads back every column's own
+  // pivot sequence - at first the last one found for this pattern, else
+  // none; any start ends at the same pivots - and reads back every column's own
   // choice; from the first column that disagrees on, the choices become the
   // next candidate. The columns before that one are final (a column's values
   // depend only on earlier columns), so each pass settles at least one more
@@ -602,6 +609,11 @@ struct gpuklu_handle {
       return GPUKLU_OK;
     }
     std::vector<int> cand(nn, -1), cand_row(nn, -1), want(nn, -1);
+    if ((int)piv_cand.size() == nn) cand = piv_cand;
+    for (int k = 0; k < nn; ++k) {
+      if (!(cand[k] > P.dslot[k] && cand[k] < P.col_ptr[k + 1])) cand[k] = -1;
+      cand_row[k] = cand[k] >= 0 ? P.slot_row[cand[k]] : -1;
+    }
     std::vector<i32> aptr, aidx;
     cudaError_t e = d_cand.resize(nn);
     if (e == cudaSuccess) e = d_want.resize(nn);
@@ -642,6 +654,7 @@ struct gpuklu_handle {
       while (k1 < nn && want[k1] == cand[k1]) ++k1;
       if (k1 == nn) {
         settled = true;
+        piv_cand.swap(cand);
         return GPUKLU_OK;
       }
       for (int k = k1; k < nn; ++k) {

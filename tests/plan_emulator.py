@@ -143,22 +143,23 @@ def staged_refactor(P: native.Plan, ax, lists, cand, tol):
     return lu, want
 
 
-def staged_first_factor(P: native.Plan, ax, tol=0.001, max_passes=8):
+def staged_first_factor(P: native.Plan, ax, tol=0.001, max_passes=8, start=None):
     """The pivot pass as the host runs it on the device: refactorizations of
-    the pivot-free pattern with a candidate pivot sequence (at first none);
-    from the first column whose choice disagrees with the candidate on, the
-    choices become the next candidate, until a pass agrees everywhere.
-    Returns (lu, rperm, passes), or None when max_passes did not settle it
-    (the sequential pass runs then)."""
+    the pivot-free pattern with a candidate pivot sequence (start: per column
+    an L slot or -1, e.g. the last sequence found for this pattern; default
+    none); from the first column whose choice disagrees with the candidate
+    on, the choices become the next candidate, until a pass agrees
+    everywhere. Returns (lu, rperm, passes, cand), or None when max_passes
+    did not settle it (the sequential pass runs then)."""
     n = P.n
-    cand = np.full(n, -1, np.int64)
+    cand = np.full(n, -1, np.int64) if start is None else np.array(start, np.int64)
     for p in range(max_passes):
         rows = {k: int(P.slot_row[c]) for k, c in enumerate(cand) if c >= 0}
         lists, rperm = staged_amap(P, rows)
         lu, want = staged_refactor(P, ax, lists, cand, tol)
         bad = np.nonzero(want != cand)[0]
         if len(bad) == 0:
-            return lu, rperm, p + 1
+            return lu, rperm, p + 1, cand
         cand[bad[0]:] = want[bad[0]:]
     return None
 

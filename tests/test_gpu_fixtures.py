@@ -56,7 +56,8 @@ def test_pivot_pass_refactorizations(mode, kind, kernels, monkeypatch):
     (the default) and as the sequential one-warp kernel give the same
     pivots and factor: solutions equal bit for bit and equal to the
     oracle's, the same swap count, and the number of passes the CPU
-    restatement of the host loop predicts."""
+    restatement of the host loop predicts. A second first factorization of
+    the same pattern starts from the pivots found and settles in one pass."""
     from plan_emulator import staged_first_factor
     from test_plan_parity import PIVOT_SYSTEMS
     for name, ap, ai, ax in PIVOT_SYSTEMS:
@@ -70,6 +71,10 @@ def test_pivot_pass_refactorizations(mode, kind, kernels, monkeypatch):
             g = GpuKluSolver(n, pivot_mode=mode)
             x = _gpu_solve(g, ap, ai, ax, b)
             got[pp] = (x, g.stats()["pivot_swaps"], g.pivot_passes())
+            if pp == "refactor" and expect > 0:
+                g.reset_pattern()
+                x2 = _gpu_solve(g, ap, ai, ax, b)
+                assert np.array_equal(x2, x) and g.pivot_passes() == 1, name
         _, xo = _oracle_solve(kind, ap, ai, ax, b)
         assert np.array_equal(got["refactor"][0], got["sequential"][0]), name
         assert np.array_equal(got["refactor"][0], xo), name

@@ -106,12 +106,23 @@ def test_pivot_pass_as_refactorizations(sysm, mode):
         lu, rperm = first_factor(P, a)
         r = staged_first_factor(P, a, max_passes=n + 1)
         assert r is not None
-        lu2, rperm2, passes = r
+        lu2, rperm2, passes, found = r
         assert np.array_equal(rperm2, rperm)
         assert np.array_equal(lu2, lu), np.max(np.abs(lu2 - lu))
         assert passes <= n + 1
         swaps = int(np.sum(rperm != np.arange(n) - P.block_ptr[P.pos_block]))
         assert (passes == 1) == (swaps == 0)
+        # a start from the sequence found settles in one pass; a start from
+        # arbitrary L slots still ends at the same pivots and factor
+        r = staged_first_factor(P, a, max_passes=1, start=found)
+        assert r is not None and np.array_equal(r[0], lu) and np.array_equal(r[1], rperm)
+        rng = np.random.default_rng(n)
+        junk = np.full(n, -1, np.int64)
+        for k in range(n):
+            if P.col_ptr[k + 1] > P.dslot[k] + 1 and rng.random() < 0.3:
+                junk[k] = rng.integers(P.dslot[k] + 1, P.col_ptr[k + 1])
+        r = staged_first_factor(P, a, max_passes=n + 2, start=junk)
+        assert r is not None and np.array_equal(r[0], lu) and np.array_equal(r[1], rperm)
 
 
 def test_mesh_dimensions():
