@@ -420,7 +420,8 @@ struct gpuklu_handle {
   // across reset(): a prepare(n) that changes n and comes back, as the
   // engine's DC entry does, costs a pattern compare, and a first factor that
   // picks the same pivots as last time costs a pivot compare. The first
-  // factor itself always runs, as in the reference.
+  // factor itself always runs, as in the reference (its pivot pass checks
+  // every column, even when it starts from the last pivots found).
   gk::Plan plan;
   PlanDev pd;
   gk::Plan sym_plan;

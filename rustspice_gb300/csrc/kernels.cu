@@ -6,7 +6,10 @@
 //                    discovers the pivot sequence. k_first_factor_s keeps the
 //                    working column and each column's update operands in
 //                    shared memory; k_first_factor is the fallback for blocks
-//                    too large for that.
+//                    too large for that. From 512 rows on the host runs the
+//                    same pass as refactorizations in their pivot-pass mode
+//                    (PivotCheck) instead, and these kernels only when that
+//                    does not settle.
 //  * refactor      - left-looking refactorization with frozen pivots. Warps
 //                    take columns in increasing order from an atomic counter
 //                    and wait on per-column completion flags of exactly the
