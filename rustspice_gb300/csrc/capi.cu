@@ -102,16 +102,14 @@ std::vector<i32> make_tasks(const gk::Plan& p, bool transpose) {
 // solve order, the coupling rows, the forward sweep and the backward sweep,
 // cut so that the slots each chunk needs are contiguous and at most
 // gk::kSolveChunk long; consecutive pieces share a chunk while their slots fit.
-void make_cta_solve(const gk::Plan& p, std::vector<i32>& chunk, std::vector<i32>& op) {
-  chunk.clear();
-  op.clear();
+// Appends the schedule of the given BTF blocks, in that order.
+void cta_solve_blocks(const gk::Plan& p, const std::vector<int>& blocks, std::vector<i32>& chunk,
+                      std::vector<i32>& op) {
   struct Piece {
     int code, a, b, lo, hi;  // slot range [lo, hi), empty when lo == hi
   };
   std::vector<Piece> ps;
-  const bool fwd = p.offd_lower;
-  for (int bb = 0; bb < p.nblocks; ++bb) {
-    const int b = fwd ? bb : p.nblocks - 1 - bb;
+  for (const int b : blocks) {
     const int b0 = p.block_ptr[b], b1 = p.block_ptr[b + 1];
     if (p.offd_ptr[b1] > p.offd_ptr[b0]) ps.push_back({0, b0, b1, 0, 0});
     std::vector<std::pair<int, int>> cut;  // column pieces
@@ -133,7 +131,7 @@ void make_cta_solve(const gk::Plan& p, std::vector<i32>& chunk, std::vector<i32>
                     direct ? 0 : hi});
     }
   }
-  int lo = 0, hi = 0, o0 = 0;
+  int lo = 0, hi = 0, o0 = (int)(op.size() / 3);
   auto close = [&]() {
     const int o1 = (int)(op.size() / 3);
     if (o1 > o0) chunk.insert(chunk.end(), {lo, hi, o0, o1});
@@ -162,13 +160,51 @@ void make_cta_solve(const gk::Plan& p, std::vector<i32>& chunk, std::vector<i32>
   close();
 }
 
+void make_cta_solve(const gk::Plan& p, std::vector<i32>& chunk, std::vector<i32>& op) {
+  chunk.clear();
+  op.clear();
+  std::vector<int> blocks(p.nblocks);
+  for (int bb = 0; bb < p.nblocks; ++bb) blocks[bb] = p.offd_lower ? bb : p.nblocks - 1 - bb;
+  cta_solve_blocks(p, blocks, chunk, op);
+}
+
+// The one-block solve split over thread blocks, for plans of several BTF
+// blocks without coupling (each BTF block's solve is then independent):
+// consecutive BTF blocks are grouped up to max(largest block, n / SMs) rows,
+// and group g gets grp[4g..4g+3] = first row, end row, first chunk, end
+// chunk. Returns the largest group's rows, or 0 when the plan does not
+// qualify.
+int make_cta_groups(const gk::Plan& p, int sms, std::vector<i32>& grp, std::vector<i32>& chunk,
+                    std::vector<i32>& op) {
+  grp.clear();
+  chunk.clear();
+  op.clear();
+  if (p.nblocks < 2 || (!p.offd_ptr.empty() && p.offd_ptr.back() > 0)) return 0;
+  int maxb = 0;
+  for (int b = 0; b < p.nblocks; ++b) maxb = std::max(maxb, p.block_ptr[b + 1] - p.block_ptr[b]);
+  const int target = std::max(maxb, (p.n + sms - 1) / std::max(sms, 1));
+  int rows = 0;
+  for (int b = 0; b < p.nblocks;) {
+    int e = b + 1;
+    while (e < p.nblocks && p.block_ptr[e + 1] - p.block_ptr[b] <= target) ++e;
+    std::vector<int> blocks;
+    for (int k = b; k < e; ++k) blocks.push_back(k);
+    const int c0 = (int)(chunk.size() / 4);
+    cta_solve_blocks(p, blocks, chunk, op);
+    grp.insert(grp.end(), {p.block_ptr[b], p.block_ptr[e], c0, (int)(chunk.size() / 4)});
+    rows = std::max(rows, p.block_ptr[e] - p.block_ptr[b]);
+    b = e;
+  }
+  return rows;
+}
+
 // Device copy of a Plan.
 struct PlanDev {
   DBuf<i32> col_ptr, dslot, slot_row, upd_ptr, upd_dst, col_single, amap_ptr, amap_idx,
       offd_ptr, offd_col, offd_raw, offdT_ptr, offdT_row, offdT_raw, lrow_ptr, lrow_col,
       lrow_slot, urow_ptr, urow_col,
       urow_slot, in_row, out_col, pcol_ptr, pcol_raw, pcol_q, pos_block, block_ptr, task,
-      ttask, cs_chunk, cs_op;
+      ttask, cs_chunk, cs_op, cs_grp, cs_gchunk, cs_gop;
   gk::DPlan dp{}, dpt{};
   int64_t updates = 0;  // multiply-subtract pairs of one refactorization
 
@@ -192,10 +228,14 @@ struct PlanDev {
     std::vector<i32> t = make_tasks(p, false), tt = make_tasks(p, true);
     if (e == cudaSuccess) e = task.upload(t, s);
     if (e == cudaSuccess) e = ttask.upload(tt, s);
-    std::vector<i32> hc, ho;
+    std::vector<i32> hc, ho, hg, hgc, hgo;
     make_cta_solve(p, hc, ho);
     if (e == cudaSuccess) e = cs_chunk.upload(hc, s);
     if (e == cudaSuccess) e = cs_op.upload(ho, s);
+    const int grp_rows = make_cta_groups(p, sm_count(), hg, hgc, hgo);
+    if (e == cudaSuccess) e = cs_grp.upload(hg, s);
+    if (e == cudaSuccess) e = cs_gchunk.upload(hgc, s);
+    if (e == cudaSuccess) e = cs_gop.upload(hgo, s);
     updates = (int64_t)p.upd_dst.size();
     gk::DPlan d{};
     d.n = p.n;
@@ -203,6 +243,11 @@ struct PlanDev {
     d.cs_nchunk = (int)(hc.size() / 4);
     d.cs_chunk = cs_chunk.p;
     d.cs_op = cs_op.p;
+    d.cs_ngrp = (int)(hg.size() / 4);
+    d.cs_grp_rows = grp_rows;
+    d.cs_grp = cs_grp.p;
+    d.cs_gchunk = cs_gchunk.p;
+    d.cs_gop = cs_gop.p;
     d.nslots = p.nslots();
     d.nblocks = p.nblocks;
     d.ntask = (int)t.size();
@@ -445,6 +490,7 @@ struct gpuklu_handle {
   unsigned epoch = 0, sepoch = 0;
   int64_t factor_count = 0, refactor_count = 0;
   bool cta_ref = false, cta_sol = false;  // one-block refactor / solve for this plan
+  bool cta_grp = false;  // the one-block solve over groups of uncoupled BTF blocks
   // Plans with up to this many multiply-subtract pairs refactor in one block.
   // FP64 issue on one SM (a warp instruction per 16 cycles) bounds that
   // kernel: the 32x32 diode mesh (273k pairs) already refactors faster over
@@ -501,6 +547,11 @@ struct gpuklu_handle {
     const bool allow = !(ob && ob[0] == '0');
     cta_ref = allow && pd.updates <= kOneBlockUpdates && gk::refactor_cta_fits(pd.dp);
     cta_sol = allow && gk::solve_cta_fits(pd.dp);
+    // the solve split over groups of uncoupled BTF blocks when one block does
+    // not hold the plan (GPUKLU_SOLVE_GROUPS=1: whenever the plan has groups)
+    const char* eg = getenv("GPUKLU_SOLVE_GROUPS");
+    const bool prefer_grp = eg && eg[0] == '1';
+    cta_grp = allow && (prefer_grp || !cta_sol) && gk::solve_groups_fit(pd.dp);
     return GPUKLU_OK;
   }
 
@@ -728,8 +779,11 @@ struct gpuklu_handle {
 
   // Solve with rhs in d_rhs; result in d_out (original column order).
   int solve_on_device(bool transpose, bool sync) {
-    if (cta_sol && !transpose) {
-      gk::launch_solve_cta(pd.dp, d_rhs.p, d_ax.p, d_lu.p, d_out.p, stream);
+    if ((cta_sol || cta_grp) && !transpose) {
+      if (cta_grp)
+        gk::launch_solve_groups(pd.dp, d_rhs.p, d_ax.p, d_lu.p, d_out.p, stream);
+      else
+        gk::launch_solve_cta(pd.dp, d_rhs.p, d_ax.p, d_lu.p, d_out.p, stream);
       if (!sync) return GPUKLU_OK;
       return check_status("solve");
     }
@@ -2979,6 +3033,11 @@ int64_t gpuklu_plan_array(const gpuklu_plan* P, const char* name, int64_t* out, 
     return (int64_t)v.size();
   };
   if (k == "info") return put(P->info);
+  if (k == "cs_grp" || k == "cs_gchunk" || k == "cs_gop") {  // its grouped form
+    std::vector<i32> hg, hc, ho;  // grouped for 152 SMs (the device path asks the device)
+    make_cta_groups(p, 152, hg, hc, ho);
+    return put(k == "cs_grp" ? hg : (k == "cs_gchunk" ? hc : ho));
+  }
   if (k == "cs_chunk" || k == "cs_op") {  // the one-block solve's schedule
     std::vector<i32> hc, ho;
     make_cta_solve(p, hc, ho);

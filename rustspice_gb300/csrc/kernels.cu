@@ -749,30 +749,45 @@ __global__ void __launch_bounds__(1024) k_refactor_cta(DPlan P, const double* __
 // backward over columns [a, b); direct: a column larger than a chunk, read
 // from memory. Shared: w[n] f64, 2 x chunk values f64, then (i32) 2 x chunk
 // rows, col_ptr[n+1], dslot[n], offd_ptr[n+1] (when there is coupling).
+//
+// With grouped != 0 the block is one of P.cs_ngrp: it solves rows [r0, r1)
+// (whole uncoupled BTF blocks) with its own chunk range; the shared arrays
+// then cover only those rows and are indexed by position - r0.
 __global__ void __launch_bounds__(256) k_solve_cta(DPlan P, const double* __restrict__ rhs,
                                                    const double* __restrict__ ax,
                                                    const double* __restrict__ lu, double* out,
-                                                   int chunk) {
+                                                   int chunk, int grouped) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int n = P.n, tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x, lane = tid & 31;
+  int r0 = 0, r1 = P.n, c0 = 0, c1 = P.cs_nchunk;
+  const int *CH = P.cs_chunk, *OP = P.cs_op;
+  if (grouped) {
+    const int* g = P.cs_grp + 4 * blockIdx.x;
+    r0 = g[0];
+    r1 = g[1];
+    c0 = g[2];
+    c1 = g[3];
+    CH = P.cs_gchunk;
+    OP = P.cs_gop;
+  }
+  const int m = r1 - r0;
   const bool coupled = P.noffd > 0;
   double* const w = reinterpret_cast<double*>(smem_raw);
-  double* const bval = w + n;
+  double* const bval = w + m;
   int* const brow = reinterpret_cast<int*>(bval + 2 * chunk);
   int* const scp = brow + 2 * chunk;
-  int* const sds = scp + n + 1;
-  int* const sop = sds + n;
-  for (int i = tid; i <= n; i += blockDim.x) {
-    cp_async4(&scp[i], &P.col_ptr[i]);
-    if (i < n) cp_async4(&sds[i], &P.dslot[i]);
-    if (coupled) cp_async4(&sop[i], &P.offd_ptr[i]);
+  int* const sds = scp + m + 1;
+  int* const sop = sds + m;
+  for (int i = tid; i <= m; i += blockDim.x) {
+    cp_async4(&scp[i], &P.col_ptr[r0 + i]);
+    if (i < m) cp_async4(&sds[i], &P.dslot[r0 + i]);
+    if (coupled) cp_async4(&sop[i], &P.offd_ptr[r0 + i]);
   }
-  for (int i = tid; i < n; i += blockDim.x) w[i] = rhs[P.in_row[i]];
+  for (int i = tid; i < m; i += blockDim.x) w[i] = rhs[P.in_row[r0 + i]];
   cp_async_wait_all();
-  const int nchunk = P.cs_nchunk;
   const int nprod = blockDim.x - 32;
   auto load = [&](int c) {
-    const int lo = P.cs_chunk[4 * c], hi = P.cs_chunk[4 * c + 1];
+    const int lo = CH[4 * c], hi = CH[4 * c + 1];
     double* const bv = bval + (c & 1) * chunk;
     int* const br = brow + (c & 1) * chunk;
     for (int s = lo + tid - 32; s < hi; s += nprod) {  // all copies in flight at once
@@ -781,17 +796,17 @@ __global__ void __launch_bounds__(256) k_solve_cta(DPlan P, const double* __rest
     }
     cp_async_wait_all();
   };
-  if (tid >= 32 && nchunk > 0) load(0);
+  if (tid >= 32 && c1 > c0) load(c0);
   __syncthreads();
-  for (int c = 0; c < nchunk; ++c) {
+  for (int c = c0; c < c1; ++c) {
     if (tid >= 32) {
-      if (c + 1 < nchunk) load(c + 1);
+      if (c + 1 < c1) load(c + 1);
     } else {
-      const int lo = P.cs_chunk[4 * c], o0 = P.cs_chunk[4 * c + 2], o1 = P.cs_chunk[4 * c + 3];
+      const int lo = CH[4 * c], o0 = CH[4 * c + 2], o1 = CH[4 * c + 3];
       const double* const bv = bval + (c & 1) * chunk - lo;  // indexed by slot
       const int* const br = brow + (c & 1) * chunk - lo;
       for (int o = o0; o < o1; ++o) {
-        const int code = P.cs_op[3 * o], a = P.cs_op[3 * o + 1], b = P.cs_op[3 * o + 2];
+        const int code = OP[3 * o], a = OP[3 * o + 1] - r0, b = OP[3 * o + 2] - r0;
         // forward: L columns ascending. The next column's range is read, and
         // this column's first rows and values are loaded, before the value
         // of x(j) is: only the subtraction waits for the previous column.
@@ -807,13 +822,13 @@ __global__ void __launch_bounds__(256) k_solve_cta(DPlan P, const double* __rest
             int r = 0;
             double v = 0.0;
             if (q < cq1) {
-              r = R[q];
+              r = R[q] - r0;
               v = V[q];
             }
             const double xj = w[j];
             if (q < cq1) w[r] = w[r] - v * xj;
             for (int qq = q + 32; qq < cq1; qq += 32) {
-              const int rr = R[qq];
+              const int rr = R[qq] - r0;
               w[rr] = w[rr] - V[qq] * xj;
             }
             __syncwarp();
@@ -826,13 +841,13 @@ __global__ void __launch_bounds__(256) k_solve_cta(DPlan P, const double* __rest
             int r = 0;
             double v = 0.0;
             if (q < ds) {
-              r = R[q];
+              r = R[q] - r0;
               v = V[q];
             }
             const double xj = w[j] / V[ds];
             if (q < ds) w[r] = w[r] - v * xj;
             for (int qq = q + 32; qq < ds; qq += 32) {
-              const int rr = R[qq];
+              const int rr = R[qq] - r0;
               w[rr] = w[rr] - V[qq] * xj;
             }
             __syncwarp();
@@ -844,7 +859,8 @@ __global__ void __launch_bounds__(256) k_solve_cta(DPlan P, const double* __rest
         if ((code & 3) == 0) {  // coupling to the blocks solved before
           for (int i = a + lane; i < b; i += 32) {
             double v = w[i];
-            for (int e = sop[i]; e < sop[i + 1]; ++e) v = v - ax[P.offd_raw[e]] * w[P.offd_col[e]];
+            for (int e = sop[i]; e < sop[i + 1]; ++e)
+              v = v - ax[P.offd_raw[e]] * w[P.offd_col[e] - r0];
             w[i] = v;
           }
         } else if ((code & 3) == 1) {
@@ -863,7 +879,7 @@ __global__ void __launch_bounds__(256) k_solve_cta(DPlan P, const double* __rest
     }
     __syncthreads();
   }
-  for (int i = tid; i < n; i += blockDim.x) out[P.out_col[i]] = w[i];
+  for (int i = tid; i < m; i += blockDim.x) out[P.out_col[r0 + i]] = w[i];
 }
 
 // --------------------------------------------------------------- devices
@@ -1503,10 +1519,11 @@ void launch_refactor_cta(const DPlan& P, const double* ax, double* lu, int* stat
 }
 
 namespace {
-size_t solve_cta_bytes(const DPlan& P) {
-  return (size_t)8 * P.n + (size_t)24 * kSolveChunk + (size_t)4 * (2 * (size_t)P.n + 1) +
-         (P.noffd > 0 ? (size_t)4 * (P.n + 1) : 0) + 16;
+size_t solve_cta_bytes(const DPlan& P, int rows) {
+  return (size_t)8 * rows + (size_t)24 * kSolveChunk + (size_t)4 * (2 * (size_t)rows + 1) +
+         (P.noffd > 0 ? (size_t)4 * (rows + 1) : 0) + 16;
 }
+size_t solve_cta_bytes(const DPlan& P) { return solve_cta_bytes(P, P.n); }
 }  // namespace
 
 bool solve_cta_fits(const DPlan& P) {
@@ -1518,7 +1535,20 @@ void launch_solve_cta(const DPlan& P, const double* rhs, const double* ax, const
   const size_t bytes = solve_cta_bytes(P);
   if (bytes > 48 * 1024)
     cudaFuncSetAttribute(k_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  k_solve_cta<<<1, 256, bytes, s>>>(P, rhs, ax, lu, out, kSolveChunk);
+  k_solve_cta<<<1, 256, bytes, s>>>(P, rhs, ax, lu, out, kSolveChunk, 0);
+}
+
+bool solve_groups_fit(const DPlan& P) {
+  return P.cs_ngrp > 0 && P.noffd == 0 &&
+         solve_cta_bytes(P, P.cs_grp_rows) <= (size_t)smem_optin();
+}
+
+void launch_solve_groups(const DPlan& P, const double* rhs, const double* ax, const double* lu,
+                         double* out, cudaStream_t s) {
+  const size_t bytes = solve_cta_bytes(P, P.cs_grp_rows);
+  if (bytes > 48 * 1024)
+    cudaFuncSetAttribute(k_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k_solve_cta<<<P.cs_ngrp, 256, bytes, s>>>(P, rhs, ax, lu, out, kSolveChunk, 1);
 }
 
 void launch_solve(const DPlan& P, const double* rhs, const double* ax, const double* lu,

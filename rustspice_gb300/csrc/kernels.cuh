@@ -19,6 +19,11 @@ struct DPlan {
   int noffd;                    // block-coupling entries
   int cs_nchunk;                // one-block solve schedule (k_solve_cta)
   const int *cs_chunk, *cs_op;
+  // The same solve with one thread block per group of consecutive BTF blocks
+  // (plans without block coupling): group g covers rows [grp[4g], grp[4g+1])
+  // and chunks [grp[4g+2], grp[4g+3]) of cs_gchunk / cs_gop.
+  int cs_ngrp, cs_grp_rows;     // groups; rows of the largest
+  const int *cs_grp, *cs_gchunk, *cs_gop;
 };
 
 // Device form of a compiled circuit (device list + stamp-to-slot map).
@@ -200,6 +205,11 @@ bool refactor_cta_fits(const DPlan& P);
 void launch_refactor_cta(const DPlan& P, const double* ax, double* lu, int* status,
                          cudaStream_t s, const PivotCheck& pc = PivotCheck());
 bool solve_cta_fits(const DPlan& P);
+// One block per group of uncoupled BTF blocks (cs_grp); fits when the
+// largest group's rows fit one block's shared memory.
+bool solve_groups_fit(const DPlan& P);
+void launch_solve_groups(const DPlan& P, const double* rhs, const double* ax, const double* lu,
+                         double* out, cudaStream_t s);
 void launch_solve_cta(const DPlan& P, const double* rhs, const double* ax, const double* lu,
                       double* out, cudaStream_t s);
 void launch_solve(const DPlan& P, const double* rhs, const double* ax, const double* lu,

@@ -161,7 +161,7 @@ class Plan:
              "offd_ptr", "offd_col", "offd_raw", "in_pos", "out_pos", "block_ptr", "col_single",
              "pcol_ptr", "pcol_raw", "pcol_q", "pos_block", "raw_slot", "row_perm",
              "lrow_ptr", "lrow_col", "lrow_slot", "urow_ptr", "urow_col", "urow_slot",
-             "cs_chunk", "cs_op", "task", "ttask"]
+             "cs_chunk", "cs_op", "cs_grp", "cs_gchunk", "cs_gop", "task", "ttask"]
 
     def __init__(self, n, ap, ai, pivot_mode=PIVOT_REFERENCE, row_perm=None):
         L = lib()

@@ -275,6 +275,59 @@ def solve_one_block(P: native.Plan, ax, lu, rhs):
     return out
 
 
+def solve_groups(P: native.Plan, ax, lu, rhs):
+    """The one-block solve split over thread blocks (cs_grp): every group
+    sweeps its own chunks with its rows in a local array indexed by position
+    minus its first row. Checks that the groups cover the rows in order, that
+    their chunk ranges cover the schedule in order, and that every op and
+    every row an update writes lies inside its group."""
+    n = P.n
+    grp = P.cs_grp.reshape(-1, 4)
+    ch, op = P.cs_gchunk.reshape(-1, 4), P.cs_gop.reshape(-1, 3)
+    assert grp.shape[0] > 0 and grp[0, 0] == 0 and grp[-1, 1] == n
+    assert grp[0, 2] == 0 and grp[-1, 3] == ch.shape[0] and ch[-1, 3] == op.shape[0]
+    in_row = np.zeros(n, np.int64)
+    in_row[P.in_pos] = np.arange(n)
+    x = np.zeros(n)
+    for g in range(grp.shape[0]):
+        r0, r1, c0, c1 = (int(v) for v in grp[g])
+        if g + 1 < grp.shape[0]:
+            assert grp[g + 1, 0] == r1 and grp[g + 1, 2] == c1
+        w = np.asarray(rhs, np.float64)[in_row[r0:r1]].copy()
+        for c in range(c0, c1):
+            lo, hi, o0, o1 = (int(v) for v in ch[c])
+            assert 0 <= lo <= hi <= P.nslots and hi - lo <= SOLVE_CHUNK
+
+            def at(q, direct):
+                if not direct:
+                    assert lo <= q < hi
+                return lu[q], int(P.slot_row[q])
+
+            for o in range(o0, o1):
+                code, a, b = (int(v) for v in op[o])
+                direct = bool(code & 4)
+                assert r0 <= a < b <= r1 and code & 3 != 0
+                if code & 3 == 1:
+                    for j in range(a, b):
+                        xj = w[j - r0]
+                        for q in range(P.dslot[j] + 1, P.col_ptr[j + 1]):
+                            val, r = at(q, direct)
+                            assert j < r < r1
+                            w[r - r0] = w[r - r0] - val * xj
+                else:
+                    for j in range(b - 1, a - 1, -1):
+                        ds = P.dslot[j]
+                        dv, _ = at(ds, direct)
+                        xj = w[j - r0] / dv
+                        for q in range(P.col_ptr[j], ds):
+                            val, r = at(q, direct)
+                            assert r0 <= r < j
+                            w[r - r0] = w[r - r0] - val * xj
+                        w[j - r0] = xj
+        x[r0:r1] = w
+    return x[P.out_pos]
+
+
 class EmulatedSolver:
     """LinearSolver call sequence over the emulated kernels."""
 

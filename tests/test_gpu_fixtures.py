@@ -83,6 +83,27 @@ def test_pivot_pass_refactorizations(mode, kind, kernels, monkeypatch):
 
 
 @pytest.mark.parametrize("mode,kind", MODES, ids=["reference", "exact"])
+def test_grouped_one_block_solve(mode, kind, monkeypatch):
+    """The one-block solve split over thread blocks (one per group of
+    uncoupled BTF blocks), forced on systems whose whole plan would also fit
+    one block: solutions equal to the oracle's bit for bit."""
+    from test_plan_parity import GROUP_SYSTEMS
+    monkeypatch.setenv("GPUKLU_SOLVE_GROUPS", "1")
+    for name, ap, ai, ax, b in GROUP_SYSTEMS:
+        n = len(ap) - 1
+        g = GpuKluSolver(n, pivot_mode=mode)
+        x = _gpu_solve(g, ap, ai, ax, b)
+        _, xo = _oracle_solve(kind, ap, ai, ax, b)
+        assert np.array_equal(x, xo), name
+        ax2 = ax * (1.0 + 0.05 * np.random.default_rng(1).standard_normal(len(ax)))
+        x = _gpu_solve(g, ap, ai, ax2, b)  # a refactorization, then the solve again
+        s, _ = _oracle_solve(kind, ap, ai, ax, b)
+        assert s.factor(ap, ai, ax2) == 0
+        st, xo = s.solve(b)
+        assert st == 0 and np.array_equal(x, xo), name
+
+
+@pytest.mark.parametrize("mode,kind", MODES, ids=["reference", "exact"])
 def test_kats(mode, kind, kernels):
     for k in KATS["solve"]:
         n = len(k["ap"]) - 1

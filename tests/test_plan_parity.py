@@ -14,8 +14,8 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as po
-from plan_emulator import (SOLVE_CHUNK, EmulatedSolver, first_factor, solve_one_block,
-                            staged_first_factor)
+from plan_emulator import (SOLVE_CHUNK, EmulatedSolver, first_factor, solve_groups,
+                            solve_one_block, staged_first_factor)
 from rustspice_gb300 import circuits as cz
 from rustspice_gb300 import native as N
 
@@ -170,6 +170,52 @@ def test_one_block_solve_direct_column(mode, kind):
     assert st == 0
     xb = solve_one_block(es.plan, es.ax, es.lu, rhs)
     assert np.array_equal(xb, xo)
+
+
+def _disjoint_meshes(sides, seed):
+    """Block-diagonal MNA system of independent diode meshes (BTF finds one
+    block per mesh, with no coupling between them)."""
+    rng = np.random.default_rng(seed)
+    aps, ais, axs, rhss, off = [], [], [], [], 0
+    for side in sides:
+        c = cz.mesh_dc(side=side, ndiodes=side, seed=int(rng.integers(1000)))
+        n, ap, ai, ax, rhs = po.mna(c, rng.uniform(0, 0.7, c.node_count))
+        aps.append(ap[1:] + (aps[-1][-1] if aps else 0))
+        ais.append(ai + off)
+        axs.append(ax)
+        rhss.append(rhs)
+        off += n
+    ap = np.concatenate([[0], *aps]).astype(np.int64)
+    return ap, np.concatenate(ais), np.concatenate(axs), np.concatenate(rhss)
+
+
+GROUP_SYSTEMS = [s for s in SYSTEMS if s[0] in ("block_diagonal_4", "chain8", "chain40",
+                                                 "adder_dcop_01")]
+GROUP_SYSTEMS.append(("meshes", *_disjoint_meshes([6, 9, 4, 12, 7, 5, 10], 3)))
+
+
+@pytest.mark.parametrize("mode,kind", MODES, ids=["reference", "exact"])
+@pytest.mark.parametrize("sysm", GROUP_SYSTEMS, ids=[s[0] for s in GROUP_SYSTEMS])
+def test_grouped_one_block_solve(sysm, mode, kind):
+    """The one-block solve split over thread blocks, one per group of
+    uncoupled BTF blocks: the groups' schedules stay inside their rows, and
+    the result is the row-ordered solve's (and the oracle's) bit for bit."""
+    name, ap, ai, ax, rhs = sysm
+    n = len(ap) - 1
+    es = EmulatedSolver(mode)
+    es.factor(n, ap, ai, ax)
+    P = es.plan
+    if len(P.cs_grp) == 0:  # the exact mode keeps BTF coupling: no groups
+        assert P.noffdiag > 0 and mode == N.PIVOT_EXACT
+        return
+    assert P.noffdiag == 0 and len(P.cs_grp) // 4 >= 2
+    xg = solve_groups(P, es.ax, es.lu, rhs)
+    assert np.array_equal(xg, es.solve(rhs))
+    s = po.Solver(kind, n)
+    s.prepare(n)
+    assert s.factor(ap, ai, ax) == 0
+    st, xo = s.solve(rhs)
+    assert st == 0 and np.array_equal(xg, xo)
 
 
 def test_one_block_schedule_mesh():
