@@ -194,6 +194,33 @@ GROUP_SYSTEMS = [s for s in SYSTEMS if s[0] in ("block_diagonal_4", "chain8", "c
 GROUP_SYSTEMS.append(("meshes", *_disjoint_meshes([6, 9, 4, 12, 7, 5, 10], 3)))
 
 
+def _two_stars(n, seed):
+    """Two independent hub systems of n rows each: every group holds a column
+    longer than a chunk (a direct piece read straight from memory)."""
+    ap1, ai1, ax1, b1 = _star(n, seed)
+    ap2, ai2, ax2, b2 = _star(n, seed + 1)
+    ap = np.concatenate([ap1, ap2[1:] + ap1[-1]])
+    return ap, np.concatenate([ai1, ai2 + n]), np.concatenate([ax1, ax2]), np.concatenate([b1, b2])
+
+
+@pytest.mark.parametrize("mode,kind", MODES, ids=["reference", "exact"])
+def test_grouped_solve_direct_columns(mode, kind):
+    """Groups whose blocks hold a column longer than a chunk: the direct
+    pieces stay inside their group and the result is the oracle's."""
+    n = SOLVE_CHUNK + 300
+    ap, ai, ax, rhs = _two_stars(n, 5)
+    es = EmulatedSolver(mode)
+    es.factor(2 * n, ap, ai, ax)
+    P = es.plan
+    assert len(P.cs_grp) // 4 == 2 and np.any(P.cs_gop.reshape(-1, 3)[:, 0] & 4)
+    xg = solve_groups(P, es.ax, es.lu, rhs)
+    s = po.Solver(kind, 2 * n)
+    s.prepare(2 * n)
+    assert s.factor(ap, ai, ax) == 0
+    st, xo = s.solve(rhs)
+    assert st == 0 and np.array_equal(xg, xo)
+
+
 @pytest.mark.parametrize("mode,kind", MODES, ids=["reference", "exact"])
 @pytest.mark.parametrize("sysm", GROUP_SYSTEMS, ids=[s[0] for s in GROUP_SYSTEMS])
 def test_grouped_one_block_solve(sysm, mode, kind):
