@@ -120,7 +120,7 @@ void* gpuklu_stream(gpuklu_handle* h);
 
 /* Solve without allocating: for callers that cannot call cudaMalloc where
  * they solve (a stream being captured into a CUDA graph, a host callback, a
- * real-time loop with a fixed memory budget, a runtime that only lends
+ * real-time loop with a fixed memory limit, a runtime that only lends
  * buffers). No counterpart in the reference; it is an addition of this
  * library. Solves A x = b with the handle's current factors: d_rhs (n
  * values, device memory) is read, d_x (n values, device memory) receives x.

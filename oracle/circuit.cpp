@@ -1,5 +1,5 @@
 // Oracle (test infrastructure only): MNA assembly, device stamps and the
-// Newton driver restated from the reference.
+// Newton loop restated from the reference.
 //   SparseBuilder / StampContext   crates/sim-core/src/mna.rs:89-168, 320-347, 452-525
 //   stamps                         crates/sim-core/src/stamp.rs:242-297, 351-545, 759-787
 //   level-1 MOSFET                 crates/sim-devices/src/bsim/evaluate.rs:285-356,

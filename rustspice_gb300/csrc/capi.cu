@@ -1,5 +1,5 @@
 // Host side of libgpuklu: the GpuKluSolver handle behind the LinearSolver C
-// ABI, the device-stamp compiler, the device-resident Newton driver and the
+// ABI, the device-stamp compiler, the device-resident Newton loop and the
 // batched Newton. The numeric work is all in kernels.cu; this file owns the
 // device memory, the pattern cache and the call sequence.
 #include <cuda_runtime.h>
@@ -2930,7 +2930,7 @@ int gpuklu_bbd_newton_dc(gpuklu_bbd* b, gpuklu_circuit* c, const gpuklu_newton_c
 // ====================================================================== no-allocation solve
 // Some callers cannot call cudaMalloc at the point where they solve: code
 // running while a stream is being captured into a CUDA graph, a simulator
-// step inside a host callback or a real-time loop with a fixed memory budget,
+// step inside a host callback or a real-time loop with a fixed memory limit,
 // or a foreign runtime that owns all device memory and only lends buffers.
 // gpuklu_solve_device_noalloc serves them: the caller passes device buffers
 // for the right-hand side and the solution, and the solve kernel's scratch
