@@ -39,12 +39,21 @@ would run it:
   iterations (100), ``vntol`` absolute (1e-6), ``reltol`` relative (1e-3),
   ``gmin`` (1e-12).
 
-Subcircuits, includes, parameters expressions and the other device kinds are
-outside this path and raise ``NetlistError``.
+* ``.include`` (netlist.rs:1205-1260, ``load`` only, as the reference's
+  ``parse_netlist_file``): a line whose trimmed, lower-cased text starts with
+  ``.include`` is replaced by the named file (second token, quotes stripped,
+  relative to the including file's directory), recursively; a file already
+  on the include path is a circular reference. A missing path, an unreadable
+  file and a cycle are errors.
+
+Subcircuits, parameter expressions and the other device kinds are outside
+this path and raise ``NetlistError`` (so does ``.include`` in text given to
+``compile_deck``, which has no directory to resolve it against).
 """
 from __future__ import annotations
 
 import dataclasses
+import os
 import re
 
 import numpy as np
@@ -300,6 +309,50 @@ def compile_deck(text: str, name: str = "") -> Deck:
     return Deck(c, order, dev_names, options, initial, analyses or [".op"])
 
 
+def _path_key(path: str):
+    """A path compared as the reference's PathBuf compares: by components,
+    with ``.`` after the first one and empty components dropped."""
+    parts = path.split("/")
+    return (parts[0],) + tuple(q for q in parts[1:] if q not in ("", "."))
+
+
+def read_with_includes(path: str, visited: set, errors: list) -> str:
+    """The deck text with its ``.include`` lines replaced by the included
+    files (netlist.rs:1205-1260): every other line is kept with a newline; an
+    included file's text is followed by one more newline."""
+    key = _path_key(path)
+    if key in visited:
+        errors.append(f"include circular reference: {path}")
+        return ""
+    visited.add(key)
+    try:
+        with open(path) as f:
+            content = f.read()
+    except OSError:
+        errors.append(f"cannot read file: {path}")
+        content = ""
+    base = os.path.dirname(path) or "."
+    out = []
+    for line in content.splitlines():
+        t = line.strip()
+        if t.lower().startswith(".include"):
+            toks = t.split()
+            inc = toks[1].strip('"') if len(toks) > 1 else ""
+            if not inc:
+                errors.append(f"include statement missing path: {path}")
+                continue
+            out.append(read_with_includes(os.path.join(base, inc), visited, errors))
+            out.append("\n")
+        else:
+            out.append(line + "\n")
+    return "".join(out)
+
+
 def load(path: str) -> Deck:
-    with open(path) as f:
-        return compile_deck(f.read(), name=path)
+    """A deck file with its includes resolved (the reference's
+    ``parse_netlist_file``), compiled as ``compile_deck`` does."""
+    errors: list = []
+    text = read_with_includes(path, set(), errors)
+    if errors:
+        raise NetlistError("; ".join(errors))
+    return compile_deck(text, name=path)

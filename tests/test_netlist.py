@@ -121,3 +121,38 @@ def test_reference_fixture_decks():
     # the BSIM3 deck is outside this path
     with pytest.raises(nl.NetlistError):
         nl.load(os.path.join(REF, "nmos_dc.cir"))
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
+def test_reference_include_fixture():
+    """The reference's include test deck (netlist_tests.rs:111-127): the
+    child's resistor is read in place of the .include line."""
+    deck = nl.load(os.path.join(REF, "include_parent.cir"))
+    assert deck.device_names == ["R1", "R2"]
+    assert deck.node_names == ["0", "in", "out"]
+    assert deck.circuit.nodes[:, :2].tolist() == [[1, 2], [2, 0]]
+    assert deck.circuit.p[:, 0].tolist() == [1000.0, 2000.0]
+
+
+def test_includes(tmp_path):
+    """Includes resolve against the including file's directory, recursively,
+    with quotes stripped; a cycle, a missing file and a missing path are
+    errors."""
+    sub = tmp_path / "lib"
+    sub.mkdir()
+    (sub / "leaf.cir").write_text("R3 b 0 3k\n")
+    (sub / "mid.cir").write_text("R2 a b 2k\n.INCLUDE leaf.cir\n")
+    (tmp_path / "top.cir").write_text('* top\nV1 a 0 DC 1\n.include "lib/mid.cir"\nR1 a 0 1k\n.end\n')
+    deck = nl.load(str(tmp_path / "top.cir"))
+    assert deck.device_names == ["V1", "R2", "R3", "R1"]
+    assert deck.circuit.p[1:, 0].tolist() == [2000.0, 3000.0, 1000.0]
+    (tmp_path / "a.cir").write_text("R1 x 0 1\n.include b.cir\n")
+    (tmp_path / "b.cir").write_text("R2 x 0 1\n.include ./a.cir\n")
+    with pytest.raises(nl.NetlistError, match="circular"):
+        nl.load(str(tmp_path / "a.cir"))
+    (tmp_path / "c.cir").write_text("R1 x 0 1\n.include nothere.cir\n")
+    with pytest.raises(nl.NetlistError, match="cannot read file"):
+        nl.load(str(tmp_path / "c.cir"))
+    (tmp_path / "d.cir").write_text("R1 x 0 1\n.include\n")
+    with pytest.raises(nl.NetlistError, match="missing path"):
+        nl.load(str(tmp_path / "d.cir"))
