@@ -46,9 +46,22 @@ would run it:
   on the include path is a circular reference. A missing path, an unreadable
   file and a cycle are errors.
 
-Subcircuits, parameter expressions and the other device kinds are outside
-this path and raise ``NetlistError`` (so does ``.include`` in text given to
-``compile_deck``, which has no directory to resolve it against).
+* ``.param`` and subcircuits (netlist.rs:857-925, 1262-1460, 1557-1955):
+  parameters evaluate in order (numbers with suffixes, names, ``+ - * / ^``
+  left-associative, a ``-`` after no value taken as ``0 -``, ``max min abs
+  if``); a device's value, model and parameter values resolve from its
+  scope's table, the global one, or their own evaluation, else stay as
+  written; ``X`` lines expand the subcircuit named by their last token:
+  devices become ``<instance>.<name>``, ports map to the instance's nodes,
+  other nodes become ``<instance>:<node>``, nested instances expand in the
+  enclosing scope (its own, body ``.param`` and instance parameters), and a
+  ``.model`` in a body is kept as ``<instance>.<name>``, which a device's
+  unscoped model name does not reach. A ``.subckt`` ends at the first
+  ``.ends``.
+
+The other device kinds are outside this path and raise ``NetlistError`` (so
+does ``.include`` in text given to ``compile_deck``, which has no directory
+to resolve it against).
 """
 from __future__ import annotations
 
@@ -169,6 +182,370 @@ def parse(text: str):
     return stmts, errors
 
 
+# ------------------------------------------------------------ parameters
+# .param values, subcircuit parameters and device fields are evaluated as the
+# reference's elaboration does (crates/sim-core/src/netlist.rs:1262-1350,
+# 1557-1860): tables map lower-cased names to text - an evaluated value in
+# the text Rust's f64 Display gives it, or the raw text when the expression
+# does not evaluate.
+
+def _f64_text(v: float) -> str:
+    """Rust's ``f64`` Display: the shortest round-trip digits, positional."""
+    if v != v:
+        return "NaN"
+    if v in (float("inf"), float("-inf")):
+        return "inf" if v > 0 else "-inf"
+    import decimal
+    t = format(decimal.Decimal(repr(v)), "f")
+    if "." in t:
+        t = t.rstrip("0").rstrip(".")
+    return t
+
+
+def _f64_parse(text: str):
+    """Rust's ``str::parse::<f64>`` (no suffix)."""
+    t = text.strip()
+    return float(t) if _FLOAT.match(t) else None
+
+
+def _tokens(expr: str):
+    """netlist.rs:1589-1633: numbers (with suffix) and identifiers split at
+    blanks and at ``+ - * / ^ , ( )``."""
+    out, buf = [], []
+
+    def push():
+        if buf:
+            word = "".join(buf)
+            x = parse_number(word)
+            out.append(("num", x) if x is not None else ("id", word))
+            buf.clear()
+
+    for ch in expr:
+        if ch.isspace():
+            push()
+        elif ch in "+-*/^":
+            push()
+            out.append(("op", ch))
+        elif ch == ",":
+            push()
+            out.append(("comma", None))
+        elif ch == "(":
+            push()
+            out.append(("lp", None))
+        elif ch == ")":
+            push()
+            out.append(("rp", None))
+        else:
+            buf.append(ch)
+    push()
+    return out
+
+
+_PREC = {"+": 1, "-": 1, "*": 2, "/": 2, "^": 3}
+
+
+def _rpn(tokens):
+    """netlist.rs:1681-1772 (shunting-yard): a ``-`` after no value gets a 0
+    pushed before it; operators of higher or equal precedence pop (all of
+    them left-associative); an identifier before ``(`` is a function whose
+    argument count the commas give; a parenthesis left at the end fails."""
+    output, ops, argc = [], [], []
+    prev_value = False
+    for i, tok in enumerate(tokens):
+        kind, val = tok
+        nxt = tokens[i + 1] if i + 1 < len(tokens) else None
+        if kind == "num":
+            output.append(tok)
+        elif kind == "id":
+            if nxt is not None and nxt[0] == "lp":
+                ops.append(("func", [val, 0]))
+            else:
+                output.append(tok)
+        elif kind == "op":
+            if not prev_value and val == "-":
+                output.append(("num", 0.0))
+            while ops and ops[-1][0] == "op" and _PREC[ops[-1][1]] >= _PREC[val]:
+                output.append(ops.pop())
+            ops.append(tok)
+        elif kind == "comma":
+            while ops and ops[-1][0] != "lp":
+                output.append(ops.pop())
+            if argc:
+                argc[-1] += 1
+        elif kind == "lp":
+            if ops and ops[-1][0] == "func":
+                argc.append(0)
+            ops.append(tok)
+        elif kind == "rp":
+            while ops:
+                top = ops.pop()
+                if top[0] == "lp":
+                    break
+                output.append(top)
+            if ops and ops[-1][0] == "func":
+                name = ops.pop()[1][0]
+                output.append(("call", (name, (argc.pop() if argc else 0) + 1)))
+        prev_value = kind in ("num", "id", "rp")
+    while ops:
+        top = ops.pop()
+        if top[0] in ("lp", "rp"):
+            return None
+        output.append(top)
+    return output
+
+
+def _lookup(name, local, parent, glob):
+    key = name.lower()
+    for table in (local, parent, glob):
+        if key in table:
+            text = table[key]
+            x = parse_number(text)
+            return x if x is not None else _f64_parse(text)
+    return None
+
+
+def _rmax(a, b):  # f64::max / f64::min: a NaN operand yields the other
+    return b if a != a else (a if b != b else (a if a > b else b))
+
+
+def _rmin(a, b):
+    return b if a != a else (a if b != b else (a if a < b else b))
+
+
+def _evaluate(expr, local, parent, glob):
+    """netlist.rs:1564-1587, 1781-1845: the value of an expression, or None."""
+    toks = _tokens(expr)
+    if not toks:
+        return None
+    rpn = _rpn(toks)
+    if rpn is None:
+        return None
+    stack = []
+    with np.errstate(all="ignore"):
+        for kind, val in rpn:
+            if kind == "num":
+                stack.append(val)
+            elif kind == "id":
+                x = _lookup(val, local, parent, glob)
+                if x is None:
+                    return None
+                stack.append(x)
+            elif kind == "op":
+                if len(stack) < 2:
+                    return None
+                b, a = stack.pop(), stack.pop()
+                fa, fb = np.float64(a), np.float64(b)
+                r = {"+": fa + fb, "-": fa - fb, "*": fa * fb, "/": fa / fb,
+                     "^": np.power(fa, fb)}[val]
+                stack.append(float(r))
+            elif kind == "call":
+                name, n = val
+                if len(stack) < n:
+                    return None
+                args = [stack.pop() for _ in range(n)][::-1]
+                f = name.lower()
+                if f == "max" and n == 2:
+                    stack.append(_rmax(*args))
+                elif f == "min" and n == 2:
+                    stack.append(_rmin(*args))
+                elif f == "abs" and n == 1:
+                    stack.append(abs(args[0]))
+                elif f == "if" and n == 3:
+                    stack.append(args[1] if args[0] != 0.0 else args[2])
+                else:
+                    return None
+            else:
+                return None
+    return stack[0] if len(stack) == 1 else None
+
+
+def _param_entry(table, key, value, parent, glob):
+    x = _evaluate(value, table, parent, glob)
+    table[key.lower()] = _f64_text(x) if x is not None else value
+
+
+def _resolve(local, glob, token):
+    """netlist.rs:1338-1349: a field's text from the local table, the global
+    one, or its own evaluation; None leaves the field as written."""
+    key = token.lower()
+    if key in local:
+        return local[key]
+    if key in glob:
+        return glob[key]
+    x = _evaluate(token, local, {}, glob)
+    return None if x is None else _f64_text(x)
+
+
+def _fields(st):
+    """Positions of a device line's nodes, value and model in its positional
+    tokens (split_device_fields, netlist.rs:398-520, for the kinds this
+    reader maps; other kinds keep every token as written)."""
+    a, k = st.args, st.kind
+    if k in "RCLVI":
+        if len(a) >= 3:
+            if a[2].lower() == "dc" and len(a) >= 4:
+                return [0, 1], 3, None
+            if k in "VI" and _is_waveform(a[2]):
+                return [0, 1], None, None
+            return [0, 1], 2, None
+        return list(range(len(a))), None, None
+    if k == "D":
+        return ([0, 1], None, 2) if len(a) >= 3 else (list(range(len(a))), None, None)
+    if k == "M":
+        if len(a) >= 5:
+            return [0, 1, 2, 3], None, 4
+        if len(a) == 4:
+            return [0, 1, 2], None, 3
+        return list(range(len(a))), None, None
+    if k == "X":
+        if len(a) >= 2:
+            return list(range(len(a) - 1)), None, len(a) - 1
+        return list(range(len(a))), None, None
+    return [], None, None
+
+
+def _is_waveform(tok):
+    u = tok.upper()
+    return u in ("AC", "SIN", "PULSE", "EXP", "SFFM", "PWL") or u.startswith(
+        ("SIN(", "PULSE(", "EXP(", "SFFM(", "PWL("))
+
+
+def _apply_params(st, local, glob):
+    """netlist.rs:1316-1336: the value, the model and the parameter values
+    of a device resolved in its scope."""
+    _, vi, mi = _fields(st)
+    args = list(st.args)
+    for i in (vi, mi):
+        if i is not None:
+            r = _resolve(local, glob, args[i])
+            if r is not None:
+                args[i] = r
+    params = []
+    for k, v in st.params:
+        r = _resolve(local, glob, v)
+        params.append((k, v if r is None else r))
+    return dataclasses.replace(st, args=args, params=params)
+
+
+@dataclasses.dataclass
+class Subckt:
+    name: str
+    ports: list
+    params: list
+    body: list
+    line: int
+
+
+def _extract_subckts(stmts):
+    """netlist.rs:1351-1406: a ``.subckt`` takes the statements up to the
+    next ``.ends`` (the first one: definitions do not nest)."""
+    top, defs, i = [], [], 0
+    while i < len(stmts):
+        st = stmts[i]
+        if st.control == ".subckt":
+            if not st.args:
+                raise NetlistError(f"line {st.line}: subckt statement missing name")
+            body, i, closed = [], i + 1, False
+            while i < len(stmts):
+                if stmts[i].control == ".ends":
+                    closed, i = True, i + 1
+                    break
+                body.append(stmts[i])
+                i += 1
+            if not closed:
+                raise NetlistError(f"line {st.line}: subckt {st.args[0]} missing .ends")
+            defs.append(Subckt(st.args[0], st.args[1:], list(st.params), body, st.line))
+        else:
+            top.append(st)
+            i += 1
+    return top, defs
+
+
+def _body_params(body):
+    """netlist.rs:1408-1427: the ``.param`` entries of a body outside the
+    ``.subckt`` ... ``.ends`` ranges inside it."""
+    out, depth = [], 0
+    for st in body:
+        if st.control == ".subckt":
+            depth += 1
+        elif st.control == ".ends":
+            depth = max(0, depth - 1)
+        elif st.control == ".param" and depth == 0:
+            out.extend(st.params)
+    return out
+
+
+def _local_params(d, inst, parent, glob):
+    """netlist.rs:1283-1314: the subcircuit's own parameters, then its body's
+    ``.param`` entries, then the instance's, each evaluated in order."""
+    table = {}
+    for k, v in list(d.params) + _body_params(d.body) + list(inst.params):
+        _param_entry(table, k, v, parent, glob)
+    return table
+
+
+def _expand(inst, d, defs, local, glob, models):
+    """netlist.rs:1869-1955: the body's devices named ``<instance>.<name>``,
+    ports mapped to the instance's nodes (case-insensitively), other nodes
+    named ``<instance>:<node>``; nested instances expanded in the scope of
+    this one; the body's ``.model`` cards kept as ``<instance>.<name>``."""
+    body, nested = _extract_subckts(d.body)
+    scope = {x.name: x for x in nested}
+    for k, v in defs.items():
+        scope.setdefault(k, v)
+    inst_nodes = [inst.args[i] for i in _fields(inst)[0]]
+    ports = {p.lower(): n for p, n in zip(d.ports, inst_nodes)}
+    out = []
+    for st in body:
+        if st.control == ".model":
+            if st.args:
+                models.append(dataclasses.replace(st, args=[f"{inst.name}.{st.args[0]}"] +
+                                                  st.args[1:]))
+            continue
+        if st.control:
+            continue
+        nodes, _, mi = _fields(st)
+        args = list(st.args)
+        for i in nodes:
+            args[i] = ports.get(args[i].lower(), f"{inst.name}:{args[i]}")
+        sc = dataclasses.replace(st, name=f"{inst.name}.{st.name}", args=args)
+        if st.kind == "X":
+            child = scope.get(args[mi]) if mi is not None else None
+            if child is None:
+                raise NetlistError(f"line {st.line}: subcircuit not defined: {sc.name}")
+            out.extend(_expand(sc, child, scope, _local_params(child, sc, local, glob), glob,
+                               models))
+            continue
+        out.append(_apply_params(sc, local, glob))
+    return out
+
+
+def elaborate(stmts):
+    """netlist.rs:857-925: the top-level controls, the flat device list
+    (subcircuit instances expanded, parameters applied) and the ``.model``
+    cards found inside subcircuits."""
+    top, defs = _extract_subckts(stmts)
+    glob = {}
+    for st in top:
+        if st.control == ".param":
+            for k, v in st.params:
+                _param_entry(glob, k, v, glob, glob)
+    subckts = {d.name: d for d in defs}
+    controls, devices, models = [], [], []
+    for st in top:
+        if st.control:
+            controls.append(st)
+        elif st.kind == "X":
+            mi = _fields(st)[2]
+            d = subckts.get(st.args[mi]) if mi is not None else None
+            if d is None:
+                raise NetlistError(f"line {st.line}: subcircuit not defined: {st.name}")
+            devices.extend(_expand(st, d, subckts, _local_params(d, st, {}, glob), glob, models))
+        else:
+            devices.append(_apply_params(st, {}, glob))
+    return controls, devices, models
+
+
 @dataclasses.dataclass
 class Deck:
     circuit: Circuit
@@ -211,6 +588,7 @@ def compile_deck(text: str, name: str = "") -> Deck:
     stmts, errors = parse(text)
     if errors:
         raise NetlistError("; ".join(f"line {n}: {m}" for n, m in errors))
+    controls, devices, sub_models = elaborate(stmts)
     names = {"0": 0}
     order = ["0"]
 
@@ -221,9 +599,7 @@ def compile_deck(text: str, name: str = "") -> Deck:
         return names[s]
 
     models, options, initial, analyses = {}, {}, {}, []
-    for st in stmts:  # controls first (as the reference builds the circuit)
-        if not st.control:
-            continue
+    for st in controls:  # controls first (as the reference builds the circuit)
         if st.control == ".model":
             if len(st.args) < 2:
                 raise NetlistError(f"line {st.line}: model statement missing name/type")
@@ -239,14 +615,15 @@ def compile_deck(text: str, name: str = "") -> Deck:
                 x = parse_number(v)
                 if key.startswith("v(") and key.endswith(")") and x is not None:
                     initial[node(key[2:-1].strip())] = x
-        elif st.control in (".subckt", ".include", ".inc", ".lib", ".param"):
+        elif st.control in (".include", ".inc", ".lib"):
             raise NetlistError(f"line {st.line}: {st.control} is outside this path")
         elif st.control in (".op", ".dc", ".tran", ".ac"):
             analyses.append(st.control)
+    for st in sub_models:  # cards from subcircuit bodies, under <instance>.<name>
+        if len(st.args) >= 2:
+            models[st.args[0].lower()] = {k.lower(): v for k, v in st.params}
     t, nd, p, dev_names = [], [], [], []
-    for st in stmts:
-        if st.control:
-            continue
+    for st in devices:
         prm = {}
         a = st.args
         if st.kind in "RCVI":

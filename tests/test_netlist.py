@@ -156,3 +156,89 @@ def test_includes(tmp_path):
     (tmp_path / "d.cir").write_text("R1 x 0 1\n.include\n")
     with pytest.raises(nl.NetlistError, match="missing path"):
         nl.load(str(tmp_path / "d.cir"))
+
+
+def _elab(text):
+    stmts, errors = nl.parse(text)
+    assert not errors
+    return nl.elaborate(stmts)[1]
+
+
+@pytest.mark.parametrize("text,name,args", [
+    # crates/sim-core/tests/netlist_tests.rs:80-90, 93-100, 103-109, 131-137, 148-154,
+    # 157-163, 186-193, 321-327, 330-340
+    (".subckt buf in out\nR1 in out 1k\n.ends\nX1 a b buf\n.end\n", "X1.R1", ["a", "b", "1000"]),
+    (".param RVAL=5k\nR1 in out RVAL\n.end\n", "R1", ["in", "out", "5000"]),
+    (".subckt buf in out RVAL=1k\nR1 in out RVAL\n.ends\nX1 a b buf RVAL=2k\n.end\n", "X1.R1",
+     ["a", "b", "2000"]),
+    (".param RVAL=1k+1k\nR1 in out RVAL\n.end\n", "R1", ["in", "out", "2000"]),
+    (".param RVAL=max(1k,2k)\nR1 in out RVAL\n.end\n", "R1", ["in", "out", "2000"]),
+    (".param RVAL=if(1,1k,2k)\nR1 in out RVAL\n.end\n", "R1", ["in", "out", "1000"]),
+    (".param RVAL=-1k+2^3\nR1 in out RVAL\n.end\n", "R1", ["in", "out", "-992"]),
+    (".subckt buf in out\n.param RVAL=3k\nR1 in out RVAL\n.ends\nX1 a b buf\n.end\n", "X1.R1",
+     ["a", "b", "3000"]),
+    (".subckt leaf a b\nR1 a b 1k\n.ends\n.subckt mid in out\nX1 in out leaf\n.ends\n"
+     "Xtop n1 n2 mid\n.end\n", "Xtop.X1.R1", ["n1", "n2", "1000"]),
+])
+def test_reference_elaboration_vectors(text, name, args):
+    d = _elab(text)
+    assert len(d) == 1 and d[0].name == name and d[0].args == args
+
+
+@pytest.mark.parametrize("expr,text", [
+    ("2*-3", "-3"),            # a '-' after an operator is '0 -' placed after that operator
+    ("2^3^2", "64"),           # '^' is left-associative
+    ("(1k+1k)/4", "500"),
+    ("min(3,abs(-7))", "3"),
+    ("1/0", "inf"),
+    ("1e-3", "1e-3"),          # the tokenizer splits at '-': no value, kept as written
+    ("sqrt(4)", "sqrt(4)"),    # unknown function: kept as written
+    ("(1+2", "(1+2"),          # unbalanced: kept as written
+    ("1u*3", "0.000003"),
+])
+def test_expression_rules(expr, text):
+    d = _elab(f".param P={expr}\nR1 a 0 P\n")
+    assert d[0].args[2] == text
+
+
+def test_subckt_deck_matches_flat_deck():
+    """An inverter chain through a subcircuit compiles to exactly the flat
+    deck's device list (names, nodes, values): ports map, parameters resolve
+    in order (body .param, then the instance's)."""
+    sub = (".model nm nmos level=1 vto=0.5\n"
+           ".subckt inv in out vdd vss\nM1 out in vss vss nm W=2u\nR1 vdd out RL\n"
+           ".param RL=20k\n.ends\n"
+           "V1 vdd 0 DC 1.2\nV2 a 0 DC 0.9\nX1 a b vdd 0 inv\nX2 b c vdd 0 inv RL=10k\n.op\n")
+    flat = (".model nm nmos level=1 vto=0.5\nV1 vdd 0 DC 1.2\nV2 a 0 DC 0.9\n"
+            "M1 b a 0 0 nm W=2u\nR1 vdd b 20000\nM2 c b 0 0 nm W=2u\nR2 vdd c 10000\n.op\n")
+    s, f = nl.compile_deck(sub), nl.compile_deck(flat)
+    assert s.node_names == ["0", "vdd", "a", "b", "c"] == f.node_names
+    assert s.device_names == ["V1", "V2", "X1.M1", "X1.R1", "X2.M1", "X2.R1"]
+    assert np.array_equal(s.circuit.type, f.circuit.type)
+    assert np.array_equal(s.circuit.nodes, f.circuit.nodes)
+    assert np.array_equal(s.circuit.p, f.circuit.p)
+
+
+def test_subckt_scoping_rules():
+    """As the reference's expansion does it: a body node that is not a port,
+    ground included, becomes <instance>:<node>; a body .model is kept as
+    <instance>.<name>, which the body's devices do not reach (they see the
+    global card of that name, or none); an instance parameter evaluates in
+    the enclosing instance's scope."""
+    deck = nl.compile_deck(".subckt s a\nR1 a 0 1k\n.ends\nX1 n s\nR2 n 0 1k\n")
+    assert deck.node_names == ["0", "n", "X1:0"]
+    text = (".subckt s a b\n.model dm d is=1e-9\nD1 a b dm\n.ends\n"
+            "V1 p 0 DC 0.5\nX1 p 0 s\n")
+    assert nl.compile_deck(text).circuit.p[1, 0] == 1e-14
+    assert nl.compile_deck(text + ".model dm d is=2e-9\n").circuit.p[1, 0] == 2e-9
+    d = _elab(".subckt leaf a b R=1\nR1 a b R\n.ends\n.subckt mid a b K=3\nX1 a b leaf R=K*2\n"
+              ".ends\nXt p q mid K=5\n")
+    assert d[0].name == "Xt.X1.R1" and d[0].args == ["p", "q", "10"]
+
+
+@pytest.mark.parametrize("text", [".subckt s a\nR1 a 0 1\n", "X1 a b nosuch\n",
+                                  ".subckt\nR1 a 0 1\n.ends\n",
+                                  ".subckt s a\nX1 a q\n.ends\nX2 n s\n"])
+def test_subckt_errors(text):
+    with pytest.raises(nl.NetlistError):
+        nl.compile_deck(text)
