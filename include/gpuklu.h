@@ -119,19 +119,21 @@ void* gpuklu_stream(gpuklu_handle* h);
 #define GPUKLU_NOALLOC_MAX_N 65536
 
 /* Solve without allocating: for callers that cannot call cudaMalloc where
- * they solve (a stream being captured into a CUDA graph, a host callback, a
- * real-time loop with a fixed memory limit, a runtime that only lends
- * buffers). No counterpart in the reference; it is an addition of this
- * library. Solves A x = b with the handle's current factors: d_rhs (n
- * values, device memory) is read, d_x (n values, device memory) receives x.
- * The solve kernel's scratch (about 1.5 MB, held by every GPU that loads the
- * library until the process exits) is a fixed array inside the library, not
- * the handle's buffers, so the call allocates nothing. The first call on a
- * device looks up that array's device address; make that first call before
- * any stream capture. All calls share the one array: calls that overlap on
- * the GPU (two handles on different streams at once) race, so serialise
- * them. n above GPUKLU_NOALLOC_MAX_N gives GPUKLU_INVALID_MATRIX. Returns
- * after the solve has finished (it waits on the handle's stream). */
+ * they solve - a simulator step run from a host callback where allocation is
+ * not allowed, a real-time loop with a fixed device-memory budget, or a
+ * foreign runtime that owns all device memory and only lends buffers. No
+ * counterpart in the reference; it is an addition of this library. Solves
+ * A x = b with the handle's current factors: d_rhs (n values, device memory)
+ * is read, d_x (n values, device memory) receives x. The solve kernel's
+ * scratch (about 1.5 MB, held by every GPU that loads the library until the
+ * process exits) is a fixed array inside the library, not the handle's
+ * buffers, so the call allocates nothing. The first call on a device looks
+ * up that array's device address; make that first call before any stream
+ * capture. All calls share the one array and each clears the flags it needs:
+ * calls that overlap on the GPU (two handles on different streams at once)
+ * race, so serialise them. n above GPUKLU_NOALLOC_MAX_N gives
+ * GPUKLU_INVALID_MATRIX. The call reads the solve's status back and waits
+ * for the handle's stream, so it returns after the solve has finished. */
 int gpuklu_solve_device_noalloc(gpuklu_handle* h, const double* d_rhs, double* d_x);
 
 /* ------------------------------------------------ device stamping + Newton */

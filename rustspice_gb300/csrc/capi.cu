@@ -2928,16 +2928,17 @@ int gpuklu_bbd_newton_dc(gpuklu_bbd* b, gpuklu_circuit* c, const gpuklu_newton_c
 }  // extern "C"
 
 // ====================================================================== no-allocation solve
-// Some callers cannot call cudaMalloc at the point where they solve: code
-// running while a stream is being captured into a CUDA graph, a simulator
-// step inside a host callback or a real-time loop with a fixed memory limit,
-// or a foreign runtime that owns all device memory and only lends buffers.
+// Some callers cannot call cudaMalloc at the point where they solve: a
+// simulator step inside a host callback where allocation is not allowed, a
+// real-time loop with a fixed device-memory budget, or a foreign runtime that
+// owns all device memory and only lends buffers.
 // gpuklu_solve_device_noalloc serves them: the caller passes device buffers
 // for the right-hand side and the solution, and the solve kernel's scratch
 // (the forward and backward vectors, the per-row completion flags and the
 // task counter) lives in the file-scope array below instead of the handle's
 // buffers. Every GPU that loads the library holds this array until the
-// process exits.
+// process exits. The call ends by reading the kernel's status back and
+// synchronising the handle's stream.
 namespace {
 constexpr size_t kNoallocFlagBytes = 256 + 2 * (size_t)GPUKLU_NOALLOC_MAX_N * sizeof(unsigned);
 constexpr size_t kNoallocBytes = kNoallocFlagBytes + 2 * (size_t)GPUKLU_NOALLOC_MAX_N * sizeof(double);

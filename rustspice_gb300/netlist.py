@@ -144,6 +144,18 @@ class Statement:
     params: list = dataclasses.field(default_factory=list)
 
 
+def rust_lines(text: str):
+    """Lines as Rust's ``str::lines`` gives them (the reference reads decks
+    with it, netlist.rs:150, 1238): split on ``\n`` only, one trailing
+    ``\r`` removed from each line, no empty line after a final newline."""
+    parts = text.split("\n")
+    last = parts.pop()  # the text after the final newline (no line ending)
+    out = [q[:-1] if q.endswith("\r") else q for q in parts]
+    if last:
+        out.append(last)
+    return out
+
+
 def parse(text: str):
     """Statements of a deck and the errors the reader recorded (line, text)."""
     stmts, errors, pending, pending_line = [], [], "", 0
@@ -163,7 +175,7 @@ def parse(text: str):
             return
         stmts.append(Statement(line_no, name=first, kind=kind, args=args, params=params))
 
-    lines = text.splitlines()
+    lines = rust_lines(text)
     for no, raw in enumerate(lines, 1):
         s = raw.strip()
         if not s or s.startswith("*"):
@@ -504,6 +516,11 @@ def _expand(inst, d, defs, local, glob, models):
             continue
         if st.control:
             continue
+        if st.kind == "M" and len(st.args) == 4:
+            # drain gate source model: the reader adds the bulk "0" when it
+            # splits the line (netlist.rs:450-454), before the expansion maps
+            # the nodes, so inside a body it becomes "<instance>:0"
+            st = dataclasses.replace(st, args=st.args[:3] + ["0"] + st.args[3:])
         nodes, _, mi = _fields(st)
         args = list(st.args)
         for i in nodes:
@@ -710,7 +727,7 @@ def read_with_includes(path: str, visited: set, errors: list) -> str:
         content = ""
     base = os.path.dirname(path) or "."
     out = []
-    for line in content.splitlines():
+    for line in rust_lines(content):
         t = line.strip()
         if t.lower().startswith(".include"):
             toks = t.split()

@@ -1,8 +1,7 @@
 """Writes the golden fixtures under tests/golden/ from the reference's own tests.
 
-Run in a checkout next to the reference (its root is the first argument,
-default /root/reference); the fixtures it writes are committed, so nothing
-at test time reads the reference.
+Run it with the reference checkout's root as its one argument; the fixtures
+it writes are committed, so nothing at test time reads the reference.
 
 * ``kats.json`` -- the known-answer systems of the reference's solver and
   stamp tests, restated as data with the file:line each comes from.
@@ -17,6 +16,9 @@ at test time reads the reference.
   (tests/fixtures/netlists/began_small_pgrid.sp, R/I/V only) as a device
   list: nodes numbered by first appearance with ground "0" as node 0
   (crates/sim-core/src/circuit.rs:37-57), devices in netlist order.
+* ``decks/`` -- the reference's fixture decks the netlist reader's tests read
+  (tests/fixtures/netlists/{basic_dc,nmos_dc,include_parent,include_child}.cir
+  and began_small_pgrid.sp), copied byte for byte.
 """
 from __future__ import annotations
 
@@ -206,7 +208,20 @@ def main(ref: str) -> None:
     np.savez_compressed(os.path.join(HERE, "began_small_pgrid.npz"), node_count=nc, type=t,
                         nodes=nd, p=p)
     print("began_small_pgrid", nc, len(t))
+    os.makedirs(os.path.join(HERE, "decks"), exist_ok=True)
+    for name in DECKS:
+        with open(os.path.join(ref, "tests/fixtures/netlists", name), "rb") as f:
+            data = f.read()
+        with open(os.path.join(HERE, "decks", name), "wb") as f:
+            f.write(data)
+        print("deck", name, len(data))
+
+
+DECKS = ("basic_dc.cir", "nmos_dc.cir", "include_parent.cir", "include_child.cir",
+         "began_small_pgrid.sp")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference checkout root>")
+    main(sys.argv[1])

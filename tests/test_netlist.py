@@ -2,8 +2,9 @@
 
 Small decks written here exercise each rule (numbers, continuation lines,
 parameters, models, MOSFET level and polarity, node numbering); the
-reference's own fixture decks, where the reference tree is present, are read
-and solved with the oracle for the answers its tests expect. No GPU.
+reference's own fixture decks (copied into tests/golden/decks by
+tests/golden/make_golden.py) are read and solved with the oracle for the
+answers its tests expect. No GPU.
 """
 import os
 
@@ -14,8 +15,8 @@ from oracle import pyoracle as po
 from rustspice_gb300 import circuits as cz
 from rustspice_gb300 import netlist as nl
 
-REF = "/root/reference/tests/fixtures/netlists"
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+REF = os.path.join(GOLD, "decks")
 
 
 @pytest.mark.parametrize("tok,val", [("1k", 1e3), ("2.2MEG", 2.2e6), ("10u", 1e-5), ("3m", 3e-3),
@@ -103,7 +104,6 @@ def test_outside_the_path(text):
         nl.compile_deck(text)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
 def test_reference_fixture_decks():
     # the reference's end-to-end divider: vin = 1, vout = 2/3
     deck = nl.load(os.path.join(REF, "basic_dc.cir"))
@@ -123,7 +123,6 @@ def test_reference_fixture_decks():
         nl.load(os.path.join(REF, "nmos_dc.cir"))
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
 def test_reference_include_fixture():
     """The reference's include test deck (netlist_tests.rs:111-127): the
     child's resistor is read in place of the .include line."""
@@ -242,3 +241,43 @@ def test_subckt_scoping_rules():
 def test_subckt_errors(text):
     with pytest.raises(nl.NetlistError):
         nl.compile_deck(text)
+
+
+def test_three_node_mosfet_bulk_inside_a_subcircuit():
+    """A MOSFET written with drain, gate and source gets the bulk "0" when
+    the reader splits its line (netlist.rs:450-454), before the expansion
+    maps nodes, so inside a body the bulk is "<instance>:0"
+    (map_subckt_node, netlist.rs:1429-1439) while at the top level it is
+    ground."""
+    deck = nl.compile_deck("""* 3-node level-1 MOSFETs
+.model nm nmos level=1 vto=0.5
+.subckt cell d g
+M1 d g 0 nm
+.ends
+VDD vdd 0 1.2
+X1 vdd in cell
+M2 vdd in 0 nm
+.end
+""")
+    names = deck.node_names
+    c = deck.circuit
+    i1, i2 = deck.device_names.index("X1.M1"), deck.device_names.index("M2")
+    assert [names[k] for k in c.nodes[i1]] == ["vdd", "in", "X1:0", "X1:0"]
+    assert [names[k] for k in c.nodes[i2]] == ["vdd", "in", "0", "0"]
+
+
+@pytest.mark.parametrize("text,lines", [
+    ("", []), ("a", ["a"]), ("a\n", ["a"]), ("a\n\n", ["a", ""]),
+    ("a\r\nb\r\n", ["a", "b"]), ("a\rb\n", ["a\rb"]), ("x\fy\nz\r", ["x\fy", "z\r"]),
+    ("p\x85q\u2028r\vs\n", ["p\x85q\u2028r\vs"])])
+def test_line_splitting_as_rust_str_lines(text, lines):
+    """Only \\n ends a line; one \\r before it is dropped (Rust's
+    str::lines, which the reference reads decks with, netlist.rs:150,1238)."""
+    assert nl.rust_lines(text) == lines
+
+
+def test_lone_carriage_return_keeps_one_line():
+    """R1 and R2 written on one line split by a lone CR are one statement
+    for the reference, so the deck has one resistor with extra tokens."""
+    deck = nl.compile_deck("V1 a 0 1\nR1 a 0 1k\rR2 a 0 2k\n.end\n")
+    assert deck.device_names == ["V1", "R1"]

@@ -1,8 +1,8 @@
 """The no-allocation solve entry point, against the regular solve.
 
 gpuklu_solve_device_noalloc exists for callers that cannot call cudaMalloc
-where they solve (for example while a stream is being captured into a CUDA
-graph, or inside a runtime that only lends device buffers); its kernel
+where they solve (for example inside a runtime that owns all device memory
+and only lends buffers, or a loop with a fixed device-memory budget); its kernel
 scratch is a fixed array inside the library. This test drives it through the
 C ABI with device buffers the test owns, twice in a row with different
 right-hand sides, and requires results identical to gpuklu_solve (the same
