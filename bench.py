@@ -484,25 +484,17 @@ def run_gpu(a):
     fp64_tflops = fp64 / (ms_step * 1e-3) / 1e12
     fp64_peak = float(N.lib().gpuklu_fp64_peak_tflops())
 
-    # one-at-a-time GpuKluSolver on a sample (the metric's comparison)
-    rng = np.random.default_rng(0)
-    sample = rng.choice(B.ninst, 24, replace=False)
-    t_one, it_one = 0.0, 0
-    g = GpuKluSolver(1, pivot_mode=N.PIVOT_EXACT)
-    for i in sample:
-        c = B.circuits[B.inst_circ[i]]
-        c2 = c.__class__(**{**c.__dict__})
-        c2.p = c.p.copy()
-        c2.p[1, 0] = B.inst_val[i]
-        dc = DeviceCircuit(c2)
-        x0 = B.x0[B.x0_off[i]:B.x0_off[i] + c.node_count]
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        r = newton_dc(g, dc, cfg, x0=x0)
-        t_one += time.perf_counter() - t1
-        it_one += r.iterations_total
-        g.reset_pattern()
-    one_at_a_time = it_one / t_one
+    # converged-only rates, and the time of the instances that run to the
+    # iteration cap: the same step with only the converged instances, timed
+    # the same way (the difference is what the capped ones cost)
+    conv_mask = rs == 0
+    conv_iters = int(itt[conv_mask].sum())
+    capped = _converged_only_step(B, conv_mask, cfg, flush, dev, a.steps)
+    # one-at-a-time GpuKluSolver: the engine's DC sweep of a chain over the
+    # 61 input points, one handle per chain, the pattern analysed on the
+    # sweep's first point and reused for the others (engine.rs:684-820)
+    one = _one_at_a_time(B, cfg, torch)
+    one_at_a_time = one["value"]
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
@@ -512,7 +504,9 @@ def run_gpu(a):
         "config": {"workload": WORKLOAD, "chains": a.chains, "vin_points": a.nvin,
                    "instances": int(B.ninst), "newton_iterations_per_step": iters_per_step,
                    "converged_fraction": conv, "max_final_residual": resid,
-                   "newton": dict(wl.TIGHT), "mos_model": "level-1, consistent linearisation",
+                   "newton": dict(wl.TIGHT),
+                   "mos_model": "level-1, consistent linearisation (MC)",
+                   "pivot_mode": "exact pattern (nativeklu_exact)",
                    "initial_iterate": "logic-level nodeset",
                    "l2": "256 MB buffer written before every timed step; inputs 270 MB > L2",
                    "parallelism": f"replicas x{ws}"},
@@ -520,9 +514,10 @@ def run_gpu(a):
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": e2e_step},
         "gpu_launches": a.steps * bt.info()["launches"],
-        "one_at_a_time": {"value": one_at_a_time, "unit": UNIT,
-                          "how": "GpuKluSolver newton_dc, one instance at a time, 24 sampled",
-                          "batched_over_one_at_a_time": value / one_at_a_time},
+        "converged_iters_per_s": conv_iters / (ms_step * 1e-3),
+        "converged_solves_per_s": int(conv_mask.sum()) / (ms_step * 1e-3),
+        "capped_instances": capped,
+        "one_at_a_time": dict(one, batched_over_one_at_a_time=value / one_at_a_time),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                      "traffic_source": traffic_src,
@@ -535,6 +530,8 @@ def run_gpu(a):
         "clocks": clocks,
         "wall_s_timed": wall,
     }
+    if not a.no_secondary:
+        line["reference_level1"] = _reference_model_line(a, cfg, flush, dev, rank)
     if not a.no_cpu_baseline and rank == 0:
         line["cpu_baseline"] = cpu_baseline(B, a, cfg_dict=wl.TIGHT)
     if not a.no_secondary and rank == 0:
@@ -543,6 +540,115 @@ def run_gpu(a):
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _timed_runs(bt, cfg, flush, steps):
+    """Mean device time [ms] of `steps` runs of a batch, each behind an L2
+    flush, with CUDA events on the batch's stream."""
+    import torch
+    stream = torch.cuda.ExternalStream(bt.stream(), device=flush.device)
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            flush.fill_(1)
+            bt.run(cfg)
+        evs = []
+        for _ in range(steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            flush.fill_(1)
+            e0.record(stream)
+            bt.run(cfg)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+    return float(np.mean([e0.elapsed_time(e1) for e0, e1 in evs]))
+
+
+def _converged_only_step(B, conv, cfg, flush, dev, steps):
+    """The batch restricted to the instances that converged, timed like the
+    full step: what the instances that run to the iteration cap cost is the
+    difference."""
+    from rustspice_gb300.solver import Batch
+    idx = np.flatnonzero(conv)
+    x0 = np.concatenate([B.x0[B.x0_off[i]:B.x0_off[i] + B.circuits[B.inst_circ[i]].node_count]
+                         for i in idx])
+    off = np.concatenate([[0], np.cumsum([B.circuits[B.inst_circ[i]].node_count
+                                          for i in idx])[:-1]]).astype(np.int64)
+    bt = Batch(B.circuits, B.inst_circ[idx], B.inst_dev[idx], B.inst_val[idx], x0, off)
+    ms = _timed_runs(bt, cfg, flush, max(3, steps // 2))
+    _, itt, rs, _ = bt.results(with_x=False)
+    ph = bt.phase_ms()
+    bt.close()
+    return {"instances": int(B.ninst - len(idx)), "converged_only_ms_per_step": ms,
+            "converged_only_iterations": int(itt.sum()),
+            "converged_only_kernel_ms": {"k_batch_lanes": ph["lanes_ms"],
+                                         "k_batch_newton": ph["warps_ms"]},
+            "how": "the same batch with only the converged instances, timed the same way; "
+                   "the capped instances cost the difference to ms_per_step"}
+
+
+def _one_at_a_time(B, cfg, torch, chains=4):
+    """The plain GpuKluSolver, one operating point at a time, as the engine's
+    DC sweep runs it: per sampled chain one handle and one compiled circuit,
+    the input source set for each of the sweep's points in order, each point
+    a Newton solve from its nodeset. The first point of a chain (pattern
+    analysis and pivot pass) is reported apart."""
+    from rustspice_gb300 import native as N
+    from rustspice_gb300.solver import DeviceCircuit, GpuKluSolver, newton_dc
+    rng = np.random.default_rng(0)
+    nvin = int(np.sum(B.inst_circ == 0))
+    picks = rng.choice(len(B.circuits), chains, replace=False)
+    t_first = t_rest = 0.0
+    it_first = it_rest = 0
+    for ci in picks:
+        c = B.circuits[ci]
+        g = GpuKluSolver(1, pivot_mode=N.PIVOT_EXACT)
+        dc = DeviceCircuit(c)
+        p = c.p.copy()
+        for k in range(nvin):
+            i = ci * nvin + k
+            p[1, 0] = B.inst_val[i]
+            dc.set_params(p)
+            x0 = B.x0[B.x0_off[i]:B.x0_off[i] + c.node_count]
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            r = newton_dc(g, dc, cfg, x0=x0)
+            dt = time.perf_counter() - t1
+            if k == 0:
+                t_first += dt
+                it_first += r.iterations_total
+            else:
+                t_rest += dt
+                it_rest += r.iterations_total
+        dc.close()
+        g.close()
+    return {"value": it_rest / t_rest, "unit": UNIT,
+            "first_point_iters_per_s": it_first / t_first,
+            "first_point_ms": t_first * 1e3 / chains,
+            "how": f"GpuKluSolver newton_dc over the {nvin}-point input sweep of {chains} "
+                   "sampled chains, one handle per chain; value excludes each sweep's first "
+                   "point (analysis and pivot pass), reported apart"}
+
+
+def _reference_model_line(a, cfg, flush, dev, rank):
+    """The same workload with the reference's own level-1 evaluator (M),
+    from the same nodeset: its converged fraction and rates."""
+    from rustspice_gb300 import ranks
+    from rustspice_gb300 import workloads as wl
+    from rustspice_gb300.solver import Batch
+    B = wl.inverter_batch(a.chains, a.nvin, seed=ranks.shard_seed(rank),
+                          mos_model="reference")
+    bt = Batch(B.circuits, B.inst_circ, B.inst_dev, B.inst_val, B.x0, B.x0_off)
+    ms = _timed_runs(bt, cfg, flush, max(3, a.steps // 2))
+    _, itt, rs, _ = bt.results(with_x=False)
+    bt.close()
+    conv = rs == 0
+    return {"mos_model": "level-1 as the reference evaluates it (M)",
+            "ms_per_step": ms, "value": float(itt.sum()) / (ms * 1e-3), "unit": UNIT,
+            "newton_iterations_per_step": int(itt.sum()),
+            "converged_fraction": float(np.mean(conv)),
+            "converged_iters_per_s": float(itt[conv].sum()) / (ms * 1e-3),
+            "converged_solves_per_s": int(conv.sum()) / (ms * 1e-3)}
 
 
 def _cpu_sample(B, count, seed=1):
@@ -568,6 +674,8 @@ def _cpu_run(B, idx, threads, cfg_dict):
     it, rs, _ = po.dc_batch(circuits, ic, B.inst_dev[idx], B.inst_val[idx], "nativeklu_exact",
                             nthreads=threads, x0=x0, x0_off=off, **kw)
     dt = time.perf_counter() - t0
+    _cpu_run.last_converged_iters = int(it[rs == 0].sum())
+    _cpu_run.last_converged = int(np.sum(rs == 0))
     return int(it.sum()), dt, float(np.mean(rs == 0))
 
 
@@ -581,6 +689,8 @@ def cpu_baseline(B, a, cfg_dict):
         idx = _cpu_sample(B, count)
         iters, dt, conv = _cpu_run(B, idx, threads, cfg_dict)
     return {"value": iters / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "converged_iters_per_s": _cpu_run.last_converged_iters / dt,
+            "converged_solves_per_s": _cpu_run.last_converged / dt,
             "sample": f"{len(idx)} of {B.ninst} instances (random, seed 1), "
                       f"{iters} Newton iterations in {dt:.2f} s, converged {conv:.4f}; "
                       "oracle C++ NativeKLU (exact pivots) + reference Newton loop"}
@@ -605,6 +715,9 @@ def run_reference(a):
         tot_it = iters
     ms = float(np.mean(per)) * 1e3
     value = tot_it / (ms * 1e-3)
+    conv_rates = {"converged_iters_per_s": _cpu_run.last_converged_iters / (ms * 1e-3),
+                  "converged_solves_per_s": _cpu_run.last_converged / (ms * 1e-3),
+                  "converged_fraction": conv}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -612,6 +725,7 @@ def run_reference(a):
         "config": {"workload": WORKLOAD, "chains": a.chains, "vin_points": a.nvin,
                    "step": f"bounded sample of {len(idx)} instances per step"},
         "impl": "reference",
+        **conv_rates,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{len(idx)} of {B.ninst} instances per step (seed 1); "
                                    "oracle C++ restatement of NativeKLU (exact pivots) and the "

@@ -241,7 +241,12 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg);
 /* Results: per instance iterations (final run), total iterations, exit
  * reason, and x (n of its circuit values, at x_out + x_off[i]; x_off may be
  * NULL to skip). When x_off is the batch's own layout (consecutive
- * instances, n values each) x arrives in one copy, a DMA into pinned x_out. */
+ * instances, n values each) x arrives in one copy, a DMA into pinned x_out.
+ * An instance whose iterate turns non-finite stops there with reason 1 and,
+ * as its final run's iteration count, the cap: the count the reference
+ * reports, whose loop runs on to the cap because a non-finite entry never
+ * turns finite again (newton.rs:93-107). Its total counts the iterations the
+ * device executed, and its x is the non-finite iterate. */
 int gpuklu_batch_results(gpuklu_batch* b, int64_t* iters, int64_t* iters_total, int32_t* reason,
                          double* x_out, const int64_t* x_off);
 /* Host->device copy of new per-instance values and initial iterates

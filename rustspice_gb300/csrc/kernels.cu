@@ -1448,8 +1448,8 @@ __global__ void k_batch_newton(BatchArgs A) {
           }
         }
         if (rsn >= 0) {
-          if (sl == 0) {
-            A.iters[inst] = it;
+          if (sl == 0) {  // non-finite: the reference's run ends at the cap
+            A.iters[inst] = (rsn == 1 && nfin) ? cfg.max_iters : it;
             A.iters_total[inst] = total;
             A.reason[inst] = rsn;
           }

@@ -238,7 +238,10 @@ __global__ void k_batch_lanes(BatchArgs A) {
           }
         }
         if (rsn >= 0) {
-          A.iters[inst] = it;
+          // a run stopped at a non-finite iterate ends, in the reference, at
+          // the iteration cap (a non-finite entry never turns finite again);
+          // that is the count reported, iters_total counts executed ones
+          A.iters[inst] = (rsn == 1 && !fin) ? cfg.max_iters : it;
           A.iters_total[inst] = total;
           A.reason[inst] = rsn;
           inst = -1;

@@ -50,13 +50,19 @@ class InverterBatch:
 
 
 def inverter_batch(nchains: int = 4096, nvin: int = 61, seed: int = 3,
-                   lo: int = 8, hi: int = 256, mos_model: str = "consistent") -> InverterBatch:
+                   lo: int = 8, hi: int = 256, mos_model: str = "consistent",
+                   chain_ids=None) -> InverterBatch:
     """nchains chains x nvin input points; instance i = (chain i // nvin,
-    vin point i % nvin). The input source is device 1 of every chain."""
+    vin point i % nvin). The input source is device 1 of every chain.
+    chain_ids: only these chains of the nchains-chain workload (each keeps
+    its stage count and its seeded parameters), in the order given."""
     stages = cz.chain_lengths(nchains, lo, hi, seed)
+    ids = np.arange(nchains) if chain_ids is None else np.asarray(chain_ids, np.int64)
+    stages = stages[ids]
+    nchains = len(ids)
     vins = cz.vin_points(nvin)
-    circuits = [cz.inverter_chain(int(s), 0.0, seed=seed, chain_id=i, mos_model=mos_model)
-                for i, s in enumerate(stages)]
+    circuits = [cz.inverter_chain(int(s), 0.0, seed=seed, chain_id=int(i), mos_model=mos_model)
+                for i, s in zip(ids, stages)]
     ninst = nchains * nvin
     inst_circ = np.repeat(np.arange(nchains, dtype=np.int64), nvin)
     inst_dev = np.full(ninst, 1, np.int64)
@@ -67,6 +73,19 @@ def inverter_batch(nchains: int = 4096, nvin: int = 61, seed: int = 3,
                          for i in range(ninst)])
     return InverterBatch(circuits, inst_circ, inst_dev, inst_val, x0, x0_off, stages,
                          inst_val.copy())
+
+
+def stratified_chains(nchains: int = 4096, seed: int = 3, lo: int = 8, hi: int = 256):
+    """Ids of the first chain of every stage count lo..hi in the nchains-chain
+    workload: a sample of it that covers each chain length once."""
+    stages = cz.chain_lengths(nchains, lo, hi, seed)
+    ids = []
+    for s in range(lo, hi + 1):
+        hit = np.flatnonzero(stages == s)
+        if len(hit) == 0:
+            raise ValueError(f"no chain of {s} stages among {nchains}")
+        ids.append(int(hit[0]))
+    return np.asarray(ids, np.int64)
 
 
 # Newton settings of the parity and bench runs: the engine's option names
