@@ -588,46 +588,47 @@ def _converged_only_step(B, conv, cfg, flush, dev, steps):
 
 
 def _one_at_a_time(B, cfg, torch, chains=4):
-    """The plain GpuKluSolver, one operating point at a time, as the engine's
-    DC sweep runs it: per sampled chain one handle and one compiled circuit,
-    the input source set for each of the sweep's points in order, each point
-    a Newton solve from its nodeset. The first point of a chain (pattern
-    analysis and pivot pass) is reported apart."""
+    """The plain GpuKluSolver, one operating point at a time, as the
+    reference's DC sweep runs it (gpuklu_dc_sweep, engine.rs:684-820): per
+    sampled chain one handle, the input source stepped through the sweep's
+    points in order, one Newton solve per point on the device from the
+    point's nodeset, the pattern and pivots of the first point kept. The
+    first point (pattern analysis and pivot pass) is timed apart, from a
+    one-point sweep, and taken out of the value."""
     from rustspice_gb300 import native as N
-    from rustspice_gb300.solver import DeviceCircuit, GpuKluSolver, newton_dc
+    from rustspice_gb300.solver import DeviceCircuit, GpuKluSolver, dc_sweep
     rng = np.random.default_rng(0)
     nvin = int(np.sum(B.inst_circ == 0))
     picks = rng.choice(len(B.circuits), chains, replace=False)
-    t_first = t_rest = 0.0
-    it_first = it_rest = 0
+    t_all = t_first = 0.0
+    it_all = it_first = 0
     for ci in picks:
         c = B.circuits[ci]
         g = GpuKluSolver(1, pivot_mode=N.PIVOT_EXACT)
         dc = DeviceCircuit(c)
-        p = c.p.copy()
-        for k in range(nvin):
-            i = ci * nvin + k
-            p[1, 0] = B.inst_val[i]
-            dc.set_params(p)
-            x0 = B.x0[B.x0_off[i]:B.x0_off[i] + c.node_count]
+        idx = np.arange(ci * nvin, (ci + 1) * nvin)
+        x0 = np.stack([B.x0[B.x0_off[i]:B.x0_off[i] + c.node_count] for i in idx])
+        vals = B.inst_val[idx]
+        for npts in (1, nvin):
             torch.cuda.synchronize()
             t1 = time.perf_counter()
-            r = newton_dc(g, dc, cfg, x0=x0)
+            r = dc_sweep(g, dc, cfg, 1, vals[:npts], x0=x0[:npts], stop_on_failure=False)
             dt = time.perf_counter() - t1
-            if k == 0:
+            if npts == 1:
                 t_first += dt
-                it_first += r.iterations_total
+                it_first += int(r.iterations_total.sum())
             else:
-                t_rest += dt
-                it_rest += r.iterations_total
+                t_all += dt
+                it_all += int(r.iterations_total.sum())
         dc.close()
         g.close()
+    t_rest, it_rest = t_all - t_first, it_all - it_first
     return {"value": it_rest / t_rest, "unit": UNIT,
             "first_point_iters_per_s": it_first / t_first,
             "first_point_ms": t_first * 1e3 / chains,
-            "how": f"GpuKluSolver newton_dc over the {nvin}-point input sweep of {chains} "
-                   "sampled chains, one handle per chain; value excludes each sweep's first "
-                   "point (analysis and pivot pass), reported apart"}
+            "how": f"gpuklu_dc_sweep over the {nvin}-point input sweep of {chains} sampled "
+                   "chains (one handle per sweep, pivots of the first point kept); the first "
+                   "point's time, from a one-point sweep, is taken out of the value"}
 
 
 def _reference_model_line(a, cfg, flush, dev, rank):
@@ -652,9 +653,15 @@ def _reference_model_line(a, cfg, flush, dev, rank):
 
 
 def _cpu_sample(B, count, seed=1):
-    """Stratified sample of instances (every stage count represented)."""
+    """Whole chains sampled at random, each with all its input points (the
+    points of one chain's sweep share one solver on the CPU as on the
+    device), about `count` instances in all."""
     rng = np.random.default_rng(seed)
-    return np.sort(rng.choice(B.ninst, min(count, B.ninst), replace=False))
+    nchains = len(B.circuits)
+    per = max(1, B.ninst // nchains)
+    k = max(1, min(nchains, -(-count // per)))
+    chains = np.sort(rng.choice(nchains, k, replace=False))
+    return np.flatnonzero(np.isin(B.inst_circ, chains))
 
 
 def _cpu_run(B, idx, threads, cfg_dict):
@@ -691,7 +698,7 @@ def cpu_baseline(B, a, cfg_dict):
     return {"value": iters / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "converged_iters_per_s": _cpu_run.last_converged_iters / dt,
             "converged_solves_per_s": _cpu_run.last_converged / dt,
-            "sample": f"{len(idx)} of {B.ninst} instances (random, seed 1), "
+            "sample": f"{len(idx)} of {B.ninst} instances (whole chains at random, seed 1), "
                       f"{iters} Newton iterations in {dt:.2f} s, converged {conv:.4f}; "
                       "oracle C++ NativeKLU (exact pivots) + reference Newton loop"}
 
@@ -727,7 +734,8 @@ def run_reference(a):
         "impl": "reference",
         **conv_rates,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{len(idx)} of {B.ninst} instances per step (seed 1); "
+                         "sample": f"{len(idx)} of {B.ninst} instances per step (whole chains "
+                                   "at random, seed 1); "
                                    "oracle C++ restatement of NativeKLU (exact pivots) and the "
                                    "reference Newton loop"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

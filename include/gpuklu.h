@@ -191,6 +191,26 @@ int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_co
                      const double* x0, double* x_out, int64_t x_cap, int64_t* x_len,
                      int64_t* iters, int64_t* iters_total, int* reason);
 
+/* DC sweep (the reference's .dc, crates/sim-core/src/engine.rs:684-820) of
+ * one source: device src_dev's first parameter takes values[0..npts) in
+ * order, one Newton solve per point on the device as gpuklu_newton_dc runs
+ * it. As in the reference one solver serves the whole sweep (prepare(
+ * node_count) once, engine.rs:747), so the pattern and the pivots of the
+ * first point's first factorization are kept for every later point. x0 ==
+ * NULL: each point starts from the previous point's final iterate (the
+ * reference's continuation; after a converged point that is the full
+ * solution with its aux currents, and the convergence test then covers
+ * them too); else point k starts from x0 + k * x0_stride (node_count
+ * values). stop_on_failure != 0 ends the sweep at the first point that does
+ * not converge, as the reference does (engine.rs:785-796). Per point:
+ * x_out + k * x_stride receives n values (zero beyond *x_len[k]), iters,
+ * iters_total and reason as gpuklu_newton_dc gives them; points not run
+ * have reason -1. The circuit keeps the last value. */
+int gpuklu_dc_sweep(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_config* cfg,
+                    int64_t src_dev, const double* values, int64_t npts, const double* x0,
+                    int64_t x0_stride, int stop_on_failure, double* x_out, int64_t x_stride,
+                    int64_t* x_len, int64_t* iters, int64_t* iters_total, int* reason);
+
 /* AC small-signal sweep at a DC solution: the reference's .ac
  * (crates/sim-core/src/engine.rs:829-930) with its AC stamps (stamp.rs:
  * 1525-1747) and dense complex LU with partial pivoting (complex_solver.rs:

@@ -20,6 +20,14 @@ Circuit make_circuit(int64_t node_count, int64_t ndev, const int32_t* type,
   return c;
 }
 IVec ivec(const int64_t* p, int64_t n) { return IVec(p, p + n); }
+// The DC build closure of the sweep (engine.rs:761-775) over the current
+// source value.
+struct DcSweepCtx {
+  const Circuit* c;
+};
+MnaSystem dc_sweep_build(void* p, const Vec& x, double gmin, double scale) {
+  return build_mna(*static_cast<DcSweepCtx*>(p)->c, x, gmin, scale);
+}
 }  // namespace
 
 extern "C" {
@@ -272,13 +280,59 @@ double orc_residual(int64_t node_count, int64_t ndev, const int32_t* type,
 // inst_val[i] (inst_dev < 0: no override). Circuits are concatenated device
 // lists delimited by dev_off[ncirc + 1]. Per instance: iterations, exit
 // reason, and x (x_cap entries, zero padded).
+// The reference's DC sweep (engine.rs:684-820): one solver, prepare(
+// node_count) once (engine.rs:747) and x = zeros(node_count); per value the
+// source's value is set and run_newton_with_stepping runs from x (the
+// previous point's final iterate) or, when x0 is given, from that point's
+// own initial iterate; a point that does not converge ends the sweep when
+// stop != 0 (engine.rs:785-796). Points not run get reason -1.
+void orc_dc_sweep(int64_t node_count, int64_t ndev, const int32_t* type, const int32_t* nodes,
+                  const double* p, const char* solver_kind, int64_t max_iters, double abs_tol,
+                  double rel_tol, double gmin, int64_t gmin_steps, int64_t src_dev,
+                  const double* values, int64_t npts, const double* x0, int64_t x0_stride,
+                  int stop, double* x_out, int64_t x_stride, int64_t* x_len, int64_t* iters,
+                  int32_t* reason) {
+  Circuit c = make_circuit(node_count, ndev, type, nodes, p);
+  NewtonConfig cfg;
+  cfg.max_iters = (size_t)max_iters;
+  cfg.abs_tol = abs_tol;
+  cfg.rel_tol = rel_tol;
+  cfg.gmin = gmin;
+  cfg.gmin_steps = (size_t)gmin_steps;
+  auto s = make_solver(solver_kind, c.node_count);
+  for (int64_t k = 0; k < npts; ++k) {
+    iters[k] = 0;
+    reason[k] = -1;
+    x_len[k] = 0;
+  }
+  s->prepare(c.node_count);
+  Vec x(c.node_count, 0.0);
+  for (int64_t k = 0; k < npts; ++k) {
+    c.p[(size_t)src_dev * NPARAM] = values[k];
+    NewtonResult r;
+    if (x0) {
+      r = dc_sweep_point(c, cfg, *s, x, x0 + k * x0_stride);
+    } else {
+      DcSweepCtx ctx{&c};
+      r = run_newton_with_stepping(cfg, x, dc_sweep_build, &ctx, *s);
+    }
+    iters[k] = (int64_t)r.iterations;
+    reason[k] = r.reason;
+    x_len[k] = (int64_t)x.size();
+    for (int64_t i = 0; i < x_stride; ++i)
+      x_out[k * x_stride + i] = (size_t)i < x.size() ? x[(size_t)i] : 0.0;
+    if (r.reason != NR_CONVERGED && stop) break;
+  }
+}
+
 void orc_dc_batch(int64_t ncirc, const int64_t* dev_off, const int64_t* node_counts,
                   const int32_t* type, const int32_t* nodes, const double* p,
                   int64_t ninst, const int64_t* inst_circ, const int64_t* inst_dev,
                   const double* inst_val, const char* solver_kind, int64_t max_iters,
                   double abs_tol, double rel_tol, double gmin, int64_t gmin_steps,
                   const double* x0, const int64_t* x0_off, int64_t nthreads, int64_t* iters,
-                  int32_t* reason, double* x_out, int64_t x_cap) {
+                  int32_t* reason, double* x_out, int64_t x_cap, int sweep,
+                  int64_t* perturbed) {
   std::vector<Circuit> circs((size_t)ncirc);
   for (int64_t c = 0; c < ncirc; ++c) {
     int64_t d0 = dev_off[c], d1 = dev_off[c + 1];
@@ -291,24 +345,43 @@ void orc_dc_batch(int64_t ncirc, const int64_t* dev_off, const int64_t* node_cou
   cfg.rel_tol = rel_tol;
   cfg.gmin = gmin;
   cfg.gmin_steps = (size_t)gmin_steps;
+  // sweep != 0: each circuit's instances are the points of that circuit's
+  // DC sweep. As in the reference's sweep (engine.rs:684-820) one solver
+  // serves every point and prepare(node_count) runs once before the first,
+  // so the solver keeps the pattern and the pivots the first point's first
+  // factorization chose (native_klu.rs:1020-1148) for all later points.
+  // Unlike that sweep, every point starts from its own initial iterate and a
+  // point that fails does not end the others.
+  // sweep == 0: every instance is its own DC operating point (engine.rs:
+  // 249-283), whose prepare(node_count) resets the pattern (a size other
+  // than the matrix's, which has one aux row per voltage source), so each
+  // instance's pivots come from its own first matrix.
   std::string kind(solver_kind);
+  std::vector<std::vector<int64_t>> by_circ((size_t)ncirc);
+  for (int64_t i = 0; i < ninst; ++i) by_circ[(size_t)inst_circ[i]].push_back(i);
   std::atomic<int64_t> next(0);
   auto worker = [&]() {
     while (true) {
-      int64_t i = next.fetch_add(1);
-      if (i >= ninst) break;
-      Circuit c = circs[(size_t)inst_circ[i]];
-      if (inst_dev[i] >= 0) c.p[(size_t)inst_dev[i] * NPARAM] = inst_val[i];
-      auto s = make_solver(kind, c.node_count);
-      Vec x;
-      const double* xi = (x0 && x0_off && x0_off[i] >= 0) ? x0 + x0_off[i] : nullptr;
-      NewtonResult r = dc_op(c, cfg, *s, x, xi);
-      iters[i] = (int64_t)r.iterations;
-      reason[i] = r.reason;
-      double* xo = x_out ? x_out + i * x_cap : nullptr;
-      if (xo)
-        for (int64_t k = 0; k < x_cap; ++k)
-          xo[k] = (size_t)k < x.size() ? x[(size_t)k] : 0.0;
+      int64_t ci = next.fetch_add(1);
+      if (ci >= ncirc) break;
+      if (by_circ[(size_t)ci].empty()) continue;
+      auto s = make_solver(kind, circs[(size_t)ci].node_count);
+      s->prepare(circs[(size_t)ci].node_count);
+      for (int64_t i : by_circ[(size_t)ci]) {
+        Circuit c = circs[(size_t)ci];
+        if (inst_dev[i] >= 0) c.p[(size_t)inst_dev[i] * NPARAM] = inst_val[i];
+        Vec x;
+        const double* xi = (x0 && x0_off && x0_off[i] >= 0) ? x0 + x0_off[i] : nullptr;
+        const size_t p0 = perturbed_pivots;
+        NewtonResult r = sweep ? dc_sweep_point(c, cfg, *s, x, xi) : dc_op(c, cfg, *s, x, xi);
+        if (perturbed) perturbed[i] = (int64_t)(perturbed_pivots - p0);
+        iters[i] = (int64_t)r.iterations;
+        reason[i] = r.reason;
+        double* xo = x_out ? x_out + i * x_cap : nullptr;
+        if (xo)
+          for (int64_t k = 0; k < x_cap; ++k)
+            xo[k] = (size_t)k < x.size() ? x[(size_t)k] : 0.0;
+      }
     }
   };
   int64_t nt = nthreads < 1 ? 1 : nthreads;

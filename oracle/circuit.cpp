@@ -385,6 +385,15 @@ NewtonResult dc_op(const Circuit& c, const NewtonConfig& cfg,
   return run_newton_with_stepping(cfg, x, dc_build, &ctx, solver);
 }
 
+NewtonResult dc_sweep_point(const Circuit& c, const NewtonConfig& cfg, LinearSolver& solver,
+                            Vec& x, const double* x0) {  // engine.rs:750-775
+  x.assign(c.node_count, 0.0);
+  if (x0)
+    for (size_t i = 0; i < c.node_count; ++i) x[i] = x0[i];
+  DcCtx ctx{&c};
+  return run_newton_with_stepping(cfg, x, dc_build, &ctx, solver);
+}
+
 double residual_inf(const Circuit& c, const Vec& x, double gmin) {
   MnaSystem s = build_mna(c, x, gmin, 1.0);
   size_t n = s.n;

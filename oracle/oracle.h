@@ -166,6 +166,11 @@ struct KluConfig {
   bool exact_pivots = false;
 };
 
+// Pivots the NativeKLU factorization replaced by its +-1e-14 perturbation
+// (native_klu.rs:1229-1231, 1344-1348) on this thread so far (a diagnostic
+// of the oracle; the reference keeps no such count).
+extern thread_local size_t perturbed_pivots;
+
 struct KluStats {
   size_t factor_count = 0, refactor_count = 0, nnz_l = 0, nnz_u = 0,
          nblocks = 0, noffdiag = 0;
@@ -341,6 +346,12 @@ NewtonResult run_newton_with_stepping(const NewtonConfig& cfg, Vec& x,
 
 // Engine DC operating point (crates/sim-core/src/engine.rs:249-311) on a
 // circuit. `x` returns the solution (length n when converged).
+// One point of the engine's DC sweep (engine.rs:684-820): the sweep calls
+// prepare(node_count) once before its first point, so its solver keeps the
+// pattern and pivots the first point found; each point here starts from x0
+// (or zero) instead of the previous point's solution.
+NewtonResult dc_sweep_point(const Circuit& c, const NewtonConfig& cfg, LinearSolver& solver,
+                            Vec& x, const double* x0);
 NewtonResult dc_op(const Circuit& c, const NewtonConfig& cfg,
                    LinearSolver& solver, Vec& x, const double* x0 = nullptr);
 

@@ -66,10 +66,13 @@ def lib():
         L.orc_ac_sweep.argtypes = [_I64, _I64, _P, _P, _P, _P, _I64, _P, _I64, _P, _P, _I64, _P]
         L.orc_tran_adjoint.restype = C.c_int
         L.orc_tran_adjoint.argtypes = [_I64, _I64, _P, _P, _P, _D, _I64, _P, _I64, _D, _D, _P]
+        L.orc_dc_sweep.argtypes = [_I64, _I64, _P, _P, _P, C.c_char_p, _I64, _D, _D, _D, _I64,
+                                   _I64, _P, _I64, _P, _I64, C.c_int, _P, _I64, _P, _P, _P]
         L.orc_residual.restype = _D
         L.orc_residual.argtypes = [_I64, _I64, _P, _P, _P, _P, _I64, _D]
         L.orc_dc_batch.argtypes = [_I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, C.c_char_p,
-                                   _I64, _D, _D, _D, _I64, _P, _P, _I64, _P, _P, _P, _I64]
+                                   _I64, _D, _D, _D, _I64, _P, _P, _I64, _P, _P, _P, _I64,
+                                   C.c_int, _P]
         _lib = L
     return _lib
 
@@ -273,6 +276,29 @@ def dc_op_bbd(c, assignment, num_blocks, max_iters=100, abs_tol=1e-6, rel_tol=1e
     return REASONS[r], it.value, x[:xl.value]
 
 
+def dc_sweep(c, src_dev, values, solver="nativeklu", max_iters=100, abs_tol=1e-6,
+             rel_tol=1e-3, gmin=1e-12, gmin_steps=0, x0=None, stop_on_failure=True):
+    """The reference's .dc sweep (engine.rs:684-820). Returns (reason,
+    iterations, x [points, n], x_len) per point; reason -1: not run."""
+    _, t, nd, p = _circ_arrays(c)
+    vals = _f64(values)
+    npts = len(vals)
+    x0a = None
+    stride = 0
+    if x0 is not None:
+        x0a = _f64(np.asarray(x0).reshape(npts, -1))
+        stride = x0a.shape[1]
+    xo = np.zeros((npts, c.n))
+    xl = np.zeros(npts, np.int64)
+    it = np.zeros(npts, np.int64)
+    rs = np.zeros(npts, np.int32)
+    lib().orc_dc_sweep(c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p), solver.encode(),
+                       max_iters, abs_tol, rel_tol, gmin, gmin_steps, src_dev, _ptr(vals), npts,
+                       _ptr(x0a) if x0a is not None else None, stride, int(bool(stop_on_failure)),
+                       _ptr(xo), c.n, _ptr(xl), _ptr(it), _ptr(rs))
+    return rs, it, xo, xl
+
+
 def residual(c, x, gmin=1e-12):
     _, t, nd, p = _circ_arrays(c)
     x = _f64(x)
@@ -282,8 +308,15 @@ def residual(c, x, gmin=1e-12):
 
 def dc_batch(circuits, inst_circ, inst_dev, inst_val, solver="nativeklu", max_iters=100,
              abs_tol=1e-6, rel_tol=1e-3, gmin=1e-12, gmin_steps=0, nthreads=1, x_cap=0,
-             x0=None, x0_off=None):
-    """Independent DC operating points over a thread pool."""
+             x0=None, x0_off=None, sweep=True, perturbed_out=None):
+    """DC operating points over a thread pool, circuit by circuit.
+
+    sweep=True: the instances of a circuit are the points of its DC sweep,
+    one solver for all of them, so the pivots of the first point are kept
+    (the reference's .dc, engine.rs:684-820), each point from its own x0.
+    sweep=False: every instance a separate .op with pivots of its own
+    (engine.rs:249-283). perturbed_out (int64, one per instance): how many
+    pivots NativeKLU replaced by +-1e-14 during the instance's solve."""
     x0a = _f64(x0) if x0 is not None else None
     x0o = _i64(x0_off) if x0_off is not None else None
     dev_off = np.zeros(len(circuits) + 1, np.int64)
@@ -303,5 +336,6 @@ def dc_batch(circuits, inst_circ, inst_dev, inst_val, solver="nativeklu", max_it
                        abs_tol, rel_tol, gmin, gmin_steps,
                        _ptr(x0a) if x0a is not None else None,
                        _ptr(x0o) if x0o is not None else None, nthreads, _ptr(iters),
-                       _ptr(reason), _ptr(xo) if x_cap > 0 else None, x_cap)
+                       _ptr(reason), _ptr(xo) if x_cap > 0 else None, x_cap, int(sweep),
+                       _ptr(perturbed_out) if perturbed_out is not None else None)
     return iters, reason, (xo if x_cap > 0 else None)

@@ -751,6 +751,8 @@ NativeKluSolver::Symbolic NativeKluSolver::resymbolic(const Symbolic& sym,
   return s;
 }
 
+thread_local size_t perturbed_pivots = 0;
+
 NativeKluSolver::Numeric NativeKluSolver::factor_block(
     const Symbolic& sym, const IVec& ap, const IVec& ai, const Vec& ax,
     const Numeric* old, bool refactor) const {  // :1194-1382
@@ -764,7 +766,10 @@ NativeKluSolver::Numeric NativeKluSolver::factor_block(
       size_t row = (size_t)ai[idx];
       if (row < n && sym.col_perm[row] == 0) diag += ax[idx];
     }
-    if (std::fabs(diag) < 1e-300) diag = 1e-14;
+    if (std::fabs(diag) < 1e-300) {
+      diag = 1e-14;
+      ++perturbed_pivots;
+    }
     num.u_val = {diag};
     num.u_diag = {diag};
     num.row_perm = {0};
@@ -824,7 +829,10 @@ NativeKluSolver::Numeric NativeKluSolver::factor_block(
     }
     for (size_t ui = us; ui < ue; ++ui) num.u_val[ui] = work[sym.u_idx[ui]];
     double diag = work[k];
-    if (std::fabs(diag) < 1e-14) diag = diag >= 0.0 ? 1e-14 : -1e-14;
+    if (std::fabs(diag) < 1e-14) {
+      diag = diag >= 0.0 ? 1e-14 : -1e-14;
+      ++perturbed_pivots;
+    }
     num.u_val[sym.u_ptr[k + 1] - 1] = diag;
     num.u_diag[k] = diag;
     for (size_t li = ls; li < le; ++li) num.l_val[li] = work[sym.l_idx[li]] / diag;

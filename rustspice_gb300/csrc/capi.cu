@@ -1160,12 +1160,24 @@ int gpuklu_ac_sweep(gpuklu_handle* h, gpuklu_circuit* c, const double* x_dc, int
   return GPUKLU_OK;
 }
 
-int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_config* cfg,
-                     const double* x0, double* x_out, int64_t x_cap, int64_t* x_len,
-                     int64_t* iters, int64_t* iters_total, int* reason) {
-  if (!h || !c || !cfg) return GPUKLU_INVALID_MATRIX;
-  // Engine::run_dc_result: x = zeros(node_count), solver.prepare(node_count)
-  gpuklu_prepare(h, c->node_count);
+}  // extern "C"
+
+namespace {
+// The Newton loop of the engine's DC analyses on the device
+// (run_newton_with_stepping, newton.rs:142-185, with run_newton, :65-117):
+// stamping, factor, solve and the update on the device, the pattern and
+// pivots kept by the handle between calls. d_newx holds the starting
+// iterate: x0 (nc values, the rest zero) when x0 is given, else whatever the
+// previous call left there (the sweep's continuation). m: the iterate's
+// length, node_count on a fresh start (x = zeros(node_count),
+// engine.rs:252), n once a converged solution with its aux currents has
+// become the iterate (run_newton's x = x_new, newton.rs:97-98): the
+// convergence test and the damping run over the first m entries. On return
+// *m_out is the length of x afterwards and x_out receives min(x_cap, that)
+// values.
+int dc_newton_run(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_config* cfg,
+                  const double* x0, int m, double* x_out, int64_t x_cap, int64_t* x_len,
+                  int64_t* iters, int64_t* iters_total, int* reason) {
   // build(x) returns n = node_count + aux; run_newton calls prepare(n)
   gpuklu_prepare(h, c->n);
   int st = gpuklu_analyze(h, c->ap.data(), (int64_t)c->ap.size(), c->ai.data(),
@@ -1174,11 +1186,15 @@ int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_co
   const int nc = c->node_count, n = c->n;
   cudaError_t e = h->d_rhs_c.resize(std::max(c->ncontrib, 1));
   if (e != cudaSuccess) return h->cuda_fail(e, "newton buffers");
-  std::vector<double> xinit(n, 0.0);
-  if (x0) std::copy(x0, x0 + nc, xinit.begin());
-  e = cudaMemcpyAsync(h->d_newx.p, xinit.data(), n * sizeof(double), cudaMemcpyHostToDevice,
-                      h->stream);
-  if (e != cudaSuccess) return h->cuda_fail(e, "newton x0");
+  if (x0) {
+    std::vector<double> xinit(n, 0.0);
+    std::copy(x0, x0 + nc, xinit.begin());
+    m = nc;
+    e = cudaMemcpyAsync(h->d_newx.p, xinit.data(), n * sizeof(double), cudaMemcpyHostToDevice,
+                        h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "newton x0");
+  }
   gk::NewtonCfg nc_{};
   nc_.max_iters = (int)cfg->max_iters;
   nc_.gmin_steps = (int)cfg->gmin_steps;
@@ -1214,7 +1230,7 @@ int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_co
           ++it;
           break;
         }
-        gk::launch_newton_update(nc, n, h->d_newx.p, h->d_out.p, h->d_nstate.p, nc_,
+        gk::launch_newton_update(m, n, h->d_newx.p, h->d_out.p, h->d_nstate.p, nc_,
                                  h->d_status.p, h->stream);
         gk::NewtonState hs;
         int dst = 0;
@@ -1244,7 +1260,7 @@ int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_co
       last_iters = it;
     }
   }
-  const int64_t len = conv ? n : nc;
+  const int64_t len = conv ? n : m;
   std::vector<double> xh(n);
   e = cudaMemcpyAsync(xh.data(), h->d_newx.p, n * sizeof(double), cudaMemcpyDeviceToHost,
                       h->stream);
@@ -1255,6 +1271,74 @@ int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_co
   if (iters) *iters = last_iters;
   if (iters_total) *iters_total = total;
   if (reason) *reason = rsn;
+  return GPUKLU_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int gpuklu_newton_dc(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_config* cfg,
+                     const double* x0, double* x_out, int64_t x_cap, int64_t* x_len,
+                     int64_t* iters, int64_t* iters_total, int* reason) {
+  if (!h || !c || !cfg) return GPUKLU_INVALID_MATRIX;
+  // Engine::run_dc_result: x = zeros(node_count), solver.prepare(node_count)
+  // (a size other than the matrix's when there are voltage sources, so the
+  // pattern and the pivots are found anew)
+  gpuklu_prepare(h, c->node_count);
+  std::vector<double> zero;
+  if (!x0) {
+    zero.assign(c->node_count, 0.0);
+    x0 = zero.data();
+  }
+  return dc_newton_run(h, c, cfg, x0, c->node_count, x_out, x_cap, x_len, iters, iters_total,
+                       reason);
+}
+
+int gpuklu_dc_sweep(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_config* cfg,
+                    int64_t src_dev, const double* values, int64_t npts, const double* x0,
+                    int64_t x0_stride, int stop_on_failure, double* x_out, int64_t x_stride,
+                    int64_t* x_len, int64_t* iters, int64_t* iters_total, int* reason) {
+  if (!h || !c || !cfg || !values || npts < 0) return GPUKLU_INVALID_MATRIX;
+  if (src_dev < 0 || src_dev >= c->ndev)
+    return h->fail(GPUKLU_INVALID_MATRIX, "gpuklu_dc_sweep: no device " +
+                                              std::to_string(src_dev) + " to sweep");
+  if (x0 && x0_stride < c->node_count)
+    return h->fail(GPUKLU_INVALID_MATRIX, "gpuklu_dc_sweep: x0_stride below node_count");
+  if (x_out && x_stride < c->n)
+    return h->fail(GPUKLU_INVALID_MATRIX, "gpuklu_dc_sweep: x_stride below n");
+  for (int64_t k = 0; k < npts; ++k) {  // points not run: reason -1
+    if (iters) iters[k] = 0;
+    if (iters_total) iters_total[k] = 0;
+    if (reason) reason[k] = -1;
+    if (x_len) x_len[k] = 0;
+  }
+  // engine.rs:746-748: x = zeros(node_count), prepare(node_count) once
+  gpuklu_prepare(h, c->node_count);
+  cudaError_t e = cudaMemsetAsync(h->d_newx.p, 0, (size_t)c->n * sizeof(double), h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  int m = c->node_count;
+  std::vector<double> xbuf(c->n);
+  for (int64_t k = 0; k < npts; ++k) {
+    // the swept source's value (engine.rs:758) in the device parameters
+    c->p[(size_t)src_dev * 6] = values[k];
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->d_p.p + (size_t)src_dev * 6, &c->p[(size_t)src_dev * 6],
+                          sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "dc sweep source value");
+    int64_t len = 0, it = 0, itt = 0;
+    int rsn = 1;
+    const int st = dc_newton_run(h, c, cfg, x0 ? x0 + k * x0_stride : nullptr, m, xbuf.data(),
+                                 c->n, &len, &it, &itt, &rsn);
+    if (st != GPUKLU_OK) return st;
+    m = (int)len;
+    if (x_out)
+      for (int64_t i = 0; i < c->n; ++i) x_out[k * x_stride + i] = i < len ? xbuf[i] : 0.0;
+    if (x_len) x_len[k] = len;
+    if (iters) iters[k] = it;
+    if (iters_total) iters_total[k] = itt;
+    if (reason) reason[k] = rsn;
+    if (rsn != 0 && stop_on_failure) break;  // engine.rs:785-796
+  }
   return GPUKLU_OK;
 }
 
@@ -1337,9 +1421,18 @@ struct gpuklu_batch {
     gk::BatchArgs args{};
   };
   std::vector<std::unique_ptr<Class>> classes;
+  // Continuation phase behind the lane kernel: one warp per parked instance
+  // with its own staged program, warps in one-warp blocks; classes by the
+  // per-warp shared memory (program + instance region) so a small program
+  // is not given the largest one's slice. Largest first.
+  std::vector<std::unique_ptr<Class>> cont_classes;
   // warps of a block that shares one program: up to this many, as the
   // group's program and instance regions fit the block's shared memory
   static constexpr int kSharedWarpsMax = 16;
+  // continuation tiles per group (one-warp blocks), and whether the
+  // continuation runs them (else the shared-program blocks of `classes`)
+  static constexpr int kContTiles = 4;
+  bool cont_warps = true;
   cudaEvent_t start_ev = nullptr;
   // timing events of the last run: before the lane kernel, after it, after
   // the warp kernels joined back
@@ -1934,6 +2027,47 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       return nullptr;
     B->classes.push_back(std::move(C));
   }
+  if (lanes_on) {
+    // continuation classes by per-warp footprint: program ints x 4 plus the
+    // instance region's doubles x 8 (M = 1)
+    const int bounds_kb[] = {8, 12, 16, 24, 32, 48, 64, 96, 160, 227};
+    const int nb = (int)(sizeof(bounds_kb) / sizeof(bounds_kb[0]));
+    std::vector<std::vector<int>> cm(nb);
+    for (int g : gorder) {  // most expensive programs first
+      const gk::GroupHdr& h = B->groups[g];
+      if (h.inst_count == 0) continue;
+      const size_t f = (size_t)h.prog * 4 + (size_t)gregion[g] * 8;
+      int k = 0;
+      while (k < nb - 1 && f > (size_t)bounds_kb[k] * 1024) ++k;
+      cm[k].push_back(g);
+    }
+    for (int k = nb - 1; k >= 0; --k) {
+      if (cm[k].empty()) continue;
+      auto C = std::make_unique<gpuklu_batch::Class>();
+      C->m = 1;
+      C->warps_per_block = 1;
+      for (int g : cm[k]) {
+        const gk::GroupHdr& h = B->groups[g];
+        C->region = std::max(C->region, gregion[g]);
+        C->prog_ints = std::max(C->prog_ints, h.prog);
+        // a few tiles per group: a group rarely parks more instances, and
+        // a warp that finds its group's instances taken moves on at once
+        for (int t = 0; t < std::min(h.inst_count, gpuklu_batch::kContTiles); ++t)
+          C->tiles.push_back(g);
+      }
+      gk::batch_kernel_info(1, 1, C->region, C->prog_ints, &C->regs, &C->blocks_per_sm);
+      if (C->blocks_per_sm <= 0) {
+        fprintf(stderr, "gpuklu_batch_create: a circuit needs %d KB of shared memory\n",
+                (int)((C->region * 8 + C->prog_ints * 4) / 1024));
+        return nullptr;
+      }
+      C->grid = std::min<int>(sm_count() * C->blocks_per_sm, (int)C->tiles.size());
+      if (cudaStreamCreateWithFlags(&C->stream, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&C->done, cudaEventDisableTiming) != cudaSuccess)
+        return nullptr;
+      B->cont_classes.push_back(std::move(C));
+    }
+  }
   if (cudaEventCreateWithFlags(&B->start_ev, cudaEventDisableTiming) != cudaSuccess) return nullptr;
   for (auto& ev : B->ph_ev)
     if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
@@ -1968,10 +2102,16 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     if (e == cudaSuccess) e = C->d_tiles3.upload(C->tiles3, s);
     if (e == cudaSuccess) e = C->d_counter.resize(1);
   }
+  for (auto& C : B->cont_classes) {
+    if (e == cudaSuccess) e = C->d_tiles.upload(C->tiles, s);
+    if (e == cudaSuccess) e = C->d_counter.resize(1);
+  }
   // Lane phase: every group split into tiles of about lane_target instances,
   // most expensive programs first; a scratch of region x 32 doubles per warp.
   {
     B->lanes = lanes_on;
+    const char* econt = getenv("GPUKLU_CONT");
+    B->cont_warps = !(econt && strcmp(econt, "shared") == 0);
     const char* ecap = getenv("GPUKLU_LANE_CAP");
     B->lane_cap = ecap ? std::max(1, atoi(ecap)) : 6;
     const char* etgt = getenv("GPUKLU_LANE_TARGET");
@@ -2084,15 +2224,16 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     a.cont_prev = B->d_cont_prev.p;
   }
   B->args = a;
-  for (auto& C : B->classes) {
-    C->args = a;
-    C->args.tile_group = C->d_tiles.p;
-    C->args.ntiles = (int)C->tiles.size();
-    C->args.counter = C->d_counter.p;
-    C->args.region = C->region;
-    C->args.prog_ints = C->prog_ints;
-    C->args.shared_bytes = C->shared_bytes;
-  }
+  for (auto* cl : {&B->classes, &B->cont_classes})
+    for (auto& C : *cl) {
+      C->args = a;
+      C->args.tile_group = C->d_tiles.p;
+      C->args.ntiles = (int)C->tiles.size();
+      C->args.counter = C->d_counter.p;
+      C->args.region = C->region;
+      C->args.prog_ints = C->prog_ints;
+      C->args.shared_bytes = C->shared_bytes;
+    }
   B->transient = transient;
   B->dt = dt;
   return B.release();
@@ -2284,6 +2425,7 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
   cudaStream_t s = b->stream;
   cudaMemsetAsync(b->d_gnext.p, 0, b->d_gnext.n * sizeof(unsigned), s);
   for (auto& C : b->classes) cudaMemsetAsync(C->d_counter.p, 0, sizeof(unsigned), s);
+  for (auto& C : b->cont_classes) cudaMemsetAsync(C->d_counter.p, 0, sizeof(unsigned), s);
   if (b->lanes) {  // phase 1: lane per instance, then the warp classes take the parked ones
     cudaMemsetAsync(b->d_lcounter.p, 0, sizeof(unsigned), s);
     cudaMemsetAsync(b->d_cont_count.p, 0, b->d_cont_count.n * sizeof(unsigned), s);
@@ -2297,6 +2439,21 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
   }
   cudaEventRecord(b->ph_ev[1], s);
   cudaEventRecord(b->start_ev, s);
+  if (b->lanes && b->cont_warps && !b->cont_classes.empty()) {
+    for (auto& C : b->cont_classes) {  // largest programs first, all classes concurrent
+      cudaStreamWaitEvent(C->stream, b->start_ev, 0);
+      C->args.cfg = c;
+      gk::BatchArgs ca = C->args;
+      ca.cont_mode = 1;
+      gk::launch_batch_newton(ca, 1, C->grid, 1, C->stream, false);
+      cudaEventRecord(C->done, C->stream);
+      cudaStreamWaitEvent(s, C->done, 0);
+    }
+    cudaEventRecord(b->ph_ev[2], s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return b->fail(cuda_msg(e, "batch launch"));
+    return GPUKLU_OK;
+  }
   for (auto& C : b->classes) {  // largest programs first, all classes concurrent
     cudaStreamWaitEvent(C->stream, b->start_ev, 0);
     C->args.cfg = c;
@@ -2389,7 +2546,10 @@ int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out) {
   if (!b) return GPUKLU_INVALID_MATRIX;
   for (int q = 0; q < 8; ++q) out[q] = 0;
   out[2] = (int64_t)b->groups.size();
-  out[6] = (int64_t)b->classes.size() + (b->lanes ? 1 : 0);
+  out[6] = (int64_t)(b->lanes && b->cont_warps && !b->cont_classes.empty()
+                         ? b->cont_classes.size()
+                         : b->classes.size()) +
+           (b->lanes ? 1 : 0);
   for (auto& C : b->classes) {  // the largest class (first) describes the launch
     out[0] += C->grid;
     if (out[1] == 0) {

@@ -42,6 +42,7 @@
 // the Newton tolerance.
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 
 #include "batch_common.cuh"
 #include "device.cuh"
@@ -1327,6 +1328,12 @@ __global__ void k_batch_newton(BatchArgs A) {
     }
     if (ti >= A.ntiles) return;
     const int g = A.tile_group[ti];
+    // a continuation tile whose group has no parked instance left is
+    // skipped before its program is staged (tiles outnumber the instances
+    // the lane phase parks)
+    if (!SHARED && A.cont_mode &&
+        *(volatile unsigned*)&A.gnext2[g] >= *(volatile unsigned*)&A.cont_count[g])
+      continue;
     const GroupHdr G = A.groups[g];
     const int pg = SHARED ? G.prog : A.prog_ints;
     const int rg = SHARED ? G.region : A.region;
@@ -1622,9 +1629,25 @@ static size_t smem_bytes(const BatchArgs& a, int warps_per_block) {
   return ((size_t)a.prog_ints * 4 + (size_t)a.region * M * sizeof(double)) * warps_per_block;
 }
 
+// The dynamic shared-memory limit of an instantiation is one attribute for
+// every launch of it; launches of different sizes (the batch's classes)
+// raise it to the largest size any of them needs.
+template <int M, bool SHARED>
+static void raise_smem_limit(size_t bytes) {
+  static std::mutex mu;
+  static size_t set = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  if (bytes > set) {
+    cudaFuncSetAttribute(k_batch_newton<M, SHARED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)bytes);
+    set = bytes;
+  }
+}
+
 template <int M, bool SHARED>
 static void launch_m(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s) {
   const size_t sm = smem_bytes<M, SHARED>(a, warps_per_block);
+  raise_smem_limit<M, SHARED>(sm);
   k_batch_newton<M, SHARED><<<grid, 32 * warps_per_block, sm, s>>>(a);
 }
 
@@ -1658,8 +1681,7 @@ static void info_m(int warps_per_block, int region, int prog_ints, int* regs,
   *regs = fa.numRegs;
   const size_t per = (size_t)region * M * sizeof(double);
   const size_t sm = SHARED ? shared_bytes : ((size_t)prog_ints * 4 + per) * warps_per_block;
-  cudaFuncSetAttribute(k_batch_newton<M, SHARED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sm);
+  raise_smem_limit<M, SHARED>(sm);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_batch_newton<M, SHARED>,
                                                 32 * warps_per_block, sm);
 }

@@ -29,7 +29,7 @@ SYMBOLS = [
     "gpuklu_set_pivot_mode", "gpuklu_get_stats", "gpuklu_last_error", "gpuklu_pivot_pass_count", "gpuklu_factor_device",
     "gpuklu_solve_device", "gpuklu_tsolve", "gpuklu_stream", "gpuklu_compile_devices",
     "gpuklu_circuit_free", "gpuklu_circuit_dims", "gpuklu_circuit_pattern",
-    "gpuklu_circuit_set_params", "gpuklu_stamp", "gpuklu_newton_dc", "gpuklu_batch_create",
+    "gpuklu_circuit_set_params", "gpuklu_stamp", "gpuklu_newton_dc", "gpuklu_dc_sweep", "gpuklu_batch_create",
     "gpuklu_batch_destroy", "gpuklu_batch_run", "gpuklu_batch_results",
     "gpuklu_batch_update_inputs", "gpuklu_batch_last_error", "gpuklu_batch_info",
     "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_batch_phase_ms", "gpuklu_ac_sweep", "gpuklu_tran_create", "gpuklu_tran_forward",
@@ -93,6 +93,8 @@ def lib(build_if_missing: bool = True):
         "gpuklu_stamp": (C.c_int, [_P, _P, _P, _I64, _D, _D, _D, _P, _D, _P, _P]),
         "gpuklu_newton_dc": (C.c_int, [_P, _P, C.POINTER(NewtonConfig), _P, _P, _I64, _P, _P,
                                        _P, _P]),
+        "gpuklu_dc_sweep": (C.c_int, [_P, _P, C.POINTER(NewtonConfig), _I64, _P, _I64, _P,
+                                      _I64, C.c_int, _P, _I64, _P, _P, _P, _P]),
         "gpuklu_batch_create": (_P, [_I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _I64]),
         "gpuklu_batch_destroy": (None, [_P]),
         "gpuklu_batch_run": (C.c_int, [_P, C.POINTER(NewtonConfig)]),

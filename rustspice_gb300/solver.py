@@ -195,6 +195,42 @@ def newton_dc(solver: GpuKluSolver, dc: DeviceCircuit, cfg: N.NewtonConfig,
     return NewtonResult(rs.value == 0, it.value, itt.value, REASONS[rs.value], x[:xl.value])
 
 
+@dataclasses.dataclass
+class SweepResult:
+    reason: np.ndarray          # per point: 0 converged, 1 max iterations, 2 solver failure,
+    iterations: np.ndarray      # -1 not run (the sweep stopped before it)
+    iterations_total: np.ndarray
+    x: np.ndarray               # [points, n]; zero beyond x_len
+    x_len: np.ndarray
+
+
+def dc_sweep(solver: GpuKluSolver, dc: DeviceCircuit, cfg: N.NewtonConfig, src_dev: int,
+             values, x0=None, stop_on_failure: bool = True) -> SweepResult:
+    """The reference's .dc sweep of one source on the device
+    (engine.rs:684-820): one solver for all points, so the first point's
+    pivots are kept. x0 None: continuation from the previous point; else an
+    array [points, node_count] of initial iterates."""
+    vals = N.f64(values)
+    npts = len(vals)
+    n = dc.n
+    xo = np.zeros((npts, n))
+    xl = np.zeros(npts, np.int64)
+    it = np.zeros(npts, np.int64)
+    itt = np.zeros(npts, np.int64)
+    rs = np.zeros(npts, np.int32)
+    x0a = None
+    stride = 0
+    if x0 is not None:
+        x0a = N.f64(np.asarray(x0).reshape(npts, -1))
+        stride = x0a.shape[1]
+    st = N.lib().gpuklu_dc_sweep(solver.handle, dc.handle, C.byref(cfg), int(src_dev),
+                                 N.ptr(vals), npts, N.ptr(x0a) if x0a is not None else None,
+                                 stride, int(bool(stop_on_failure)), N.ptr(xo), n, N.ptr(xl),
+                                 N.ptr(it), N.ptr(itt), N.ptr(rs))
+    solver._check(st)
+    return SweepResult(rs, it, itt, xo, xl)
+
+
 def ac_sweep(solver: GpuKluSolver, dc: DeviceCircuit, x_dc, freqs) -> np.ndarray:
     """AC small-signal solutions at the operating point x_dc for every
     frequency (the reference's .ac): complex array [len(freqs), n]. V and I
