@@ -90,6 +90,21 @@ void gpuklu_set_parallel_threads(gpuklu_handle* h, size_t threads);
 
 /* Pivot mode for the next analysis (default GPUKLU_PIVOT_REFERENCE). */
 int gpuklu_set_pivot_mode(gpuklu_handle* h, int mode);
+/* Growth-triggered re-pivot, off by default (the reference's refactorization
+ * always keeps the first factorization's pivots, native_klu.rs:1020-1148,
+ * and only perturbs a tiny one to +-1e-14, :1344-1348). On: after every
+ * refactorization the device checks each BTF block's multipliers; a block
+ * with one above 1/0.001 (its kept pivot below a thousandth of the largest
+ * entry under it, the threshold the first factorization swaps on,
+ * :1295-1334) is factored afresh on the device - the first factorization's
+ * pivot choice for the current values and, in GPUKLU_PIVOT_EXACT, that
+ * block's exact pattern, the other blocks keeping their pivots; in
+ * GPUKLU_PIVOT_REFERENCE every block afresh, as after reset_pattern. The
+ * factor then equals a fresh first factorization of those values. Costs a
+ * growth scan and a device-to-host read after each refactorization. */
+int gpuklu_set_repivot(gpuklu_handle* h, int on);
+/* Re-pivots since the last pattern change (the count reset_pattern clears). */
+int64_t gpuklu_repivot_count(const gpuklu_handle* h);
 /* Counters of NativeKluStats (native_klu.rs:584-594) plus device figures. */
 int gpuklu_get_stats(gpuklu_handle* h, gpuklu_stats* out);
 /* Text of the last error on this handle ("" if none). */

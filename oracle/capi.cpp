@@ -77,6 +77,8 @@ int orc_solve(void* h, double* rhs, int64_t len) {
 
 // NativeKLU counters: out[0..5] = factor, refactor, nnz_l, nnz_u, nblocks,
 // noffdiag; *rcond = rcond.
+// out[0..6]: factor and refactor counts, nnz(L), nnz(U), blocks, coupling
+// entries, growth-triggered re-pivots
 int orc_klu_stats(void* h, int64_t* out, double* rcond) {
   auto* k = dynamic_cast<NativeKluSolver*>(static_cast<LinearSolver*>(h));
   if (!k) return -1;
@@ -87,6 +89,7 @@ int orc_klu_stats(void* h, int64_t* out, double* rcond) {
   out[3] = (int64_t)s.nnz_u;
   out[4] = (int64_t)s.nblocks;
   out[5] = (int64_t)s.noffdiag;
+  out[6] = (int64_t)s.repivots;
   *rcond = s.rcond;
   return 0;
 }

@@ -164,6 +164,14 @@ struct KluConfig {
   // the row-permuted block and every factorization (the first included)
   // refactors that exact pattern with the frozen pivots.
   bool exact_pivots = false;
+  // Growth-triggered re-pivot (not in the reference, whose refactorization
+  // always keeps the first pivots): after a refactorization, a BTF block
+  // with a multiplier |l_ik| above 1 / pivot_tol (its kept pivot is smaller
+  // than pivot_tol times the column's largest entry below it, the threshold
+  // the first factorization swaps on) is factored afresh: new pivots by the
+  // first-factorization pass and, in exact mode, its exact pattern for them.
+  // In the reference's mode a trigger refactors every block afresh.
+  bool repivot = false;
 };
 
 // Pivots the NativeKLU factorization replaced by its +-1e-14 perturbation
@@ -173,7 +181,7 @@ extern thread_local size_t perturbed_pivots;
 
 struct KluStats {
   size_t factor_count = 0, refactor_count = 0, nnz_l = 0, nnz_u = 0,
-         nblocks = 0, noffdiag = 0;
+         nblocks = 0, noffdiag = 0, repivots = 0;
   double rcond = 0.0;
 };
 
@@ -212,6 +220,8 @@ class NativeKluSolver : public LinearSolver {
   enum State { EMPTY, ANALYZED, FACTORED };
   int do_analyze(const IVec& ap, const IVec& ai);
   int do_factor(const IVec& ap, const IVec& ai, const Vec& ax);
+  bool growth(const Numeric& nm) const;
+  int refactor_afresh(const IVec& ap, const IVec& ai, const Vec& ax);
   Symbolic symbolic_for_block(size_t n, const IVec& ap, const IVec& ai) const;
   static void symbolic_dfs(size_t n, const IVec& pap, const IVec& pai,
                            Symbolic& s);
@@ -229,6 +239,7 @@ class NativeKluSolver : public LinearSolver {
   bool has_btf_ = false;
   Btf btf_;
   std::vector<Symbolic> sym_;
+  std::vector<Symbolic> sym_free_;  // the pivot-free patterns (re-pivot)
   std::vector<Numeric> num_;
   std::vector<OffDiag> off_;
   IVec last_ap_, last_ai_;

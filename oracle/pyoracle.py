@@ -126,11 +126,12 @@ class Solver:
         return st, x
 
     def klu_stats(self):
-        out = np.zeros(6, np.int64)
+        out = np.zeros(7, np.int64)
         rc = C.c_double()
         if lib().orc_klu_stats(self.h, _ptr(out), C.byref(rc)) != 0:
             return None
-        keys = ["factor_count", "refactor_count", "nnz_l", "nnz_u", "nblocks", "noffdiag"]
+        keys = ["factor_count", "refactor_count", "nnz_l", "nnz_u", "nblocks", "noffdiag",
+                "repivots"]
         d = {k: int(v) for k, v in zip(keys, out)}
         d["rcond"] = rc.value
         return d

@@ -628,6 +628,7 @@ int NativeKluSolver::do_analyze(const IVec& ap, const IVec& ai) {  // :704-761
   state_ = ANALYZED;
   last_ap_ = ap;
   last_ai_ = ai;
+  sym_free_ = sym_;
   for (auto& s : sym_) {
     stats_.nnz_l += s.l_idx.size();
     stats_.nnz_u += s.u_idx.size();
@@ -847,6 +848,28 @@ NativeKluSolver::Numeric NativeKluSolver::factor_block(
   return num;
 }
 
+bool NativeKluSolver::growth(const Numeric& nm) const {
+  const double lim = 1.0 / cfg_.pivot_tol;
+  for (double l : nm.l_val)
+    if (std::fabs(l) > lim || std::isnan(l)) return true;
+  return false;
+}
+
+int NativeKluSolver::refactor_afresh(const IVec& ap, const IVec& ai, const Vec& ax) {
+  // the reference's mode: every block's first factorization again (as after
+  // reset_pattern), counted as a refactorization with one re-pivot
+  KluStats keep = stats_;
+  state_ = ANALYZED;
+  sym_ = sym_free_;
+  const int st = do_factor(ap, ai, ax);
+  const double rc = stats_.rcond;
+  stats_ = keep;
+  stats_.rcond = rc;
+  ++stats_.refactor_count;
+  ++stats_.repivots;
+  return st;
+}
+
 int NativeKluSolver::do_factor(const IVec& ap, const IVec& ai, const Vec& ax) {
   // :1020-1148
   bool same = state_ == FACTORED && pattern_matches(ap, ai);
@@ -876,6 +899,15 @@ int NativeKluSolver::do_factor(const IVec& ap, const IVec& ai, const Vec& ax) {
         sym_[k] = resymbolic(sym_[k], nm, bap, bai);
         nm = factor_block(sym_[k], bap, bai, bax, &nm, true);
       }
+      if (same && cfg_.repivot && growth(nm)) {
+        if (!cfg_.exact_pivots) return refactor_afresh(ap, ai, ax);
+        ++stats_.repivots;  // this block afresh: its first factorization
+        nm = factor_block(sym_free_[k], bap, bai, bax, nullptr, false);
+        if (sym_free_[k].n > 1) {
+          sym_[k] = resymbolic(sym_free_[k], nm, bap, bai);
+          nm = factor_block(sym_[k], bap, bai, bax, &nm, true);
+        }
+      }
       nn.push_back(std::move(nm));
     }
     num_ = std::move(nn);
@@ -898,6 +930,15 @@ int NativeKluSolver::do_factor(const IVec& ap, const IVec& ai, const Vec& ax) {
     if (cfg_.exact_pivots && !same && sym_[0].n > 1) {
       sym_[0] = resymbolic(sym_[0], nm, ap, ai);
       nm = factor_block(sym_[0], ap, ai, ax, &nm, true);
+    }
+    if (same && cfg_.repivot && growth(nm)) {
+      if (!cfg_.exact_pivots) return refactor_afresh(ap, ai, ax);
+      ++stats_.repivots;
+      nm = factor_block(sym_free_[0], ap, ai, ax, nullptr, false);
+      if (sym_free_[0].n > 1) {
+        sym_[0] = resymbolic(sym_free_[0], nm, ap, ai);
+        nm = factor_block(sym_[0], ap, ai, ax, &nm, true);
+      }
     }
     num_.clear();
     num_.push_back(std::move(nm));
@@ -922,9 +963,11 @@ std::unique_ptr<LinearSolver> make_solver(const std::string& kind, size_t n) {
   if (kind == "dense") return std::make_unique<DenseSolver>(n);
   if (kind == "sparselu") return std::make_unique<SparseLuSolver>(n);
   if (kind == "sparselubtf") return std::make_unique<SparseLuBtfSolver>(n);
-  if (kind == "nativeklu_exact") {
+  if (kind == "nativeklu_exact" || kind == "nativeklu_exact_repivot" ||
+      kind == "nativeklu_repivot") {
     KluConfig cfg;
-    cfg.exact_pivots = true;
+    cfg.exact_pivots = kind != "nativeklu_repivot";
+    cfg.repivot = kind != "nativeklu_exact";
     return std::make_unique<NativeKluSolver>(n, cfg);
   }
   return std::make_unique<NativeKluSolver>(n);

@@ -514,6 +514,13 @@ struct gpuklu_handle {
   bool rcond_valid = false;
   std::string err;
   int grid_cols = 1;
+  // Growth-triggered re-pivot (off: the reference's frozen pivots): after a
+  // refactorization, a BTF block with a multiplier above 1 / kPivotTol is
+  // factored afresh (see repivot_grown).
+  bool repivot = false;
+  int64_t repivot_count = 0;
+  DBuf<int> d_grow;
+  static constexpr double kPivotTol = 0.001;
 
   int fail(int code, const std::string& m) {
     err = m;
@@ -527,7 +534,7 @@ struct gpuklu_handle {
     state = EMPTY;
     last_ap.clear();
     last_ai.clear();
-    factor_count = refactor_count = 0;
+    factor_count = refactor_count = repivot_count = 0;
     rcond = 0.0;
     rcond_valid = false;
   }
@@ -719,19 +726,14 @@ struct gpuklu_handle {
     return GPUKLU_OK;
   }
 
-  int factor_on_device(bool sync) {
-    rcond_valid = false;
-    if (state == FACTORED) {
-      refactor_launch();
-      ++refactor_count;
-      if (!sync) return GPUKLU_OK;
-      return check_status("refactor");
-    }
-    // First factorization: the reference's pivot pass, as refactorizations
-    // from kPivotPassMinN rows on, else (or when those do not settle) the
-    // sequential one-warp kernel. GPUKLU_PIVOT_PASS=refactor / sequential
-    // picks one for every size.
-    std::vector<i32> rperm(n);
+  // The pivots of the reference's first factorization for the values in
+  // d_ax (block-local row order per position): the pivot pass as
+  // refactorizations from kPivotPassMinN rows on, else (or when those do not
+  // settle) the sequential one-warp kernel. GPUKLU_PIVOT_PASS=refactor /
+  // sequential picks one for every size. d_lu is left with the pass's
+  // values in the pivot-free pattern.
+  int first_pivots(std::vector<i32>& rperm) {
+    rperm.assign(n, 0);
     bool settled = false;
     pivot_passes = 0;
     const char* pp = getenv("GPUKLU_PIVOT_PASS");
@@ -748,13 +750,80 @@ struct gpuklu_handle {
       for (int b = 0; b < sym_plan.nblocks; ++b)
         maxblk = std::max(maxblk, sym_plan.block_ptr[b + 1] - sym_plan.block_ptr[b]);
       gk::launch_first_factor(pd_sym.dp, maxblk, d_ax.p, d_lu.p, d_work.p, d_rperm.p,
-                              d_rinv.p, no_swap ? 0.0 : 0.001, d_status.p, stream);
+                              d_rinv.p, no_swap ? 0.0 : kPivotTol, d_status.p, stream);
       cudaError_t e = cudaMemcpyAsync(rperm.data(), d_rperm.p, n * sizeof(i32),
                                       cudaMemcpyDeviceToHost, stream);
       if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
       if (e != cudaSuccess) return cuda_fail(e, "first factor");
     }
-    int st = check_status("first factor");
+    return check_status("first factor");
+  }
+
+  // After a refactorization with the kept pivots: blocks whose multipliers
+  // grew past 1 / kPivotTol get the first factorization's pivots for the
+  // current values. In the exact-pattern mode only those blocks change (the
+  // pass's choice for a block depends on that block's values alone, so the
+  // other blocks keep theirs) and the new plan refactors; in the reference's
+  // mode every block is factored afresh, as after reset_pattern.
+  int repivot_grown() {
+    const gk::Plan& P = plan;
+    cudaError_t e = d_grow.resize(std::max(P.nblocks, 1));
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_grow.p, 0, P.nblocks * sizeof(int), stream);
+    if (e != cudaSuccess) return cuda_fail(e, "growth check");
+    gk::launch_growth(pd.dp, d_lu.p, 1.0 / kPivotTol, d_grow.p, stream);
+    std::vector<int> grow(P.nblocks, 0);
+    e = cudaMemcpyAsync(grow.data(), d_grow.p, P.nblocks * sizeof(int), cudaMemcpyDeviceToHost,
+                        stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_fail(e, "growth check");
+    if (std::none_of(grow.begin(), grow.end(), [](int g) { return g != 0; })) return GPUKLU_OK;
+    ++repivot_count;
+    if (pivot_mode != GPUKLU_PIVOT_EXACT) {  // every block afresh
+      const int64_t fc = factor_count;
+      state = ANALYZED;
+      const int st = factor_on_device(true);
+      factor_count = fc;
+      return st;
+    }
+    std::vector<i32> fresh;
+    int st = first_pivots(fresh);
+    if (st) return st;
+    std::vector<i32> merged = piv_rperm;
+    for (int k = 0; k < (int)n; ++k)
+      if (grow[P.pos_block[k]]) merged[k] = fresh[k];
+    if (merged != piv_rperm) {
+      plan = sym_plan;
+      gk::set_pivots(plan, last_ap.data(), last_ai.data(), merged);
+      if (plan.too_large) {
+        state = ANALYZED;
+        return fail(GPUKLU_INVALID_MATRIX,
+                    "the factorization's update lists exceed 2^31 entries "
+                    "(fill too large for this solver)");
+      }
+      st = upload_plan();
+      if (st) return st;
+      piv_rperm.swap(merged);
+    }
+    refactor_launch();
+    return GPUKLU_OK;
+  }
+
+  int factor_on_device(bool sync) {
+    rcond_valid = false;
+    if (state == FACTORED) {
+      refactor_launch();
+      ++refactor_count;
+      if (repivot && !no_swap) {
+        const int st = repivot_grown();
+        if (st) return st;
+      }
+      if (!sync) return GPUKLU_OK;
+      return check_status("refactor");
+    }
+    // First factorization: the reference's pivot choice, then the plan for
+    // those pivots.
+    std::vector<i32> rperm;
+    int st = first_pivots(rperm);
     if (st) return st;
     if (!(piv_ok && rperm == piv_rperm)) {
       piv_ok = false;
@@ -914,6 +983,14 @@ void gpuklu_reset_pattern(gpuklu_handle* h) {
 const char* gpuklu_name(const gpuklu_handle*) { return "GpuKLU"; }
 
 void gpuklu_set_parallel_threads(gpuklu_handle*, size_t) {}
+
+int gpuklu_set_repivot(gpuklu_handle* h, int on) {
+  if (!h) return GPUKLU_INVALID_MATRIX;
+  h->repivot = on != 0;
+  return GPUKLU_OK;
+}
+
+int64_t gpuklu_repivot_count(const gpuklu_handle* h) { return h ? h->repivot_count : 0; }
 
 int gpuklu_set_pivot_mode(gpuklu_handle* h, int mode) {
   if (!h || (mode != GPUKLU_PIVOT_REFERENCE && mode != GPUKLU_PIVOT_EXACT))
@@ -1314,21 +1391,21 @@ int gpuklu_dc_sweep(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_con
   }
   // engine.rs:746-748: x = zeros(node_count), prepare(node_count) once
   gpuklu_prepare(h, c->node_count);
-  cudaError_t e = cudaMemsetAsync(h->d_newx.p, 0, (size_t)c->n * sizeof(double), h->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  const std::vector<double> zero(c->node_count, 0.0);
   int m = c->node_count;
   std::vector<double> xbuf(c->n);
   for (int64_t k = 0; k < npts; ++k) {
     // the swept source's value (engine.rs:758) in the device parameters
     c->p[(size_t)src_dev * 6] = values[k];
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(c->d_p.p + (size_t)src_dev * 6, &c->p[(size_t)src_dev * 6],
-                          sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    cudaError_t e = cudaMemcpyAsync(c->d_p.p + (size_t)src_dev * 6, &c->p[(size_t)src_dev * 6],
+                                    sizeof(double), cudaMemcpyHostToDevice, h->stream);
     if (e != cudaSuccess) return h->cuda_fail(e, "dc sweep source value");
+    // the start: the point's own x0, or zeros at the first point of a
+    // continuation sweep, else the previous point's final iterate
+    const double* start = x0 ? x0 + k * x0_stride : (k == 0 ? zero.data() : nullptr);
     int64_t len = 0, it = 0, itt = 0;
     int rsn = 1;
-    const int st = dc_newton_run(h, c, cfg, x0 ? x0 + k * x0_stride : nullptr, m, xbuf.data(),
-                                 c->n, &len, &it, &itt, &rsn);
+    const int st = dc_newton_run(h, c, cfg, start, m, xbuf.data(), c->n, &len, &it, &itt, &rsn);
     if (st != GPUKLU_OK) return st;
     m = (int)len;
     if (x_out)
@@ -1421,18 +1498,10 @@ struct gpuklu_batch {
     gk::BatchArgs args{};
   };
   std::vector<std::unique_ptr<Class>> classes;
-  // Continuation phase behind the lane kernel: one warp per parked instance
-  // with its own staged program, warps in one-warp blocks; classes by the
-  // per-warp shared memory (program + instance region) so a small program
-  // is not given the largest one's slice. Largest first.
-  std::vector<std::unique_ptr<Class>> cont_classes;
   // warps of a block that shares one program: up to this many, as the
   // group's program and instance regions fit the block's shared memory
   static constexpr int kSharedWarpsMax = 16;
-  // continuation tiles per group (one-warp blocks), and whether the
-  // continuation runs them (else the shared-program blocks of `classes`)
-  static constexpr int kContTiles = 4;
-  bool cont_warps = true;
+
   cudaEvent_t start_ev = nullptr;
   // timing events of the last run: before the lane kernel, after it, after
   // the warp kernels joined back
@@ -1975,10 +2044,10 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       for (int t = 0; t < std::min(nt, 12); ++t) C->tiles3.push_back(g);
     }
     if (C->tiles.empty()) continue;
-    // shared-program tiles: two consecutive ones per group (measured best
-    // against one, three, four, eight, and round-robin orders)
-    for (int g : members)
-      for (int t = 0; t < 2; ++t) C->tiles2.push_back(g);
+    // shared-program tiles of the continuation: one per group; the block's
+    // warps take every instance the lane phase parked in it, and a group
+    // that parked none is skipped before its program is staged
+    for (int g : members) C->tiles2.push_back(g);
     gk::batch_kernel_info(C->m, C->warps_per_block, C->region, C->prog_ints, &C->regs,
                           &C->blocks_per_sm);
     if (C->blocks_per_sm <= 0) {
@@ -2027,47 +2096,6 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       return nullptr;
     B->classes.push_back(std::move(C));
   }
-  if (lanes_on) {
-    // continuation classes by per-warp footprint: program ints x 4 plus the
-    // instance region's doubles x 8 (M = 1)
-    const int bounds_kb[] = {8, 12, 16, 24, 32, 48, 64, 96, 160, 227};
-    const int nb = (int)(sizeof(bounds_kb) / sizeof(bounds_kb[0]));
-    std::vector<std::vector<int>> cm(nb);
-    for (int g : gorder) {  // most expensive programs first
-      const gk::GroupHdr& h = B->groups[g];
-      if (h.inst_count == 0) continue;
-      const size_t f = (size_t)h.prog * 4 + (size_t)gregion[g] * 8;
-      int k = 0;
-      while (k < nb - 1 && f > (size_t)bounds_kb[k] * 1024) ++k;
-      cm[k].push_back(g);
-    }
-    for (int k = nb - 1; k >= 0; --k) {
-      if (cm[k].empty()) continue;
-      auto C = std::make_unique<gpuklu_batch::Class>();
-      C->m = 1;
-      C->warps_per_block = 1;
-      for (int g : cm[k]) {
-        const gk::GroupHdr& h = B->groups[g];
-        C->region = std::max(C->region, gregion[g]);
-        C->prog_ints = std::max(C->prog_ints, h.prog);
-        // a few tiles per group: a group rarely parks more instances, and
-        // a warp that finds its group's instances taken moves on at once
-        for (int t = 0; t < std::min(h.inst_count, gpuklu_batch::kContTiles); ++t)
-          C->tiles.push_back(g);
-      }
-      gk::batch_kernel_info(1, 1, C->region, C->prog_ints, &C->regs, &C->blocks_per_sm);
-      if (C->blocks_per_sm <= 0) {
-        fprintf(stderr, "gpuklu_batch_create: a circuit needs %d KB of shared memory\n",
-                (int)((C->region * 8 + C->prog_ints * 4) / 1024));
-        return nullptr;
-      }
-      C->grid = std::min<int>(sm_count() * C->blocks_per_sm, (int)C->tiles.size());
-      if (cudaStreamCreateWithFlags(&C->stream, cudaStreamNonBlocking) != cudaSuccess ||
-          cudaEventCreateWithFlags(&C->done, cudaEventDisableTiming) != cudaSuccess)
-        return nullptr;
-      B->cont_classes.push_back(std::move(C));
-    }
-  }
   if (cudaEventCreateWithFlags(&B->start_ev, cudaEventDisableTiming) != cudaSuccess) return nullptr;
   for (auto& ev : B->ph_ev)
     if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
@@ -2102,16 +2130,10 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     if (e == cudaSuccess) e = C->d_tiles3.upload(C->tiles3, s);
     if (e == cudaSuccess) e = C->d_counter.resize(1);
   }
-  for (auto& C : B->cont_classes) {
-    if (e == cudaSuccess) e = C->d_tiles.upload(C->tiles, s);
-    if (e == cudaSuccess) e = C->d_counter.resize(1);
-  }
   // Lane phase: every group split into tiles of about lane_target instances,
   // most expensive programs first; a scratch of region x 32 doubles per warp.
   {
     B->lanes = lanes_on;
-    const char* econt = getenv("GPUKLU_CONT");
-    B->cont_warps = !(econt && strcmp(econt, "shared") == 0);
     const char* ecap = getenv("GPUKLU_LANE_CAP");
     B->lane_cap = ecap ? std::max(1, atoi(ecap)) : 6;
     const char* etgt = getenv("GPUKLU_LANE_TARGET");
@@ -2224,16 +2246,15 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     a.cont_prev = B->d_cont_prev.p;
   }
   B->args = a;
-  for (auto* cl : {&B->classes, &B->cont_classes})
-    for (auto& C : *cl) {
-      C->args = a;
-      C->args.tile_group = C->d_tiles.p;
-      C->args.ntiles = (int)C->tiles.size();
-      C->args.counter = C->d_counter.p;
-      C->args.region = C->region;
-      C->args.prog_ints = C->prog_ints;
-      C->args.shared_bytes = C->shared_bytes;
-    }
+  for (auto& C : B->classes) {
+    C->args = a;
+    C->args.tile_group = C->d_tiles.p;
+    C->args.ntiles = (int)C->tiles.size();
+    C->args.counter = C->d_counter.p;
+    C->args.region = C->region;
+    C->args.prog_ints = C->prog_ints;
+    C->args.shared_bytes = C->shared_bytes;
+  }
   B->transient = transient;
   B->dt = dt;
   return B.release();
@@ -2425,7 +2446,6 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
   cudaStream_t s = b->stream;
   cudaMemsetAsync(b->d_gnext.p, 0, b->d_gnext.n * sizeof(unsigned), s);
   for (auto& C : b->classes) cudaMemsetAsync(C->d_counter.p, 0, sizeof(unsigned), s);
-  for (auto& C : b->cont_classes) cudaMemsetAsync(C->d_counter.p, 0, sizeof(unsigned), s);
   if (b->lanes) {  // phase 1: lane per instance, then the warp classes take the parked ones
     cudaMemsetAsync(b->d_lcounter.p, 0, sizeof(unsigned), s);
     cudaMemsetAsync(b->d_cont_count.p, 0, b->d_cont_count.n * sizeof(unsigned), s);
@@ -2439,21 +2459,6 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
   }
   cudaEventRecord(b->ph_ev[1], s);
   cudaEventRecord(b->start_ev, s);
-  if (b->lanes && b->cont_warps && !b->cont_classes.empty()) {
-    for (auto& C : b->cont_classes) {  // largest programs first, all classes concurrent
-      cudaStreamWaitEvent(C->stream, b->start_ev, 0);
-      C->args.cfg = c;
-      gk::BatchArgs ca = C->args;
-      ca.cont_mode = 1;
-      gk::launch_batch_newton(ca, 1, C->grid, 1, C->stream, false);
-      cudaEventRecord(C->done, C->stream);
-      cudaStreamWaitEvent(s, C->done, 0);
-    }
-    cudaEventRecord(b->ph_ev[2], s);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return b->fail(cuda_msg(e, "batch launch"));
-    return GPUKLU_OK;
-  }
   for (auto& C : b->classes) {  // largest programs first, all classes concurrent
     cudaStreamWaitEvent(C->stream, b->start_ev, 0);
     C->args.cfg = c;
@@ -2546,10 +2551,7 @@ int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out) {
   if (!b) return GPUKLU_INVALID_MATRIX;
   for (int q = 0; q < 8; ++q) out[q] = 0;
   out[2] = (int64_t)b->groups.size();
-  out[6] = (int64_t)(b->lanes && b->cont_warps && !b->cont_classes.empty()
-                         ? b->cont_classes.size()
-                         : b->classes.size()) +
-           (b->lanes ? 1 : 0);
+  out[6] = (int64_t)b->classes.size() + (b->lanes ? 1 : 0);
   for (auto& C : b->classes) {  // the largest class (first) describes the launch
     out[0] += C->grid;
     if (out[1] == 0) {

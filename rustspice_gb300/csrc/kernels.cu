@@ -1277,6 +1277,21 @@ __global__ void k_rcond(DPlan P, const double* __restrict__ lu, double* out) {
   }
 }
 
+// Pivot growth after a refactorization with kept pivots: one thread per
+// column scans its multipliers (L slots after the pivot); a block with one
+// above lim - the kept pivot is below 1/lim of the largest entry under it,
+// the rule the first factorization swaps on - is marked.
+__global__ void k_growth(DPlan P, const double* __restrict__ lu, double lim, int* grow) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= P.n) return;
+  const int s1 = P.col_ptr[k + 1];
+  for (int s = P.dslot[k] + 1; s < s1; ++s)
+    if (!(fabs(lu[s]) <= lim)) {
+      grow[P.pos_block[k]] = 1;
+      return;
+    }
+}
+
 // --------------------------------------------------------------- batched
 // One warp owns M instances of one circuit program at a time and keeps all
 // of their state in shared memory (batch_common.cuh); each Newton iteration
@@ -1319,7 +1334,18 @@ __global__ void k_batch_newton(BatchArgs A) {
   while (true) {
     int ti = 0;
     if (SHARED) {
-      if (threadIdx.x == 0) s_tile = (int)atomicAdd(A.counter, 1u);
+      // a continuation tile whose group has no parked instance left is
+      // skipped before its program is staged: most groups park none
+      if (threadIdx.x == 0) {
+        int t = (int)atomicAdd(A.counter, 1u);
+        while (A.cont_mode && t < A.ntiles) {
+          const int gg = A.tile_group[t];
+          if (*(volatile unsigned*)&A.gnext2[gg] < *(volatile unsigned*)&A.cont_count[gg])
+            break;
+          t = (int)atomicAdd(A.counter, 1u);
+        }
+        s_tile = t;
+      }
       __syncthreads();
       ti = s_tile;
     } else {
@@ -1328,12 +1354,6 @@ __global__ void k_batch_newton(BatchArgs A) {
     }
     if (ti >= A.ntiles) return;
     const int g = A.tile_group[ti];
-    // a continuation tile whose group has no parked instance left is
-    // skipped before its program is staged (tiles outnumber the instances
-    // the lane phase parks)
-    if (!SHARED && A.cont_mode &&
-        *(volatile unsigned*)&A.gnext2[g] >= *(volatile unsigned*)&A.cont_count[g])
-      continue;
     const GroupHdr G = A.groups[g];
     const int pg = SHARED ? G.prog : A.prog_ints;
     const int rg = SHARED ? G.region : A.region;
@@ -1589,6 +1609,11 @@ void launch_param_grad(const DCircuit& C, const double* x, int xlen, const doubl
 void launch_newton_update(int m, int n, double* x, const double* xnew, NewtonState* st,
                           NewtonCfg cfg, int* status, cudaStream_t s) {
   k_newton_update<<<1, 1024, 0, s>>>(m, n, x, xnew, st, cfg, status);
+}
+
+void launch_growth(const DPlan& P, const double* lu, double lim, int* grow, cudaStream_t s) {
+  if (P.n <= 0) return;
+  k_growth<<<(P.n + 255) / 256, 256, 0, s>>>(P, lu, lim, grow);
 }
 
 void launch_rcond(const DPlan& P, const double* lu, double* out2, cudaStream_t s) {

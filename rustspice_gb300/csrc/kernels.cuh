@@ -225,6 +225,9 @@ void launch_param_grad(const DCircuit& C, const double* x, int xlen, const doubl
 void launch_newton_update(int m, int n, double* x, const double* xnew, NewtonState* st,
                           NewtonCfg cfg, int* status, cudaStream_t s);
 void launch_rcond(const DPlan& P, const double* lu, double* out2, cudaStream_t s);
+// Pivot growth of a factorization: grow[b] = 1 for every BTF block b with a
+// multiplier |l_ik| > lim (or a NaN one); grow is not cleared here.
+void launch_growth(const DPlan& P, const double* lu, double lim, int* grow, cudaStream_t s);
 // Measured FP64 fused multiply-add throughput of the current device [TFLOP/s].
 double fp64_peak_tflops();
 // m: instances per warp (1, 2 or 4); region: shared doubles per instance.

@@ -101,6 +101,14 @@ class GpuKluSolver:
     def set_pivot_mode(self, mode: int) -> None:
         self._check(N.lib().gpuklu_set_pivot_mode(self._h, mode))
 
+    def set_repivot(self, on: bool) -> None:
+        """Growth-triggered re-pivot after refactorizations (off: the
+        reference's kept pivots)."""
+        self._check(N.lib().gpuklu_set_repivot(self.handle, int(bool(on))))
+
+    def repivots(self) -> int:
+        return int(N.lib().gpuklu_repivot_count(self.handle))
+
     def stats(self) -> dict:
         s = N.Stats()
         self._check(N.lib().gpuklu_get_stats(self._h, C.byref(s)))

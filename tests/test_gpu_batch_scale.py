@@ -32,8 +32,10 @@ derivatives of the stamped current), so the damping rule's comparison of
 successive step norms decides on near ties. There the contracted arithmetic
 of the batch kernels and the oracle's part ways: the converged sets may
 differ on at most 2 % of the instances and the iteration counts of the
-instances both converge on may differ on at most 15 %, every converged
-operating point still within 1e-10. test_device_sweep_matches_oracle runs
+instances both converge on may differ on at most 15 %. Converging linearly,
+an iterate that passes the step test (1e-10 relative) can still be farther
+than that from the fixed point, so the converged operating points are held
+to 1e-9 relative for this model. test_device_sweep_matches_oracle runs
 the same points through the bit-exact single-circuit kernels and agrees with
 the oracle at every point.
 """
@@ -67,10 +69,10 @@ def _run(model):
     return B, bt, it, rs, x, it_o, rs_o, x_o
 
 
-@pytest.mark.parametrize("model,frac,set_diff,it_agree",
-                         [("consistent", (0.98, 0.99), 0.0, 0.99),
-                          ("reference", (0.55, 0.65), 0.02, 0.85)])
-def test_stratified_batch_matches_oracle(model, frac, set_diff, it_agree):
+@pytest.mark.parametrize("model,frac,set_diff,it_agree,xtol",
+                         [("consistent", (0.98, 0.99), 0.0, 0.99, 1e-10),
+                          ("reference", (0.55, 0.65), 0.02, 0.85, 1e-9)])
+def test_stratified_batch_matches_oracle(model, frac, set_diff, it_agree, xtol):
     B, bt, it, rs, x, it_o, rs_o, x_o = _run(model)
     conv_o = rs_o == 0
     conv = rs == 0
@@ -94,7 +96,7 @@ def test_stratified_batch_matches_oracle(model, frac, set_diff, it_agree):
         xo = x_o[i, :n]
         worst = max(worst, float(np.max(np.abs(xg - xo)) / max(1.0, np.max(np.abs(xo)))))
     print(f"{model}: worst relative difference of a converged operating point {worst:.2e}")
-    assert worst <= 1e-10
+    assert worst <= xtol
     # the failures sit where the first stage switches: by input point
     bad_vin = np.unique(B.vin[~conv_o])
     print(f"{model}: input points with a non-converged instance: {bad_vin.round(2).tolist()}")
@@ -131,24 +133,43 @@ def test_device_sweep_matches_oracle(model, chains):
 
 def test_device_sweep_continuation_matches_oracle():
     """The reference's .dc exactly: each point from the previous point's
-    solution, stopping at the first failure. A consistent-model chain sweeps
-    all 61 points; the reference model from the zero start fails at the first
-    point and the sweep ends there, as the reference's does."""
+    solution (with its aux currents, which the convergence test then covers)
+    and a stop at the first failure. A diode ladder's source swept up from
+    0 V beside two resistor-loaded NMOS stages converges at every point; a
+    reference-model inverter chain from the engine's zero start fails at the
+    first point and the sweep ends there, on the device as in the oracle."""
     from rustspice_gb300 import circuits as cz
+    from rustspice_gb300 import netlist as nl
     from rustspice_gb300.solver import DeviceCircuit, GpuKluSolver, dc_sweep
-    vals = cz.vin_points(61)
+    deck = nl.compile_deck("""* resistor-loaded NMOS stages beside a diode ladder
+VDD vdd 0 DC 1.8
+VIN in 0 DC 0.9
+RL1 vdd mid 20k
+MN1 mid in 0 0 nch W=2u L=1u
+RL2 vdd out 20k
+MN2 out mid 0 0 nch W=2u L=1u
+V1 a 0 DC 0.0
+R1 a b 1k
+D1 b 0 dx
+R2 b c 2k
+D2 c 0 dx
+.model nch nmos level=1 vto=0.45 u0=400
+.model dx d is=1e-14
+.end
+""")
+    chain = cz.inverter_chain(24, 0.0, seed=3, chain_id=7, mos_model="reference")
     cfg = N.newton_config(**wl.TIGHT)
-    for model, c in (("consistent", cz.inverter_chain(24, 0.0, seed=3, chain_id=7)),
-                     ("reference", cz.inverter_chain(24, 0.0, seed=3, chain_id=7,
-                                                     mos_model="reference"))):
-        rs_o, it_o, x_o, xl_o = po.dc_sweep(c, 1, vals, "nativeklu_exact", **NEWTON)
+    for name, c, src, vals in (("ladder", deck.circuit, deck.device_names.index("V1"),
+                                np.linspace(0.0, 1.0, 21)),
+                               ("chain", chain, 1, cz.vin_points(61))):
+        rs_o, it_o, x_o, xl_o = po.dc_sweep(c, src, vals, "nativeklu_exact", **NEWTON)
         g = GpuKluSolver(1, pivot_mode=N.PIVOT_EXACT)
-        r = dc_sweep(g, DeviceCircuit(c), cfg, 1, vals)
-        assert np.array_equal(r.reason, rs_o) and np.array_equal(r.iterations, it_o), model
+        r = dc_sweep(g, DeviceCircuit(c), cfg, src, vals)
+        assert np.array_equal(r.reason, rs_o) and np.array_equal(r.iterations, it_o), name
         assert np.array_equal(r.x_len, xl_o)
         for q in np.flatnonzero(rs_o == 0):
             assert np.max(np.abs(r.x[q] - x_o[q])) <= 1e-12 * max(1.0, np.max(np.abs(x_o[q])))
-        if model == "consistent":
+        if name == "ladder":
             assert np.all(rs_o == 0)
         else:
             assert rs_o[0] == 1 and np.all(rs_o[1:] == -1)
