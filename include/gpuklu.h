@@ -105,6 +105,21 @@ int gpuklu_set_pivot_mode(gpuklu_handle* h, int mode);
 int gpuklu_set_repivot(gpuklu_handle* h, int on);
 /* Re-pivots since the last pattern change (the count reset_pattern clears). */
 int64_t gpuklu_repivot_count(const gpuklu_handle* h);
+/* Failure detection; no counterpart in the reference, whose solver runs on
+ * the CPU and cannot stall (its error paths are SolverError, solver.rs:
+ * 76-92, and the Newton loop's SolverFailure, newton.rs:85-91).
+ * Spin limit: polls of a dependency flag (grid refactorization, grid and
+ * transpose solves, the one-block refactorization) before the waiting warp
+ * gives up; the kernel then ends normally and the call returns
+ * GPUKLU_DEVICE_TIMEOUT, with the handle still usable. 0 restores the
+ * default, 2^22 polls (seconds of waiting). */
+int gpuklu_set_spin_limit(gpuklu_handle* h, uint32_t polls);
+/* Off (default): a Newton iterate with a NaN or an infinity runs on to the
+ * iteration cap and ends with reason 1, as the reference's loop does (its
+ * convergence test is false for NaN). On: gpuklu_newton_dc and
+ * gpuklu_dc_sweep end at the first such iterate with GPUKLU_NONFINITE,
+ * reason 2 and the iterations run so far. */
+int gpuklu_set_stop_on_nonfinite(gpuklu_handle* h, int on);
 /* Counters of NativeKluStats (native_klu.rs:584-594) plus device figures. */
 int gpuklu_get_stats(gpuklu_handle* h, gpuklu_stats* out);
 /* Text of the last error on this handle ("" if none). */

@@ -279,6 +279,7 @@ struct PlanDev {
     d.pos_block = pos_block.p;
     d.block_ptr = block_ptr.p;
     d.task = task.p;
+    d.spin_limit = gk::kSpinLimit;
     dp = d;
     dpt = d;
     dpt.task = ttask.p;
@@ -521,6 +522,16 @@ struct gpuklu_handle {
   int64_t repivot_count = 0;
   DBuf<int> d_grow;
   static constexpr double kPivotTol = 0.001;
+  // Polls of a dependency flag before a waiting warp gives up
+  // (gpuklu_set_spin_limit); applied to both resident plans.
+  unsigned spin_limit = gk::kSpinLimit;
+  // End the device Newton loop at the first non-finite iterate
+  // (gpuklu_set_stop_on_nonfinite; off: the reference runs on to the cap).
+  bool stop_nonfinite = false;
+
+  void apply_spin_limit() {
+    for (PlanDev* p : {&pd, &pd_sym}) p->dp.spin_limit = p->dpt.spin_limit = spin_limit;
+  }
 
   int fail(int code, const std::string& m) {
     err = m;
@@ -547,6 +558,7 @@ struct gpuklu_handle {
 
   int upload_plan() {
     cudaError_t e = pd.upload(plan, stream);
+    apply_spin_limit();
     if (e == cudaSuccess) e = d_lu.resize(std::max(plan.nslots(), 1));
     if (e != cudaSuccess) return cuda_fail(e, "upload plan");
     // one-block refactor and solve for small factorizations (GPUKLU_ONE_BLOCK=0: off)
@@ -588,6 +600,7 @@ struct gpuklu_handle {
     cudaError_t e = cudaSuccess;
     if (!pd_sym_ok) {
       e = pd_sym.upload(sym_plan, stream);
+      apply_spin_limit();
       if (e != cudaSuccess) return cuda_fail(e, "upload plan");
       pd_sym_ok = true;
     }
@@ -992,6 +1005,19 @@ int gpuklu_set_repivot(gpuklu_handle* h, int on) {
 
 int64_t gpuklu_repivot_count(const gpuklu_handle* h) { return h ? h->repivot_count : 0; }
 
+int gpuklu_set_stop_on_nonfinite(gpuklu_handle* h, int on) {
+  if (!h) return GPUKLU_INVALID_MATRIX;
+  h->stop_nonfinite = on != 0;
+  return GPUKLU_OK;
+}
+
+int gpuklu_set_spin_limit(gpuklu_handle* h, uint32_t polls) {
+  if (!h) return GPUKLU_INVALID_MATRIX;
+  h->spin_limit = polls == 0 ? gk::kSpinLimit : polls;
+  h->apply_spin_limit();
+  return GPUKLU_OK;
+}
+
 int gpuklu_set_pivot_mode(gpuklu_handle* h, int mode) {
   if (!h || (mode != GPUKLU_PIVOT_REFERENCE && mode != GPUKLU_PIVOT_EXACT))
     return GPUKLU_INVALID_MATRIX;
@@ -1282,7 +1308,7 @@ int dc_newton_run(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_confi
   nc_.damping_min = cfg->damping_min;
   const double gstart = std::max(cfg->gmin * 1e3, 1e-6);
   int64_t total = 0, last_iters = 0;
-  int rsn = 1;
+  int rsn = 1, ret = GPUKLU_OK;
   bool conv = false, failed = false;
   for (int64_t gi = 0; gi <= cfg->gmin_steps && !conv && !failed; ++gi) {
     const double gmin =
@@ -1302,6 +1328,7 @@ int dc_newton_run(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_confi
         st = h->factor_on_device(h->state != gpuklu_handle::FACTORED);
         if (st == GPUKLU_OK) st = h->solve_on_device(false, false);
         if (st != GPUKLU_OK) {
+          if (st == GPUKLU_DEVICE_TIMEOUT) ret = st;
           rsn = 2;
           failed = true;
           ++it;
@@ -1320,12 +1347,21 @@ int dc_newton_run(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_confi
         if (dst == GPUKLU_DEVICE_TIMEOUT) {
           cudaMemset(h->d_status.p, 0, sizeof(int));
           h->err = "device dependency wait timed out";
+          ret = GPUKLU_DEVICE_TIMEOUT;
           rsn = 2;
           failed = true;
           ++it;
           break;
         }
         if (dst) cudaMemset(h->d_status.p, 0, sizeof(int));
+        if (dst == GPUKLU_NONFINITE && h->stop_nonfinite) {
+          h->err = "non-finite Newton iterate at iteration " + std::to_string(it + 1);
+          ret = GPUKLU_NONFINITE;
+          rsn = 2;
+          failed = true;
+          ++it;
+          break;
+        }
         if (hs.converged) {
           conv = true;
           rsn = 0;
@@ -1348,7 +1384,7 @@ int dc_newton_run(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_confi
   if (iters) *iters = last_iters;
   if (iters_total) *iters_total = total;
   if (reason) *reason = rsn;
-  return GPUKLU_OK;
+  return ret;
 }
 }  // namespace
 
@@ -1406,7 +1442,8 @@ int gpuklu_dc_sweep(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_con
     int64_t len = 0, it = 0, itt = 0;
     int rsn = 1;
     const int st = dc_newton_run(h, c, cfg, start, m, xbuf.data(), c->n, &len, &it, &itt, &rsn);
-    if (st != GPUKLU_OK) return st;
+    // a wait that timed out or a non-finite stop still reports its point
+    if (st != GPUKLU_OK && st != GPUKLU_DEVICE_TIMEOUT && st != GPUKLU_NONFINITE) return st;
     m = (int)len;
     if (x_out)
       for (int64_t i = 0; i < c->n; ++i) x_out[k * x_stride + i] = i < len ? xbuf[i] : 0.0;
@@ -1414,6 +1451,7 @@ int gpuklu_dc_sweep(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_con
     if (iters) iters[k] = it;
     if (iters_total) iters_total[k] = itt;
     if (reason) reason[k] = rsn;
+    if (st != GPUKLU_OK) return st;
     if (rsn != 0 && stop_on_failure) break;  // engine.rs:785-796
   }
   return GPUKLU_OK;

@@ -13,11 +13,6 @@ enum DevStatus : int {
   DS_NONFINITE = 8,
 };
 
-// Upper bound on polls of a dependency flag before a kernel gives up, sets
-// DS_TIMEOUT and returns. With the back-off below this is a few seconds of
-// waiting at most.
-constexpr unsigned kSpinLimit = 1u << 22;
-
 // Arithmetic without contraction: every product is rounded before it is
 // added, as in the reference (Rust never fuses multiply-add), so results are
 // reproducible bit for bit against the CPU restatement.
@@ -35,12 +30,14 @@ __device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
 }
 __device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
 
-// Waits until flag == epoch. Returns false on timeout or when another warp
-// has already reported an error; the caller then stops its work.
-__device__ __forceinline__ bool wait_flag(const unsigned* flag, unsigned epoch, int* status) {
+// Waits until flag == epoch, at most `limit` polls (DPlan::spin_limit).
+// Returns false on timeout or when another warp has already reported an
+// error; the caller then stops its work.
+__device__ __forceinline__ bool wait_flag(const unsigned* flag, unsigned epoch, int* status,
+                                          unsigned limit) {
   unsigned spins = 0;
   while (ld_acquire(flag) != epoch) {
-    if (++spins > kSpinLimit) {
+    if (++spins > limit) {
       atomicCAS(status, DS_OK, DS_TIMEOUT);
       return false;
     }

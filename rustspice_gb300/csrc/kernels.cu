@@ -445,7 +445,7 @@ __global__ void k_refactor(DPlan P, const double* __restrict__ ax, double* lu,
         if (i + 1 < cnt) fetch(i + 1);  // independent of this entry's update
         if (!((ready >> i) & 1u)) {
           int ok = 1;
-          if (lane == 0) ok = wait_flag(&flags[cj], epoch, status);
+          if (lane == 0) ok = wait_flag(&flags[cj], epoch, status, P.spin_limit);
           if (!__shfl_sync(FULL, ok, 0)) return;
           __syncwarp();
           const int q = cqa + lane;
@@ -494,7 +494,7 @@ __global__ void k_refactor(DPlan P, const double* __restrict__ ax, double* lu,
 template <class Coef, class Dep>
 __device__ __forceinline__ bool ordered_dot(double& v, int e0, int e1, Coef coef, Dep dep,
                                             const unsigned* flag, const double* val,
-                                            unsigned epoch, int* status) {
+                                            unsigned epoch, int* status, unsigned limit) {
   const int lane = threadIdx.x & 31;
   for (int base = e0; base < e1; base += 32) {
     const int e = base + lane;
@@ -502,7 +502,7 @@ __device__ __forceinline__ bool ordered_dot(double& v, int e0, int e1, Coef coef
     int ok = 1;
     if (e < e1) {
       const int d = dep(e);
-      ok = wait_flag(&flag[d], epoch, status);
+      ok = wait_flag(&flag[d], epoch, status, limit);
       if (ok) prod = coef(e) * ld_cg(&val[d]);
     }
     if (!__all_sync(FULL, ok)) return false;
@@ -531,11 +531,11 @@ __global__ void k_solve(DPlan P, const double* __restrict__ rhs, const double* _
       double v = rhs[P.in_row[i]];
       bool ok = ordered_dot(
           v, P.offd_ptr[i], P.offd_ptr[i + 1], [&](int e) { return ax[P.offd_raw[e]]; },
-          [&](int e) { return P.offd_col[e]; }, xflag, x, epoch, status);
+          [&](int e) { return P.offd_col[e]; }, xflag, x, epoch, status, P.spin_limit);
       if (ok)
         ok = ordered_dot(
             v, P.lrow_ptr[i], P.lrow_ptr[i + 1], [&](int e) { return lu[P.lrow_slot[e]]; },
-            [&](int e) { return P.lrow_col[e]; }, zflag, z, epoch, status);
+            [&](int e) { return P.lrow_col[e]; }, zflag, z, epoch, status, P.spin_limit);
       if (!ok) return;
       if (lane == 0) {
         z[i] = v;
@@ -544,12 +544,12 @@ __global__ void k_solve(DPlan P, const double* __restrict__ rhs, const double* _
       }
     } else {  // backward: U
       int ok = 1;
-      if (lane == 0) ok = wait_flag(&zflag[i], epoch, status);
+      if (lane == 0) ok = wait_flag(&zflag[i], epoch, status, P.spin_limit);
       if (!__shfl_sync(FULL, ok, 0)) return;
       double v = ld_cg(&z[i]);
       ok = ordered_dot(
           v, P.urow_ptr[i], P.urow_ptr[i + 1], [&](int e) { return lu[P.urow_slot[e]]; },
-          [&](int e) { return P.urow_col[e]; }, xflag, x, epoch, status);
+          [&](int e) { return P.urow_col[e]; }, xflag, x, epoch, status, P.spin_limit);
       if (!ok) return;
       if (lane == 0) {
         v = v / lu[P.dslot[i]];
@@ -581,11 +581,11 @@ __global__ void k_tsolve(DPlan P, const double* __restrict__ g, const double* __
       double v = g[P.out_col[k]];
       bool ok = ordered_dot(
           v, P.offdT_ptr[k], P.offdT_ptr[k + 1], [&](int e) { return ax[P.offdT_raw[e]]; },
-          [&](int e) { return P.offdT_row[e]; }, xflag, x, epoch, status);
+          [&](int e) { return P.offdT_row[e]; }, xflag, x, epoch, status, P.spin_limit);
       if (ok)
         ok = ordered_dot(
             v, P.col_ptr[k], P.dslot[k], [&](int e) { return lu[e]; },
-            [&](int e) { return P.slot_row[e]; }, zflag, z, epoch, status);
+            [&](int e) { return P.slot_row[e]; }, zflag, z, epoch, status, P.spin_limit);
       if (!ok) return;
       if (lane == 0) {
         v = v / lu[P.dslot[k]];
@@ -595,12 +595,12 @@ __global__ void k_tsolve(DPlan P, const double* __restrict__ g, const double* __
       }
     } else {  // L^T row k = L column k
       int ok = 1;
-      if (lane == 0) ok = wait_flag(&zflag[k], epoch, status);
+      if (lane == 0) ok = wait_flag(&zflag[k], epoch, status, P.spin_limit);
       if (!__shfl_sync(FULL, ok, 0)) return;
       double v = ld_cg(&z[k]);
       ok = ordered_dot(
           v, P.dslot[k] + 1, P.col_ptr[k + 1], [&](int e) { return lu[e]; },
-          [&](int e) { return P.slot_row[e]; }, xflag, x, epoch, status);
+          [&](int e) { return P.slot_row[e]; }, xflag, x, epoch, status, P.spin_limit);
       if (!ok) return;
       if (lane == 0) {
         x[k] = v;
@@ -686,7 +686,7 @@ __global__ void __launch_bounds__(1024) k_refactor_cta(DPlan P, const double* __
       if (lane == 0) {
         unsigned spins = 0;
         while (ld_acquire_cta(&sdone[j0]) == 0u) {
-          if (++spins > kSpinLimit) {
+          if (++spins > P.spin_limit) {
             atomicCAS(status, DS_OK, DS_TIMEOUT);
             ok = 0;
             break;

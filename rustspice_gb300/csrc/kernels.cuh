@@ -5,6 +5,11 @@
 
 namespace gk {
 
+// Default bound on polls of a dependency flag before a waiting warp gives up,
+// sets DS_TIMEOUT and returns. With the kernels' back-off this is a few
+// seconds of waiting at most. A handle may lower it (gpuklu_set_spin_limit).
+constexpr unsigned kSpinLimit = 1u << 22;
+
 // Device pointers of one Plan (see analysis.h for the meaning of each array).
 struct DPlan {
   int n, nslots, nblocks, ntask;
@@ -24,6 +29,9 @@ struct DPlan {
   // and chunks [grp[4g+2], grp[4g+3]) of cs_gchunk / cs_gop.
   int cs_ngrp, cs_grp_rows;     // groups; rows of the largest
   const int *cs_grp, *cs_gchunk, *cs_gop;
+  // Polls of a dependency flag before a waiting warp gives up and reports
+  // DS_TIMEOUT (kSpinLimit unless the handle sets another).
+  unsigned spin_limit;
 };
 
 // Device form of a compiled circuit (device list + stamp-to-slot map).

@@ -26,7 +26,8 @@ PIVOT_REFERENCE, PIVOT_EXACT = 0, 1
 SYMBOLS = [
     "gpuklu_create", "gpuklu_destroy", "gpuklu_prepare", "gpuklu_analyze", "gpuklu_factor",
     "gpuklu_solve", "gpuklu_reset_pattern", "gpuklu_name", "gpuklu_set_parallel_threads",
-    "gpuklu_set_pivot_mode", "gpuklu_set_repivot", "gpuklu_repivot_count", "gpuklu_get_stats", "gpuklu_last_error", "gpuklu_pivot_pass_count", "gpuklu_factor_device",
+    "gpuklu_set_pivot_mode", "gpuklu_set_repivot", "gpuklu_repivot_count",
+    "gpuklu_set_spin_limit", "gpuklu_set_stop_on_nonfinite", "gpuklu_get_stats", "gpuklu_last_error", "gpuklu_pivot_pass_count", "gpuklu_factor_device",
     "gpuklu_solve_device", "gpuklu_tsolve", "gpuklu_stream", "gpuklu_compile_devices",
     "gpuklu_circuit_free", "gpuklu_circuit_dims", "gpuklu_circuit_pattern",
     "gpuklu_circuit_set_params", "gpuklu_stamp", "gpuklu_newton_dc", "gpuklu_dc_sweep", "gpuklu_batch_create",
@@ -80,6 +81,8 @@ def lib(build_if_missing: bool = True):
         "gpuklu_set_pivot_mode": (C.c_int, [_P, C.c_int]),
         "gpuklu_set_repivot": (C.c_int, [_P, C.c_int]),
         "gpuklu_repivot_count": (_I64, [_P]),
+        "gpuklu_set_spin_limit": (C.c_int, [_P, C.c_uint32]),
+        "gpuklu_set_stop_on_nonfinite": (C.c_int, [_P, C.c_int]),
         "gpuklu_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
         "gpuklu_last_error": (C.c_char_p, [_P]),
         "gpuklu_pivot_pass_count": (_I64, [_P]),

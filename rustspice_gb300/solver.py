@@ -109,6 +109,17 @@ class GpuKluSolver:
     def repivots(self) -> int:
         return int(N.lib().gpuklu_repivot_count(self.handle))
 
+    def set_spin_limit(self, polls: int) -> None:
+        """Polls of a device dependency flag before the waiting warp gives up
+        and the call raises SolverError(DEVICE_TIMEOUT); 0: the default."""
+        self._check(N.lib().gpuklu_set_spin_limit(self.handle, int(polls)))
+
+    def set_stop_on_nonfinite(self, on: bool) -> None:
+        """End the device Newton loop at the first NaN/Inf iterate with
+        SolverError(NONFINITE) (off: run on to the iteration cap, as the
+        reference does)."""
+        self._check(N.lib().gpuklu_set_stop_on_nonfinite(self.handle, int(bool(on))))
+
     def stats(self) -> dict:
         s = N.Stats()
         self._check(N.lib().gpuklu_get_stats(self._h, C.byref(s)))
