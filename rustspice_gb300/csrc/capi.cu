@@ -2082,10 +2082,15 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       for (int t = 0; t < std::min(nt, 12); ++t) C->tiles3.push_back(g);
     }
     if (C->tiles.empty()) continue;
-    // shared-program tiles of the continuation: one per group; the block's
-    // warps take every instance the lane phase parked in it, and a group
-    // that parked none is skipped before its program is staged
-    for (int g : members) C->tiles2.push_back(g);
+    // shared-program tiles of the continuation: two consecutive ones per
+    // group, so two blocks share the parked instances of a large program
+    // whose block holds few warps (one tile per group: 122 ms for the
+    // iteration-capped instances of the inverter-chain batch against 59;
+    // two were measured best against three, four, eight and round-robin
+    // orders). A tile whose group has nothing parked left is skipped before
+    // its program is staged.
+    for (int g : members)
+      for (int t = 0; t < 2; ++t) C->tiles2.push_back(g);
     gk::batch_kernel_info(C->m, C->warps_per_block, C->region, C->prog_ints, &C->regs,
                           &C->blocks_per_sm);
     if (C->blocks_per_sm <= 0) {
