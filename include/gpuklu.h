@@ -90,6 +90,31 @@ void gpuklu_set_parallel_threads(gpuklu_handle* h, size_t threads);
 
 /* Pivot mode for the next analysis (default GPUKLU_PIVOT_REFERENCE). */
 int gpuklu_set_pivot_mode(gpuklu_handle* h, int mode);
+/* Which of the reference's LinearSolver implementations the handle
+ * restates (default NATIVEKLU); a change resets the pattern. Each is a drop-
+ * in for its namesake, bit for bit:
+ * NATIVEKLU     NativeKluSolver (native_klu.rs:659-1675);
+ * SPARSELU      SparseLuSolver (sparse_lu.rs:217-745): one block, AMD, no
+ *               row exchanges, pivots below 1e-14 set to +-1e-14;
+ * SPARSELU_BTF  SparseLuBtfSolver (sparse_lu_btf.rs:137-672): BTF when
+ *               should_use_btf (btf.rs:560-573) gives >= 2 blocks below n,
+ *               one SparseLU per block, the block coupling applied as its
+ *               solve_btf does (:441-561); else one SparseLU;
+ * DENSE         DenseSolver (solver.rs:596-724): the values summed into a
+ *               row-major n x n array, LU with partial pivoting (the first
+ *               row of largest magnitude), GPUKLU_FACTOR_FAILED for a column
+ *               without a nonzero candidate; any pattern is accepted by
+ *               analyze, a wrong ap length fails the factorization with
+ *               GPUKLU_ANALYZE_FAILED; n up to GPUKLU_DENSE_MAX_N; no
+ *               transpose solve. */
+enum {
+  GPUKLU_KIND_NATIVEKLU = 0,
+  GPUKLU_KIND_SPARSELU = 1,
+  GPUKLU_KIND_SPARSELU_BTF = 2,
+  GPUKLU_KIND_DENSE = 3
+};
+#define GPUKLU_DENSE_MAX_N 2048
+int gpuklu_set_solver_kind(gpuklu_handle* h, int kind);
 /* Growth-triggered re-pivot, off by default (the reference's refactorization
  * always keeps the first factorization's pivots, native_klu.rs:1020-1148,
  * and only perturbs a tiny one to +-1e-14, :1344-1348). On: after every
@@ -390,7 +415,8 @@ double gpuklu_fp64_peak_tflops(void);
 /* ------------------------------------------------ host-only diagnostics */
 
 /* The symbolic plan the handle would build for a pattern (host work only; no
- * device needed): BTF + AMD + symbolic, and, if row_perm is not NULL, the
+ * device needed) in a pivot mode and for a solver kind (GPUKLU_KIND_*): BTF +
+ * AMD + symbolic, and, if row_perm is not NULL, the
  * pivot sequence installed as a first factorization would (block-local
  * row_perm per position). Arrays are read back by name with
  * gpuklu_plan_array: "col_ptr", "dslot", "slot_row", "upd_ptr", "upd_dst",
@@ -401,9 +427,14 @@ double gpuklu_fp64_peak_tflops(void);
  * nnz_u, noffdiag, offd_lower, swaps). */
 typedef struct gpuklu_plan gpuklu_plan;
 gpuklu_plan* gpuklu_plan_build(int64_t n, const int64_t* ap, const int64_t* ai, int pivot_mode,
-                               const int32_t* row_perm);
+                               int kind, const int32_t* row_perm);
 int64_t gpuklu_plan_array(const gpuklu_plan* p, const char* name, int64_t* out, int64_t cap);
 void gpuklu_plan_free(gpuklu_plan* p);
+/* btf_decompose (crates/sim-core/src/btf.rs:143-550) on the host: out[0] the
+ * number of blocks, out[1] the largest block's size - what
+ * MatrixProperties::analyze (solver.rs:276-301) reads for the solver
+ * selector. */
+int gpuklu_btf_info(int64_t n, const int64_t* ap, const int64_t* ai, int64_t* out);
 
 #ifdef __cplusplus
 }

@@ -428,11 +428,13 @@ const char* const kTooLarge =
     "the factorization's update lists exceed 2^31 entries (fill too large for this solver)";
 
 std::string analyze(int n, const i64* ap, const i64* ai, int pivot_mode, Plan& p,
-                    const std::vector<int>* given_blocks) {
+                    const std::vector<int>* given_blocks, int kind) {
   p = Plan();
   p.n = n;
   p.nnz_raw = ap[n];
   p.pivot_mode = pivot_mode;
+  p.kind = kind;
+  p.no_singleton = kind != KIND_NATIVEKLU || given_blocks != nullptr;
   for (int c = 0; c < n; ++c) {
     if (ap[c + 1] < ap[c]) return "column pointers decrease";
     for (i64 t = ap[c]; t < ap[c + 1]; ++t)
@@ -457,6 +459,16 @@ std::string analyze(int n, const i64* ap, const i64* ai, int pivot_mode, Plan& p
     b.col_inv.resize(n);
     for (int i = 0; i < n; ++i) b.col_perm[i] = b.row_inv[i] = b.col_inv[i] = i;
     keep = b.nblocks >= 2;
+  } else if (kind == KIND_SPARSELU) {
+    keep = false;
+  } else if (kind == KIND_SPARSELU_BTF) {
+    // should_use_btf (btf.rs:560-573) on the raw entry count, then the
+    // decomposition's own test (sparse_lu_btf.rs:197-208)
+    const double density = (double)ap[n] / ((double)n * (double)n);
+    if (n >= 50 && !(density > 0.25)) {
+      b = btf_decompose(n, ap, ai);
+      keep = b.nblocks >= 2 && b.max_block < n;
+    }
   } else if (n >= 4 && !structurally_irreducible(n, ap, ai)) {
     b = btf_decompose(n, ap, ai);
     keep = b.nblocks >= 2 && b.max_block < n;
@@ -578,7 +590,7 @@ void finalize_plan(Plan& p, const i64* ap, const i64* ai, const std::vector<Patt
     for (int c = 0; c < nb; ++c) {
       int kg = b0 + c;
       p.pos_block[kg] = k;
-      p.col_single[kg] = nb == 1;
+      p.col_single[kg] = nb == 1 && !p.no_singleton;
       p.col_ptr[kg] = (int)p.slot_row.size();
       for (int q = s.up[c]; q < s.up[c + 1]; ++q) p.slot_row.push_back(b0 + s.ui[q]);
       p.dslot[kg] = (int)p.slot_row.size() - 1;

@@ -54,6 +54,16 @@ void symbolic_dfs(int n, const std::vector<i64>& pap, const std::vector<i64>& pa
 
 enum PivotMode : int { PIVOT_REFERENCE = 0, PIVOT_EXACT = 1 };
 
+// Which of the reference's sparse solvers a plan restates:
+// NATIVEKLU  native_klu.rs: BTF (n >= 4, >= 2 blocks, largest < n), AMD per
+//            block, threshold pivoting, singleton rule for 1x1 blocks;
+// SPARSELU   sparse_lu.rs: one block, AMD, no row exchanges, every pivot
+//            below 1e-14 in magnitude set to +-1e-14 (:117, :495-499);
+// SPARSELU_BTF sparse_lu_btf.rs: BTF when should_use_btf (btf.rs:560-573:
+//            n >= 50, density <= 0.25) finds >= 2 blocks all below n
+//            (:191-226), then one SparseLU per block; else one SparseLU.
+enum SolverKind : int { KIND_NATIVEKLU = 0, KIND_SPARSELU = 1, KIND_SPARSELU_BTF = 2 };
+
 // Everything the kernels need for one matrix pattern.
 struct Plan {
   int n = 0;
@@ -81,6 +91,11 @@ struct Plan {
   // index), as NativeKLU's row_perm / row_perm_inv.
   std::vector<i32> row_perm, row_inv;  // [n], block-local values
   int pivot_mode = PIVOT_REFERENCE;
+  int kind = KIND_NATIVEKLU;
+  // 1x1 blocks take the general +-1e-14 rule instead of the singleton rule
+  // (SparseLU's blocks, and the BBD solver's, which the reference factors
+  // with SparseLU)
+  bool no_singleton = false;
   bool too_large = false;  // update lists beyond int32 indexing: not factorable here
   bool pivots_known = false;
   i64 swaps = 0;
@@ -129,12 +144,13 @@ struct Plan {
 };
 
 // Builds the Plan for pattern (ap, ai) of dimension n: BTF kept under the
-// reference's rule (n >= 4, >= 2 blocks, largest block < n), AMD per block,
-// symbolic DFS. Pivots start as the identity.
+// rule of the solver kind, AMD per block, symbolic DFS. Pivots start as the
+// identity.
 // given_blocks: boundaries of diagonal blocks the caller guarantees (no
 // entry outside them); they replace the BTF, with the identity row order.
 std::string analyze(int n, const i64* ap, const i64* ai, int pivot_mode, Plan& p,
-                    const std::vector<int>* given_blocks = nullptr);
+                    const std::vector<int>* given_blocks = nullptr,
+                    int kind = KIND_NATIVEKLU);
 
 // Installs a pivot sequence (block-local row_perm for every position) found
 // by the first factorization and rebuilds what depends on it: in exact mode

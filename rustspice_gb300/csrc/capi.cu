@@ -482,6 +482,46 @@ struct gpuklu_handle {
   // the first factorization (the reference's SparseLU keeps the diagonal).
   std::vector<int> given_blocks;
   bool no_swap = false;
+  // Which of the reference's sparse solvers this handle restates
+  // (gpuklu_set_solver_kind); the SparseLU kinds never exchange rows.
+  int kind = GPUKLU_KIND_NATIVEKLU;
+  bool swap_off() const { return no_swap || kind != GPUKLU_KIND_NATIVEKLU; }
+  // DenseSolver (GPUKLU_KIND_DENSE): the pattern on the device, the row-major
+  // LU and its row order
+  DBuf<int64_t> d_dap, d_dai;
+  DBuf<double> d_dense;
+  DBuf<int> d_dpiv;
+  static constexpr int64_t kDenseMaxN = GPUKLU_DENSE_MAX_N;
+
+  int dense_analyze(const int64_t* ap, int64_t ap_len, const int64_t* ai, int64_t ai_len) {
+    if (ap_len != n + 1)  // build_dense (solver.rs:621-623)
+      return fail(GPUKLU_ANALYZE_FAILED, "Column pointer length " + std::to_string(ap_len) +
+                                             " != expected " + std::to_string(n + 1));
+    if (n > kDenseMaxN)
+      return fail(GPUKLU_INVALID_MATRIX, "dense solver: n = " + std::to_string(n) +
+                                             " above GPUKLU_DENSE_MAX_N = " +
+                                             std::to_string(kDenseMaxN));
+    if (ap[n] != ai_len || ap[0] != 0)
+      return fail(GPUKLU_INVALID_MATRIX, "ap[n] does not match the row index count");
+    last_ap.assign(ap, ap + ap_len);
+    last_ai.assign(ai, ai + ai_len);
+    const size_t nn = (size_t)std::max<int64_t>(n, 1);
+    cudaError_t e = d_dap.upload(last_ap, stream);
+    if (e == cudaSuccess) e = d_dai.resize(std::max<int64_t>(ai_len, 1));
+    if (e == cudaSuccess && ai_len > 0)
+      e = cudaMemcpyAsync(d_dai.p, ai, ai_len * sizeof(int64_t), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = d_ax.resize(std::max<int64_t>(ai_len, 1));
+    if (e == cudaSuccess) e = d_dense.resize(nn * nn);
+    if (e == cudaSuccess) e = d_dpiv.resize(nn);
+    for (auto* b : {&d_rhs, &d_out, &d_xnew, &d_newx})  // solve and Newton vectors
+      if (e == cudaSuccess) e = b->resize(nn);
+    if (e == cudaSuccess) e = d_status.resize(1);
+    if (e == cudaSuccess) e = d_nstate.resize(1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_status.p, 0, sizeof(int), stream);
+    if (e != cudaSuccess) return cuda_fail(e, "dense buffers");
+    state = ANALYZED;
+    return GPUKLU_OK;
+  }
   cudaStream_t stream = nullptr;
   DBuf<double> d_ax, d_lu, d_z, d_x, d_out, d_rhs, d_work, d_rc, d_rhs_c, d_xnew, d_newx,
       d_scratch2;
@@ -577,23 +617,25 @@ struct gpuklu_handle {
   const gk::Plan& cur_plan() const { return state == FACTORED ? plan : sym_plan; }
 
   int do_analyze(const int64_t* ap, int64_t ap_len, const int64_t* ai, int64_t ai_len) {
+    if (kind == GPUKLU_KIND_DENSE) return dense_analyze(ap, ap_len, ai, ai_len);
     if (ap_len != n + 1)
       return fail(GPUKLU_INVALID_MATRIX, "Column pointer length " + std::to_string(ap_len) +
                                              " != expected " + std::to_string(n + 1));
     if (ap[n] != ai_len || ap[0] != 0)
       return fail(GPUKLU_INVALID_MATRIX, "ap[n] does not match the row index count");
-    if (!(sym_mode == pivot_mode && sym_plan.n == n && (int64_t)sym_ap.size() == ap_len &&
+    const int key = pivot_mode + 4 * kind;
+    if (!(sym_mode == key && sym_plan.n == n && (int64_t)sym_ap.size() == ap_len &&
           (int64_t)sym_ai.size() == ai_len && std::equal(sym_ap.begin(), sym_ap.end(), ap) &&
           std::equal(sym_ai.begin(), sym_ai.end(), ai))) {
       pd_sym_ok = piv_ok = false;
       piv_cand.clear();
       sym_mode = -1;
       std::string m = gk::analyze((int)n, ap, ai, pivot_mode, sym_plan,
-                                  given_blocks.empty() ? nullptr : &given_blocks);
+                                  given_blocks.empty() ? nullptr : &given_blocks, kind);
       if (!m.empty()) return fail(GPUKLU_INVALID_MATRIX, m);
       sym_ap.assign(ap, ap + ap_len);
       sym_ai.assign(ai, ai + ai_len);
-      sym_mode = pivot_mode;
+      sym_mode = key;
     }
     last_ap.assign(ap, ap + ap_len);
     last_ai.assign(ai, ai + ai_len);
@@ -696,7 +738,7 @@ struct gpuklu_handle {
     gk::PivotCheck pc;
     pc.cand = d_cand.p;
     pc.want = d_want.p;
-    pc.tol = no_swap ? 0.0 : 0.001;
+    pc.tol = swap_off() ? 0.0 : 0.001;
     for (int pass = 0; pass < kMaxPivotPasses; ++pass) {
       gk::pivot_pass_amap(P, cand_row, aptr, aidx, rperm);
       e = d_pamap_ptr.upload(aptr, stream);
@@ -763,7 +805,7 @@ struct gpuklu_handle {
       for (int b = 0; b < sym_plan.nblocks; ++b)
         maxblk = std::max(maxblk, sym_plan.block_ptr[b + 1] - sym_plan.block_ptr[b]);
       gk::launch_first_factor(pd_sym.dp, maxblk, d_ax.p, d_lu.p, d_work.p, d_rperm.p,
-                              d_rinv.p, no_swap ? 0.0 : kPivotTol, d_status.p, stream);
+                              d_rinv.p, swap_off() ? 0.0 : kPivotTol, d_status.p, stream);
       cudaError_t e = cudaMemcpyAsync(rperm.data(), d_rperm.p, n * sizeof(i32),
                                       cudaMemcpyDeviceToHost, stream);
       if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
@@ -823,10 +865,19 @@ struct gpuklu_handle {
 
   int factor_on_device(bool sync) {
     rcond_valid = false;
+    if (kind == GPUKLU_KIND_DENSE) {  // every factorization is a full one
+      gk::launch_dense_factor((int)n, d_dap.p, d_dai.p, d_ax.p, d_dense.p, d_dpiv.p, d_status.p,
+                              stream);
+      ++factor_count;
+      state = FACTORED;
+      const int st = check_status("dense factor");
+      if (st) state = ANALYZED;
+      return st;
+    }
     if (state == FACTORED) {
       refactor_launch();
       ++refactor_count;
-      if (repivot && !no_swap) {
+      if (repivot && !swap_off()) {
         const int st = repivot_grown();
         if (st) return st;
       }
@@ -861,6 +912,12 @@ struct gpuklu_handle {
 
   // Solve with rhs in d_rhs; result in d_out (original column order).
   int solve_on_device(bool transpose, bool sync) {
+    if (kind == GPUKLU_KIND_DENSE) {
+      if (transpose) return fail(GPUKLU_SOLVE_FAILED, "dense solver: no transpose solve");
+      gk::launch_dense_solve((int)n, d_dense.p, d_dpiv.p, d_rhs.p, d_out.p, d_status.p, stream);
+      if (!sync) return GPUKLU_OK;
+      return check_status("dense solve");
+    }
     if ((cta_sol || cta_grp) && !transpose) {
       if (cta_grp)
         gk::launch_solve_groups(pd.dp, d_rhs.p, d_ax.p, d_lu.p, d_out.p, stream);
@@ -922,6 +979,9 @@ void gpuklu_prepare(gpuklu_handle* h, int64_t n) {
 int gpuklu_analyze(gpuklu_handle* h, const int64_t* ap, int64_t ap_len, const int64_t* ai,
                    int64_t ai_len) {
   if (!h) return GPUKLU_INVALID_MATRIX;
+  // DenseSolver::analyze accepts any pattern (solver.rs:680-682); its factor
+  // reports a bad one
+  if (h->kind == GPUKLU_KIND_DENSE && ap_len != h->n + 1) return GPUKLU_OK;
   if (h->state != gpuklu_handle::EMPTY && h->same_pattern(ap, ap_len, ai, ai_len))
     return GPUKLU_OK;
   return h->do_analyze(ap, ap_len, ai, ai_len);
@@ -950,9 +1010,10 @@ int gpuklu_factor_device(gpuklu_handle* h, const double* d_ax) {
 
 int gpuklu_solve(gpuklu_handle* h, double* rhs, int64_t len) {
   if (!h || h->state != gpuklu_handle::FACTORED) return GPUKLU_SOLVE_FAILED;
-  if (len != h->n)
-    return h->fail(GPUKLU_INVALID_MATRIX, "RHS length " + std::to_string(len) +
-                                              " != matrix dimension " + std::to_string(h->n));
+  if (len != h->n)  // DenseSolver::solve reports SolveFailed (solver.rs:689-691)
+    return h->fail(h->kind == GPUKLU_KIND_DENSE ? GPUKLU_SOLVE_FAILED : GPUKLU_INVALID_MATRIX,
+                   "RHS length " + std::to_string(len) + " != matrix dimension " +
+                       std::to_string(h->n));
   cudaError_t e = cudaMemcpyAsync(h->d_rhs.p, rhs, len * sizeof(double),
                                   cudaMemcpyHostToDevice, h->stream);
   if (e != cudaSuccess) return h->cuda_fail(e, "solve upload");
@@ -993,7 +1054,12 @@ void gpuklu_reset_pattern(gpuklu_handle* h) {
   if (h) h->reset();
 }
 
-const char* gpuklu_name(const gpuklu_handle*) { return "GpuKLU"; }
+const char* gpuklu_name(const gpuklu_handle* h) {
+  if (h && h->kind == GPUKLU_KIND_SPARSELU) return "GpuSparseLU";
+  if (h && h->kind == GPUKLU_KIND_SPARSELU_BTF) return "GpuSparseLU-BTF";
+  if (h && h->kind == GPUKLU_KIND_DENSE) return "GpuDense";
+  return "GpuKLU";
+}
 
 void gpuklu_set_parallel_threads(gpuklu_handle*, size_t) {}
 
@@ -1018,6 +1084,16 @@ int gpuklu_set_spin_limit(gpuklu_handle* h, uint32_t polls) {
   return GPUKLU_OK;
 }
 
+int gpuklu_set_solver_kind(gpuklu_handle* h, int kind) {
+  if (!h || kind < GPUKLU_KIND_NATIVEKLU || kind > GPUKLU_KIND_DENSE)
+    return GPUKLU_INVALID_MATRIX;
+  if (kind != h->kind) {
+    h->kind = kind;
+    h->reset();
+  }
+  return GPUKLU_OK;
+}
+
 int gpuklu_set_pivot_mode(gpuklu_handle* h, int mode) {
   if (!h || (mode != GPUKLU_PIVOT_REFERENCE && mode != GPUKLU_PIVOT_EXACT))
     return GPUKLU_INVALID_MATRIX;
@@ -1030,7 +1106,8 @@ int gpuklu_set_pivot_mode(gpuklu_handle* h, int mode) {
 
 int gpuklu_get_stats(gpuklu_handle* h, gpuklu_stats* out) {
   if (!h || !out) return GPUKLU_INVALID_MATRIX;
-  if (h->state == gpuklu_handle::FACTORED && !h->rcond_valid) {
+  if (h->state == gpuklu_handle::FACTORED && !h->rcond_valid &&
+      h->kind != GPUKLU_KIND_DENSE) {
     gk::launch_rcond(h->pd.dp, h->d_lu.p, h->d_rc.p, h->stream);
     double mm[2];
     cudaMemcpyAsync(mm, h->d_rc.p, sizeof(mm), cudaMemcpyDeviceToHost, h->stream);
@@ -3173,6 +3250,8 @@ cudaError_t noalloc_scratch(unsigned char** out) {
 
 extern "C" int gpuklu_solve_device_noalloc(gpuklu_handle* h, const double* d_rhs, double* d_x) {
   if (!h || h->state != gpuklu_handle::FACTORED) return GPUKLU_SOLVE_FAILED;
+  if (h->kind == GPUKLU_KIND_DENSE)
+    return h->fail(GPUKLU_SOLVE_FAILED, "gpuklu_solve_device_noalloc: not for the dense solver");
   if (h->n > GPUKLU_NOALLOC_MAX_N)
     return h->fail(GPUKLU_INVALID_MATRIX,
                    "gpuklu_solve_device_noalloc: n = " + std::to_string(h->n) +
@@ -3215,10 +3294,22 @@ extern "C" {
 
 double gpuklu_fp64_peak_tflops(void) { return gk::fp64_peak_tflops(); }
 
+int gpuklu_btf_info(int64_t n, const int64_t* ap, const int64_t* ai, int64_t* out) {
+  if (n < 0 || !out || (n > 0 && (!ap || !ai))) return GPUKLU_INVALID_MATRIX;
+  if (n == 0) {
+    out[0] = out[1] = 0;
+    return GPUKLU_OK;
+  }
+  const gk::BtfResult b = gk::btf_decompose((int)n, ap, ai);
+  out[0] = b.nblocks;
+  out[1] = b.max_block;
+  return GPUKLU_OK;
+}
+
 gpuklu_plan* gpuklu_plan_build(int64_t n, const int64_t* ap, const int64_t* ai, int pivot_mode,
-                               const int32_t* row_perm) {
+                               int kind, const int32_t* row_perm) {
   auto P = std::make_unique<gpuklu_plan>();
-  std::string m = gk::analyze((int)n, ap, ai, pivot_mode, P->p);
+  std::string m = gk::analyze((int)n, ap, ai, pivot_mode, P->p, nullptr, kind);
   if (!m.empty()) {
     fprintf(stderr, "gpuklu_plan_build: %s\n", m.c_str());
     return nullptr;

@@ -253,6 +253,11 @@ void launch_bbd_ysolve(const DPlan& P, const double* lu, const double* ax, const
 void launch_bbd_schur(const double* ax, const BbdArgs& B, const double* ybuf, double* S,
                       cudaStream_t s);
 void launch_dense_lu(double* S, int bs, cudaStream_t s);
+// The reference's DenseSolver (dense.cu).
+void launch_dense_factor(int n, const int64_t* ap, const int64_t* ai, const double* ax,
+                         double* A, int* piv, int* status, cudaStream_t s);
+void launch_dense_solve(int n, const double* A, const int* piv, const double* rhs, double* out,
+                        int* status, cudaStream_t s);
 void launch_dense_lu_solve(const double* S, int bs, double* x, cudaStream_t s);
 void launch_bbd_border_rhs(const double* ax, const double* rhs, const double* z,
                            const BbdArgs& B, double* bb, cudaStream_t s);

@@ -21,12 +21,14 @@ _lib = None
 OK, ANALYZE_FAILED, FACTOR_FAILED, SOLVE_FAILED, SINGULAR, ILL_CONDITIONED, \
     INVALID_MATRIX, DEVICE_TIMEOUT, NONFINITE, CUDA_ERROR = range(10)
 PIVOT_REFERENCE, PIVOT_EXACT = 0, 1
+# Solver kinds (gpuklu_set_solver_kind), by the oracle's / reference's names
+KINDS = {"nativeklu": 0, "sparselu": 1, "sparselubtf": 2, "dense": 3}
 
 # Every symbol the header declares; a test checks the library exports them.
 SYMBOLS = [
     "gpuklu_create", "gpuklu_destroy", "gpuklu_prepare", "gpuklu_analyze", "gpuklu_factor",
     "gpuklu_solve", "gpuklu_reset_pattern", "gpuklu_name", "gpuklu_set_parallel_threads",
-    "gpuklu_set_pivot_mode", "gpuklu_set_repivot", "gpuklu_repivot_count",
+    "gpuklu_set_pivot_mode", "gpuklu_set_solver_kind", "gpuklu_set_repivot", "gpuklu_repivot_count",
     "gpuklu_set_spin_limit", "gpuklu_set_stop_on_nonfinite", "gpuklu_get_stats", "gpuklu_last_error", "gpuklu_pivot_pass_count", "gpuklu_factor_device",
     "gpuklu_solve_device", "gpuklu_tsolve", "gpuklu_stream", "gpuklu_compile_devices",
     "gpuklu_circuit_free", "gpuklu_circuit_dims", "gpuklu_circuit_pattern",
@@ -35,7 +37,7 @@ SYMBOLS = [
     "gpuklu_batch_update_inputs", "gpuklu_batch_last_error", "gpuklu_batch_info",
     "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_batch_phase_ms", "gpuklu_ac_sweep", "gpuklu_tran_create", "gpuklu_tran_forward",
     "gpuklu_tran_backward", "gpuklu_bbd_create", "gpuklu_bbd_destroy", "gpuklu_bbd_last_error",
-    "gpuklu_bbd_info", "gpuklu_bbd_perm", "gpuklu_bbd_factor", "gpuklu_bbd_solve", "gpuklu_bbd_newton_dc", "gpuklu_fp64_peak_tflops", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free",
+    "gpuklu_bbd_info", "gpuklu_bbd_perm", "gpuklu_bbd_factor", "gpuklu_bbd_solve", "gpuklu_bbd_newton_dc", "gpuklu_fp64_peak_tflops", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free", "gpuklu_btf_info",
 ]
 
 
@@ -80,6 +82,7 @@ def lib(build_if_missing: bool = True):
         "gpuklu_set_parallel_threads": (None, [_P, C.c_size_t]),
         "gpuklu_set_pivot_mode": (C.c_int, [_P, C.c_int]),
         "gpuklu_set_repivot": (C.c_int, [_P, C.c_int]),
+        "gpuklu_set_solver_kind": (C.c_int, [_P, C.c_int]),
         "gpuklu_repivot_count": (_I64, [_P]),
         "gpuklu_set_spin_limit": (C.c_int, [_P, C.c_uint32]),
         "gpuklu_set_stop_on_nonfinite": (C.c_int, [_P, C.c_int]),
@@ -126,9 +129,10 @@ def lib(build_if_missing: bool = True):
         "gpuklu_fp64_peak_tflops": (_D, []),
         "gpuklu_solve_device_noalloc": (C.c_int, [_P, _P, _P]),
         "gpuklu_dc_backward": (C.c_int, [_P, _P, _P, _I64, _P, _D, _P, _P]),
-        "gpuklu_plan_build": (_P, [_I64, _P, _P, C.c_int, _P]),
+        "gpuklu_plan_build": (_P, [_I64, _P, _P, C.c_int, C.c_int, _P]),
         "gpuklu_plan_array": (_I64, [_P, C.c_char_p, _P, _I64]),
         "gpuklu_plan_free": (None, [_P]),
+        "gpuklu_btf_info": (C.c_int, [_I64, _P, _P, _P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -170,11 +174,11 @@ class Plan:
              "lrow_ptr", "lrow_col", "lrow_slot", "urow_ptr", "urow_col", "urow_slot",
              "cs_chunk", "cs_op", "cs_grp", "cs_gchunk", "cs_gop", "task", "ttask"]
 
-    def __init__(self, n, ap, ai, pivot_mode=PIVOT_REFERENCE, row_perm=None):
+    def __init__(self, n, ap, ai, pivot_mode=PIVOT_REFERENCE, row_perm=None, kind="nativeklu"):
         L = lib()
         ap, ai = i64(ap), i64(ai)
         rp = i32(row_perm) if row_perm is not None else None
-        h = L.gpuklu_plan_build(n, ptr(ap), ptr(ai), pivot_mode,
+        h = L.gpuklu_plan_build(n, ptr(ap), ptr(ai), pivot_mode, KINDS[kind],
                                 ptr(rp) if rp is not None else None)
         if not h:
             raise ValueError("plan build failed")

@@ -571,15 +571,28 @@ class Deck:
     options: dict              # lower-case option -> value string
     initial: dict              # node id -> .ic voltage
     analyses: list             # control commands seen (".op", ".dc", ...)
+    option_seq: list = dataclasses.field(default_factory=list)  # (key, value) in deck order
+
+    def sim_options(self):
+        """The deck's .option values as the reference's SimOptions holds them
+        (types, ranges and defaults of options.rs), set in deck order."""
+        from .options import SimOptions
+        return SimOptions.from_pairs(self.option_seq)
 
     def newton_options(self) -> dict:
-        """The Newton settings the reference derives from the options."""
-        def num(key, default):
-            v = self.options.get(key)
-            x = parse_number(v) if v is not None else None
-            return default if x is None else x
-        return {"max_iters": int(num("itl1", 100)), "abs_tol": num("vntol", 1e-6),
-                "rel_tol": num("reltol", 1e-3), "gmin": num("gmin", 1e-12)}
+        """The Newton settings the reference derives from the options
+        (engine.rs:986-999)."""
+        o = self.sim_options()
+        return {"max_iters": o.get_int("itl1"), "abs_tol": o.get_float("vntol"),
+                "rel_tol": o.get_float("reltol"), "gmin": o.get_float("gmin")}
+
+    def solver_kind(self) -> str:
+        """The device solver kind for `.option solver=` (engine.rs:971-984,
+        solver.rs:169-230), sized by the node count as the engine does."""
+        from .options import solver_type_from_options
+        from .solver import solver_kind
+        return solver_kind(solver_type_from_options(self.sim_options()),
+                           self.circuit.node_count)
 
     def transient_x0(self) -> np.ndarray:
         """A transient's starting point: zeros with the .ic voltages
@@ -615,7 +628,7 @@ def compile_deck(text: str, name: str = "") -> Deck:
             order.append(s)
         return names[s]
 
-    models, options, initial, analyses = {}, {}, {}, []
+    models, options, initial, analyses, option_seq = {}, {}, {}, [], []
     for st in controls:  # controls first (as the reference builds the circuit)
         if st.control == ".model":
             if len(st.args) < 2:
@@ -624,8 +637,10 @@ def compile_deck(text: str, name: str = "") -> Deck:
         elif st.control == ".option" or st.control == ".options":
             for k, v in st.params:
                 options[k.lower()] = v
+                option_seq.append((k, v))
             for a in st.args:
                 options[a.lower()] = "true"
+                option_seq.append((a, "true"))
         elif st.control == ".ic":
             for k, v in st.params:
                 key = k.strip().lower()
@@ -700,7 +715,7 @@ def compile_deck(text: str, name: str = "") -> Deck:
         dev_names.append(st.name)
     c = Circuit(len(order), np.asarray(t, np.int32), np.asarray(nd, np.int32).reshape(-1, 4),
                 np.asarray(p, np.float64).reshape(-1, NPARAM), name)
-    return Deck(c, order, dev_names, options, initial, analyses or [".op"])
+    return Deck(c, order, dev_names, options, initial, analyses or [".op"], option_seq)
 
 
 def _path_key(path: str):

@@ -37,7 +37,10 @@ class SolverError(RuntimeError):
 class GpuKluSolver:
     """Drop-in for NativeKluSolver / KluSolver behind the LinearSolver trait."""
 
-    def __init__(self, n: int = 0, pivot_mode: int = N.PIVOT_REFERENCE):
+    def __init__(self, n: int = 0, pivot_mode: int = N.PIVOT_REFERENCE,
+                 kind: str = "nativeklu"):
+        """kind: the reference solver restated - "nativeklu" (NativeKluSolver),
+        "sparselu" (SparseLuSolver) or "sparselubtf" (SparseLuBtfSolver)."""
         L = N.lib()
         self._h = L.gpuklu_create(n)
         if not self._h:
@@ -45,6 +48,8 @@ class GpuKluSolver:
         self._n = n
         if pivot_mode != N.PIVOT_REFERENCE:
             L.gpuklu_set_pivot_mode(self._h, pivot_mode)
+        if kind != "nativeklu":
+            self._check(L.gpuklu_set_solver_kind(self._h, N.KINDS[kind]))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -536,3 +541,117 @@ class BbdSolver:
                                                  C.byref(itt), C.byref(rs)))
         return NewtonResult(rs.value == 0, it.value, itt.value, REASONS[rs.value], x[:xl.value])
 
+
+
+# ---------------------------------------------------------------- selection
+# The reference's solver factory and selector (crates/sim-core/src/solver.rs:
+# 169-258, 262-562) for its default build, which has neither the `klu`
+# feature nor faer: KLU and Faer requests fall back to SparseLU (:174-196),
+# and "auto" is Dense up to 50 unknowns, SparseLU up to 500, SparseLU-BTF
+# beyond (:215-246). Every kind runs on the device through GpuKluSolver.
+SOLVER_TYPES = ("dense", "sparselu", "sparselubtf", "bbd", "faer", "klu", "nativeklu", "auto")
+
+
+def solver_kind(solver_type: str, n: int) -> str:
+    """The device solver kind create_solver(solver_type, n) amounts to."""
+    if solver_type not in SOLVER_TYPES:
+        raise ValueError(f"unknown solver type {solver_type!r}")
+    if solver_type == "auto":
+        if n <= 50:
+            return "dense"
+        return "sparselubtf" if n > 500 else "sparselu"
+    if solver_type in ("klu", "faer"):
+        return "sparselu"
+    if solver_type == "bbd":
+        raise NotImplementedError("the BBD solver here takes a known partition: use BbdSolver")
+    return solver_type
+
+
+def create_solver(solver_type: str, n: int) -> GpuKluSolver:
+    """create_solver (solver.rs:169-200)."""
+    return GpuKluSolver(n, kind=solver_kind(solver_type, n))
+
+
+def create_solver_auto(n: int) -> GpuKluSolver:
+    """create_solver_auto (solver.rs:215-246)."""
+    return create_solver("auto", n)
+
+
+@dataclasses.dataclass
+class MatrixProperties:
+    """MatrixProperties (solver.rs:243-338)."""
+    n: int
+    nnz: int
+    density: float
+    avg_degree: float
+    has_block_structure: bool
+    num_blocks: int
+    max_block_ratio: float
+
+    @classmethod
+    def analyze(cls, n: int, ap, ai) -> "MatrixProperties":
+        if n == 0:
+            return cls(0, 0, 0.0, 0.0, False, 0, 0.0)
+        ap, ai = N.i64(ap), N.i64(ai)
+        nnz = int(ap[n])
+        out = np.zeros(2, np.int64)
+        st = N.lib().gpuklu_btf_info(n, N.ptr(ap), N.ptr(ai), N.ptr(out))
+        if st != N.OK:
+            raise SolverError(st, "btf analysis")
+        nb, mx = int(out[0]), int(out[1])
+        return cls(n, nnz, nnz / float(n * n), nnz / float(n), nb > 1 and mx < n, nb, mx / float(n))
+
+    @classmethod
+    def analyze_quick(cls, n: int, ap, _ai=None) -> "MatrixProperties":
+        if n == 0:
+            return cls(0, 0, 0.0, 0.0, False, 1, 1.0)
+        nnz = int(np.asarray(ap)[n])
+        return cls(n, nnz, nnz / float(n * n), nnz / float(n), False, 1, 1.0)
+
+
+@dataclasses.dataclass
+class SolverSelector:
+    """SolverSelector (solver.rs:383-527): the decision tree of the default
+    build on a matrix's properties, with the reason text."""
+    properties: MatrixProperties
+    selected: str
+    reason: str
+
+    @classmethod
+    def select(cls, n: int, ap, ai) -> "SolverSelector":
+        return cls.select_from_properties(MatrixProperties.analyze(n, ap, ai))
+
+    @classmethod
+    def select_quick(cls, n: int, ap, ai=None) -> "SolverSelector":
+        return cls.select_from_properties(MatrixProperties.analyze_quick(n, ap, ai))
+
+    @classmethod
+    def select_from_properties(cls, p: MatrixProperties) -> "SolverSelector":
+        n, density = p.n, p.density
+        if n <= 50:
+            return cls(p, "dense", f"Small matrix (n={n}) - Dense solver has lowest overhead")
+        if density > 0.3 and n <= 200:
+            return cls(p, "dense", f"Dense matrix ({density * 100.0:.1f}% fill, n={n}) - "
+                                   "Dense solver efficient")
+        if p.has_block_structure and p.num_blocks > 1:
+            est = p.num_blocks ** 2 / (1.0 + p.max_block_ratio ** 3 * p.num_blocks)
+            return cls(p, "sparselubtf",
+                       f"Block structure detected ({p.num_blocks} blocks, max "
+                       f"{p.max_block_ratio * 100.0:.0f}% of n) - SparseLU-BTF "
+                       f"~{max(est, 1.0):.1f}x faster")
+        if n >= 200 and density < 0.15:
+            return cls(p, "bbd", f"Large sparse matrix (n={n}, {density * 100.0:.1f}% fill) - "
+                                 "BBD partitioning")
+        if n > 500:
+            return cls(p, "sparselubtf",
+                       f"Large matrix (n={n}) - SparseLU-BTF may find hidden structure")
+        return cls(p, "sparselu", f"Medium sparse matrix (n={n}, {density * 100.0:.1f}% fill) - "
+                                  "SparseLU selected")
+
+    def create_solver(self) -> GpuKluSolver:
+        return create_solver(self.selected, self.properties.n)
+
+
+def create_solver_for_matrix(n: int, ap, ai) -> GpuKluSolver:
+    """create_solver_for_matrix (solver.rs:551-554)."""
+    return SolverSelector.select(n, ap, ai).create_solver()

@@ -331,8 +331,11 @@ def solve_groups(P: native.Plan, ax, lu, rhs):
 class EmulatedSolver:
     """LinearSolver call sequence over the emulated kernels."""
 
-    def __init__(self, mode=native.PIVOT_REFERENCE):
+    def __init__(self, mode=native.PIVOT_REFERENCE, kind="nativeklu"):
         self.mode = mode
+        self.kind = kind
+        # the SparseLU kinds never exchange rows
+        self.tol = 0.001 if kind == "nativeklu" else 0.0
         self.plan = None
         self.key = None
         self.lu = None
@@ -342,11 +345,11 @@ class EmulatedSolver:
         key = (n, ap.tobytes(), ai.tobytes())
         if key != self.key:
             self.key = key
-            self.plan = native.Plan(n, ap, ai, self.mode)
+            self.plan = native.Plan(n, ap, ai, self.mode, kind=self.kind)
             self.factored = False
         if not self.factored:
-            lu, rperm = first_factor(self.plan, ax)
-            self.plan = native.Plan(n, ap, ai, self.mode, row_perm=rperm)
+            lu, rperm = first_factor(self.plan, ax, self.tol)
+            self.plan = native.Plan(n, ap, ai, self.mode, row_perm=rperm, kind=self.kind)
             self.lu = lu if self.mode == native.PIVOT_REFERENCE else refactor(self.plan, ax)
             self.factored = True
         else:

@@ -16,7 +16,7 @@ from oracle import pyoracle as po
 from rustspice_gb300 import circuits as cz
 from rustspice_gb300 import native as N
 from rustspice_gb300 import workloads as wl
-from rustspice_gb300.solver import DeviceCircuit, GpuKluSolver, newton_dc
+from rustspice_gb300.solver import DeviceCircuit, GpuKluSolver, SolverError, newton_dc
 
 pytestmark = pytest.mark.gpu
 
@@ -206,4 +206,166 @@ def test_mesh_solve_both_kernel_sets(mode, kind, kernels):
         assert s.factor(ap, ai, a) == 0
         st, xo = s.solve(rhs)
         assert np.array_equal(x, xo), np.max(np.abs(x - xo))
+    g.close()
+
+
+SPARSE_KINDS = ["sparselu", "sparselubtf"]
+
+
+@pytest.mark.parametrize("kind", SPARSE_KINDS)
+def test_sparselu_kinds_kats_and_mesh(kind, kernels):
+    """The device handle as the reference's SparseLuSolver and
+    SparseLuBtfSolver (no row exchanges, the +-1e-14 pivot rule in every
+    block, SparseLU-BTF's BTF rule): bit for bit the oracle's, on the solver
+    known answers and on the 32x32 diode mesh across a refactorization."""
+    for k in KATS["solve"]:
+        n = len(k["ap"]) - 1
+        g = GpuKluSolver(n, kind=kind)
+        x = _gpu_solve(g, k["ap"], k["ai"], k["ax"], k["b"])
+        _, xo = _oracle_solve(kind, k["ap"], k["ai"], k["ax"], k["b"])
+        assert np.array_equal(x, xo), k["name"]
+        assert g.name() == ("GpuSparseLU" if kind == "sparselu" else "GpuSparseLU-BTF")
+        g.close()
+    c = cz.mesh_dc()
+    n, ap, ai, ax, rhs = po.mna(c, np.random.default_rng(11).uniform(0, 0.8, c.node_count))
+    g = GpuKluSolver(n, kind=kind)
+    s = po.Solver(kind, n)
+    s.prepare(n)
+    ax2 = ax * (1.0 + 1e-3 * np.random.default_rng(2).standard_normal(len(ax)))
+    for a in (ax, ax2):
+        x = _gpu_solve(g, ap, ai, a, rhs)
+        assert s.factor(ap, ai, a) == 0
+        st, xo = s.solve(rhs)
+        assert np.array_equal(x, xo), np.max(np.abs(x - xo))
+    assert g.stats()["pivot_swaps"] == 0
+    g.close()
+
+
+@pytest.mark.parametrize("kind", SPARSE_KINDS)
+@pytest.mark.parametrize("name", ["adder_dcop_01", "circuit_1", "rajat01"])
+def test_sparselu_kinds_matrix_market(name, kind, kernels):
+    z = np.load(os.path.join(GOLD, f"mtx_{name}.npz"))
+    ap, ai, ax, rhs = z["ap"].astype(np.int64), z["ai"].astype(np.int64), z["ax"], z["rhs"]
+    n = len(ap) - 1
+    g = GpuKluSolver(n, kind=kind)
+    s = po.Solver(kind, n)
+    s.prepare(n)
+    ax2 = ax * (1.0 + 1e-3 * np.random.default_rng(1).standard_normal(len(ax)))
+    for a in (ax, ax2):
+        x = _gpu_solve(g, ap, ai, a, rhs)
+        assert s.factor(ap, ai, a) == 0
+        st, xo = s.solve(rhs)
+        assert np.array_equal(x, xo), np.max(np.abs(x - xo))
+    g.close()
+
+
+@pytest.mark.parametrize("kind", SPARSE_KINDS)
+def test_sparselu_kinds_newton(kind):
+    """The engine's DC loop on the device with the SparseLU kinds: the
+    reference's iterations and operating point (the divider's known answer,
+    the 32x32 diode mesh with gmin stepping)."""
+    d = KATS["divider"]
+    div = cz.Circuit(d["node_count"], np.array(d["type"], np.int32),
+                     np.array(d["nodes"], np.int32), np.array(d["p"], np.float64))
+    for c, extra in ((div, {}), (cz.mesh_dc(), {"gmin_steps": 10})):
+        cfg = dict(wl.TIGHT, **extra)
+        ocfg = {k: cfg[k] for k in ("max_iters", "abs_tol", "rel_tol", "gmin", "gmin_steps",
+                                    "source_steps")}
+        g = GpuKluSolver(1, kind=kind)
+        r = newton_dc(g, DeviceCircuit(c), N.newton_config(**cfg))
+        ro, ito, xo = po.dc_op(c, kind, **ocfg)
+        assert r.reason == ro and r.iterations == ito
+        assert np.max(np.abs(r.x - xo)) <= 1e-10 * np.max(np.abs(xo))
+        g.close()
+
+
+def test_dense_kind_matches_the_reference_dense_solver():
+    """The device DenseSolver (solver.rs:596-724) bit for bit against the
+    oracle's restatement: the known answers, small inverter chains, the
+    32x32 diode mesh (n = 1026) across new values, and its failure paths."""
+    from rustspice_gb300.solver import create_solver_auto, create_solver_for_matrix
+    for k in KATS["solve"]:
+        n = len(k["ap"]) - 1
+        g = GpuKluSolver(n, kind="dense")
+        x = _gpu_solve(g, k["ap"], k["ai"], k["ax"], k["b"])
+        _, xo = _oracle_solve("dense", k["ap"], k["ai"], k["ax"], k["b"])
+        assert np.array_equal(x, xo), k["name"]
+        g.close()
+    systems = [po.mna(cz.inverter_chain(s, v), wl.chain_nodeset(s, v)) for s, v in
+               [(8, 0.3), (40, 0.7)]]
+    c = cz.mesh_dc()
+    systems.append(po.mna(c, np.random.default_rng(11).uniform(0, 0.8, c.node_count)))
+    for n, ap, ai, ax, rhs in systems:
+        g = GpuKluSolver(n, kind="dense")
+        s = po.Solver("dense", n)
+        s.prepare(n)
+        for a in (ax, ax * (1.0 + 1e-3 * np.random.default_rng(2).standard_normal(len(ax)))):
+            x = _gpu_solve(g, ap, ai, a, rhs)
+            assert s.factor(ap, ai, a) == 0
+            st, xo = s.solve(rhs)
+            assert st == 0 and np.array_equal(x, xo), (n, np.max(np.abs(x - xo)))
+        assert g.name() == "GpuDense"
+        g.close()
+    # a column without a nonzero candidate fails the factorization
+    # (solver_tests.rs singular case: diag(1, 0, 1))
+    g = GpuKluSolver(3, kind="dense")
+    with pytest.raises(SolverError) as e:
+        g.factor([0, 1, 2, 3], [0, 1, 2], [1.0, 0.0, 1.0])
+    assert e.value.status == N.FACTOR_FAILED
+    assert po.Solver("dense", 3).factor([0, 1, 2, 3], [0, 1, 2], [1.0, 0.0, 1.0]) == 2
+    with pytest.raises(SolverError) as e:  # solve before a successful factorization
+        g.solve(np.ones(3))
+    assert e.value.status == N.SOLVE_FAILED
+    g.factor([0, 1, 2, 3], [0, 1, 2], [1.0, 2.0, 4.0])
+    with pytest.raises(SolverError) as e:  # wrong length: SolveFailed (solver.rs:689-691)
+        g.solve(np.ones(4))
+    assert e.value.status == N.SOLVE_FAILED
+    g.analyze([0, 1], [0])  # analyze accepts any pattern
+    with pytest.raises(SolverError) as e:
+        g.factor([0, 1], [0], [1.0])
+    assert e.value.status == N.ANALYZE_FAILED
+    g.close()
+    # the factory: auto picks Dense for 10 unknowns; the matrix selector's
+    # example system (solver_tests.rs:95-110)
+    a = create_solver_auto(10)
+    assert a.name() == "GpuDense"
+    a.close()
+    m = create_solver_for_matrix(2, [0, 2, 4], [0, 1, 0, 1])
+    m.prepare(2)
+    m.analyze([0, 2, 4], [0, 1, 0, 1])
+    m.factor([0, 2, 4], [0, 1, 0, 1], [3.0, 1.0, 1.0, 2.0])
+    x = np.array([9.0, 8.0])
+    m.solve(x)
+    assert np.max(np.abs(x - [2.0, 3.0])) < 1e-9
+
+
+@pytest.mark.parametrize("solver", ["dense", "auto", "sparselubtf", "nativeklu"])
+def test_deck_solver_option_on_the_device(solver):
+    """`.option solver=` picks the device solver kind as the engine picks its
+    solver (engine.rs:971-984, solver.rs:169-246, by node count); the device
+    Newton loop then gives the oracle's iterations and operating point with
+    the same solver."""
+    from rustspice_gb300 import netlist as nl
+    deck = nl.compile_deck(f"""* divider with a diode
+V1 in 0 1.0
+R1 in out 1k
+R2 out 0 2k
+D1 out 0 dmod
+.model dmod d is=1e-14 n=1
+.option solver={solver} reltol=1e-10 vntol=1e-12 itl1=200
+.end
+""")
+    kind = deck.solver_kind()
+    assert kind == {"dense": "dense", "auto": "dense", "sparselubtf": "sparselubtf",
+                    "nativeklu": "nativeklu"}[solver]
+    opts = deck.newton_options()
+    g = GpuKluSolver(1, kind=kind)
+    r = newton_dc(g, DeviceCircuit(deck.circuit), N.newton_config(**opts))
+    ro, ito, xo = po.dc_op(deck.circuit, kind, **opts)
+    # NativeKLU's pivot rule drops entries on this deck and stalls at the cap
+    # (the reference's Q6 behaviour); the others converge
+    assert r.reason == ro and r.iterations == ito
+    assert r.converged == (kind != "nativeklu")
+    if r.converged:
+        assert np.max(np.abs(r.x - xo)) <= 1e-12 * np.max(np.abs(xo))
     g.close()

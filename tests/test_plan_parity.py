@@ -71,6 +71,41 @@ def test_plan_emulation_bit_exact(sysm, mode, kind):
         assert es.plan.nnz_l == st["nnz_l"]
 
 
+KINDS = ["sparselu", "sparselubtf"]
+KIND_SYSTEMS = SYSTEMS + [("chain120", *po.mna(cz.inverter_chain(120, 0.4),
+                                                np.random.default_rng(4).uniform(
+                                                    0, 1.2, cz.inverter_chain(120, 0.4)
+                                                    .node_count))[1:])]
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("sysm", KIND_SYSTEMS, ids=[s[0] for s in KIND_SYSTEMS])
+def test_plan_emulation_sparselu_kinds(sysm, kind):
+    """The plan of the SparseLU kinds (no row exchanges, the general pivot
+    perturbation in every block, SparseLU-BTF's BTF rule) run through the
+    kernels' operation sequence equals the oracle's SparseLuSolver and
+    SparseLuBtfSolver bit for bit, across a refactorization with new values."""
+    name, ap, ai, ax, rhs = sysm
+    n = len(ap) - 1
+    ax2 = ax * (1.0 + 0.1 * np.random.default_rng(7).standard_normal(len(ax)))
+    es = EmulatedSolver(N.PIVOT_REFERENCE, kind)
+    s = po.Solver(kind, n)
+    s.prepare(n)
+    assert s.analyze(ap, ai) == 0
+    for a in (ax, ax2):
+        es.factor(n, ap, ai, a)
+        assert s.factor(ap, ai, a) == 0
+        st, xo = s.solve(rhs)
+        assert st == 0
+        xe = es.solve(rhs)
+        assert np.array_equal(xe, xo), np.max(np.abs(xe - xo))
+        xb = solve_one_block(es.plan, es.ax, es.lu, rhs)
+        assert np.array_equal(xb, xo), np.max(np.abs(xb - xo))
+    assert es.plan.swaps == 0
+    if kind == "sparselu" or n < 50:
+        assert es.plan.nblocks == 1
+
+
 def _weak_diagonal(n, seed):
     """Random sparse matrix whose diagonal is often far below its column:
     the threshold rule exchanges many rows, in chains."""
