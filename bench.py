@@ -369,7 +369,30 @@ def _bbd(out, with_cpu, timed, ocfg):
             po.dc_op_bbd(c, asg, nb, x0=x0, **dict(ocfg, max_iters=k))
             ts.append(time.perf_counter() - t0)
         e["oracle_ms_per_iteration_1core"] = (ts[1] - ts[0]) * 1e3 / 2
+    e["schur_lu"] = _schur_lu(info["border_size"])
     out["bbd"] = e
+
+
+def _schur_lu(bs):
+    """The dense LU of a border-sized Schur complement on its own, each
+    variant timed with CUDA events (best of three, S resident in L2 as in the
+    BBD iteration), against the measured FP64 FMA and DMMA peaks."""
+    from rustspice_gb300 import native as N
+    from rustspice_gb300.solver import dense_lu_nopivot
+    rng = np.random.default_rng(5)
+    a = rng.uniform(-1.0, 1.0, (bs, bs))
+    a[np.arange(bs), np.arange(bs)] += bs  # no pivoting needed
+    flops = 2.0 * bs ** 3 / 3.0 - bs ** 2 / 2.0 - bs / 6.0
+    dfma = float(N.lib().gpuklu_fp64_peak_tflops())
+    dmma = float(N.lib().gpuklu_fp64_mma_peak_tflops())
+    r = {"n": bs, "flops": flops, "dfma_peak_tflops": dfma, "dmma_peak_tflops": dmma}
+    for name, v in (("panels", 0), ("coop_fma", 1), ("coop_dmma", 2)):
+        dense_lu_nopivot(a, v)
+        ms = min(dense_lu_nopivot(a, v)[1] for _ in range(3))
+        tf = flops / (ms * 1e-3) / 1e12
+        r[name] = {"ms": ms, "tflops": tf, "frac_of_dfma_peak": tf / dfma if dfma else None,
+                   "frac_of_dmma_peak": tf / dmma if dmma else None}
+    return r
 
 
 def run_gpu(a):

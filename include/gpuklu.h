@@ -411,6 +411,19 @@ int gpuklu_tran_backward(gpuklu_batch* b, const gpuklu_newton_config* cfg, doubl
  * TFLOP/s (a short microbenchmark; the denominator of FP64 roofline
  * fractions). */
 double gpuklu_fp64_peak_tflops(void);
+/* The same for the FP64 tensor cores: mma.sync m8n8k4 f64 (DMMA), four
+ * independent accumulations per warp. */
+double gpuklu_fp64_mma_peak_tflops(void);
+/* The BBD solver's dense Schur LU on its own (bbd_solver.rs:811-896: no
+ * pivoting, pivots below 1e-14 set to +-1e-14) for a host column-major n x n
+ * matrix, factored in place (L below the diagonal, unit diagonal implied; U
+ * on and above). variant 0: 32-wide panel kernels, four launches per panel;
+ * 1: one cooperative launch, FP64 FMA updates, pivots applied through their
+ * reciprocals (agrees with variant 0 to rounding); 2: the cooperative launch
+ * with DMMA updates. *ms_out: device time of the
+ * factorization. No counterpart in the reference (its BbdSolver factors S
+ * inside factor_bbd). */
+int gpuklu_dense_lu_nopivot(double* a, int64_t n, int variant, double* ms_out);
 
 /* ------------------------------------------------ host-only diagnostics */
 

@@ -2720,6 +2720,11 @@ struct gpuklu_bbd {
   DBuf<double> d_ax, d_rhs, d_rhs_c, d_x, d_newx, d_y, d_S, d_xT, d_z;
   DBuf<gk::NewtonState> d_nstate;
   DBuf<int> d_status;
+  DBuf<unsigned> d_bar;  // grid barrier of the cooperative Schur LU
+  // Dense LU of S: 0 the 32-wide panel kernels (four launches per panel), 1
+  // one cooperative launch with FP64 FMA updates, 2 the same with DMMA
+  // updates (GPUKLU_SCHUR_LU=panels|fma|mma).
+  int schur_lu = gk::kSchurLuDefault;
   gk::BbdArgs args{};
   std::string err;
   ~gpuklu_bbd() {
@@ -2972,8 +2977,16 @@ struct gpuklu_bbd {
     }
     gk::launch_bbd_ysolve(M->pd.dp, M->d_lu.p, d_ax.p, args, d_y.p, s);
     gk::launch_bbd_schur(d_ax.p, args, d_y.p, d_S.p, s);
-    gk::launch_dense_lu(d_S.p, d.border_size, s);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaSuccess;
+    if (schur_lu == 0) {
+      gk::launch_dense_lu(d_S.p, d.border_size, s);
+    } else {
+      e = d_bar.resize(gk::schur_lu_bar_words(d.border_size));
+      if (e == cudaSuccess)
+        e = gk::launch_schur_lu(d_S.p, d.border_size, schur_lu == 2, d_bar.p, M->d_status.p, s);
+      if (e != cudaSuccess) return fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "schur lu"));
+    }
+    e = cudaGetLastError();
     if (e == cudaSuccess && sync) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(GPUKLU_CUDA_ERROR, cuda_msg(e, "bbd factor"));
     if (sync) {
@@ -3035,6 +3048,8 @@ gpuklu_bbd* gpuklu_bbd_create(int64_t n, const int64_t* ap, int64_t ap_len, cons
   }
   B->M = gpuklu_create(B->fallback ? n : d.border_start);
   if (!B->M) return nullptr;
+  if (const char* es = getenv("GPUKLU_SCHUR_LU"))
+    B->schur_lu = strcmp(es, "panels") == 0 ? 0 : strcmp(es, "mma") == 0 ? 2 : 1;
   gpuklu_set_pivot_mode(B->M, GPUKLU_PIVOT_EXACT);
   if (!B->fallback) {  // SparseLU per block (bbd_solver.rs:436-444): AMD, no row exchanges
     gpuklu_set_pivot_mode(B->M, GPUKLU_PIVOT_REFERENCE);
@@ -3293,6 +3308,50 @@ struct gpuklu_plan {
 extern "C" {
 
 double gpuklu_fp64_peak_tflops(void) { return gk::fp64_peak_tflops(); }
+
+double gpuklu_fp64_mma_peak_tflops(void) { return gk::dmma_peak_tflops(); }
+
+int gpuklu_dense_lu_nopivot(double* a, int64_t n, int variant, double* ms_out) {
+  if (!a || n <= 0 || n > 16384 || variant < 0 || variant > 2) return GPUKLU_INVALID_MATRIX;
+  const size_t bytes = (size_t)n * n * sizeof(double);
+  DBuf<double> dS;
+  DBuf<unsigned> bar;
+  DBuf<int> status;
+  cudaStream_t s = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = dS.resize((size_t)n * n);
+  if (e == cudaSuccess) e = bar.resize(gk::schur_lu_bar_words((int)n));
+  if (e == cudaSuccess) e = status.resize(1);
+  if (e == cudaSuccess) e = cudaMemsetAsync(status.p, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dS.p, a, bytes, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+  if (e == cudaSuccess) {
+    if (variant == 0)
+      gk::launch_dense_lu(dS.p, (int)n, s);
+    else
+      e = gk::launch_schur_lu(dS.p, (int)n, variant == 2, bar.p, status.p, s);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+  int st = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(a, dS.p, bytes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&st, status.p, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  float ms = 0.f;
+  if (e == cudaSuccess && ms_out) e = cudaEventElapsedTime(&ms, e0, e1);
+  if (ms_out) *ms_out = ms;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (s) cudaStreamDestroy(s);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "gpuklu_dense_lu_nopivot: %s\n", cudaGetErrorString(e));
+    return GPUKLU_CUDA_ERROR;
+  }
+  return st == 0 ? GPUKLU_OK : st;
+}
 
 int gpuklu_btf_info(int64_t n, const int64_t* ap, const int64_t* ai, int64_t* out) {
   if (n < 0 || !out || (n > 0 && (!ap || !ai))) return GPUKLU_INVALID_MATRIX;

@@ -253,6 +253,16 @@ void launch_bbd_ysolve(const DPlan& P, const double* lu, const double* ax, const
 void launch_bbd_schur(const double* ax, const BbdArgs& B, const double* ybuf, double* S,
                       cudaStream_t s);
 void launch_dense_lu(double* S, int bs, cudaStream_t s);
+// The same factorization as one cooperative launch (schur.cu): FP64 FMA
+// updates (mma = false) or DMMA updates; both agree with launch_dense_lu's
+// factor to rounding.
+// bar: schur_lu_bar_words(bs) words of scratch (a grid barrier, block 0's
+// SM and one tile counter per panel).
+cudaError_t launch_schur_lu(double* S, int bs, bool mma, unsigned* bar, int* status,
+                            cudaStream_t s);
+inline int schur_lu_bar_words(int bs) { return 3 + (bs + 31) / 32; }
+constexpr int kSchurLuDefault = 1;  // 0 panels, 1 cooperative FMA, 2 cooperative DMMA
+double dmma_peak_tflops();
 // The reference's DenseSolver (dense.cu).
 void launch_dense_factor(int n, const int64_t* ap, const int64_t* ai, const double* ax,
                          double* A, int* piv, int* status, cudaStream_t s);

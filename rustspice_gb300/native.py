@@ -37,7 +37,7 @@ SYMBOLS = [
     "gpuklu_batch_update_inputs", "gpuklu_batch_last_error", "gpuklu_batch_info",
     "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_batch_phase_ms", "gpuklu_ac_sweep", "gpuklu_tran_create", "gpuklu_tran_forward",
     "gpuklu_tran_backward", "gpuklu_bbd_create", "gpuklu_bbd_destroy", "gpuklu_bbd_last_error",
-    "gpuklu_bbd_info", "gpuklu_bbd_perm", "gpuklu_bbd_factor", "gpuklu_bbd_solve", "gpuklu_bbd_newton_dc", "gpuklu_fp64_peak_tflops", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free", "gpuklu_btf_info",
+    "gpuklu_bbd_info", "gpuklu_bbd_perm", "gpuklu_bbd_factor", "gpuklu_bbd_solve", "gpuklu_bbd_newton_dc", "gpuklu_fp64_peak_tflops", "gpuklu_fp64_mma_peak_tflops", "gpuklu_dense_lu_nopivot", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free", "gpuklu_btf_info",
 ]
 
 
@@ -127,6 +127,8 @@ def lib(build_if_missing: bool = True):
         "gpuklu_bbd_solve": (C.c_int, [_P, _P, _I64]),
         "gpuklu_bbd_newton_dc": (C.c_int, [_P, _P, _P, _P, _P, _I64, _P, _P, _P, _P]),
         "gpuklu_fp64_peak_tflops": (_D, []),
+        "gpuklu_fp64_mma_peak_tflops": (_D, []),
+        "gpuklu_dense_lu_nopivot": (C.c_int, [_P, _I64, C.c_int, _P]),
         "gpuklu_solve_device_noalloc": (C.c_int, [_P, _P, _P]),
         "gpuklu_dc_backward": (C.c_int, [_P, _P, _P, _I64, _P, _D, _P, _P]),
         "gpuklu_plan_build": (_P, [_I64, _P, _P, C.c_int, C.c_int, _P]),

@@ -655,3 +655,21 @@ class SolverSelector:
 def create_solver_for_matrix(n: int, ap, ai) -> GpuKluSolver:
     """create_solver_for_matrix (solver.rs:551-554)."""
     return SolverSelector.select(n, ap, ai).create_solver()
+
+
+def dense_lu_nopivot(a, variant: int = 1):
+    """The BBD solver's dense Schur LU (no pivoting, +-1e-14 rule) of a square
+    matrix on the device: returns (lu, ms) with L below the diagonal (unit
+    diagonal implied) and U on and above it, and the factorization's device
+    time. variant 0: panel kernels; 1: one cooperative launch, FP64 FMA
+    updates; 2: the same with DMMA updates (1 and 2 agree with 0 to
+    rounding)."""
+    a = np.asarray(a, np.float64)
+    n = a.shape[0]
+    work = np.asfortranarray(a.copy())  # column-major on the device
+    buf = work.ravel(order="F").copy()
+    ms = C.c_double()
+    st = N.lib().gpuklu_dense_lu_nopivot(N.ptr(buf), n, int(variant), C.byref(ms))
+    if st != N.OK:
+        raise SolverError(st, "dense_lu_nopivot")
+    return buf.reshape((n, n), order="F"), ms.value

@@ -108,3 +108,48 @@ def test_plain_solver_refuses_the_whole_bordered_matrix():
     with pytest.raises(SolverError) as e:
         newton_dc(h, dc, N.newton_config(**wl.TIGHT), x0=wl.bordered_nodeset(c))
     assert "2^31" in str(e.value)
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 100, 257, 1025])
+def test_dense_schur_lu_variants(n):
+    """The cooperative Schur LU (FMA or DMMA updates) within 1e-12 of the
+    panel kernels' factor, and L U = A; a zero pivot takes the +-1e-14
+    rule in all three."""
+    from rustspice_gb300.solver import dense_lu_nopivot
+    rng = np.random.default_rng(n)
+    a = rng.uniform(-1.0, 1.0, (n, n))
+    a[np.arange(n), np.arange(n)] += n
+    if n >= 33:
+        a[5, :] = 0.0  # a zero pivot: the +-1e-14 rule
+        a[5, 5] = 0.0
+    f0, _ = dense_lu_nopivot(a, 0)
+    f1, _ = dense_lu_nopivot(a, 1)
+    f2, _ = dense_lu_nopivot(a, 2)
+    for f in (f1, f2):
+        assert np.max(np.abs(f - f0)) <= 1e-12 * max(1.0, np.max(np.abs(f0)))
+    if n < 33:
+        for f in (f0, f1, f2):
+            L = np.tril(f, -1) + np.eye(n)
+            U = np.triu(f)
+            assert np.max(np.abs(L @ U - a)) <= 1e-12 * np.max(np.abs(a))
+    else:
+        assert f0[5, 5] == f1[5, 5] == f2[5, 5] == 1e-14
+
+
+def test_dmma_probe_and_bbd_newton_with_each_schur_lu(monkeypatch):
+    from rustspice_gb300 import native as N
+    assert N.lib().gpuklu_fp64_mma_peak_tflops() > 0.0
+    c, asg, nb = cz.bordered_meshes(nblocks=6, nborder=96, side_lo=8, side_hi=14, ndiodes=4)
+    dc = DeviceCircuit(c)
+    ap, ai = dc.pattern()
+    cfg = N.newton_config(**wl.TIGHT)
+    x0 = wl.bordered_nodeset(c)
+    res = {}
+    for v in ("panels", "fma", "mma"):
+        monkeypatch.setenv("GPUKLU_SCHUR_LU", v)
+        bb = BbdSolver(ap, ai, asg, nb)
+        res[v] = bb.newton_dc(dc, cfg, x0=x0)
+        bb.close()
+    assert res["panels"].iterations == res["fma"].iterations == res["mma"].iterations
+    for v in ("fma", "mma"):
+        assert np.max(np.abs(res[v].x - res["panels"].x)) <= 1e-10 * np.max(np.abs(res["panels"].x))
