@@ -47,6 +47,8 @@ def _args():
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="instances timed on the host cores (0: sized for ~15 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the batch's default schedule instead of tuning it first")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the single-circuit, adjoint, transient and bordered-block lines")
     ap.add_argument("--only", choices=SECONDARY,
@@ -420,6 +422,12 @@ def run_gpu(a):
         bt.run(cfg)
 
     with torch.cuda.stream(stream):
+        # the project's autotuner picks the lane-phase cap and the
+        # continuation's tiles per program from timed runs of this batch
+        if a.no_autotune:
+            tune = {"lane_cap": 6, "cont_tiles": 2, "runs": 0, "autotuned": False}
+        else:
+            tune = dict(bt.autotune(cfg), autotuned=True)
         for _ in range(a.warmup):
             step()
         stream.synchronize()
@@ -532,7 +540,8 @@ def run_gpu(a):
                    "pivot_mode": "exact pattern (nativeklu_exact)",
                    "initial_iterate": "logic-level nodeset",
                    "l2": "256 MB buffer written before every timed step; inputs 270 MB > L2",
-                   "parallelism": f"replicas x{ws}"},
+                   "parallelism": f"replicas x{ws}",
+                   "schedule": tune},
         "e2e": {"value": iters_all / (e2e_step * 1e-3), "unit": UNIT,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": e2e_step},

@@ -345,6 +345,22 @@ void* gpuklu_batch_stream(gpuklu_batch* b);
  * iterations an instance runs in the lane kernel before it is parked (0: no
  * lane phase). */
 int gpuklu_batch_phase_ms(gpuklu_batch* b, double* out);
+/* The batch's schedule; no counterpart in the reference. lane_cap: Newton
+ * iterations an instance runs in the lane-per-instance phase before it is
+ * parked for the warp kernels (default 6; ignored when that phase is off);
+ * cont_tiles: shared-program tiles per circuit program in the continuation
+ * (default 2). Results agree across schedules to the batch's 1e-10 bar
+ * (an instance's arithmetic differs between the lane and warp kernels only
+ * in rounding). */
+int gpuklu_batch_set_schedule(gpuklu_batch* b, int lane_cap, int cont_tiles);
+/* Autotuner: times one run of the batch per candidate schedule (lane_cap in
+ * {3, 4, 5, 6, 8, 10, 12}, cont_tiles in {1, 2, 3, 4}; two rounds of
+ * coordinate descent from the current schedule, CUDA events around the
+ * kernels) and keeps the fastest. out[0..2] = lane_cap, cont_tiles, runs;
+ * *best_ms its device time. The batch's results afterwards are those of the
+ * last trial: run it again for the tuned run's. */
+int gpuklu_batch_autotune(gpuklu_batch* b, const gpuklu_newton_config* cfg, int64_t* out,
+                          double* best_ms);
 
 /* ------------------------------------------ bordered block diagonal */
 /* The reference's BbdSolver (crates/sim-core/src/bbd_solver.rs:86-1095,

@@ -1607,6 +1607,7 @@ struct gpuklu_batch {
     // program, tiles3 for one warp per tile
     std::vector<i32> tiles, tiles2, tiles3;
     DBuf<i32> d_tiles, d_tiles2, d_tiles3;
+    std::vector<int> members;  // its groups, most expensive first
     DBuf<unsigned> d_counter;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
@@ -1616,6 +1617,9 @@ struct gpuklu_batch {
   // warps of a block that shares one program: up to this many, as the
   // group's program and instance regions fit the block's shared memory
   static constexpr int kSharedWarpsMax = 16;
+  // continuation tiles per group (gpuklu_batch_set_schedule / autotune)
+  static constexpr int kContTilesDefault = 2;
+  int cont_tiles = kContTilesDefault;
 
   cudaEvent_t start_ev = nullptr;
   // timing events of the last run: before the lane kernel, after it, after
@@ -2167,7 +2171,8 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     // orders). A tile whose group has nothing parked left is skipped before
     // its program is staged.
     for (int g : members)
-      for (int t = 0; t < 2; ++t) C->tiles2.push_back(g);
+      for (int t = 0; t < gpuklu_batch::kContTilesDefault; ++t) C->tiles2.push_back(g);
+    C->members = members;
     gk::batch_kernel_info(C->m, C->warps_per_block, C->region, C->prog_ints, &C->regs,
                           &C->blocks_per_sm);
     if (C->blocks_per_sm <= 0) {
@@ -2598,6 +2603,87 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return b->fail(cuda_msg(e, "batch launch"));
   return GPUKLU_OK;
+}
+
+int gpuklu_batch_set_schedule(gpuklu_batch* b, int lane_cap, int cont_tiles) {
+  if (!b) return GPUKLU_INVALID_MATRIX;
+  if (cont_tiles < 1 || cont_tiles > 16 || (b->lanes && (lane_cap < 1 || lane_cap > 100)))
+  {
+    b->err = "gpuklu_batch_set_schedule: lane_cap in 1..100 and cont_tiles in 1..16";
+    return GPUKLU_INVALID_MATRIX;
+  }
+  cudaError_t e = cudaStreamSynchronize(b->stream);  // no run may still read the tiles
+  if (b->lanes) {
+    b->lane_cap = lane_cap;
+    b->args.cap = lane_cap;
+    for (auto& C : b->classes) C->args.cap = lane_cap;
+  }
+  if (cont_tiles != b->cont_tiles) {
+    for (auto& C : b->classes) {
+      C->tiles2.clear();
+      for (int g : C->members)
+        for (int t = 0; t < cont_tiles; ++t) C->tiles2.push_back(g);
+      if (e == cudaSuccess) e = C->d_tiles2.upload(C->tiles2, b->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    b->cont_tiles = cont_tiles;
+  }
+  if (e != cudaSuccess) return b->fail(cuda_msg(e, "batch schedule"));
+  return GPUKLU_OK;
+}
+
+int gpuklu_batch_autotune(gpuklu_batch* b, const gpuklu_newton_config* cfg, int64_t* out,
+                          double* best_ms) {
+  if (!b || !cfg) return GPUKLU_INVALID_MATRIX;
+  if (b->transient) {
+    b->err = "gpuklu_batch_autotune: a transient batch has no schedule";
+    return GPUKLU_INVALID_MATRIX;
+  }
+  // one timed run of the batch per candidate: the lane phase's iteration cap,
+  // then the continuation's tiles per group, each with the other at its best
+  // so far (two rounds of coordinate descent from the current schedule)
+  auto timed = [&](int cap, int ct, double* ms) -> int {
+    int st = gpuklu_batch_set_schedule(b, cap, ct);
+    if (st == GPUKLU_OK) st = gpuklu_batch_run(b, cfg);
+    double ph[3] = {0, 0, 0};
+    if (st == GPUKLU_OK) st = gpuklu_batch_phase_ms(b, ph);
+    *ms = ph[0] + ph[1];
+    return st;
+  };
+  static const int caps[] = {3, 4, 5, 6, 8, 10, 12};
+  static const int cts[] = {1, 2, 3, 4};
+  int cap = b->lanes ? b->lane_cap : 1, ct = b->cont_tiles, trials = 0;
+  double best = 0.0;
+  int st = timed(cap, ct, &best);  // warm-up, then the current schedule
+  if (st == GPUKLU_OK) st = timed(cap, ct, &best);
+  trials += 2;
+  for (int round = 0; round < 2 && st == GPUKLU_OK; ++round) {
+    const int cap0 = cap, ct0 = ct;
+    if (b->lanes)
+      for (int c : caps) {
+        if (c == cap || st != GPUKLU_OK) continue;
+        double ms = 0.0;
+        st = timed(c, ct, &ms);
+        ++trials;
+        if (st == GPUKLU_OK && ms < best) best = ms, cap = c;
+      }
+    for (int c : cts) {
+      if (c == ct || st != GPUKLU_OK) continue;
+      double ms = 0.0;
+      st = timed(cap, c, &ms);
+      ++trials;
+      if (st == GPUKLU_OK && ms < best) best = ms, ct = c;
+    }
+    if (cap == cap0 && ct == ct0) break;
+  }
+  if (st == GPUKLU_OK) st = gpuklu_batch_set_schedule(b, cap, ct);
+  if (out) {
+    out[0] = b->lanes ? cap : 0;
+    out[1] = ct;
+    out[2] = trials;
+  }
+  if (best_ms) *best_ms = best;
+  return st;
 }
 
 int gpuklu_batch_phase_ms(gpuklu_batch* b, double* out) {

@@ -35,7 +35,7 @@ SYMBOLS = [
     "gpuklu_circuit_set_params", "gpuklu_stamp", "gpuklu_newton_dc", "gpuklu_dc_sweep", "gpuklu_batch_create",
     "gpuklu_batch_destroy", "gpuklu_batch_run", "gpuklu_batch_results",
     "gpuklu_batch_update_inputs", "gpuklu_batch_last_error", "gpuklu_batch_info",
-    "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_batch_phase_ms", "gpuklu_ac_sweep", "gpuklu_tran_create", "gpuklu_tran_forward",
+    "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_batch_phase_ms", "gpuklu_batch_set_schedule", "gpuklu_batch_autotune", "gpuklu_ac_sweep", "gpuklu_tran_create", "gpuklu_tran_forward",
     "gpuklu_tran_backward", "gpuklu_bbd_create", "gpuklu_bbd_destroy", "gpuklu_bbd_last_error",
     "gpuklu_bbd_info", "gpuklu_bbd_perm", "gpuklu_bbd_factor", "gpuklu_bbd_solve", "gpuklu_bbd_newton_dc", "gpuklu_fp64_peak_tflops", "gpuklu_fp64_mma_peak_tflops", "gpuklu_dense_lu_nopivot", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free", "gpuklu_btf_info",
 ]
@@ -113,6 +113,8 @@ def lib(build_if_missing: bool = True):
         "gpuklu_batch_stream": (_P, [_P]),
         "gpuklu_batch_work": (C.c_int, [_P, _P, _P]),
         "gpuklu_batch_phase_ms": (C.c_int, [_P, _P]),
+        "gpuklu_batch_set_schedule": (C.c_int, [_P, C.c_int, C.c_int]),
+        "gpuklu_batch_autotune": (C.c_int, [_P, C.POINTER(NewtonConfig), _P, _P]),
         "gpuklu_ac_sweep": (C.c_int, [_P, _P, _P, _I64, _P, _I64, _P, _P, _P]),
         "gpuklu_tran_create": (_P, [_I64, _P, _P, _P, _P, _P, _P, _P, _I64, _D, _I64, _I64, _P,
                                     _D]),

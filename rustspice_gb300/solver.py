@@ -413,6 +413,23 @@ class Batch:
             raise SolverError(st, N.lib().gpuklu_batch_last_error(self._h).decode())
         return {"lanes_ms": float(out[0]), "warps_ms": float(out[1]), "lane_cap": int(out[2])}
 
+    def set_schedule(self, lane_cap: int, cont_tiles: int) -> None:
+        """Lane-phase iteration cap and continuation tiles per program."""
+        st = N.lib().gpuklu_batch_set_schedule(self._h, int(lane_cap), int(cont_tiles))
+        if st != N.OK:
+            raise SolverError(st, N.lib().gpuklu_batch_last_error(self._h).decode())
+
+    def autotune(self, cfg: N.NewtonConfig) -> dict:
+        """Times the batch under candidate schedules and keeps the fastest
+        (the results afterwards are the last trial's: run again)."""
+        out = np.zeros(3, np.int64)
+        ms = C.c_double()
+        st = N.lib().gpuklu_batch_autotune(self._h, C.byref(cfg), N.ptr(out), C.byref(ms))
+        if st != N.OK:
+            raise SolverError(st, N.lib().gpuklu_batch_last_error(self._h).decode())
+        return {"lane_cap": int(out[0]), "cont_tiles": int(out[1]), "runs": int(out[2]),
+                "best_ms": ms.value}
+
 
 class TranBatch:
     """Fixed-step backward-Euler transient of many circuits (one instance per

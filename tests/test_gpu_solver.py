@@ -250,3 +250,39 @@ D2 c 0 dx
     res = newton_dc(g, DeviceCircuit(deck.circuit), N.newton_config(**opts))
     assert r_o == "converged" and res.converged and res.iterations == it_o
     assert np.max(np.abs(res.x - x_o)) <= 1e-10 * max(1.0, np.max(np.abs(x_o)))
+
+
+def test_batch_autotune_and_schedules():
+    """The project's autotuner times the batch under candidate schedules and
+    keeps the fastest; every schedule gives the default's operating points
+    within 1e-10, and the default schedule set back reproduces the first
+    run bit for bit."""
+    B = wl.inverter_batch(16, 21, seed=7)
+    bt = Batch(B.circuits, B.inst_circ, B.inst_dev, B.inst_val, B.x0, B.x0_off)
+    cfg = N.newton_config(**wl.TIGHT)
+    bt.run(cfg)
+    _, itt, rs, x = bt.results()
+    ch = bt.autotune(cfg)
+    assert ch["lane_cap"] in (3, 4, 5, 6, 8, 10, 12) and ch["cont_tiles"] in (1, 2, 3, 4)
+    assert ch["runs"] >= 11 and ch["best_ms"] > 0.0
+    bt.run(cfg)
+    _, itt2, rs2, x2 = bt.results()
+    assert np.mean(rs == rs2) >= 0.98
+    conv = (rs == 0) & (rs2 == 0)
+    for i in np.flatnonzero(conv):
+        n = B.circuits[B.inst_circ[i]].n
+        a, b = x[bt.x_off[i]:bt.x_off[i] + n], x2[bt.x_off[i]:bt.x_off[i] + n]
+        assert np.max(np.abs(a - b)) <= 1e-10 * max(1.0, np.max(np.abs(a)))
+    for cap, ct in ((3, 1), (12, 4)):
+        bt.set_schedule(cap, ct)
+        bt.run(cfg)
+        assert bt.phase_ms()["lane_cap"] == cap
+        _, _, rs3, x3 = bt.results()
+        assert np.mean(rs == rs3) >= 0.98
+    bt.set_schedule(6, 2)
+    bt.run(cfg)
+    _, itt4, rs4, x4 = bt.results()
+    assert np.array_equal(x, x4) and np.array_equal(itt, itt4) and np.array_equal(rs, rs4)
+    with pytest.raises(SolverError) as e:
+        bt.set_schedule(0, 2)
+    assert e.value.status == N.INVALID_MATRIX
