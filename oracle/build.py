@@ -10,7 +10,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SOURCES = ["ordering.cpp", "solvers.cpp", "circuit.cpp", "bbd.cpp", "ac.cpp", "capi.cpp"]
+SOURCES = ["ordering.cpp", "solvers.cpp", "circuit.cpp", "bbd.cpp", "ac.cpp", "transient.cpp",
+           "capi.cpp"]
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 

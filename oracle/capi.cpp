@@ -1,7 +1,9 @@
 // Oracle (test infrastructure only): a flat C interface over the CPU
 // restatement so that tests/ and bench.py's CPU-baseline leg can drive it
 // through ctypes. Nothing in the product links this library.
+#include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstring>
 #include <thread>
 
@@ -392,6 +394,142 @@ void orc_dc_batch(int64_t ncirc, const int64_t* dev_off, const int64_t* node_cou
   for (int64_t t = 1; t < nt; ++t) th.emplace_back(worker);
   worker();
   for (auto& t : th) t.join();
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- adaptive transient
+namespace {
+std::vector<Waveform> make_waves(int64_t n, const int32_t* kind, const double* p7,
+                                 const int64_t* pwl_ptr, const double* pwl_t,
+                                 const double* pwl_v) {
+  std::vector<Waveform> w((size_t)n);
+  for (int64_t d = 0; d < n; ++d) {
+    w[d].kind = kind ? kind[d] : 0;
+    if (p7)
+      for (int k = 0; k < 7; ++k) w[d].p[k] = p7[d * 7 + k];
+    if (pwl_ptr)
+      for (int64_t q = pwl_ptr[d]; q < pwl_ptr[d + 1]; ++q) w[d].pwl.push_back({pwl_t[q], pwl_v[q]});
+    // PwlParams::new sorts the points by time (a stable sort, waveform.rs:137-143)
+    std::stable_sort(w[d].pwl.begin(), w[d].pwl.end(),
+                     [](const std::pair<double, double>& a, const std::pair<double, double>& b) {
+                       return a.first < b.first;
+                     });
+  }
+  return w;
+}
+}  // namespace
+
+extern "C" {
+
+// Waveform values at nt times (kind and 7 parameters; PWL points).
+void orc_wave_eval(int32_t kind, const double* p7, int64_t npwl, const double* pwl_t,
+                   const double* pwl_v, int64_t nt, const double* ts, double* out) {
+  int64_t ptr[2] = {0, npwl};
+  std::vector<Waveform> w = make_waves(1, &kind, p7, ptr, pwl_t, pwl_v);
+  for (int64_t i = 0; i < nt; ++i) out[i] = w[0].eval(ts[i]);
+}
+
+// Breakpoint times of nw sources (sorted, unique); returns their count.
+int64_t orc_breakpoints(int64_t nw, const int32_t* kind, const double* p7,
+                        const int64_t* pwl_ptr, const double* pwl_t, const double* pwl_v,
+                        double tstop, double* out, int64_t cap) {
+  std::vector<Waveform> w = make_waves(nw, kind, p7, pwl_ptr, pwl_t, pwl_v);
+  Breakpoints b;
+  for (const Waveform& x : w) b.extract(x, tstop);
+  for (size_t i = 0; i < b.times.size() && (int64_t)i < cap; ++i) out[i] = b.times[i];
+  return (int64_t)b.times.size();
+}
+
+// limit_dt over a breakpoint set.
+double orc_bp_limit_dt(const double* times, int64_t n, double t, double dt, double margin) {
+  Breakpoints b;
+  for (int64_t i = 0; i < n; ++i) b.add(times[i]);
+  return b.limit_dt(t, dt, margin);
+}
+
+// update_settling over a sequence of (t_prev, t) pairs; settling[i] gets
+// the return value and is_settling afterwards (2 * i, 2 * i + 1).
+void orc_bp_settling(const double* times, int64_t n, int64_t steps, double factor,
+                     int64_t m, const double* tp, const double* tn, int32_t* out) {
+  Breakpoints b;
+  for (int64_t i = 0; i < n; ++i) b.add(times[i]);
+  b.settling_steps = (size_t)steps;
+  b.settling_factor = std::min(std::max(factor, 0.01), 1.0);
+  for (int64_t i = 0; i < m; ++i) {
+    out[2 * i] = b.update_settling(tp[i], tn[i]) ? 1 : 0;
+    out[2 * i + 1] = b.is_settling() ? 1 : 0;
+  }
+}
+
+// Milne's estimate: out = error_norm, max_error_node, accept, suggested_factor, raw_lte.
+void orc_lte(const double* be, const double* tr, int64_t n, double abs_tol, double rel_tol,
+             double* out) {
+  Lte l = estimate_lte_milne(Vec(be, be + n), Vec(tr, tr + n), abs_tol, rel_tol);
+  out[0] = l.error_norm;
+  out[1] = (double)l.max_error_node;
+  out[2] = l.accept ? 1.0 : 0.0;
+  out[3] = l.suggested_factor;
+  out[4] = l.raw_lte;
+}
+
+// A sequence of steps through the adaptive controller: step i feeds an LTE
+// of error_norm err[i] (accept and suggested factor as Milne's estimate
+// gives them) at dt[i] (dt[i] < 0: the previous step's next dt); out gets
+// (accept, next_dt, struggling, pi_suggest) per step.
+void orc_adaptive_sequence(double dt_min, double dt_max, int64_t m, const double* err,
+                           const double* dt, double* out) {
+  AdaptiveController c(dt_min, dt_max);
+  double cur = 0.0;
+  for (int64_t i = 0; i < m; ++i) {
+    if (dt[i] >= 0.0) cur = dt[i];
+    Lte l;
+    l.error_norm = err[i];
+    l.accept = err[i] <= 1.0;
+    l.suggested_factor = err[i] > 1e-10 ? std::min(std::max(std::pow(1.0 / err[i], 0.5) * 0.9, 0.1), 2.0) : 2.0;
+    const double s = c.pi.suggest_dt(err[i], cur);
+    std::pair<bool, double> r = c.process_lte(l, cur);
+    out[4 * i] = r.first ? 1.0 : 0.0;
+    out[4 * i + 1] = r.second;
+    out[4 * i + 2] = c.pi.is_struggling() ? 1.0 : 0.0;
+    out[4 * i + 3] = s;
+    cur = r.second;
+  }
+}
+
+// The engine's adaptive transient (tran_adaptive). Per device a waveform
+// (kind, 7 parameters, PWL points). times_out / sols_out: up to cap points,
+// sols_out cap x n_cap values; stats = accepted, rejected, newton iterations,
+// points; returns the status (0 completed, 1 rejections, 2 DC point failed).
+int orc_tran_adaptive(int64_t node_count, int64_t ndev, const int32_t* type, const int32_t* nodes,
+                      const double* p, const int32_t* wkind, const double* wp7,
+                      const int64_t* pwl_ptr, const double* pwl_t, const double* pwl_v,
+                      const char* solver_kind, int64_t max_iters, double abs_tol, double rel_tol,
+                      double gmin, double tstep, double tstop, double tstart, double tmax,
+                      double lte_abs, double lte_rel, double be_sign, const double* x_ic,
+                      int64_t cap, int64_t n_cap, double* times_out, double* sols_out,
+                      int64_t* stats) {
+  Circuit c = make_circuit(node_count, ndev, type, nodes, p);
+  std::vector<Waveform> w = make_waves(ndev, wkind, wp7, pwl_ptr, pwl_t, pwl_v);
+  NewtonConfig cfg;
+  cfg.max_iters = (size_t)max_iters;
+  cfg.abs_tol = abs_tol;
+  cfg.rel_tol = rel_tol;
+  cfg.gmin = gmin;
+  Vec xi(x_ic ? x_ic : nullptr, x_ic ? x_ic + node_count : nullptr);
+  TranAdaptiveResult r = tran_adaptive(c, w, cfg, solver_kind, tstep, tstop, tstart, tmax,
+                                       lte_abs, lte_rel, be_sign, xi);
+  const int64_t np = (int64_t)r.times.size();
+  for (int64_t i = 0; i < np && i < cap; ++i) {
+    times_out[i] = r.times[i];
+    const Vec& s = r.solutions[i];
+    for (int64_t j = 0; j < n_cap; ++j) sols_out[i * n_cap + j] = j < (int64_t)s.size() ? s[j] : 0.0;
+  }
+  stats[0] = (int64_t)r.accepted;
+  stats[1] = (int64_t)r.rejected;
+  stats[2] = (int64_t)r.newton_iterations;
+  stats[3] = np;
+  return r.status;
 }
 
 }  // extern "C"

@@ -175,6 +175,15 @@ MosJ eval_level1_consistent(double vth0, double u0, double tox, double w,
   return j;
 }
 
+namespace {
+// A source's value: its waveform at the state's time, else its DC value.
+double src_value(const Circuit& c, size_t d, const TranState* st) {
+  if (st && st->waves && d < st->waves->size() && (*st->waves)[d].kind != 0)
+    return (*st->waves)[d].eval(st->t);
+  return c.p[d * NPARAM];
+}
+}  // namespace
+
 MnaSystem build_mna(const Circuit& c, const Vec& x, double gmin,
                     double source_scale, double dt, const TranState* st,
                     double be_sign, double gdev) {
@@ -195,14 +204,14 @@ MnaSystem build_mna(const Circuit& c, const Vec& x, double gmin,
         ctx.add(bb, a, -g);
         break;
       }
-      case DEV_I: {  // stamp.rs:261-276
-        double v = p[0] * ctx.scale;
+      case DEV_I: {  // stamp.rs:261-276 (at time t: :331-349)
+        double v = src_value(c, d, st) * ctx.scale;
         ctx.add_rhs(a, -v);
         ctx.add_rhs(bb, v);
         break;
       }
-      case DEV_V: {  // stamp.rs:278-297
-        double v = p[0] * ctx.scale;
+      case DEV_V: {  // stamp.rs:278-297 (at time t: :303-325)
+        double v = src_value(c, d, st) * ctx.scale;
         size_t k = ctx.allocate_aux();
         ctx.add(a, k, 1.0);
         ctx.add(bb, k, -1.0);
@@ -266,7 +275,18 @@ MnaSystem build_mna(const Circuit& c, const Vec& x, double gmin,
         break;
       }
       case DEV_C: {
-        if (dt > 0.0) {  // backward Euler companion, stamp.rs:759-787
+        if (dt > 0.0 && st && st->method == 1) {  // trapezoidal, stamp.rs:871-915
+          double g = 2.0 * p[0] / dt;
+          double vprev = st->cap_v[d];
+          double iprev = st->cap_i.empty() ? 0.0 : st->cap_i[d];
+          double ieq = g * vprev + iprev;
+          ctx.add(a, a, g);
+          ctx.add(bb, bb, g);
+          ctx.add(a, bb, -g);
+          ctx.add(bb, a, -g);
+          ctx.add_rhs(a, ieq);
+          ctx.add_rhs(bb, -ieq);
+        } else if (dt > 0.0) {  // backward Euler companion, stamp.rs:759-787
           double g = p[0] / dt;
           double vprev = st ? st->cap_v[d] : 0.0;
           double ieq = g * vprev;

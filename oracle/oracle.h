@@ -286,9 +286,26 @@ struct MnaSystem {
   Vec ax, rhs;
 };
 
-// Per-capacitor companion state for backward Euler (v_prev per device).
+// Time-dependent source value (crates/sim-core/src/waveform.rs:31-330):
+// kind 0 none (the device's DC value), 1 PULSE(v1 v2 td tr tf pw per),
+// 2 PWL (points), 3 SIN(vo va freq td theta), 4 EXP(v1 v2 td1 tau1 td2 tau2).
+struct Waveform {
+  int kind = 0;
+  double p[7] = {0, 0, 0, 0, 0, 0, 0};
+  std::vector<std::pair<double, double>> pwl;  // sorted by time
+  double eval(double t) const;
+};
+
+// Companion state of the transient (crates/sim-core/src/stamp.rs:572-668):
+// the capacitor voltage at the last accepted point and, for the trapezoidal
+// rule, its current; the integration method; the time the sources are
+// evaluated at.
 struct TranState {
   std::vector<double> cap_v;  // indexed by device id (0 for non-capacitors)
+  std::vector<double> cap_i;  // trapezoidal history current (empty: 0)
+  int method = 0;             // 0 backward Euler, 1 trapezoidal
+  double t = 0.0;
+  const std::vector<Waveform>* waves = nullptr;  // per device, or null
 };
 
 // Builds the MNA system at x the way the engine's build closure does
@@ -371,6 +388,72 @@ NewtonResult dc_op(const Circuit& c, const NewtonConfig& cfg,
 double residual_inf(const Circuit& c, const Vec& x, double gmin);
 
 std::unique_ptr<LinearSolver> make_solver(const std::string& kind, size_t n);
+
+// ---------------------------------------------------------------- adaptive transient
+// Breakpoints of PULSE and PWL sources (waveform.rs:417-660; the engine
+// extracts only those two kinds, engine.rs:635-680): sorted, unique.
+struct Breakpoints {
+  std::vector<double> times;
+  size_t settling_steps = 5, current_settling = 0;
+  double settling_factor = 0.1;
+  void add(double t);
+  void extract(const Waveform& w, double tstop);
+  bool next(double t, double& out) const;
+  double limit_dt(double t, double dt, double min_margin) const;
+  bool crossed(double t_prev, double t) const;
+  bool update_settling(double t_prev, double t);
+  double settling_dt(double dt, double dt_min) const;
+  bool is_settling() const { return current_settling > 0; }
+};
+
+// Milne's device (analysis.rs:147-206).
+struct Lte {
+  double error_norm = 0.0, suggested_factor = 2.0, raw_lte = 0.0;
+  size_t max_error_node = 0;
+  bool accept = true;
+};
+Lte estimate_lte_milne(const Vec& x_be, const Vec& x_trap, double abs_tol, double rel_tol);
+
+// PI step controller and the adaptive controller around it
+// (analysis.rs:380-760), trapezoidal gains k_p = 0.35, k_i = 0.2.
+struct StepController {
+  double k_p = 0.35, k_i = 0.2, growth = 2.0, shrink = 0.1, safety = 0.9, reject = 1.0;
+  bool has_prev = false;
+  double prev_error = 0.0, min_dt_used = 1.7976931348623157e308, max_dt_used = 0.0;
+  size_t consecutive_rejects = 0, accepted = 0, rejected = 0;
+  double suggest_dt(double err, double dt) const;
+  void record_step(double err, double dt, bool accepted);
+  bool should_reject(double err) const { return err > reject; }
+  double emergency_dt(double dt, double dt_min) const;
+  bool is_struggling() const { return consecutive_rejects >= 3; }
+};
+struct AdaptiveController {
+  StepController pi;
+  double dt_min, dt_max;
+  AdaptiveController(double mn, double mx) : dt_min(mn), dt_max(mx) {}
+  std::pair<bool, double> process_lte(const Lte& lte, double dt);
+};
+
+// The engine's adaptive transient (engine.rs:332-602): DC operating point
+// from the .ic guess, then per step a backward-Euler and a trapezoidal
+// Newton solve, Milne's estimate, the PI controller, breakpoints and
+// settling; 10 rejections in a row end the run as failed. be_sign: -1 the
+// reference's BE companion (rhs[a] -= g v_prev), +1 the physical one. Time
+// dependent sources take their value at tstart in the DC point (the
+// reference's stamp_voltage cannot parse a waveform string and leaves such
+// a source out of the DC point; not restated). status: 0 completed, 1 a run
+// of rejections, 2 the DC point did not converge.
+struct TranAdaptiveResult {
+  int status = 0;
+  std::vector<double> times;
+  std::vector<Vec> solutions;
+  size_t accepted = 0, rejected = 0, newton_iterations = 0;
+};
+TranAdaptiveResult tran_adaptive(const Circuit& c, const std::vector<Waveform>& waves,
+                                 const NewtonConfig& cfg, const std::string& solver_kind,
+                                 double tstep, double tstop, double tstart, double tmax,
+                                 double abs_tol, double rel_tol, double be_sign,
+                                 const Vec& x_ic);
 
 // ---------------------------------------------------------------- BBD
 // bbd_decompose (crates/sim-core/src/bbd.rs:355-485) on a given partition

@@ -73,6 +73,18 @@ def lib():
         L.orc_dc_batch.argtypes = [_I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, C.c_char_p,
                                    _I64, _D, _D, _D, _I64, _P, _P, _I64, _P, _P, _P, _I64,
                                    C.c_int, _P]
+        L.orc_wave_eval.argtypes = [C.c_int32, _P, _I64, _P, _P, _I64, _P, _P]
+        L.orc_breakpoints.restype = _I64
+        L.orc_breakpoints.argtypes = [_I64, _P, _P, _P, _P, _P, _D, _P, _I64]
+        L.orc_bp_limit_dt.restype = _D
+        L.orc_bp_limit_dt.argtypes = [_P, _I64, _D, _D, _D]
+        L.orc_bp_settling.argtypes = [_P, _I64, _I64, _D, _I64, _P, _P, _P]
+        L.orc_lte.argtypes = [_P, _P, _I64, _D, _D, _P]
+        L.orc_adaptive_sequence.argtypes = [_D, _D, _I64, _P, _P, _P]
+        L.orc_tran_adaptive.restype = C.c_int
+        L.orc_tran_adaptive.argtypes = [_I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P, C.c_char_p,
+                                        _I64, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _P,
+                                        _I64, _I64, _P, _P, _P]
         _lib = L
     return _lib
 
@@ -340,3 +352,85 @@ def dc_batch(circuits, inst_circ, inst_dev, inst_val, solver="nativeklu", max_it
                        _ptr(reason), _ptr(xo) if x_cap > 0 else None, x_cap, int(sweep),
                        _ptr(perturbed_out) if perturbed_out is not None else None)
     return iters, reason, (xo if x_cap > 0 else None)
+
+
+# ---------------------------------------------------------------- adaptive transient
+def _waves(waves, ndev):
+    from rustspice_gb300 import waveforms as wf
+    return wf.pack(waves, ndev)
+
+
+def wave_eval(w, ts):
+    """WaveformSpec::evaluate of one waveform at the times ts."""
+    from rustspice_gb300 import waveforms as wf
+    kind, p7, ptr, pt, pv = wf.pack({0: w}, 1)
+    ts = _f64(ts)
+    out = np.zeros(len(ts))
+    lib().orc_wave_eval(int(kind[0]), _ptr(p7), int(ptr[1]), _ptr(pt), _ptr(pv), len(ts),
+                        _ptr(ts), _ptr(out))
+    return out
+
+
+def breakpoints(waves_list, tstop):
+    """Sorted unique breakpoint times of the sources' PULSE and PWL waveforms."""
+    kind, p7, ptr, pt, pv = _waves({i: w for i, w in enumerate(waves_list)}, len(waves_list))
+    out = np.zeros(100000)
+    n = lib().orc_breakpoints(len(waves_list), _ptr(kind), _ptr(p7), _ptr(ptr), _ptr(pt),
+                              _ptr(pv), tstop, _ptr(out), len(out))
+    return out[:n]
+
+
+def bp_limit_dt(times, t, dt, margin):
+    ts = _f64(times)
+    return lib().orc_bp_limit_dt(_ptr(ts), len(ts), t, dt, margin)
+
+
+def bp_settling(times, steps, factor, pairs):
+    ts = _f64(times)
+    tp = _f64([a for a, _ in pairs])
+    tn = _f64([b for _, b in pairs])
+    out = np.zeros(2 * len(pairs), np.int32)
+    lib().orc_bp_settling(_ptr(ts), len(ts), steps, factor, len(pairs), _ptr(tp), _ptr(tn),
+                          _ptr(out))
+    return [(bool(out[2 * i]), bool(out[2 * i + 1])) for i in range(len(pairs))]
+
+
+def lte_milne(x_be, x_trap, abs_tol, rel_tol):
+    be, tr = _f64(x_be), _f64(x_trap)
+    out = np.zeros(5)
+    lib().orc_lte(_ptr(be), _ptr(tr), len(be), abs_tol, rel_tol, _ptr(out))
+    return {"error_norm": out[0], "max_error_node": int(out[1]), "accept": bool(out[2]),
+            "suggested_factor": out[3], "raw_lte": out[4]}
+
+
+def adaptive_sequence(dt_min, dt_max, errors, dts):
+    """Feeds error ratios through the adaptive controller; per step
+    (accept, next_dt, struggling, PI suggestion)."""
+    e, d = _f64(errors), _f64(dts)
+    out = np.zeros(4 * len(e))
+    lib().orc_adaptive_sequence(dt_min, dt_max, len(e), _ptr(e), _ptr(d), _ptr(out))
+    o = out.reshape(-1, 4)
+    return [(bool(r[0]), r[1], bool(r[2]), r[3]) for r in o]
+
+
+def tran_adaptive(c, waves, tstep, tstop, tstart=0.0, tmax=None, solver="nativeklu_exact",
+                  max_iters=100, abs_tol=1e-6, rel_tol=1e-3, gmin=1e-12, lte_abs=None,
+                  lte_rel=None, be_sign=1.0, x_ic=None, cap=100000):
+    """The engine's adaptive transient. Returns dict(status, times,
+    solutions[points, n], accepted, rejected, newton_iterations)."""
+    _, t, nd, p = _circ_arrays(c)
+    kind, p7, ptr, pt, pv = _waves(waves, c.ndev)
+    xi = _f64(x_ic if x_ic is not None else np.zeros(c.node_count))
+    n = c.n
+    times = np.zeros(cap)
+    sols = np.zeros(cap * n)
+    st = np.zeros(4, np.int64)
+    r = lib().orc_tran_adaptive(
+        c.node_count, c.ndev, _ptr(t), _ptr(nd), _ptr(p), _ptr(kind), _ptr(p7), _ptr(ptr),
+        _ptr(pt), _ptr(pv), solver.encode(), max_iters, abs_tol, rel_tol, gmin, tstep, tstop,
+        tstart, tstop if tmax is None else tmax, abs_tol if lte_abs is None else lte_abs,
+        rel_tol if lte_rel is None else lte_rel, be_sign, _ptr(xi), cap, n, _ptr(times),
+        _ptr(sols), _ptr(st))
+    npts = min(int(st[3]), cap)
+    return {"status": r, "times": times[:npts], "solutions": sols.reshape(cap, n)[:npts],
+            "accepted": int(st[0]), "rejected": int(st[1]), "newton_iterations": int(st[2])}
