@@ -362,6 +362,49 @@ int gpuklu_batch_set_schedule(gpuklu_batch* b, int lane_cap, int cont_tiles);
 int gpuklu_batch_autotune(gpuklu_batch* b, const gpuklu_newton_config* cfg, int64_t* out,
                           double* best_ms);
 
+/* ------------------------------------------ adaptive transient */
+/* The engine's transient analysis (crates/sim-core/src/engine.rs:332-602),
+ * one circuit instance per warp, the whole time loop on the device: the DC
+ * operating point from the instance's initial guess x_ic (its .ic values),
+ * then per step a backward-Euler and a trapezoidal Newton solve from the
+ * last accepted point, Milne's estimate |x_trap - x_be| / 3 over the whole
+ * iterate against lte_abs + lte_rel max(|x|) (analysis.rs:147-206; the
+ * engine passes vntol and reltol), the PI controller (analysis.rs:380-760),
+ * breakpoints of PULSE and PWL sources with five settling steps at a tenth
+ * of the step after each (waveform.rs:417-660), and ten rejections in a
+ * row ending the run. Circuits as for gpuklu_tran_create (C devices take
+ * p[0] as the capacitance); per device (concatenated over the circuits) an
+ * optional waveform of a V or I source: wkind 0 none, 1 PULSE (7 parameters
+ * v1 v2 td tr tf pw per), 2 PWL (points pwl_ptr[d]..pwl_ptr[d+1] of pwl_t,
+ * pwl_v), 3 SIN (vo va freq td theta), 4 EXP (v1 v2 td1 tau1 td2 tau2), the
+ * parameters in wp7[d * 7 ..]. A waveform source takes its value at tstart
+ * in the DC point (the reference's DC stamp cannot parse a waveform and
+ * leaves the source out). probe: the node whose voltage is recorded. */
+gpuklu_batch* gpuklu_atran_create(int64_t ncirc, const int64_t* dev_off,
+                                  const int64_t* node_counts, const int32_t* type,
+                                  const int32_t* nodes, const double* p, const int32_t* wkind,
+                                  const double* wp7, const int64_t* pwl_ptr, const double* pwl_t,
+                                  const double* pwl_v, const double* x_ic,
+                                  const int64_t* x_ic_off, int64_t x_ic_len,
+                                  const int64_t* probe);
+/* Runs the adaptive transient from tstart to tstop: min step max(1e-6 tstep,
+ * 1e-15), max step min(tmax, tstop / 10), first step min(tstep, max step).
+ * be_sign: -1 the reference's backward-Euler companion (rhs[a] -= (C/dt)
+ * v_prev; every step with a charged capacitor is then rejected), +1 the
+ * physical one. cfg: the Newton settings of every solve (the engine uses
+ * the DC settings; its transient has no gmin or source stepping). Per
+ * instance i: up to max_points accepted times and probe values at
+ * i * max_points (the DC point first), npoints (all accepted points, also
+ * those beyond max_points), accepted and rejected steps, Newton
+ * iterations, status (0 completed, 1 ten rejections in a row, 2 DC point
+ * not converged, 3 max_steps step attempts spent), and the last accepted
+ * solution in x_out (the batch's x_out layout, n values per instance). */
+int gpuklu_atran_run(gpuklu_batch* b, const gpuklu_newton_config* cfg, double tstep,
+                     double tstop, double tstart, double tmax, double lte_abs, double lte_rel,
+                     double be_sign, int64_t max_points, int64_t max_steps, double* times_out,
+                     double* probe_out, int64_t* npoints, int64_t* accepted, int64_t* rejected,
+                     int32_t* status, int64_t* iters, double* x_out);
+
 /* ------------------------------------------ bordered block diagonal */
 /* The reference's BbdSolver (crates/sim-core/src/bbd_solver.rs:86-1095,
  * bbd.rs:355-485) with a known partition (the Partitioner trait's result,

@@ -1,6 +1,6 @@
 """In-tree build of libgpuklu.so for sm_103a (GB300).
 
-Nine translation units compiled in parallel by nvcc, linked into
+Ten translation units compiled in parallel by nvcc, linked into
 ``rustspice_gb300/_build/libgpuklu.so``. ``--fmad=false`` keeps every FP64
 multiply and add separately rounded, as in the reference.
 """
@@ -16,8 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgpuklu.so")
-SOURCES = ["analysis.cpp", "kernels.cu", "lanes.cu", "tran.cu", "bbd.cu", "schur.cu", "ac.cu",
-           "dense.cu", "capi.cu"]
+SOURCES = ["analysis.cpp", "kernels.cu", "lanes.cu", "tran.cu", "atran.cu", "bbd.cu", "schur.cu",
+           "ac.cu", "dense.cu", "capi.cu"]
 HEADERS = ["analysis.h", "device.cuh", "kernels.cuh", "batch_common.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

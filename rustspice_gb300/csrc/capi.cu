@@ -1645,6 +1645,14 @@ struct gpuklu_batch {
   DBuf<long long> d_ckpt_off, d_seg_off, d_grad_off;
   DBuf<unsigned> d_tcounter;
   bool tran_fwd_done = false;
+  // adaptive transient: per instance its time-dependent sources (records
+  // at_wptr[i]..at_wptr[i+1]) and the run's per-instance outputs
+  bool atran = false;
+  int at_grid = 0;
+  std::vector<i32> at_wptr, at_wdev, at_wkind, at_pwlptr;
+  std::vector<double> at_wp, at_pwlt, at_pwlv;
+  DBuf<i32> d_at_wptr, d_at_wdev, d_at_wkind, d_at_pwlptr, d_at_bpptr, d_at_out;
+  DBuf<double> d_at_wp, d_at_pwlt, d_at_pwlv, d_at_bpt, d_at_times, d_at_probe;
 
   ~gpuklu_batch() {
     for (auto& c : classes) {
@@ -2495,6 +2503,230 @@ gpuklu_batch* gpuklu_tran_create(int64_t ncirc, const int64_t* dev_off,
   a.prog_ints = prog;
   a.counter = B->d_tcounter.p;
   return B.release();
+}
+
+gpuklu_batch* gpuklu_atran_create(int64_t ncirc, const int64_t* dev_off,
+                                  const int64_t* node_counts, const int32_t* type,
+                                  const int32_t* nodes, const double* p, const int32_t* wkind,
+                                  const double* wp7, const int64_t* pwl_ptr, const double* pwl_t,
+                                  const double* pwl_v, const double* x_ic,
+                                  const int64_t* x_ic_off, int64_t x_ic_len,
+                                  const int64_t* probe) {
+  if (ncirc <= 0 || !x_ic || !x_ic_off || !probe) {
+    fprintf(stderr, "gpuklu_atran_create: invalid arguments\n");
+    return nullptr;
+  }
+  for (int64_t i = 0; i < ncirc; ++i) {
+    if (probe[i] < 0 || probe[i] >= node_counts[i] || x_ic_off[i] < 0 ||
+        x_ic_off[i] + node_counts[i] > x_ic_len) {
+      fprintf(stderr, "gpuklu_atran_create: instance %ld: probe or initial guess out of range\n",
+              (long)i);
+      return nullptr;
+    }
+    for (int64_t d = dev_off[i]; d < dev_off[i + 1]; ++d)
+      if (wkind && wkind[d] != 0 && (type[d] != 1 && type[d] != 2 || wkind[d] < 1 ||
+                                     wkind[d] > 4)) {
+        fprintf(stderr, "gpuklu_atran_create: device %ld: a waveform needs a V or I source "
+                        "and kind 1..4\n", (long)d);
+        return nullptr;
+      }
+  }
+  std::vector<int64_t> ic(ncirc);
+  for (int64_t i = 0; i < ncirc; ++i) ic[i] = i;
+  std::unique_ptr<gpuklu_batch> B(batch_build(ncirc, dev_off, node_counts, type, nodes, p, ncirc,
+                                              ic.data(), nullptr, nullptr, x_ic, x_ic_off,
+                                              x_ic_len, 1, 1.0));
+  if (!B) return nullptr;
+  B->atran = true;
+  const int64_t ninst = ncirc;
+  int region = 0, prog = 0;
+  std::vector<i32> probe_h(ninst);
+  B->at_wptr.assign(1, 0);
+  B->at_pwlptr.assign(1, 0);
+  for (int64_t i = 0; i < ninst; ++i) {
+    const gk::GroupHdr& h = B->groups[B->inst_group_h[i]];
+    region = std::max(region, 4 * h.n + 2 * h.ndev + h.ndv + h.nslots + h.noffd +
+                                  (h.n + 1) / 2 + 1);
+    prog = std::max(prog, (4 * h.n + h.nslots + (h.nseg > 0 ? h.nslots + h.nupd : 0) + 3) & ~3);
+    probe_h[i] = (i32)probe[i];
+    for (int64_t d = dev_off[i]; d < dev_off[i + 1]; ++d) {
+      if (!wkind || wkind[d] == 0) continue;
+      B->at_wdev.push_back((i32)(d - dev_off[i]));
+      B->at_wkind.push_back(wkind[d]);
+      for (int k = 0; k < 7; ++k) B->at_wp.push_back(wp7 ? wp7[d * 7 + k] : 0.0);
+      std::vector<std::pair<double, double>> pts;
+      if (pwl_ptr)
+        for (int64_t q = pwl_ptr[d]; q < pwl_ptr[d + 1]; ++q) pts.push_back({pwl_t[q], pwl_v[q]});
+      std::stable_sort(pts.begin(), pts.end(),  // PwlParams::new (waveform.rs:137-143)
+                       [](const std::pair<double, double>& a, const std::pair<double, double>& b) {
+                         return a.first < b.first;
+                       });
+      for (auto& pt : pts) {
+        B->at_pwlt.push_back(pt.first);
+        B->at_pwlv.push_back(pt.second);
+      }
+      B->at_pwlptr.push_back((i32)B->at_pwlt.size());
+    }
+    B->at_wptr.push_back((i32)B->at_wdev.size());
+  }
+  region = (region + 1) & ~1;
+  cudaStream_t s = B->stream;
+  cudaError_t e = B->d_inst_group.upload(B->inst_group_h, s);
+  if (e == cudaSuccess) e = B->d_probe.upload(probe_h, s);
+  if (e == cudaSuccess) e = B->d_at_wptr.upload(B->at_wptr, s);
+  if (e == cudaSuccess) e = B->d_at_wdev.upload(B->at_wdev, s);
+  if (e == cudaSuccess) e = B->d_at_wkind.upload(B->at_wkind, s);
+  if (e == cudaSuccess) e = B->d_at_pwlptr.upload(B->at_pwlptr, s);
+  if (e == cudaSuccess) e = B->d_at_wp.upload(B->at_wp, s);
+  if (e == cudaSuccess) e = B->d_at_pwlt.upload(B->at_pwlt, s);
+  if (e == cudaSuccess) e = B->d_at_pwlv.upload(B->at_pwlv, s);
+  if (e == cudaSuccess) e = B->d_tcounter.resize(1);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "gpuklu_atran_create: %s\n", cudaGetErrorString(e));
+    return nullptr;
+  }
+  int regs = 0, bps = 0;
+  gk::atran_kernel_info(region, prog, &regs, &bps);
+  if (bps <= 0) {
+    fprintf(stderr, "gpuklu_atran_create: a circuit needs %d KB of shared memory\n",
+            (int)((region * 8 + prog * 4) / 1024));
+    return nullptr;
+  }
+  B->at_grid = (int)std::min<int64_t>(ninst, (int64_t)sm_count() * bps);
+  gk::BatchArgs& a = B->args;
+  a.ninst = (int)ninst;
+  a.inst_group = B->d_inst_group.p;
+  a.region = region;
+  a.prog_ints = prog;
+  a.counter = B->d_tcounter.p;
+  return B.release();
+}
+
+namespace {
+// Breakpoints of one instance's PULSE and PWL sources for a run to tstop
+// (BreakpointManager::extract_from_sources, waveform.rs:459-530; the engine
+// extracts only these two kinds, engine.rs:635-680): sorted, unique.
+void instance_breakpoints(const gpuklu_batch* b, int64_t i, double tstop,
+                          std::vector<double>& out) {
+  out.clear();
+  auto add = [&](double t) {
+    if (t >= 0.0) out.push_back(t);
+  };
+  for (int r = b->at_wptr[i]; r < b->at_wptr[i + 1]; ++r) {
+    const double* q = &b->at_wp[(size_t)r * 7];
+    if (b->at_wkind[r] == 1) {
+      const double td = q[2], tr = q[3], tf = q[4], pw = q[5], per = q[6];
+      double t = td;
+      int count = 0;
+      if (td > 0.0) add(td);
+      while (t <= tstop && count < 10000) {
+        add(t);
+        const double th = t + tr;
+        if (th > tstop) break;
+        add(th);
+        const double tfl = th + pw;
+        if (tfl > tstop) break;
+        add(tfl);
+        const double tl = tfl + tf;
+        if (tl > tstop) break;
+        add(tl);
+        if (per > 0.0) {
+          t = td + per * (double)(count + 1);
+          count += 1;
+        } else {
+          break;
+        }
+      }
+    } else if (b->at_wkind[r] == 2) {
+      for (int qq = b->at_pwlptr[r]; qq < b->at_pwlptr[r + 1]; ++qq) add(b->at_pwlt[qq]);
+    }
+  }
+  std::sort(out.begin(), out.end());
+  out.erase(std::unique(out.begin(), out.end()), out.end());
+}
+}  // namespace
+
+int gpuklu_atran_run(gpuklu_batch* b, const gpuklu_newton_config* cfg, double tstep,
+                     double tstop, double tstart, double tmax, double lte_abs, double lte_rel,
+                     double be_sign, int64_t max_points, int64_t max_steps, double* times_out,
+                     double* probe_out, int64_t* npoints, int64_t* accepted, int64_t* rejected,
+                     int32_t* status, int64_t* iters, double* x_out) {
+  if (!b || !cfg || !b->atran) return GPUKLU_INVALID_MATRIX;
+  if (!(tstep > 0.0) || !(tstop > tstart) || !(tmax > 0.0) || max_points < 0 || max_steps <= 0 ||
+      max_steps > (int64_t)1 << 30 || (double)b->ninst * (double)max_points > 4e9) {
+    b->err = "gpuklu_atran_run: tstep > 0, tstop > tstart, tmax > 0, 0 <= max_points, "
+             "0 < max_steps <= 2^30";
+    return GPUKLU_INVALID_MATRIX;
+  }
+  const int64_t ni = b->ninst;
+  std::vector<i32> bp_ptr(1, 0);
+  std::vector<double> bp_t, tmp;
+  for (int64_t i = 0; i < ni; ++i) {
+    instance_breakpoints(b, i, tstop, tmp);
+    bp_t.insert(bp_t.end(), tmp.begin(), tmp.end());
+    bp_ptr.push_back((i32)bp_t.size());
+  }
+  cudaStream_t s = b->stream;
+  const size_t np = (size_t)ni * (size_t)max_points;
+  cudaError_t e = b->d_at_bpptr.upload(bp_ptr, s);
+  if (e == cudaSuccess) e = b->d_at_bpt.upload(bp_t, s);
+  if (e == cudaSuccess) e = b->d_at_times.resize(std::max<size_t>(np, 1));
+  if (e == cudaSuccess) e = b->d_at_probe.resize(std::max<size_t>(np, 1));
+  if (e == cudaSuccess) e = b->d_at_out.resize((size_t)ni * 4);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->args.counter, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return b->fail(cuda_msg(e, "adaptive transient"));
+  gk::BatchArgs a = b->args;
+  a.cfg = to_newton_cfg(*cfg);
+  gk::AtranArgs t{};
+  t.wave_ptr = b->d_at_wptr.p;
+  t.wave_dev = b->d_at_wdev.p;
+  t.wave_kind = b->d_at_wkind.p;
+  t.pwl_ptr = b->d_at_pwlptr.p;
+  t.wave_p = b->d_at_wp.p;
+  t.pwl_t = b->d_at_pwlt.p;
+  t.pwl_v = b->d_at_pwlv.p;
+  t.bp_ptr = b->d_at_bpptr.p;
+  t.bp_t = b->d_at_bpt.p;
+  t.probe = b->d_probe.p;
+  t.tstep = tstep;
+  t.tstop = tstop;
+  t.tstart = tstart;
+  t.tmax = tmax;
+  t.lte_abs = lte_abs;
+  t.lte_rel = lte_rel;
+  t.be_sign = be_sign;
+  t.max_points = (int)max_points;
+  t.max_steps = (int)max_steps;
+  t.times = b->d_at_times.p;
+  t.probe_out = b->d_at_probe.p;
+  t.status = b->d_at_out.p;
+  t.npoints = b->d_at_out.p + ni;
+  t.accepted = b->d_at_out.p + 2 * ni;
+  t.rejected = b->d_at_out.p + 3 * ni;
+  gk::launch_atran(a, t, b->at_grid, s);
+  std::vector<i32> outs((size_t)ni * 4), it(ni);
+  e = cudaGetLastError();
+  if (e == cudaSuccess && times_out && np)
+    e = cudaMemcpyAsync(times_out, b->d_at_times.p, np * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && probe_out && np)
+    e = cudaMemcpyAsync(probe_out, b->d_at_probe.p, np * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(outs.data(), b->d_at_out.p, outs.size() * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(it.data(), b->d_iters_total.p, ni * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && x_out)
+    e = cudaMemcpyAsync(x_out, b->d_xout.p, b->xout_len * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return b->fail(cuda_msg(e, "adaptive transient"));
+  for (int64_t i = 0; i < ni; ++i) {
+    if (status) status[i] = outs[i];
+    if (npoints) npoints[i] = outs[ni + i];
+    if (accepted) accepted[i] = outs[2 * ni + i];
+    if (rejected) rejected[i] = outs[3 * ni + i];
+    if (iters) iters[i] = it[i];
+  }
+  return GPUKLU_OK;
 }
 
 int gpuklu_tran_forward(gpuklu_batch* b, const gpuklu_newton_config* cfg, double* loss_out,

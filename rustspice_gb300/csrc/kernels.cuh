@@ -149,6 +149,24 @@ struct BatchArgs {
   double *cont_damp, *cont_prev;  // the iterate itself waits in x_out
 };
 
+// Batched adaptive transient (atran.cu): per instance its time-dependent
+// sources (records wave_ptr[i]..wave_ptr[i+1]: device, kind 1 PULSE 2 PWL 3
+// SIN 4 EXP, 7 parameters, PWL points at pwl_ptr) and breakpoints (bp_ptr);
+// the run's controls; per instance up to max_points accepted times and
+// probe-node values, counts and status (0 completed, 1 ten rejections in a
+// row, 2 DC point failed, 3 max_steps attempts spent).
+struct AtranArgs {
+  const int *wave_ptr, *wave_dev, *wave_kind, *pwl_ptr;
+  const double *wave_p, *pwl_t, *pwl_v;
+  const int* bp_ptr;
+  const double* bp_t;
+  const int* probe;
+  double tstep, tstop, tstart, tmax, lte_abs, lte_rel, be_sign;
+  int max_points, max_steps;
+  double *times, *probe_out;
+  int *npoints, *accepted, *rejected, *status;
+};
+
 // Bordered-block-diagonal solver: the index lists its kernels read.
 struct BbdArgs {
   int ntiles, bs, border_start;
@@ -282,6 +300,8 @@ size_t ac_smem_bytes(int n, int threads);
 void launch_ac_dense(const AcArgs& a, int nf, cudaStream_t s);
 
 // Transient forward / adjoint over a batch: one warp per instance.
+void launch_atran(const BatchArgs& a, const AtranArgs& t, int grid, cudaStream_t s);
+void atran_kernel_info(int region, int prog_ints, int* regs, int* blocks_per_sm);
 void launch_tran_forward(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
 void launch_tran_backward(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
 void tran_kernel_info(bool backward, int warps_per_block, int region, int prog_ints, int* regs,

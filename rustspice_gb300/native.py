@@ -35,7 +35,7 @@ SYMBOLS = [
     "gpuklu_circuit_set_params", "gpuklu_stamp", "gpuklu_newton_dc", "gpuklu_dc_sweep", "gpuklu_batch_create",
     "gpuklu_batch_destroy", "gpuklu_batch_run", "gpuklu_batch_results",
     "gpuklu_batch_update_inputs", "gpuklu_batch_last_error", "gpuklu_batch_info",
-    "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_batch_phase_ms", "gpuklu_batch_set_schedule", "gpuklu_batch_autotune", "gpuklu_ac_sweep", "gpuklu_tran_create", "gpuklu_tran_forward",
+    "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_batch_phase_ms", "gpuklu_batch_set_schedule", "gpuklu_batch_autotune", "gpuklu_ac_sweep", "gpuklu_tran_create", "gpuklu_tran_forward", "gpuklu_atran_create", "gpuklu_atran_run",
     "gpuklu_tran_backward", "gpuklu_bbd_create", "gpuklu_bbd_destroy", "gpuklu_bbd_last_error",
     "gpuklu_bbd_info", "gpuklu_bbd_perm", "gpuklu_bbd_factor", "gpuklu_bbd_solve", "gpuklu_bbd_newton_dc", "gpuklu_fp64_peak_tflops", "gpuklu_fp64_mma_peak_tflops", "gpuklu_dense_lu_nopivot", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free", "gpuklu_btf_info",
 ]
@@ -119,6 +119,10 @@ def lib(build_if_missing: bool = True):
         "gpuklu_tran_create": (_P, [_I64, _P, _P, _P, _P, _P, _P, _P, _I64, _D, _I64, _I64, _P,
                                     _D]),
         "gpuklu_tran_forward": (C.c_int, [_P, _P, _P, _P, _P, _P]),
+        "gpuklu_atran_create": (_P, [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I64,
+                                     _P]),
+        "gpuklu_atran_run": (C.c_int, [_P, C.POINTER(NewtonConfig), _D, _D, _D, _D, _D, _D, _D,
+                                       _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P]),
         "gpuklu_tran_backward": (C.c_int, [_P, _P, _P, _P]),
         "gpuklu_bbd_create": (_P, [_I64, _P, _I64, _P, _I64, _P, _I64]),
         "gpuklu_bbd_destroy": (None, [_P]),

@@ -431,6 +431,96 @@ class Batch:
                 "best_ms": ms.value}
 
 
+@dataclasses.dataclass
+class ATranResult:
+    status: np.ndarray          # per instance: 0 completed, 1 rejections, 2 DC failed, 3 budget
+    times: list                 # per instance: accepted times (the DC point first)
+    probe: list                 # per instance: the probe node's voltage at those times
+    npoints: np.ndarray
+    accepted: np.ndarray
+    rejected: np.ndarray
+    iterations: np.ndarray
+    x: list                     # per instance: the last accepted solution (n values)
+
+
+class ATranBatch:
+    """The engine's adaptive transient (engine.rs:332-602) on many circuits
+    at once, one warp per circuit, the time loop on the device. waves: per
+    circuit a dict {device: rustspice_gb300.waveforms.Waveform} of time
+    dependent V / I sources; x_ic: per circuit the .ic initial guess of the
+    DC point (node_count values) or None; probe: recorded node per circuit."""
+
+    def __init__(self, circuits, waves=None, x_ic=None, probe=1):
+        from . import waveforms as wf
+        self.circuits = circuits
+        n = len(circuits)
+        dev_off = np.zeros(n + 1, np.int64)
+        for i, c in enumerate(circuits):
+            dev_off[i + 1] = dev_off[i] + c.ndev
+        ncs = N.i64([c.node_count for c in circuits])
+        t = N.i32(np.concatenate([c.type for c in circuits]))
+        nd = N.i32(np.concatenate([c.nodes for c in circuits]))
+        p = N.f64(np.concatenate([c.p for c in circuits]))
+        kinds, p7s, pts_t, pts_v, ptr = [], [], [], [], [0]
+        for i, c in enumerate(circuits):
+            k, q, pp, pt, pv = wf.pack((waves or [None] * n)[i] or {}, c.ndev)
+            kinds.append(k)
+            p7s.append(q)
+            pts_t.append(pt)
+            pts_v.append(pv)
+            ptr.extend(ptr[-1] + pp[1:])
+        self._wk = N.i32(np.concatenate(kinds))
+        self._wp = N.f64(np.concatenate(p7s))
+        self._pp = N.i64(ptr)
+        self._pt = N.f64(np.concatenate(pts_t) if pts_t else np.zeros(0))
+        self._pv = N.f64(np.concatenate(pts_v) if pts_v else np.zeros(0))
+        xs = [np.zeros(c.node_count) if (x_ic is None or x_ic[i] is None) else
+              np.asarray(x_ic[i], np.float64) for i, c in enumerate(circuits)]
+        xo = np.zeros(n, np.int64)
+        for i in range(1, n):
+            xo[i] = xo[i - 1] + circuits[i - 1].node_count
+        xi = N.f64(np.concatenate(xs))
+        pr = N.i64(np.broadcast_to(np.asarray(probe, np.int64), (n,)).copy())
+        self._h = N.lib().gpuklu_atran_create(
+            n, N.ptr(dev_off), N.ptr(ncs), N.ptr(t), N.ptr(nd), N.ptr(p), N.ptr(self._wk),
+            N.ptr(self._wp), N.ptr(self._pp), N.ptr(self._pt), N.ptr(self._pv), N.ptr(xi),
+            N.ptr(N.i64(xo)), len(xi), N.ptr(pr))
+        if not self._h:
+            raise RuntimeError("gpuklu_atran_create failed")
+        self.x_off = np.cumsum([0] + [c.n for c in circuits])[:-1]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().gpuklu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def run(self, cfg: N.NewtonConfig, tstep, tstop, tstart=0.0, tmax=None, lte_abs=None,
+            lte_rel=None, be_sign=1.0, max_points=4096, max_steps=1_000_000) -> ATranResult:
+        """lte_abs / lte_rel default to the Newton config's abs_tol / rel_tol
+        (the engine passes vntol and reltol to both)."""
+        n = len(self.circuits)
+        times = np.zeros(n * max_points)
+        probe = np.zeros(n * max_points)
+        npts, acc, rej, its = (np.zeros(n, np.int64) for _ in range(4))
+        st = np.zeros(n, np.int32)
+        xo = np.zeros(int(sum(c.n for c in self.circuits)))
+        r = N.lib().gpuklu_atran_run(
+            self._h, C.byref(cfg), tstep, tstop, tstart, tstop if tmax is None else tmax,
+            cfg.abs_tol if lte_abs is None else lte_abs, cfg.rel_tol if lte_rel is None else lte_rel,
+            be_sign, max_points, max_steps, N.ptr(times), N.ptr(probe), N.ptr(npts), N.ptr(acc),
+            N.ptr(rej), N.ptr(st), N.ptr(its), N.ptr(xo))
+        if r != N.OK:
+            raise SolverError(r, N.lib().gpuklu_batch_last_error(self._h).decode())
+        k = np.minimum(npts, max_points)
+        return ATranResult(
+            st, [times[i * max_points:i * max_points + k[i]] for i in range(n)],
+            [probe[i * max_points:i * max_points + k[i]] for i in range(n)], npts, acc, rej, its,
+            [xo[self.x_off[i]:self.x_off[i] + c.n] for i, c in enumerate(self.circuits)])
+
+
 class TranBatch:
     """Fixed-step backward-Euler transient of many circuits (one instance per
     circuit) with the checkpointed adjoint of
