@@ -273,9 +273,12 @@ int gpuklu_dc_sweep(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_con
  * sources carry the AC magnitude in p[1] and the phase [deg] in p[2]. x_dc:
  * the operating point (node voltages at least); freqs: nf frequencies [Hz];
  * out_re / out_im: nf x n values (n = node_count + one aux per V source, row
- * 0 the ground); *n_out = n. n above GPUKLU_AC_MAX_N gives
- * GPUKLU_INVALID_MATRIX, a pivot below 1e-30 GPUKLU_SINGULAR. */
-#define GPUKLU_AC_MAX_N 112
+ * 0 the ground); *n_out = n. Systems up to n = 119 are factored in one
+ * block's shared memory per frequency; larger ones in per-block slices of a
+ * global scratch (up to ~2 GB, blocks looping over the frequencies) with the
+ * same arithmetic. n above GPUKLU_AC_MAX_N gives GPUKLU_INVALID_MATRIX, a
+ * pivot below 1e-30 GPUKLU_SINGULAR. */
+#define GPUKLU_AC_MAX_N 4096
 int gpuklu_ac_sweep(gpuklu_handle* h, gpuklu_circuit* c, const double* x_dc, int64_t xlen,
                     const double* freqs, int64_t nf, double* out_re, double* out_im,
                     int64_t* n_out);

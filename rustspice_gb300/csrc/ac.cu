@@ -2,10 +2,11 @@
 // crates/sim-core/src/engine.rs:829-930, complex_solver.rs:28-144).
 //
 // One thread block per frequency point keeps the dense complex system in
-// shared memory: it fills Y(w) = G + jwC cell by cell (G from the DC stamp at
-// the operating point, the capacitor terms +-w*C in insertion order), then
-// runs the reference's dense LU with partial pivoting and the back
-// substitution. Complex arithmetic is num-complex's (0.4.6): a*b = (ar br -
+// shared memory (n up to 112), or, for larger systems, in its own slice of a
+// global scratch (L2 / HBM; blocks loop over the frequencies): it fills
+// Y(w) = G + jwC cell by cell (G from the DC stamp at the operating point,
+// the capacitor terms +-w*C in insertion order), then runs the reference's
+// dense LU with partial pivoting and the back substitution. Complex arithmetic is num-complex's (0.4.6): a*b = (ar br -
 // ai bi, ar bi + ai br), a/b = ((ar br + ai bi)/n, (ai br - ar bi)/n) with
 // n = br^2 + bi^2, |a| = hypot(ar, ai). Every element sees the reference's
 // operations in the reference's order (compiled without contraction), so the
@@ -30,16 +31,11 @@ __device__ __forceinline__ Cx cdiv(Cx a, Cx b) {
   return {re / n, im / n};
 }
 
-__global__ void __launch_bounds__(256) k_ac_dense(AcArgs A) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+// One frequency: M the n x n system (row-major; shared or global), x, pr,
+// bv, bi in shared memory.
+__device__ void ac_point(const AcArgs& A, long long f, Cx* M, Cx* x, Cx* pr, double* bv,
+                         int* bi, int& s_fail) {
   const int n = A.n, tid = threadIdx.x, nt = blockDim.x;
-  Cx* const M = reinterpret_cast<Cx*>(smem_raw);  // row-major n x n
-  Cx* const x = M + (size_t)n * n;
-  Cx* const pr = x + n;                            // products of one back-substitution row
-  double* const bv = reinterpret_cast<double*>(pr + n);  // pivot search: values
-  int* const bi = reinterpret_cast<int*>(bv + nt);        //               rows
-  __shared__ int s_fail;
-  const long long f = blockIdx.x;
   const double omega = 2.0 * 3.141592653589793 * A.freqs[f];
   for (int q = tid; q < n * n; q += nt) M[q] = Cx{0.0, 0.0};
   if (tid == 0) s_fail = 0;
@@ -138,12 +134,41 @@ __global__ void __launch_bounds__(256) k_ac_dense(AcArgs A) {
   }
   if (s_fail) {
     if (tid == 0) atomicExch(A.status, 1);
+    __syncthreads();
     return;
   }
   for (int i = tid; i < n; i += nt) {
     A.out_re[f * n + i] = x[i].re;
     A.out_im[f * n + i] = x[i].im;
   }
+  __syncthreads();
+}
+
+// Systems that fit one block's shared memory.
+__global__ void __launch_bounds__(256) k_ac_dense(AcArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = A.n, nt = blockDim.x;
+  Cx* const M = reinterpret_cast<Cx*>(smem_raw);  // row-major n x n
+  Cx* const x = M + (size_t)n * n;
+  Cx* const pr = x + n;                            // products of one back-substitution row
+  double* const bv = reinterpret_cast<double*>(pr + n);  // pivot search: values
+  int* const bi = reinterpret_cast<int*>(bv + nt);        //               rows
+  __shared__ int s_fail;
+  ac_point(A, blockIdx.x, M, x, pr, bv, bi, s_fail);
+}
+
+// Larger systems: each block's matrix in its slice of the global scratch,
+// the block looping over the frequencies.
+__global__ void __launch_bounds__(256) k_ac_dense_global(AcArgs A, int nf) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = A.n, nt = blockDim.x;
+  Cx* const M = reinterpret_cast<Cx*>(A.scratch) + (size_t)blockIdx.x * n * n;
+  Cx* const x = reinterpret_cast<Cx*>(smem_raw);
+  Cx* const pr = x + n;
+  double* const bv = reinterpret_cast<double*>(pr + n);
+  int* const bi = reinterpret_cast<int*>(bv + nt);
+  __shared__ int s_fail;
+  for (long long f = blockIdx.x; f < nf; f += gridDim.x) ac_point(A, f, M, x, pr, bv, bi, s_fail);
 }
 
 }  // namespace
@@ -152,11 +177,20 @@ size_t ac_smem_bytes(int n, int threads) {
   return (size_t)16 * ((size_t)n * n + 2 * (size_t)n) + (size_t)12 * threads + 16;
 }
 
+bool ac_fits_shared(int n) { return ac_smem_bytes(n, 256) <= 227 * 1024; }
+
 void launch_ac_dense(const AcArgs& a, int nf, cudaStream_t s) {
   const int threads = 256;
   const size_t bytes = ac_smem_bytes(a.n, threads);
   cudaFuncSetAttribute(k_ac_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   k_ac_dense<<<nf, threads, bytes, s>>>(a);
+}
+
+void launch_ac_dense_global(const AcArgs& a, int nf, int blocks, cudaStream_t s) {
+  const int threads = 256;
+  const size_t bytes = (size_t)32 * a.n + (size_t)12 * threads + 16;
+  cudaFuncSetAttribute(k_ac_dense_global, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k_ac_dense_global<<<blocks, threads, bytes, s>>>(a, nf);
 }
 
 }  // namespace gk

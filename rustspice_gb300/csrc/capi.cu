@@ -1326,7 +1326,20 @@ int gpuklu_ac_sweep(gpuklu_handle* h, gpuklu_circuit* c, const double* x_dc, int
   a.out_re = d_re.p;
   a.out_im = d_im.p;
   a.status = d_status.p;
-  gk::launch_ac_dense(a, (int)nf, s);
+  DBuf<double> d_scratch;
+  if (gk::ac_fits_shared(n)) {
+    gk::launch_ac_dense(a, (int)nf, s);
+  } else {
+    // one n x n complex matrix per block in global memory, at most ~2 GB of
+    // them (and no more blocks than frequencies or two per SM)
+    const size_t per = (size_t)16 * n * n;
+    int blocks = (int)std::min<int64_t>(nf, std::max<size_t>(1, ((size_t)2 << 30) / per));
+    blocks = std::min(blocks, 2 * sm_count());
+    e = d_scratch.resize(per / 8 * blocks);
+    if (e != cudaSuccess) return h->cuda_fail(e, "ac scratch");
+    a.scratch = d_scratch.p;
+    gk::launch_ac_dense_global(a, (int)nf, blocks, s);
+  }
   int st = 0;
   e = cudaGetLastError();
   if (e == cudaSuccess)

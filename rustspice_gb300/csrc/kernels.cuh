@@ -197,6 +197,7 @@ struct AcArgs {
   const double* freqs;
   double *out_re, *out_im;          // nf x n
   int* status;                      // 1: a pivot below 1e-30
+  double* scratch;                  // global path: per block an n x n complex matrix
 };
 
 // --------------------------------------------------------------- launches
@@ -298,6 +299,8 @@ void launch_bbd_combine(const double* z, const double* w2, const double* xT, con
 // One thread block per frequency; shared memory ac_smem_bytes(n, 256).
 size_t ac_smem_bytes(int n, int threads);
 void launch_ac_dense(const AcArgs& a, int nf, cudaStream_t s);
+bool ac_fits_shared(int n);
+void launch_ac_dense_global(const AcArgs& a, int nf, int blocks, cudaStream_t s);
 
 // Transient forward / adjoint over a batch: one warp per instance.
 void launch_atran(const BatchArgs& a, const AtranArgs& t, int grid, cudaStream_t s);

@@ -23,6 +23,7 @@ OK, ANALYZE_FAILED, FACTOR_FAILED, SOLVE_FAILED, SINGULAR, ILL_CONDITIONED, \
 PIVOT_REFERENCE, PIVOT_EXACT = 0, 1
 # Solver kinds (gpuklu_set_solver_kind), by the oracle's / reference's names
 KINDS = {"nativeklu": 0, "sparselu": 1, "sparselubtf": 2, "dense": 3}
+AC_MAX_N = 4096  # GPUKLU_AC_MAX_N
 
 # Every symbol the header declares; a test checks the library exports them.
 SYMBOLS = [

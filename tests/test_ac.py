@@ -17,7 +17,8 @@ C1 out 0 1u
 
 
 def _ladder(sections=100, seed=3):
-    """An RC ladder driven by an AC source: n = sections + 2 (ground, aux)."""
+    """An RC ladder driven by an AC source: n = sections + 3 (ground, the
+    sections + 1 ladder nodes, the source's aux)."""
     rng = np.random.default_rng(seed)
     lines = ["V1 n0 0 DC 0 AC 1 30"]
     for k in range(sections):
@@ -117,7 +118,15 @@ def test_device_ac_sweep_matches_oracle():
     xo = po.ac_sweep(d.circuit, res.x, f)
     xg = ac_sweep(g, DeviceCircuit(d.circuit), res.x, f)
     assert np.max(np.abs(xg - xo)) <= 1e-12 * np.max(np.abs(xo))
-    # size limit
-    big = _ladder(200)
+    # beyond one block's shared memory (n = 203 and 603): the matrices in
+    # global scratch, the same arithmetic bit for bit
+    for sections, nf in ((200, 24), (600, 5)):
+        big = _ladder(sections, seed=sections)
+        fb = frequency_sweep("dec", 3, 1.0, 1e8)[:nf]
+        xo = po.ac_sweep(big.circuit, np.zeros(big.circuit.n), fb)
+        xg = ac_sweep(g, DeviceCircuit(big.circuit), np.zeros(big.circuit.n), fb)
+        assert xg.shape == (len(fb), sections + 3) and np.array_equal(xg, xo)
+    # size limit (n = sections + 3: ground, sections + 1 nodes, the aux)
+    huge = _ladder(N.AC_MAX_N)
     with pytest.raises(Exception):
-        ac_sweep(g, DeviceCircuit(big.circuit), np.zeros(big.circuit.n), f[:2])
+        ac_sweep(g, DeviceCircuit(huge.circuit), np.zeros(huge.circuit.n), f[:2])
