@@ -197,7 +197,8 @@ def _ncu_traffic(kernel, iters):
     return per * iters, f"{os.path.relpath(PROFILE, ROOT)} ({per:.1f} B per iteration)"
 
 
-SECONDARY = ("mesh_dc", "dc_adjoint", "transient_adjoint", "bbd", "ac_sweep")
+SECONDARY = ("mesh_dc", "dc_adjoint", "transient_adjoint", "adaptive_transient", "bbd",
+             "ac_sweep")
 
 
 def secondary(with_cpu=True, parts=SECONDARY):
@@ -225,6 +226,8 @@ def secondary(with_cpu=True, parts=SECONDARY):
         _dc_adjoint(out, timed, with_cpu, ocfg)
     if "transient_adjoint" in parts:
         _transient_adjoint(out, timed, with_cpu)
+    if "adaptive_transient" in parts:
+        _adaptive_transient(out, timed, with_cpu)
     if "bbd" in parts:
         _bbd(out, with_cpu, timed, ocfg)
     if "ac_sweep" in parts:
@@ -343,6 +346,41 @@ def _transient_adjoint(out, timed, with_cpu):
         per = (time.perf_counter() - t0) / len(sample)
         out["transient_adjoint"]["oracle_forward_ms_1core_est"] = per * len(B.circuits) * 1e3
         out["transient_adjoint"]["oracle_sample"] = "16 rings (seed 2), scaled to 1024"
+
+
+def _adaptive_transient(out, timed, with_cpu):
+    """The engine's adaptive transient (BE + trapezoidal solves, Milne's LTE,
+    PI control, breakpoints) on 1024 inverter chains of 8-64 stages driven by
+    a pulse train, 0 to 4 ns, the engine's default LTE tolerances; the
+    oracle's restatement on one host core timed on 16 chains and scaled."""
+    from rustspice_gb300 import native as N
+    from rustspice_gb300 import workloads as wl
+    from rustspice_gb300.solver import ATranBatch
+    B = wl.adaptive_batch(1024)
+    ab = ATranBatch(B.circuits, B.waves, B.x_ic, B.probe)
+    cfg = N.newton_config(max_iters=100, abs_tol=1e-9, rel_tol=1e-6, gmin=1e-12)
+    kw = dict(lte_abs=1e-6, lte_rel=1e-3, be_sign=1.0, max_points=1)
+    ab.run(cfg, wl.ATRAN_TSTEP, wl.ATRAN_TSTOP, **kw)
+    r, t = timed(lambda: ab.run(cfg, wl.ATRAN_TSTEP, wl.ATRAN_TSTOP, **kw))
+    its = int(r.iterations.sum())
+    out["adaptive_transient"] = {
+        "workload": "1024 CMOS inverter chains (8-64 stages) x pulse train, 0-4 ns, "
+                    "tstep 10 ps, LTE vntol 1e-6 / reltol 1e-3, physical BE sign",
+        "gpu_ms": t * 1e3, "completed_fraction": float(np.mean(r.status == 0)),
+        "accepted_steps": int(r.accepted.sum()), "rejected_steps": int(r.rejected.sum()),
+        "newton_iterations": its, "newton_iters_per_s": its / t}
+    ab.close()
+    if with_cpu:
+        from oracle import pyoracle as po
+        sample = np.random.default_rng(2).choice(len(B.circuits), 16, replace=False)
+        t0 = time.perf_counter()
+        for i in sample:
+            po.tran_adaptive(B.circuits[i], B.waves[i], wl.ATRAN_TSTEP, wl.ATRAN_TSTOP,
+                             x_ic=B.x_ic[i], max_iters=100, abs_tol=1e-9, rel_tol=1e-6,
+                             lte_abs=1e-6, lte_rel=1e-3, cap=1)
+        per = (time.perf_counter() - t0) / len(sample)
+        out["adaptive_transient"]["oracle_ms_1core_est"] = per * len(B.circuits) * 1e3
+        out["adaptive_transient"]["oracle_sample"] = "16 chains (seed 2), scaled to 1024"
 
 
 def _bbd(out, with_cpu, timed, ocfg):

@@ -153,3 +153,32 @@ def bordered_nodeset(c: cz.Circuit, v: float = 0.55) -> np.ndarray:
     x = np.full(c.node_count, v)
     x[0] = 0.0
     return x
+
+
+# Adaptive transient workload: inverter chains of seeded lengths (the C3
+# card, 20 fF per stage) driven by a 0 -> 1.2 V pulse train on the input
+# source (device 1), from the chains' logic-level nodeset at Vin = 0.
+ATRAN_TSTEP = 10e-12
+ATRAN_TSTOP = 4e-9
+ATRAN_PULSE = dict(v1=0.0, v2=1.2, td=0.1e-9, tr=50e-12, tf=50e-12, pw=0.95e-9, per=2e-9)
+
+
+@dataclasses.dataclass
+class AdaptiveBatch:
+    circuits: list
+    waves: list      # per circuit {device: Waveform}
+    x_ic: list       # per circuit initial guess of the DC point
+    probe: np.ndarray
+
+
+def adaptive_batch(count: int = 1024, seed: int = 13, lo: int = 8, hi: int = 64) -> AdaptiveBatch:
+    from . import waveforms as wf
+    stages = cz.chain_lengths(count, lo, hi, seed)
+    circuits, waves, xs, probe = [], [], [], []
+    for i, s in enumerate(stages):
+        c = cz.inverter_chain(int(s), 0.0, seed=seed, chain_id=i)
+        circuits.append(c)
+        waves.append({1: wf.pulse(**ATRAN_PULSE)})
+        xs.append(chain_nodeset(int(s), 0.0))
+        probe.append(c.node_count - 1)
+    return AdaptiveBatch(circuits, waves, xs, np.asarray(probe, np.int64))
