@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgpuklu.so")
-SOURCES = ["analysis.cpp", "kernels.cu", "lanes.cu", "tran.cu", "atran.cu", "bbd.cu", "schur.cu",
+SOURCES = ["analysis.cpp", "kernels.cu", "lanes.cu", "cont.cu", "tran.cu", "atran.cu", "bbd.cu", "schur.cu",
            "ac.cu", "dense.cu", "capi.cu"]
 HEADERS = ["analysis.h", "device.cuh", "kernels.cuh", "batch_common.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

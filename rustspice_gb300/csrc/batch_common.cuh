@@ -35,6 +35,12 @@ __device__ __forceinline__ double contrib(const double* dv, int code) {
   }
 }
 
+// x with its sign bit flipped where m has it (m: 0 or the sign bit); on the
+// integer pipe.
+__device__ __forceinline__ double flip_sign(double x, unsigned long long m) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)m);
+}
+
 // Device value record: R [g]; V [value]; I [value]; D [g, ieq];
 // M [gds, gm, ieq]; MC [ddd, dds, ddg, ieq]; C (transient) [g, ieq].
 // Circuit constants per device: R [1/R]; V, I [value]; D [Is, vt, Is/vt];
@@ -105,46 +111,44 @@ __device__ __forceinline__ void eval_record(int type, const int* nd, const doubl
       break;
     }
     case 6: {  // consistent level 1, Shichman-Hodges form
+      // One formula for the three regions, with the region tests, signs,
+      // absolute values and maxima on the integer pipe (on this part an FP64
+      // warp instruction costs the SM sub-partition's FP64 unit 64 cycles,
+      // and lanes of a warp evaluate devices in different regions): with
+      // vde = 0 (cutoff), vds_eff (linear) or vgs_eff - vth (saturation),
+      //   q = vde (vov - vde / 2), ids = beff q (1 + lambda vds_eff),
+      //   gm = beff (1 + lambda vds_eff) vde,
+      //   gds = max(beff (1 + lambda vds_eff) (vov - vde) + lambda beff q, gdev),
+      // which are the Shichman-Hodges current and its partials in each
+      // region (in cutoff gds comes out as the floor gdev).
+      const unsigned long long sg = 0x8000000000000000ull;
       const double lambda = 0.02;
-      const double pol = dp[0];
       const double vd = xg(nd[0]), vg = xg(nd[1]), vs = xg(nd[2]);
-      const double vgs = pol * (vg - vs), vds = pol * (vd - vs);
-      const bool rev = vds < 0.0;
-      const double vgse = rev ? vgs - vds : vgs, vdse = rev ? -vds : vds;
+      const unsigned long long fm = (unsigned long long)__double_as_longlong(dp[0]) & sg;
+      const double vgs = flip_sign(vg - vs, fm), vds = flip_sign(vd - vs, fm);
+      const unsigned long long bds = (unsigned long long)__double_as_longlong(vds);
+      const bool rev = (bds & sg) != 0 && (bds << 1) != 0;  // vds < 0
+      const double vgse = vgs - (rev ? vds : 0.0);
+      const long long bdse = (long long)(bds & ~sg);
+      const double vdse = __longlong_as_double(bdse);
       const double vth = dp[1], beff = dp[2];
-      double ids, gm, gds;
-      if (vgse <= vth) {
-        ids = 0.0;
-        gm = 0.0;
-        gds = gdev;
-      } else if (vdse < vgse - vth) {  // Shichman-Hodges: (1 + lambda vds) here too
-        const double k = 1.0 + lambda * vdse;
-        const double q = (vgse - vth) * vdse - 0.5 * vdse * vdse;
-        ids = beff * q * k;
-        gm = beff * vdse * k;
-        gds = fmax(beff * ((vgse - vth) - vdse) * k + lambda * beff * q, gdev);
-      } else {
-        const double t = vgse - vth;
-        ids = 0.5 * beff * (t * t) * (1.0 + lambda * vdse);
-        gm = beff * (vgse - vth) * (1.0 + lambda * vdse);
-        gds = fmax(0.5 * beff * (t * t) * lambda, gdev);
-      }
-      double id, ddg, ddd, dds;
-      if (!rev) {
-        id = pol * ids;
-        ddg = gm;
-        ddd = gds;
-        dds = -(gm + gds);
-      } else {
-        id = -pol * ids;
-        ddg = -gm;
-        ddd = gm + gds;
-        dds = -gds;
-      }
-      rec[0] = ddd;
-      rec[1] = dds;
-      rec[2] = ddg;
-      rec[3] = id - (ddg * vg + ddd * vd + dds * vs);
+      const double vov = vgse - vth;
+      const long long bov = __double_as_longlong(vov);
+      // non-negative doubles order as their bit patterns
+      const double vde = bov <= 0 ? 0.0 : (bdse < bov ? vdse : vov);
+      const double k = fma(lambda, vdse, 1.0);
+      const double q = vde * fma(-0.5, vde, vov);
+      const double bq = beff * q, bk = beff * k;
+      const double ids = bq * k, gm = bk * vde;
+      const double g0 = fma(lambda, bq, bk * (vov - vde));
+      const long long b0 = __double_as_longlong(g0);
+      const double gds = (b0 < 0 || b0 < __double_as_longlong(gdev)) ? gdev : g0;
+      const unsigned long long rm = rev ? sg : 0ull;
+      const double sum = gm + gds;
+      rec[0] = rev ? sum : gds;                  // ddd
+      rec[1] = flip_sign(rev ? gds : sum, sg);   // dds
+      rec[2] = flip_sign(gm, rm);                // ddg
+      rec[3] = flip_sign(ids, fm ^ rm) - fma(rec[2], vg, fma(rec[0], vd, rec[1] * vs));
       break;
     }
     default:
@@ -205,19 +209,36 @@ struct Prog {
   const int *dev_type, *dev_nodes, *dev_dv, *amap_ptr, *amap_code, *rmap_ptr, *rmap_code,
       *in_row, *out_pos, *offd_ptr, *offd_col, *bptr, *heavy;
   const int *lvl_col, *lseg_ptr, *lseg;  // level schedule of the factorization
-  int n, nc, nv, nslots, ndev, nblocks, nheavy;
+  const int2* ops;                       // staged step program (or null)
+  const int* sp;                         //   and its step pointers
+  int n, nc, nv, nslots, ndev, nblocks, nheavy, nsteps;
 };
 
 // Stages the group's factor and solve structure into shared memory and
 // returns the program view: by one warp (tid = lane, nthr = 32) or by the
-// whole block (block = true; every thread of the block calls it).
+// whole block (block = true; every thread of the block calls it). steps:
+// a group with a step program stages that instead of the column records.
 __device__ __forceinline__ Prog stage_program(const BatchArgs& A, const GroupHdr& G, int* prog,
-                                              int lane, int nthr = 32, bool block = false) {
+                                              int lane, int nthr = 32, bool block = false,
+                                              bool steps = false) {
   Prog P;
   const int n = G.n;
   int4* const colrec = reinterpret_cast<int4*>(prog);
   int* const srow = prog + 4 * n;
-  {
+  P.ops = nullptr;
+  P.sp = nullptr;
+  P.nsteps = 0;
+  if (steps && G.nsteps > 0) {
+    int2* const ops = reinterpret_cast<int2*>(prog);
+    int* const sp = prog + 2 * G.nops;
+    const int2* gops = A.ops + G.ops_off;
+    const int* gsp = A.step_ptr + G.step_off;
+    for (int q = lane; q < G.nops; q += nthr) ops[q] = gops[q];
+    for (int q = lane; q <= G.nsteps; q += nthr) sp[q] = gsp[q];
+    P.ops = ops;
+    P.sp = sp;
+    P.nsteps = G.nsteps;
+  } else {
     const int* cp = A.col_ptr + G.col_off;
     const int* dsl = A.dslot + G.col_off;
     const int* cs = A.col_single + G.col_off;
@@ -237,10 +258,11 @@ __device__ __forceinline__ Prog stage_program(const BatchArgs& A, const GroupHdr
     __syncthreads();
   else
     __syncwarp();
-  P.colrec = colrec;
-  P.srow = srow;
-  P.uptr = G.nseg > 0 ? srow + G.nslots : A.upd_ptr + G.slot_off;
-  P.udst = G.nseg > 0 ? srow + 2 * G.nslots : A.upd_dst + G.upd_off;
+  const bool cols = P.nsteps == 0;
+  P.colrec = cols ? colrec : nullptr;
+  P.srow = cols ? srow : nullptr;
+  P.uptr = cols && G.nseg > 0 ? srow + G.nslots : A.upd_ptr + G.slot_off;
+  P.udst = cols && G.nseg > 0 ? srow + 2 * G.nslots : A.upd_dst + G.upd_off;
   P.map = nullptr;
   P.dev_type = A.dev_type + G.dev_off;
   P.dev_nodes = A.dev_nodes + 4 * G.dev_off;
@@ -299,16 +321,17 @@ __device__ __forceinline__ void assemble(const Prog& P, const double* DV, double
   for (int v = sl; v < P.nv; v += LPI) {
     const int t0 = P.amap_ptr[v], t1 = P.amap_ptr[v + 1];
     if (t1 - t0 > kHeavy) continue;
-    double acc = 0.0;
-    for (int t = t0; t < t1; ++t) acc += contrib(DV, P.amap_code[t]);
+    // from the first contribution (0.0 + a is a, but for the sign of a zero)
+    double acc = t0 < t1 ? contrib(DV, P.amap_code[t0]) : 0.0;
+    for (int t = t0 + 1; t < t1; ++t) acc += contrib(DV, P.amap_code[t]);
     V[v] = acc;
   }
   for (int i = sl; i < P.n; i += LPI) {
     const int r = P.in_row[i];
     const int t0 = P.rmap_ptr[r], t1 = P.rmap_ptr[r + 1];
     if (t1 - t0 > kHeavy) continue;
-    double acc = 0.0;
-    for (int t = t0; t < t1; ++t) acc += contrib(DV, P.rmap_code[t]);
+    double acc = t0 < t1 ? contrib(DV, P.rmap_code[t0]) : 0.0;
+    for (int t = t0 + 1; t < t1; ++t) acc += contrib(DV, P.rmap_code[t]);
     T[i] = acc;
   }
   for (int h = 0; h < P.nheavy; ++h) {
@@ -491,6 +514,54 @@ __device__ __forceinline__ void factor_solve(const Prog& P, double* V, double* T
       if (sl == 0) T[k] = xk;
       __syncwarp();
     }
+  }
+}
+
+// One operation of a step program on an instance region R (X, T, V):
+// kind 0 R[d] -= R[a] * R[b] (one fma), 4 the same unless R[b] is zero (a
+// factor update by a zero U entry is skipped), 2 R[d] = R[a] * R[b], 1
+// R[d] = 1 / perturbed R[d] (a: the column is a singleton), 3 nothing.
+__device__ __forceinline__ void exec_op(int2 o, double* R) {
+  const int d = o.x & 0xffff, a = (int)((unsigned)o.x >> 16), b = o.y & 0xffff, k = o.y >> 16;
+  if (k == 1) {
+    R[d] = fast_rcp(perturb_bits(R[d], a != 0));
+    return;
+  }
+  if (k == 3) return;
+  const double va = R[a], vb = R[b];
+  if (k == 2) {
+    R[d] = va * vb;
+    return;
+  }
+  if (k == 4 && !nonzero(vb)) return;
+  R[d] = fma(-va, vb, R[d]);
+}
+
+// The factorization, forward and backward substitution as the group's step
+// program: the host lists every operation of factor_solve_columns in its
+// order and places each in the first step after the steps that write its
+// operands or read its destination, so the operations of one step are
+// independent and every value sees the same operations in the same order
+// as in the column-by-column path (the same results). The instance's lanes
+// take a step's operations in parallel; the next step's first operation is
+// loaded while the current one runs. The warp's instances run the same
+// program in step.
+template <int LPI>
+__device__ __forceinline__ void run_steps(const Prog& P, double* R, int sl) {
+  const int2 nop = make_int2(0, 3 << 16);
+  const int2* const ops = P.ops;
+  const int* const sp = P.sp;
+  int p0 = sp[0], p1 = sp[1];
+  int2 op = p0 + sl < p1 ? ops[p0 + sl] : nop;
+  for (int t = 0; t < P.nsteps; ++t) {
+    const int q0 = p1, q1 = t + 2 <= P.nsteps ? sp[t + 2] : p1;
+    const int2 next = q0 + sl < q1 ? ops[q0 + sl] : nop;
+    exec_op(op, R);
+    for (int p = p0 + sl + LPI; p < p1; p += LPI) exec_op(ops[p], R);
+    __syncwarp();
+    p0 = q0;
+    p1 = q1;
+    op = next;
   }
 }
 

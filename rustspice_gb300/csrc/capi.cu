@@ -1596,7 +1596,7 @@ struct gpuklu_batch {
   DBuf<i32> d_order, d_dev_type, d_dev_nodes, d_dev_dv, d_amap_ptr, d_amap_code,
       d_rmap_ptr, d_rmap_code, d_col_ptr, d_dslot, d_col_single, d_in_row, d_out_pos,
       d_offd_ptr, d_slot_row, d_upd_ptr, d_upd_dst, d_offd_col, d_block_ptr, d_heavy, d_ov_dev,
-      d_lvl_col, d_lseg_ptr, d_lseg, d_amap4, d_rmap4, d_lng,
+      d_lvl_col, d_lseg_ptr, d_lseg, d_amap4, d_rmap4, d_lng, d_ops, d_step_ptr,
       d_iters,
       d_iters_total, d_reason, d_status;
   DBuf<double> d_dparams, d_ov_val, d_x0, d_xout;
@@ -1646,6 +1646,13 @@ struct gpuklu_batch {
   DBuf<i32> d_ltiles, d_cont_list, d_cont_it, d_cont_total, d_cont_gstep;
   DBuf<unsigned> d_lcounter, d_cont_count, d_gnext2;
   DBuf<double> d_scratch, d_cont_damp, d_cont_prev;
+  // continuation kernel: one warp per parked instance from a queue over the
+  // groups (cont.cu); off: the warp classes continue them
+  bool cont_kernel = false;
+  int cont_grid = 0, cont_wpb = 0;
+  DBuf<i32> d_cont_groups;
+  DBuf<unsigned> d_cont_cursor;
+  DBuf<double> d_dv;
   // transient
   int transient = 0;
   double dt = 0.0;
@@ -1691,6 +1698,8 @@ struct Program {
   std::vector<i32> dev_type, dev_nodes, dev_dv, amap_ptr, amap_code, rmap_ptr, rmap_code,
       col_ptr, dslot, col_single, in_row, out_pos, offd_ptr, slot_row, upd_ptr, upd_dst,
       offd_col, block_ptr, heavy, lvl_col, lseg_ptr, lseg, amap4, rmap4, lng;
+  std::vector<i32> ops;       // step program: two ints per operation
+  std::vector<i32> step_ptr;  // nsteps + 1 (empty: no step program)
   int64_t flops = 0, bytes = 0;
   std::string key() const {
     std::string k;
@@ -1759,6 +1768,84 @@ void device_codes(int type, int dv, bool transient, int m[8], int r[2]) {
       break;
     default:
       break;
+  }
+}
+
+// The step program of the batched factorization and substitutions (see
+// bt::run_steps): every operation of the column-by-column path in its order
+// - per BTF block the coupling into the block's rows, per column its U
+// entries' updates, the pivot's reciprocal, the L scaling and the forward
+// update of the right-hand side, then the backward sweep - as offsets into
+// an instance's region (X[nc], T[n], ndv unused doubles, V; the batch kernels
+// keep their device records after V, so ndv is 0 there). Each operation goes
+// to the first step
+// after the last step that writes one of its operands or its destination
+// and after the last step that reads its destination, so a step's
+// operations are independent and each value sees its operations in the
+// original order. Regions beyond 16-bit offsets get no step program.
+void build_steps(const gk::Plan& P, int nc, int ndv, std::vector<i32>& out_ops,
+                 std::vector<i32>& out_steps) {
+  out_ops.clear();
+  out_steps.clear();
+  const int n = P.n, nslots = P.nslots();
+  const long long vbase = (long long)nc + n + ndv;
+  const long long top = vbase + nslots + (long long)P.offd_raw.size();
+  if (top >= 65536 || n == 0) return;
+  struct Op {
+    int d, a, b, k;
+  };
+  std::vector<Op> ops;
+  auto T_ = [nc](int i) { return nc + i; };
+  auto V_ = [vbase](long long v) { return (int)(vbase + v); };
+  for (int b = 0; b < P.nblocks; ++b) {
+    const int b0 = P.block_ptr[b], b1 = P.block_ptr[b + 1];
+    for (int i = b0; i < b1; ++i)
+      for (int e = P.offd_ptr[i]; e < P.offd_ptr[i + 1]; ++e)
+        ops.push_back({T_(i), V_(nslots + e), T_(P.offd_col[e]), 0});
+    for (int k = b0; k < b1; ++k) {
+      const int s0 = P.col_ptr[k], ds = P.dslot[k], s1 = P.col_ptr[k + 1];
+      for (int s = s0; s < ds; ++s) {
+        const int j = P.slot_row[s];
+        const int q0 = P.dslot[j] + 1, q1 = P.col_ptr[j + 1];
+        for (int qq = q0; qq < q1; ++qq)
+          ops.push_back({V_(P.upd_dst[P.upd_ptr[s] - q0 + qq]), V_(qq), V_(s), 4});
+      }
+      ops.push_back({V_(ds), P.col_single[k] ? 1 : 0, V_(ds), 1});
+      for (int qq = ds + 1; qq < s1; ++qq) ops.push_back({V_(qq), V_(qq), V_(ds), 2});
+      for (int qq = ds + 1; qq < s1; ++qq)
+        ops.push_back({T_(P.slot_row[qq]), V_(qq), T_(k), 0});
+    }
+    for (int k = b1 - 1; k >= b0; --k) {
+      const int s0 = P.col_ptr[k], ds = P.dslot[k];
+      ops.push_back({T_(k), T_(k), V_(ds), 2});
+      for (int s = s0; s < ds; ++s) ops.push_back({T_(P.slot_row[s]), V_(s), T_(k), 0});
+    }
+  }
+  std::vector<int> lw((size_t)top, 0), lr((size_t)top, 0), step(ops.size());
+  int nsteps = 0;
+  for (size_t q = 0; q < ops.size(); ++q) {
+    const Op& o = ops[q];
+    int st = std::max(lw[o.d], lr[o.d]) + 1;
+    if (o.k != 1) st = std::max(st, std::max(lw[o.a], lw[o.b]) + 1);
+    step[q] = st;
+    lw[o.d] = st;
+    if (o.k != 1) {
+      lr[o.a] = std::max(lr[o.a], st);
+      lr[o.b] = std::max(lr[o.b], st);
+    }
+    nsteps = std::max(nsteps, st);
+  }
+  std::vector<i32> cnt(nsteps + 2, 0);
+  for (int st : step) ++cnt[st];
+  out_steps.assign(nsteps + 1, 0);
+  for (int t = 0; t < nsteps; ++t) out_steps[t + 1] = out_steps[t] + cnt[t + 1];
+  std::vector<i32> pos(out_steps.begin(), out_steps.end() - 1);
+  out_ops.assign(2 * ops.size(), 0);
+  for (size_t q = 0; q < ops.size(); ++q) {  // program order within a step
+    const Op& o = ops[q];
+    const int at = pos[step[q] - 1]++;
+    out_ops[2 * at] = (i32)((unsigned)o.d | ((unsigned)o.a << 16));
+    out_ops[2 * at + 1] = (i32)((unsigned)o.b | ((unsigned)o.k << 16));
   }
 }
 
@@ -1905,6 +1992,8 @@ Program make_program(const gpuklu_circuit& C, const gk::Plan& P) {
       std::fill(g.lseg_ptr.begin(), g.lseg_ptr.end(), 0);
     }
   }
+  const char* esp = getenv("GPUKLU_STEP_PROGRAM");
+  if (!C.transient && !(esp && esp[0] == '0')) build_steps(P, C.node_count, 0, g.ops, g.step_ptr);
   // FP64 operations of one Newton iteration: device evaluation, assembly
   // additions, refactorization, both substitutions, block coupling, update
   const int64_t nl = P.nnz_l, nu = P.nnz_u - P.n;
@@ -2056,7 +2145,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   const int ng = (int)progs.size();
   std::vector<i32> dev_type, dev_nodes, dev_dv, amap_ptr, amap_code, rmap_ptr, rmap_code,
       col_ptr, dslot, col_single, in_row, out_pos, offd_ptr, slot_row, upd_ptr, upd_dst,
-      offd_col, block_ptr, heavy, lvl_col, lseg_ptr, lseg, amap4, rmap4, lng;
+      offd_col, block_ptr, heavy, lvl_col, lseg_ptr, lseg, amap4, rmap4, lng, ops, step_ptr;
   auto cat = [](std::vector<i32>& dst, const std::vector<i32>& src) {
     dst.insert(dst.end(), src.begin(), src.end());
   };
@@ -2081,6 +2170,12 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     h.amap4_off = (int)amap4.size();
     h.rmap4_off = (int)rmap4.size();
     h.lng_off = (int)lng.size();
+    h.ops_off = (int)(ops.size() / 2);
+    h.nops = (int)(pr.ops.size() / 2);
+    h.step_off = (int)step_ptr.size();
+    h.nsteps = pr.step_ptr.empty() ? 0 : (int)pr.step_ptr.size() - 1;
+    cat(ops, pr.ops);
+    cat(step_ptr, pr.step_ptr);
     cat(dev_type, pr.dev_type);
     cat(dev_nodes, pr.dev_nodes);
     cat(dev_dv, pr.dev_dv);
@@ -2166,7 +2261,8 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     gk::GroupHdr& h = B->groups[g];
     h.region = gregion[g];
     // column records, slot rows (and the update lists for leveled programs)
-    h.prog = (4 * h.n + h.nslots + (h.nseg > 0 ? h.nslots + h.nupd : 0) + 3) & ~3;
+    h.prog = h.nsteps > 0 ? (2 * h.nops + h.nsteps + 1 + 3) & ~3
+                          : (4 * h.n + h.nslots + (h.nseg > 0 ? h.nslots + h.nupd : 0) + 3) & ~3;
   }
   for (int ci = 0; ci < 4; ++ci) {
     auto C = std::make_unique<gpuklu_batch::Class>();
@@ -2266,7 +2362,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   UP(d_offd_ptr, offd_ptr) UP(d_slot_row, slot_row) UP(d_upd_ptr, upd_ptr)
   UP(d_upd_dst, upd_dst) UP(d_offd_col, offd_col) UP(d_block_ptr, block_ptr)
   UP(d_heavy, heavy) UP(d_lvl_col, lvl_col) UP(d_lseg_ptr, lseg_ptr) UP(d_lseg, lseg)
-  UP(d_amap4, amap4) UP(d_rmap4, rmap4) UP(d_lng, lng)
+  UP(d_amap4, amap4) UP(d_rmap4, rmap4) UP(d_lng, lng) UP(d_ops, ops) UP(d_step_ptr, step_ptr)
   UP(d_dparams, dparams) UP(d_p_off, poff) UP(d_ov_dev, ov_dev) UP(d_ov_val, ov_val)
   UP(d_x0_off, x0o) UP(d_x_off, B->x_off)
 #undef UP
@@ -2312,6 +2408,37 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       if (e == cudaSuccess) e = B->d_cont_count.resize(std::max(ngr, 1));
       if (e == cudaSuccess) e = B->d_gnext2.resize(std::max(ngr, 1));
       B->args.warp_stride = stride;
+      // continuation kernel: a warp's shared slice holds X, T and the LU
+      // values of the largest program, its global slice the device records;
+      // as many warps per block as the slices fit (at most 16)
+      const char* eck = getenv("GPUKLU_CONT_KERNEL");
+      int slice = 0, dvs = 0;
+      bool steps_all = true;
+      for (int g : gorder) {
+        const gk::GroupHdr& h = B->groups[g];
+        slice = std::max(slice, h.node_count + h.n + h.nslots + h.noffd);
+        dvs = std::max(dvs, h.ndv);
+        if (h.inst_count > 0 && h.nsteps == 0) steps_all = false;
+      }
+      slice = (slice + 1) & ~1;
+      dvs = (dvs + 3) & ~3;
+      const int wpb = std::min(16, (int)((size_t)(227 * 1024) / ((size_t)slice * 8)));
+      if (!(eck && eck[0] == '0') && steps_all && wpb >= 1) {
+        int r3 = 0, b3 = 0;
+        gk::cont_kernel_info(wpb, slice, &r3, &b3);
+        if (b3 > 0) {
+          B->cont_kernel = true;
+          B->cont_wpb = wpb;
+          B->cont_grid = sm_count() * b3;
+          B->args.slice = slice;
+          B->args.dv_stride = dvs;
+          std::vector<i32> cg(gorder.begin(), gorder.end());
+          if (e == cudaSuccess) e = B->d_cont_groups.upload(cg, s);
+          if (e == cudaSuccess) e = B->d_cont_cursor.resize(1);
+          if (e == cudaSuccess)
+            e = B->d_dv.resize((size_t)B->cont_grid * wpb * (size_t)dvs);
+        }
+      }
     } else {
       B->lanes = false;
     }
@@ -2363,6 +2490,8 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
   a.amap4 = B->d_amap4.p;
   a.rmap4 = B->d_rmap4.p;
   a.lng = B->d_lng.p;
+  a.ops = reinterpret_cast<const int2*>(B->d_ops.p);
+  a.step_ptr = B->d_step_ptr.p;
   a.inst_p_off = B->d_p_off.p;
   a.dparams = B->d_dparams.p;
   a.inst_ov_dev = B->d_ov_dev.p;
@@ -2390,6 +2519,14 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
     a.cont_gstep = B->d_cont_gstep.p;
     a.cont_damp = B->d_cont_damp.p;
     a.cont_prev = B->d_cont_prev.p;
+    if (B->cont_kernel) {
+      a.cont_groups = B->d_cont_groups.p;
+      a.cont_ngroups = (int)B->d_cont_groups.n;
+      a.cont_cursor = B->d_cont_cursor.p;
+      a.dv_scratch = B->d_dv.p;
+      a.dv_stride = B->args.dv_stride;
+      a.slice = B->args.slice;
+    }
   }
   B->args = a;
   for (auto& C : B->classes) {
@@ -2828,6 +2965,16 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
     gk::launch_batch_lanes(la, b->lane_grid, b->lane_wpb, s);
   }
   cudaEventRecord(b->ph_ev[1], s);
+  if (b->lanes && b->cont_kernel) {  // phase 2: one warp per parked instance
+    cudaMemsetAsync(b->d_cont_cursor.p, 0, sizeof(unsigned), s);
+    gk::BatchArgs ca = b->args;
+    ca.cfg = c;
+    gk::launch_batch_cont(ca, b->cont_grid, b->cont_wpb, s);
+    cudaEventRecord(b->ph_ev[2], s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return b->fail(cuda_msg(e, "batch launch"));
+    return GPUKLU_OK;
+  }
   cudaEventRecord(b->start_ev, s);
   for (auto& C : b->classes) {  // largest programs first, all classes concurrent
     cudaStreamWaitEvent(C->stream, b->start_ev, 0);
@@ -3002,7 +3149,7 @@ int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out) {
   if (!b) return GPUKLU_INVALID_MATRIX;
   for (int q = 0; q < 8; ++q) out[q] = 0;
   out[2] = (int64_t)b->groups.size();
-  out[6] = (int64_t)b->classes.size() + (b->lanes ? 1 : 0);
+  out[6] = b->lanes && b->cont_kernel ? 2 : (int64_t)b->classes.size() + (b->lanes ? 1 : 0);
   for (auto& C : b->classes) {  // the largest class (first) describes the launch
     out[0] += C->grid;
     if (out[1] == 0) {
@@ -3694,6 +3841,16 @@ int gpuklu_btf_info(int64_t n, const int64_t* ap, const int64_t* ai, int64_t* ou
   out[0] = b.nblocks;
   out[1] = b.max_block;
   return GPUKLU_OK;
+}
+
+int64_t gpuklu_plan_steps(const gpuklu_plan* p, int32_t nc, int32_t ndv, int32_t* ops,
+                          int64_t ops_cap, int32_t* step_ptr, int64_t steps_cap) {
+  if (!p || nc < 0 || ndv < 0) return -1;
+  std::vector<i32> o, sp;
+  build_steps(p->p, nc, ndv, o, sp);
+  if (ops && (int64_t)o.size() <= ops_cap) std::copy(o.begin(), o.end(), ops);
+  if (step_ptr && (int64_t)sp.size() <= steps_cap) std::copy(sp.begin(), sp.end(), step_ptr);
+  return (int64_t)(o.size() / 2) * ((int64_t)1 << 32) + (int64_t)sp.size();
 }
 
 gpuklu_plan* gpuklu_plan_build(int64_t n, const int64_t* ap, const int64_t* ai, int pivot_mode,

@@ -1361,14 +1361,16 @@ __global__ void k_batch_newton(BatchArgs A) {
         SHARED ? min((int)(blockDim.x >> 5), (A.shared_bytes - pg * 4) / (rg * 8 * M)) : 1;
     double* const region = reinterpret_cast<double*>(slice + (size_t)pg * 4) +
                            (size_t)((SHARED ? warp * M : 0) + sub) * rg;
-    bt::Prog P = SHARED ? bt::stage_program(A, G, prog, threadIdx.x, blockDim.x, true)
-                        : bt::stage_program(A, G, prog, lane);
+    bt::Prog P = SHARED ? bt::stage_program(A, G, prog, threadIdx.x, blockDim.x, true, true)
+                        : bt::stage_program(A, G, prog, lane, 32, false, true);
     const int n = P.n, nc = P.nc;
+    // region: X[nc] T[n] V[nslots + noffd] DV[ndv], then the row -> slot map
+    // (the step program addresses X, T and V from the region's start)
     double* const X = region;
     double* const T = X + nc;
-    double* const DV = T + n;
-    double* const V = DV + G.ndv;
-    P.map = reinterpret_cast<int*>(V + G.nslots + G.noffd);
+    double* const V = T + n;
+    double* const DV = V + G.nslots + G.noffd;
+    P.map = reinterpret_cast<int*>(DV + G.ndv);
 
     int inst = -1, it = 0, total = 0, gstep = 0, ov_dev = -1;
     bool exhausted = warp >= active;  // no room for this warp's instances in this group
@@ -1423,7 +1425,10 @@ __global__ void k_batch_newton(BatchArgs A) {
       __syncwarp();
       bt::assemble<LPI>(P, DV, V, T, sl);
       __syncwarp();
-      bt::factor_solve<LPI>(P, V, T, sl);
+      if (P.nsteps > 0)
+        bt::run_steps<LPI>(P, X, sl);
+      else
+        bt::factor_solve<LPI>(P, V, T, sl);
       // ---- Newton update (crates/sim-core/src/newton.rs:93-107)
       bool conv = true, fin = true;
       for (int c = sl; c < nc; c += LPI) {

@@ -83,6 +83,10 @@ struct GroupHdr {
                    //   the columns in schedule order sit at col_off in lvl_col
   int region;      // shared-memory doubles of one instance of this program
   int prog;        // ints of the staged program (a multiple of 4)
+  // step program of the factorization and both substitutions (DC batches;
+  // nsteps 0: none): nops operations at ops_off, nsteps + 1 step pointers
+  // at step_off; the operations of one step are independent of each other
+  int ops_off, nops, step_off, nsteps;
 };
 
 // Contribution codes of the batched stamp: (index << 3) | kind with kind
@@ -106,6 +110,8 @@ struct BatchArgs {
   const int* heavy;  // (value index << 1) or (position << 1 | 1), per group
   const int *lvl_col, *lseg_ptr, *lseg;  // level-scheduled factor (see GroupHdr)
   const int *amap4, *rmap4, *lng;        // padded contribution codes (see GroupHdr)
+  const int2* ops;                       // step programs (see GroupHdr)
+  const int* step_ptr;
   const long long* inst_p_off;  // offset of the instance's circuit constants (4 per device)
   const double* dparams;
   const int* inst_ov_dev;
@@ -147,6 +153,13 @@ struct BatchArgs {
   unsigned* gnext2;            // per group: next entry of cont_list to hand out
   int *cont_it, *cont_total, *cont_gstep;
   double *cont_damp, *cont_prev;  // the iterate itself waits in x_out
+  // continuation kernel (cont.cu): one warp per parked instance, any group
+  const int* cont_groups;      // the groups, most expensive first
+  int cont_ngroups;
+  unsigned* cont_cursor;       // first entry of cont_groups that may have parked instances
+  double* dv_scratch;          // per warp: device records, dv_stride doubles
+  long long dv_stride;
+  int slice;                   // shared doubles per warp: X, T and the LU values
 };
 
 // Batched adaptive transient (atran.cu): per instance its time-dependent
@@ -263,6 +276,8 @@ void launch_batch_newton(const BatchArgs& a, int m, int grid, int warps_per_bloc
                          cudaStream_t s, bool shared = false);
 // Registers per thread and resident blocks per SM of the batched kernel.
 // Lane-per-instance batched Newton (phase 1 of gpuklu_batch_run).
+void launch_batch_cont(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
+void cont_kernel_info(int warps_per_block, int slice, int* regs, int* blocks_per_sm);
 void launch_batch_lanes(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
 void lanes_kernel_info(int warps_per_block, int* regs, int* blocks_per_sm);
 

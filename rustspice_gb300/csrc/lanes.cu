@@ -25,6 +25,7 @@ namespace gk {
 namespace {
 
 constexpr unsigned kAllLanes = 0xffffffffu;
+constexpr int kPad = 4;  // the +0.0 contribution code that pads the four-code lists
 
 __global__ void k_batch_lanes(BatchArgs A) {
   const int lane = threadIdx.x & 31;
@@ -118,21 +119,39 @@ __global__ void k_batch_lanes(BatchArgs A) {
         const int nrec = bt::record_len(type, false);
         for (int q = 0; q < nrec; ++q) AT(DV, o + q) = rec[q];
       }
-      // ---- assembly, in stamping order per slot and per row: four padded
-      // codes each (the loads of a slot issue together), longer lists after
+      // ---- assembly, in stamping order per slot and per row: up to four
+      // codes each (the loads of a slot issue together), padded with +0.0
+      // codes that are not added (the branches are the warp's: one program),
+      // longer lists after
 #pragma unroll 2
       for (int v = 0; v < nv; ++v) {
         const int4 c4 = *reinterpret_cast<const int4*>(amap4 + 4 * v);
         const double a0 = bt::contrib<32>(DV, c4.x), a1 = bt::contrib<32>(DV, c4.y);
         const double a2 = bt::contrib<32>(DV, c4.z), a3 = bt::contrib<32>(DV, c4.w);
-        AT(V, v) = (((0.0 + a0) + a1) + a2) + a3;
+        double acc = a0;
+        if (c4.y != kPad) {
+          acc += a1;
+          if (c4.z != kPad) {
+            acc += a2;
+            if (c4.w != kPad) acc += a3;
+          }
+        }
+        AT(V, v) = acc;
       }
 #pragma unroll 2
       for (int i = 0; i < n; ++i) {
         const int4 c4 = *reinterpret_cast<const int4*>(rmap4 + 4 * i);
         const double a0 = bt::contrib<32>(DV, c4.x), a1 = bt::contrib<32>(DV, c4.y);
         const double a2 = bt::contrib<32>(DV, c4.z), a3 = bt::contrib<32>(DV, c4.w);
-        AT(T, i) = (((0.0 + a0) + a1) + a2) + a3;
+        double acc = a0;
+        if (c4.y != kPad) {
+          acc += a1;
+          if (c4.z != kPad) {
+            acc += a2;
+            if (c4.w != kPad) acc += a3;
+          }
+        }
+        AT(T, i) = acc;
       }
       for (int h = 0; h < G.nlng; ++h) {
         const int code = lng[h];

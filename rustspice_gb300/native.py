@@ -38,7 +38,7 @@ SYMBOLS = [
     "gpuklu_batch_update_inputs", "gpuklu_batch_last_error", "gpuklu_batch_info",
     "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_batch_phase_ms", "gpuklu_batch_set_schedule", "gpuklu_batch_autotune", "gpuklu_ac_sweep", "gpuklu_tran_create", "gpuklu_tran_forward", "gpuklu_atran_create", "gpuklu_atran_run",
     "gpuklu_tran_backward", "gpuklu_bbd_create", "gpuklu_bbd_destroy", "gpuklu_bbd_last_error",
-    "gpuklu_bbd_info", "gpuklu_bbd_perm", "gpuklu_bbd_factor", "gpuklu_bbd_solve", "gpuklu_bbd_newton_dc", "gpuklu_fp64_peak_tflops", "gpuklu_fp64_mma_peak_tflops", "gpuklu_dense_lu_nopivot", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free", "gpuklu_btf_info",
+    "gpuklu_bbd_info", "gpuklu_bbd_perm", "gpuklu_bbd_factor", "gpuklu_bbd_solve", "gpuklu_bbd_newton_dc", "gpuklu_fp64_peak_tflops", "gpuklu_fp64_mma_peak_tflops", "gpuklu_dense_lu_nopivot", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free", "gpuklu_plan_steps", "gpuklu_btf_info",
 ]
 
 
@@ -141,6 +141,7 @@ def lib(build_if_missing: bool = True):
         "gpuklu_plan_build": (_P, [_I64, _P, _P, C.c_int, C.c_int, _P]),
         "gpuklu_plan_array": (_I64, [_P, C.c_char_p, _P, _I64]),
         "gpuklu_plan_free": (None, [_P]),
+        "gpuklu_plan_steps": (_I64, [_P, C.c_int32, C.c_int32, _P, _I64, _P, _I64]),
         "gpuklu_btf_info": (C.c_int, [_I64, _P, _P, _P]),
     }
     for name, (res, args) in sig.items():
@@ -172,6 +173,31 @@ def newton_config(max_iters=100, abs_tol=1e-6, rel_tol=1e-3, gmin=1e-12, gmin_st
     """NewtonConfig from the engine's option names (engine.rs:987-999)."""
     return NewtonConfig(max_iters, abs_tol, rel_tol, gmin, gmin_steps, source_steps, damping,
                         damping_min)
+
+
+def step_program(n, ap, ai, nc, ndv, pivot_mode=PIVOT_REFERENCE, row_perm=None,
+                 kind="nativeklu"):
+    """The batched warp kernel's step program for a pattern's plan
+    (gpuklu_plan_steps): (ops[nops, 2] int32, step_ptr[nsteps + 1] int32),
+    or None when the region exceeds 16-bit offsets."""
+    L = lib()
+    ap, ai = i64(ap), i64(ai)
+    rp = i32(row_perm) if row_perm is not None else None
+    h = L.gpuklu_plan_build(n, ptr(ap), ptr(ai), pivot_mode, KINDS[kind],
+                            ptr(rp) if rp is not None else None)
+    if not h:
+        raise ValueError("plan build failed")
+    try:
+        r = L.gpuklu_plan_steps(h, nc, ndv, None, 0, None, 0)
+        nops, nsp = r >> 32, r & 0xffffffff
+        if nsp == 0:
+            return None
+        ops = np.zeros(2 * nops, np.int32)
+        sp = np.zeros(nsp, np.int32)
+        L.gpuklu_plan_steps(h, nc, ndv, ptr(ops), len(ops), ptr(sp), len(sp))
+        return ops.reshape(nops, 2), sp
+    finally:
+        L.gpuklu_plan_free(h)
 
 
 class Plan:

@@ -358,3 +358,86 @@ class EmulatedSolver:
 
     def solve(self, rhs):
         return solve(self.plan, self.ax, self.lu, np.asarray(rhs, np.float64))
+
+
+def batch_region(P: native.Plan, ax, rhs, nc, ndv):
+    """An instance region of the batched warp kernel (X[nc], T[n], DV[ndv],
+    V[nslots + noffd]) with the LU slots, the coupling values and the
+    permuted right-hand side assembled from a matrix and a right-hand side."""
+    n = P.n
+    tb, vb = nc, nc + n + ndv
+    R = np.zeros(vb + P.nslots + len(P.offd_raw))
+    for s in range(P.nslots):
+        v = 0.0
+        for t in range(P.amap_ptr[s], P.amap_ptr[s + 1]):
+            v += ax[P.amap_idx[t]]
+        R[vb + s] = v
+    for e in range(len(P.offd_raw)):
+        R[vb + P.nslots + e] = ax[P.offd_raw[e]]
+    R[tb + P.in_pos] = rhs
+    return R
+
+
+def factor_solve_columns(P: native.Plan, R, nc, ndv):
+    """The batched kernels' column-by-column factorization with the forward
+    substitution fused, then the backward substitution, block by block
+    (bt::factor_solve_columns), on a region; a fused multiply-add is
+    emulated as a product then a difference."""
+    n, ns = P.n, P.nslots
+    T = lambda i: nc + i  # noqa: E731
+    V = lambda v: nc + n + ndv + v  # noqa: E731
+    for b in range(P.nblocks):
+        b0, b1 = P.block_ptr[b], P.block_ptr[b + 1]
+        for i in range(b0, b1):
+            for e in range(P.offd_ptr[i], P.offd_ptr[i + 1]):
+                R[T(i)] = R[T(i)] - R[V(ns + e)] * R[T(P.offd_col[e])]
+        for k in range(b0, b1):
+            s0, ds, s1 = P.col_ptr[k], P.dslot[k], P.col_ptr[k + 1]
+            for s in range(s0, ds):
+                u = R[V(s)]
+                if u != 0.0:
+                    j = P.slot_row[s]
+                    q0 = P.dslot[j] + 1
+                    for qq in range(q0, P.col_ptr[j + 1]):
+                        d = P.upd_dst[P.upd_ptr[s] - q0 + qq]
+                        R[V(d)] = R[V(d)] - R[V(qq)] * u
+            r = 1.0 / _perturb(R[V(ds)], bool(P.col_single[k]))
+            zk = R[T(k)]
+            for qq in range(ds + 1, s1):
+                lv = R[V(qq)] * r
+                R[V(qq)] = lv
+                R[T(P.slot_row[qq])] = R[T(P.slot_row[qq])] - lv * zk
+            R[V(ds)] = r
+        for k in range(b1 - 1, b0 - 1, -1):
+            s0, ds = P.col_ptr[k], P.dslot[k]
+            xk = R[T(k)] * R[V(ds)]
+            for s in range(s0, ds):
+                R[T(P.slot_row[s])] = R[T(P.slot_row[s])] - R[V(s)] * xk
+            R[T(k)] = xk
+    return R
+
+
+def run_steps(ops, sp, R, order=None):
+    """A step program (native.step_program) on a region, the operations of
+    each step in the given order ("reverse", a numpy Generator for a
+    shuffle, or None for the listed order): the results do not depend on it
+    when the operations of a step are independent."""
+    for t in range(len(sp) - 1):
+        idx = list(range(sp[t], sp[t + 1]))
+        if order == "reverse":
+            idx.reverse()
+        elif order is not None:
+            order.shuffle(idx)
+        for p in idx:
+            x, y = int(ops[p, 0]) & 0xffffffff, int(ops[p, 1]) & 0xffffffff
+            d, a, b, k = x & 0xffff, x >> 16, y & 0xffff, y >> 16
+            if k == 1:
+                R[d] = 1.0 / _perturb(R[d], a != 0)
+            elif k == 2:
+                R[d] = R[a] * R[b]
+            elif k == 4:
+                if R[b] != 0.0:
+                    R[d] = R[d] - R[a] * R[b]
+            elif k == 0:
+                R[d] = R[d] - R[a] * R[b]
+    return R

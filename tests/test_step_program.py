@@ -1,0 +1,60 @@
+"""The batched warp kernel's step program (gpuklu_plan_steps) on the CPU:
+its operations, executed step by step with each step's operations in
+reverse or shuffled order, give bit for bit the factors and the solution of
+the column-by-column path they replace, on the exact-pivot plans of the
+circuits and matrices of the plan-parity tests; the solution also agrees
+with a dense solve."""
+import numpy as np
+import pytest
+
+from plan_emulator import EmulatedSolver, batch_region, factor_solve_columns, run_steps
+from rustspice_gb300 import circuits as cz
+from rustspice_gb300 import native as N
+from rustspice_gb300 import workloads as wl
+from test_plan_parity import SYSTEMS
+
+from oracle import pyoracle as po
+
+STEP_SYSTEMS = SYSTEMS + [("chain200", *po.mna(cz.inverter_chain(200, 0.6),
+                                               wl.chain_nodeset(200, 0.6))[1:])]
+
+
+@pytest.mark.parametrize("sysm", STEP_SYSTEMS, ids=[s[0] for s in STEP_SYSTEMS])
+def test_step_program_matches_the_column_path(sysm):
+    name, ap, ai, ax, rhs = sysm
+    n = len(ap) - 1
+    es = EmulatedSolver(N.PIVOT_EXACT)
+    es.factor(n, ap, ai, ax)
+    P = es.plan
+    from plan_emulator import first_factor
+    _, rperm = first_factor(N.Plan(n, ap, ai, N.PIVOT_EXACT), ax)
+    # any region layout X[nc] T[n] DV[ndv] V[...]; offsets past 32767 too
+    for nc, ndv in ((7, 13), (40000, 9)):
+        prog = N.step_program(n, ap, ai, nc, ndv, N.PIVOT_EXACT, rperm)
+        assert prog is not None
+        ops, sp = prog
+        assert sp[0] == 0 and sp[-1] == len(ops) and np.all(np.diff(sp) > 0)
+        kinds = (ops[:, 1].astype(np.int64) & 0xffffffff) >> 16
+        assert np.sum(kinds == 1) == n  # one reciprocal per column
+        base = batch_region(P, ax, rhs, nc, ndv)
+        want = factor_solve_columns(P, base.copy(), nc, ndv)
+        for order in (None, "reverse", np.random.default_rng(5)):
+            got = run_steps(ops, sp, base.copy(), order)
+            assert np.array_equal(got, want), (order, np.max(np.abs(got - want)))
+    x = want[nc + P.out_pos]
+    a = np.zeros((n, n))
+    for j in range(n):
+        for t in range(ap[j], ap[j + 1]):
+            a[ai[t], j] += ax[t]
+    ref = np.linalg.solve(a, rhs)
+    if name not in ("adder_dcop_01",):  # the reference's pivots leave it inaccurate
+        assert np.max(np.abs(x - ref)) <= 1e-6 * max(1.0, np.max(np.abs(ref)))
+    # fewer steps than operations: the schedule finds parallel work
+    assert len(sp) - 1 < len(ops)
+
+
+def test_step_program_absent_beyond_16_bit_offsets():
+    c = cz.inverter_chain(8, 0.3)
+    n, ap, ai, ax, rhs = po.mna(c, np.zeros(c.node_count))
+    assert N.step_program(n, ap, ai, 65500, 13) is None
+    assert N.step_program(n, ap, ai, 7, 13) is not None
