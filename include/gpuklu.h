@@ -505,14 +505,15 @@ gpuklu_plan* gpuklu_plan_build(int64_t n, const int64_t* ap, const int64_t* ai, 
                                int kind, const int32_t* row_perm);
 int64_t gpuklu_plan_array(const gpuklu_plan* p, const char* name, int64_t* out, int64_t cap);
 void gpuklu_plan_free(gpuklu_plan* p);
-/* The step program the batched warp kernel runs for this plan's
+/* The step program the batched warp kernels run for this plan's
  * factorization and substitutions, with the instance region's T at offset
- * nc and V at nc + n + ndv: two int32 per operation (d | a << 16, b | kind
- * << 16; kinds: 0 R[d] -= R[a] R[b], 4 the same unless R[b] == 0, 2 R[d] =
- * R[a] R[b], 1 R[d] = 1 / perturbed R[d] with a the singleton flag) in step
- * order, and the step pointers. Returns nops << 32 | (nsteps + 1) (0: no
- * program, the region exceeds 16-bit offsets); copies when the capacities
- * (in int32) suffice. */
+ * nc and V at nc + n + ndv: two int32 per operation (d | a << 15 | kind
+ * bits 0-1 << 30, b | c << 15 | kind bits 2-3 << 30; kinds: 0 R[d] -= R[a]
+ * R[b], 4 the same unless R[b] == 0, 2 R[d] = R[a] R[b], 1 R[d] = 1 /
+ * perturbed R[d] with a the singleton flag, 5 kind 4 then R[d] *= R[c], 6
+ * kind 0 then R[d] *= R[c]) in step order, and the step pointers. Returns
+ * nops << 32 | (nsteps + 1) (0: no program, the region exceeds 15-bit
+ * offsets); copies when the capacities (in int32) suffice. */
 int64_t gpuklu_plan_steps(const gpuklu_plan* p, int32_t nc, int32_t ndv, int32_t* ops,
                           int64_t ops_cap, int32_t* step_ptr, int64_t steps_cap);
 /* btf_decompose (crates/sim-core/src/btf.rs:143-550) on the host: out[0] the

@@ -209,6 +209,9 @@ struct Prog {
   const int *dev_type, *dev_nodes, *dev_dv, *amap_ptr, *amap_code, *rmap_ptr, *rmap_code,
       *in_row, *out_pos, *offd_ptr, *offd_col, *bptr, *heavy;
   const int *lvl_col, *lseg_ptr, *lseg;  // level schedule of the factorization
+  const int4 *amap4, *rmap4;             // four padded codes per slot / permuted row
+  const int* lng;                        // slots and rows with more: (index << 1) | is_row
+  int nlng;
   const int2* ops;                       // staged step program (or null)
   const int* sp;                         //   and its step pointers
   int n, nc, nv, nslots, ndev, nblocks, nheavy, nsteps;
@@ -280,6 +283,10 @@ __device__ __forceinline__ Prog stage_program(const BatchArgs& A, const GroupHdr
   P.lvl_col = A.lvl_col + G.col_off;
   P.lseg_ptr = A.lseg_ptr + G.blk_off;
   P.lseg = A.lseg + 3 * G.seg_off;
+  P.amap4 = reinterpret_cast<const int4*>(A.amap4 + G.amap4_off);
+  P.rmap4 = reinterpret_cast<const int4*>(A.rmap4 + G.rmap4_off);
+  P.lng = A.lng + G.lng_off;
+  P.nlng = G.nlng;
   P.n = n;
   P.nc = G.node_count;
   P.nslots = G.nslots;
@@ -297,6 +304,7 @@ __device__ __forceinline__ void stamp_devices(const Prog& P, const double* dpara
                                               double ov_val, const double* X, const double* XP,
                                               double gmin, double gdev, bool transient,
                                               double* DV, int sl) {
+#pragma unroll 2
   for (int d = sl; d < P.ndev; d += LPI) {
     double dp[4];
     const double* src = dparams + 4 * d;
@@ -312,27 +320,48 @@ __device__ __forceinline__ void stamp_devices(const Prog& P, const double* dpara
   }
 }
 
-// LU slot values and the permuted right-hand side from the value records:
-// short contribution lists one lane each, long ones (the ground and supply
-// rows and columns) reduced across the instance's lanes.
+// LU slot values and the permuted right-hand side from the value records,
+// each the sum of its contributions in stamping order: lists of up to four
+// as one padded 16-byte record (code 4 pads, never added), two slots per
+// lane in flight; longer lists afterwards, one lane each, and the longest
+// (the ground and supply rows and columns) reduced across the instance's
+// lanes.
+constexpr int kPadCode = 4;
+
+__device__ __forceinline__ double sum4(const double* DV, int4 c) {
+  double acc = contrib(DV, c.x);
+  if (c.y != kPadCode) {
+    acc += contrib(DV, c.y);
+    if (c.z != kPadCode) {
+      acc += contrib(DV, c.z);
+      if (c.w != kPadCode) acc += contrib(DV, c.w);
+    }
+  }
+  return acc;
+}
+
 template <int LPI>
 __device__ __forceinline__ void assemble(const Prog& P, const double* DV, double* V, double* T,
                                          int sl) {
-  for (int v = sl; v < P.nv; v += LPI) {
-    const int t0 = P.amap_ptr[v], t1 = P.amap_ptr[v + 1];
+#pragma unroll 2
+  for (int v = sl; v < P.nv; v += LPI) V[v] = sum4(DV, __ldg(P.amap4 + v));
+#pragma unroll 2
+  for (int i = sl; i < P.n; i += LPI) T[i] = sum4(DV, __ldg(P.rmap4 + i));
+  __syncwarp();  // the longer lists below overwrite their all-pad records' zeros
+  for (int h = sl; h < P.nlng; h += LPI) {
+    const int code = P.lng[h];  // (index << 1) | is_row
+    const int idx = code >> 1;
+    const int* ptr = (code & 1) ? P.rmap_ptr : P.amap_ptr;
+    const int* cds = (code & 1) ? P.rmap_code : P.amap_code;
+    const int key = (code & 1) ? P.in_row[idx] : idx;
+    const int t0 = ptr[key], t1 = ptr[key + 1];
     if (t1 - t0 > kHeavy) continue;
-    // from the first contribution (0.0 + a is a, but for the sign of a zero)
-    double acc = t0 < t1 ? contrib(DV, P.amap_code[t0]) : 0.0;
-    for (int t = t0 + 1; t < t1; ++t) acc += contrib(DV, P.amap_code[t]);
-    V[v] = acc;
-  }
-  for (int i = sl; i < P.n; i += LPI) {
-    const int r = P.in_row[i];
-    const int t0 = P.rmap_ptr[r], t1 = P.rmap_ptr[r + 1];
-    if (t1 - t0 > kHeavy) continue;
-    double acc = t0 < t1 ? contrib(DV, P.rmap_code[t0]) : 0.0;
-    for (int t = t0 + 1; t < t1; ++t) acc += contrib(DV, P.rmap_code[t]);
-    T[i] = acc;
+    double acc = contrib(DV, cds[t0]);
+    for (int t = t0 + 1; t < t1; ++t) acc += contrib(DV, cds[t]);
+    if (code & 1)
+      T[idx] = acc;
+    else
+      V[idx] = acc;
   }
   for (int h = 0; h < P.nheavy; ++h) {
     const int code = P.heavy[h];  // (index << 1) | is_row
@@ -517,12 +546,18 @@ __device__ __forceinline__ void factor_solve(const Prog& P, double* V, double* T
   }
 }
 
-// One operation of a step program on an instance region R (X, T, V):
-// kind 0 R[d] -= R[a] * R[b] (one fma), 4 the same unless R[b] is zero (a
-// factor update by a zero U entry is skipped), 2 R[d] = R[a] * R[b], 1
-// R[d] = 1 / perturbed R[d] (a: the column is a singleton), 3 nothing.
+// One operation of a step program on an instance region R (X, T, V), two
+// 32-bit words: d | a << 15 | kind bits 0-1 << 30 and b | c << 15 | kind
+// bits 2-3 << 30. Kinds: 0 R[d] -= R[a] R[b] (one fma); 4 the same unless
+// R[b] is zero (a factor update by a zero U entry is skipped); 2 R[d] =
+// R[a] R[b]; 1 R[d] = 1 / perturbed R[d] (a: the column is a singleton); 5
+// kind 4 then R[d] *= R[c] (an L entry's last update and its scaling); 6
+// kind 0 then R[d] *= R[c] (a row's last backward update and its pivot);
+// 3 nothing.
 __device__ __forceinline__ void exec_op(int2 o, double* R) {
-  const int d = o.x & 0xffff, a = (int)((unsigned)o.x >> 16), b = o.y & 0xffff, k = o.y >> 16;
+  const unsigned x = (unsigned)o.x, y = (unsigned)o.y;
+  const int d = x & 0x7fff, a = (x >> 15) & 0x7fff, b = y & 0x7fff, c = (y >> 15) & 0x7fff;
+  const int k = (int)((x >> 30) | ((y >> 30) << 2));
   if (k == 1) {
     R[d] = fast_rcp(perturb_bits(R[d], a != 0));
     return;
@@ -533,8 +568,15 @@ __device__ __forceinline__ void exec_op(int2 o, double* R) {
     R[d] = va * vb;
     return;
   }
-  if (k == 4 && !nonzero(vb)) return;
-  R[d] = fma(-va, vb, R[d]);
+  double t = R[d];
+  if (k != 4 && k != 5) {
+    t = fma(-va, vb, t);
+  } else if (nonzero(vb)) {
+    t = fma(-va, vb, t);
+  } else if (k == 4) {
+    return;
+  }
+  R[d] = k >= 5 ? t * R[c] : t;
 }
 
 // The factorization, forward and backward substitution as the group's step
@@ -548,7 +590,7 @@ __device__ __forceinline__ void exec_op(int2 o, double* R) {
 // program in step.
 template <int LPI>
 __device__ __forceinline__ void run_steps(const Prog& P, double* R, int sl) {
-  const int2 nop = make_int2(0, 3 << 16);
+  const int2 nop = make_int2((int)(3u << 30), 0);
   const int2* const ops = P.ops;
   const int* const sp = P.sp;
   int p0 = sp[0], p1 = sp[1];

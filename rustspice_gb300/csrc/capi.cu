@@ -1776,13 +1776,17 @@ void device_codes(int type, int dv, bool transient, int m[8], int r[2]) {
 // - per BTF block the coupling into the block's rows, per column its U
 // entries' updates, the pivot's reciprocal, the L scaling and the forward
 // update of the right-hand side, then the backward sweep - as offsets into
-// an instance's region (X[nc], T[n], ndv unused doubles, V; the batch kernels
-// keep their device records after V, so ndv is 0 there). Each operation goes
-// to the first step
-// after the last step that writes one of its operands or its destination
-// and after the last step that reads its destination, so a step's
-// operations are independent and each value sees its operations in the
-// original order. Regions beyond 16-bit offsets get no step program.
+// an instance's region (X[nc], T[n], ndv unused doubles, V; the batch
+// kernels keep their device records after V, so ndv is 0 there). Two pairs
+// of operations are fused, each into one operation with the same two
+// roundings: an L entry's last update in its column with its scaling by the
+// pivot's reciprocal (nothing reads the entry in between), and a row's last
+// backward update with its multiplication by its pivot's reciprocal. Each
+// operation goes to the first step after the last step that writes one of
+// its operands or its destination and after the last step that reads its
+// destination, so a step's operations are independent and each value sees
+// its operations in the original order. Regions beyond 15-bit offsets get no
+// step program.
 void build_steps(const gk::Plan& P, int nc, int ndv, std::vector<i32>& out_ops,
                  std::vector<i32>& out_steps) {
   out_ops.clear();
@@ -1790,35 +1794,67 @@ void build_steps(const gk::Plan& P, int nc, int ndv, std::vector<i32>& out_ops,
   const int n = P.n, nslots = P.nslots();
   const long long vbase = (long long)nc + n + ndv;
   const long long top = vbase + nslots + (long long)P.offd_raw.size();
-  if (top >= 65536 || n == 0) return;
+  if (top >= 32768 || n == 0) return;
   struct Op {
-    int d, a, b, k;
+    int d, a, b, c, k;
   };
   std::vector<Op> ops;
   auto T_ = [nc](int i) { return nc + i; };
   auto V_ = [vbase](long long v) { return (int)(vbase + v); };
+  std::vector<int> pend_a((size_t)nslots, -1), pend_b((size_t)nslots, -1);
+  std::vector<long long> last_bw((size_t)n, -1);
   for (int b = 0; b < P.nblocks; ++b) {
     const int b0 = P.block_ptr[b], b1 = P.block_ptr[b + 1];
     for (int i = b0; i < b1; ++i)
       for (int e = P.offd_ptr[i]; e < P.offd_ptr[i + 1]; ++e)
-        ops.push_back({T_(i), V_(nslots + e), T_(P.offd_col[e]), 0});
+        ops.push_back({T_(i), V_(nslots + e), T_(P.offd_col[e]), 0, 0});
     for (int k = b0; k < b1; ++k) {
       const int s0 = P.col_ptr[k], ds = P.dslot[k], s1 = P.col_ptr[k + 1];
+      // the column's updates in order; the last one into each L entry waits
+      // for the reciprocal and is fused with the scaling
+      std::vector<std::pair<int, std::pair<int, int>>> upd;  // (dst slot, (a slot, u slot))
       for (int s = s0; s < ds; ++s) {
         const int j = P.slot_row[s];
         const int q0 = P.dslot[j] + 1, q1 = P.col_ptr[j + 1];
         for (int qq = q0; qq < q1; ++qq)
-          ops.push_back({V_(P.upd_dst[P.upd_ptr[s] - q0 + qq]), V_(qq), V_(s), 4});
+          upd.push_back({P.upd_dst[P.upd_ptr[s] - q0 + qq], {qq, s}});
       }
-      ops.push_back({V_(ds), P.col_single[k] ? 1 : 0, V_(ds), 1});
-      for (int qq = ds + 1; qq < s1; ++qq) ops.push_back({V_(qq), V_(qq), V_(ds), 2});
+      std::vector<char> last(upd.size(), 0);
+      for (size_t u = upd.size(); u-- > 0;) {
+        const int dst = upd[u].first;
+        if (dst > ds && dst < s1 && pend_a[dst] < 0) {
+          pend_a[dst] = upd[u].second.first;
+          pend_b[dst] = upd[u].second.second;
+          last[u] = 1;
+        }
+      }
+      for (size_t u = 0; u < upd.size(); ++u)
+        if (!last[u]) ops.push_back({V_(upd[u].first), V_(upd[u].second.first),
+                                     V_(upd[u].second.second), 0, 4});
+      ops.push_back({V_(ds), P.col_single[k] ? 1 : 0, V_(ds), 0, 1});
+      for (int qq = ds + 1; qq < s1; ++qq) {
+        if (pend_a[qq] >= 0) {
+          ops.push_back({V_(qq), V_(pend_a[qq]), V_(pend_b[qq]), V_(ds), 5});
+          pend_a[qq] = pend_b[qq] = -1;
+        } else {
+          ops.push_back({V_(qq), V_(qq), V_(ds), 0, 2});
+        }
+      }
       for (int qq = ds + 1; qq < s1; ++qq)
-        ops.push_back({T_(P.slot_row[qq]), V_(qq), T_(k), 0});
+        ops.push_back({T_(P.slot_row[qq]), V_(qq), T_(k), 0, 0});
     }
     for (int k = b1 - 1; k >= b0; --k) {
       const int s0 = P.col_ptr[k], ds = P.dslot[k];
-      ops.push_back({T_(k), T_(k), V_(ds), 2});
-      for (int s = s0; s < ds; ++s) ops.push_back({T_(P.slot_row[s]), V_(s), T_(k), 0});
+      if (last_bw[k] >= 0) {  // x_k fused into T[k]'s last update
+        ops[(size_t)last_bw[k]].c = V_(ds);
+        ops[(size_t)last_bw[k]].k = 6;
+      } else {
+        ops.push_back({T_(k), T_(k), V_(ds), 0, 2});
+      }
+      for (int s = s0; s < ds; ++s) {
+        last_bw[P.slot_row[s]] = (long long)ops.size();
+        ops.push_back({T_(P.slot_row[s]), V_(s), T_(k), 0, 0});
+      }
     }
   }
   std::vector<int> lw((size_t)top, 0), lr((size_t)top, 0), step(ops.size());
@@ -1827,12 +1863,14 @@ void build_steps(const gk::Plan& P, int nc, int ndv, std::vector<i32>& out_ops,
     const Op& o = ops[q];
     int st = std::max(lw[o.d], lr[o.d]) + 1;
     if (o.k != 1) st = std::max(st, std::max(lw[o.a], lw[o.b]) + 1);
+    if (o.k >= 5) st = std::max(st, lw[o.c] + 1);
     step[q] = st;
     lw[o.d] = st;
     if (o.k != 1) {
       lr[o.a] = std::max(lr[o.a], st);
       lr[o.b] = std::max(lr[o.b], st);
     }
+    if (o.k >= 5) lr[o.c] = std::max(lr[o.c], st);
     nsteps = std::max(nsteps, st);
   }
   std::vector<i32> cnt(nsteps + 2, 0);
@@ -1844,8 +1882,9 @@ void build_steps(const gk::Plan& P, int nc, int ndv, std::vector<i32>& out_ops,
   for (size_t q = 0; q < ops.size(); ++q) {  // program order within a step
     const Op& o = ops[q];
     const int at = pos[step[q] - 1]++;
-    out_ops[2 * at] = (i32)((unsigned)o.d | ((unsigned)o.a << 16));
-    out_ops[2 * at + 1] = (i32)((unsigned)o.b | ((unsigned)o.k << 16));
+    out_ops[2 * at] = (i32)((unsigned)o.d | ((unsigned)o.a << 15) | (((unsigned)o.k & 3u) << 30));
+    out_ops[2 * at + 1] =
+        (i32)((unsigned)o.b | ((unsigned)o.c << 15) | (((unsigned)o.k >> 2) << 30));
   }
 }
 

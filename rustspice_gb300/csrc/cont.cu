@@ -47,6 +47,10 @@ __device__ __forceinline__ bt::Prog global_view(const BatchArgs& A, const GroupH
   P.lvl_col = A.lvl_col + G.col_off;
   P.lseg_ptr = A.lseg_ptr + G.blk_off;
   P.lseg = A.lseg + 3 * G.seg_off;
+  P.amap4 = reinterpret_cast<const int4*>(A.amap4 + G.amap4_off);
+  P.rmap4 = reinterpret_cast<const int4*>(A.rmap4 + G.rmap4_off);
+  P.lng = A.lng + G.lng_off;
+  P.nlng = G.nlng;
   P.ops = A.ops + G.ops_off;
   P.sp = A.step_ptr + G.step_off;
   P.n = G.n;
@@ -63,7 +67,7 @@ __device__ __forceinline__ bt::Prog global_view(const BatchArgs& A, const GroupH
 // bt::run_steps with the program in global memory (read-only path): the
 // next step's operation and pointer are loaded a step ahead.
 __device__ __forceinline__ void run_steps_global(const bt::Prog& P, double* R, int lane) {
-  const int2 nop = make_int2(0, 3 << 16);
+  const int2 nop = make_int2((int)(3u << 30), 0);  // kind 3: nothing
   const int2* const ops = P.ops;
   const int* const sp = P.sp;
   int p0 = __ldg(sp), p1 = __ldg(sp + 1);

@@ -430,14 +430,17 @@ def run_steps(ops, sp, R, order=None):
             order.shuffle(idx)
         for p in idx:
             x, y = int(ops[p, 0]) & 0xffffffff, int(ops[p, 1]) & 0xffffffff
-            d, a, b, k = x & 0xffff, x >> 16, y & 0xffff, y >> 16
+            d, a = x & 0x7fff, (x >> 15) & 0x7fff
+            b, c = y & 0x7fff, (y >> 15) & 0x7fff
+            k = (x >> 30) | ((y >> 30) << 2)
             if k == 1:
                 R[d] = 1.0 / _perturb(R[d], a != 0)
             elif k == 2:
                 R[d] = R[a] * R[b]
-            elif k == 4:
-                if R[b] != 0.0:
-                    R[d] = R[d] - R[a] * R[b]
-            elif k == 0:
-                R[d] = R[d] - R[a] * R[b]
+            elif k in (4, 5):
+                t = R[d] - R[a] * R[b] if R[b] != 0.0 else R[d]
+                R[d] = t * R[c] if k == 5 else t
+            elif k in (0, 6):
+                t = R[d] - R[a] * R[b]
+                R[d] = t * R[c] if k == 6 else t
     return R

@@ -29,12 +29,15 @@ def test_step_program_matches_the_column_path(sysm):
     from plan_emulator import first_factor
     _, rperm = first_factor(N.Plan(n, ap, ai, N.PIVOT_EXACT), ax)
     # any region layout X[nc] T[n] DV[ndv] V[...]; offsets past 32767 too
-    for nc, ndv in ((7, 13), (40000, 9)):
+    nc_hi = 32767 - 9 - (n + P.nslots + len(P.offd_raw)) - 1  # the last fitting layout
+    for nc, ndv in ((7, 13), (nc_hi, 9)):
         prog = N.step_program(n, ap, ai, nc, ndv, N.PIVOT_EXACT, rperm)
         assert prog is not None
         ops, sp = prog
         assert sp[0] == 0 and sp[-1] == len(ops) and np.all(np.diff(sp) > 0)
-        kinds = (ops[:, 1].astype(np.int64) & 0xffffffff) >> 16
+        w0 = ops[:, 0].astype(np.int64) & 0xffffffff
+        w1 = ops[:, 1].astype(np.int64) & 0xffffffff
+        kinds = (w0 >> 30) | ((w1 >> 30) << 2)
         assert np.sum(kinds == 1) == n  # one reciprocal per column
         base = batch_region(P, ax, rhs, nc, ndv)
         want = factor_solve_columns(P, base.copy(), nc, ndv)
@@ -56,5 +59,5 @@ def test_step_program_matches_the_column_path(sysm):
 def test_step_program_absent_beyond_16_bit_offsets():
     c = cz.inverter_chain(8, 0.3)
     n, ap, ai, ax, rhs = po.mna(c, np.zeros(c.node_count))
-    assert N.step_program(n, ap, ai, 65500, 13) is None
+    assert N.step_program(n, ap, ai, 32700, 13) is None
     assert N.step_program(n, ap, ai, 7, 13) is not None
