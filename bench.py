@@ -49,6 +49,8 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the batch's default schedule instead of tuning it first")
+    ap.add_argument("--lane-cap", type=int, default=0,
+                    help="fix the lane phase's iteration cap instead of tuning it (profiling)")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the single-circuit, adjoint, transient and bordered-block lines")
     ap.add_argument("--only", choices=SECONDARY,
@@ -462,7 +464,10 @@ def run_gpu(a):
     with torch.cuda.stream(stream):
         # the project's autotuner picks the lane-phase cap and the
         # continuation's tiles per program from timed runs of this batch
-        if a.no_autotune:
+        if a.lane_cap > 0:
+            bt.set_schedule(a.lane_cap, 2)
+            tune = {"lane_cap": a.lane_cap, "cont_tiles": 2, "runs": 0, "autotuned": False}
+        elif a.no_autotune:
             tune = {"lane_cap": 6, "cont_tiles": 2, "runs": 0, "autotuned": False}
         else:
             tune = dict(bt.autotune(cfg), autotuned=True)
@@ -525,33 +530,41 @@ def run_gpu(a):
     # stamped at x by the device and evaluated on the host, normwise relative
     resid = _residual_sample(B, bt, rs)
 
-    # roofline of the dominant kernel: its share of the algorithmic bytes
-    # (iterations an instance runs in the lane kernel: min(total, cap); the
-    # rest in the warp kernel) over its own event-timed duration
+    # roofline of the dominant kernel. Both kernels keep an instance's
+    # values on chip or in L2 and run FP64 dependency chains: the bound is
+    # the FP64 rate (the DFMA peak measured in this run), with the HBM view
+    # beside it. Per kernel: the iterations an instance runs in the lane
+    # kernel (min(total, cap)) or after it, their algorithmic bytes and FP64
+    # operations, over the kernel's own event-timed duration.
     hbm_peak, peak_src = _measured_peaks()
     per_key = _alg_bytes_per_iter(B.circuits)
     keys = [(B.circuits[c].ndev, B.circuits[c].node_count) for c in B.inst_circ]
     b_inst = np.array([per_key[k] for k in keys], np.float64)
     alg_bytes = float(np.sum(b_inst * itt))
+    flops, _ = bt.work()
+    f_inst = flops.astype(np.float64)
+    fp64 = float(np.sum(f_inst * itt))
+    fp64_tflops = fp64 / (ms_step * 1e-3) / 1e12
+    fp64_peak = float(N.lib().gpuklu_fp64_peak_tflops())
     cap = phases[0]["lane_cap"]
     lane_it = np.minimum(itt, cap) if cap > 0 else np.zeros_like(itt)
+    second = "k_batch_cont" if cap > 0 and bt.info()["launches"] == 2 else "k_batch_newton"
     kern = {}
     for name, ms_k, its in (("k_batch_lanes", "lanes_ms", lane_it),
-                            ("k_batch_newton", "warps_ms", itt - lane_it)):
+                            (second, "warps_ms", itt - lane_it)):
         t_ms = float(np.median([p[ms_k] for p in phases]))
         kb = float(np.sum(b_inst * its))
+        kf = float(np.sum(f_inst * its))
         tr, tr_src = _ncu_traffic(name, int(its.sum()))
         kern[name] = {"ms_per_launch": t_ms, "newton_iterations": int(its.sum()),
                       "algorithmic_bytes_per_launch": kb,
                       "achieved_gbs": kb / (t_ms * 1e-3) / 1e9 if t_ms > 0 else None,
+                      "fp64_ops_per_launch": kf,
+                      "achieved_tflops": kf / (t_ms * 1e-3) / 1e12 if t_ms > 0 else None,
                       "dram_bytes_per_launch": tr, "traffic_source": tr_src}
     dom = max(kern, key=lambda k: kern[k]["ms_per_launch"])
-    achieved = kern[dom]["achieved_gbs"]
+    achieved = kern[dom]["achieved_tflops"]
     traffic, traffic_src = kern[dom]["dram_bytes_per_launch"], kern[dom]["traffic_source"]
-    flops, _ = bt.work()
-    fp64 = float(np.sum(flops.astype(np.float64) * itt))
-    fp64_tflops = fp64 / (ms_step * 1e-3) / 1e12
-    fp64_peak = float(N.lib().gpuklu_fp64_peak_tflops())
 
     # converged-only rates, and the time of the instances that run to the
     # iteration cap: the same step with only the converged instances, timed
@@ -588,11 +601,17 @@ def run_gpu(a):
         "converged_solves_per_s": int(conv_mask.sum()) / (ms_step * 1e-3),
         "capped_instances": capped,
         "one_at_a_time": dict(one, batched_over_one_at_a_time=value / one_at_a_time),
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
-                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                     "traffic_source": traffic_src,
-                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                     "algorithmic_bytes_per_step": alg_bytes, "kernels": kern},
+        "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": fp64_peak,
+                     "unit": "TFLOP/s", "frac": achieved / fp64_peak if fp64_peak else None,
+                     "traffic": traffic, "traffic_source": traffic_src,
+                     "peak_source": "measured DFMA microbenchmark in this run "
+                                    "(gpuklu_fp64_peak_tflops; MEASURED_PEAKS.json has no FP64)",
+                     "hbm_view": {"achieved": kern[dom]["achieved_gbs"], "peak": hbm_peak,
+                                  "unit": "GB/s",
+                                  "frac": kern[dom]["achieved_gbs"] / hbm_peak,
+                                  "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
+                     "algorithmic_bytes_per_step": alg_bytes, "fp64_ops_per_step": fp64,
+                     "kernels": kern},
         "roofline_fp64": {"achieved": fp64_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
                           "frac": fp64_tflops / fp64_peak if fp64_peak else None,
                           "peak_source": "measured DFMA microbenchmark (gpuklu_fp64_peak_tflops)",
@@ -652,7 +671,7 @@ def _converged_only_step(B, conv, cfg, flush, dev, steps):
     return {"instances": int(B.ninst - len(idx)), "converged_only_ms_per_step": ms,
             "converged_only_iterations": int(itt.sum()),
             "converged_only_kernel_ms": {"k_batch_lanes": ph["lanes_ms"],
-                                         "k_batch_newton": ph["warps_ms"]},
+                                         "continuation": ph["warps_ms"]},
             "how": "the same batch with only the converged instances, timed the same way; "
                    "the capped instances cost the difference to ms_per_step"}
 

@@ -562,21 +562,19 @@ __device__ __forceinline__ void exec_op(int2 o, double* R) {
     R[d] = fast_rcp(perturb_bits(R[d], a != 0));
     return;
   }
-  if (k == 3) return;
-  const double va = R[a], vb = R[b];
-  if (k == 2) {
-    R[d] = va * vb;
-    return;
-  }
-  double t = R[d];
-  if (k != 4 && k != 5) {
-    t = fma(-va, vb, t);
-  } else if (nonzero(vb)) {
-    t = fma(-va, vb, t);
-  } else if (k == 4) {
-    return;
-  }
-  R[d] = k >= 5 ? t * R[c] : t;
+  // The other kinds as one fma, so that lanes of a step that mix them issue
+  // one FP64 instruction (and the product only where a lane needs it): kind 2
+  // is fma(a, b, -0), which rounds like a b; kinds 0, 4, 5 and 6 are fma(-a,
+  // b, d), with d kept where kind 4 or 5 skips a zero b. The signs and the
+  // selections are integer operations.
+  const bool mul = k == 2, fused = k >= 5;
+  const double va = R[a], vb = R[b], vd = R[d];
+  const double na = flip_sign(va, mul ? 0ull : 0x8000000000000000ull);
+  const double t = fma(na, vb, mul ? -0.0 : vd);
+  const bool skip = (k == 4 || k == 5) && !nonzero(vb);
+  double r = skip ? vd : t;
+  if (fused) r = r * R[c];
+  if (k != 3) R[d] = r;
 }
 
 // The factorization, forward and backward substitution as the group's step
