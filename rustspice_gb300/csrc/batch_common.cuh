@@ -582,26 +582,30 @@ __device__ __forceinline__ void exec_op(int2 o, double* R) {
 // order and places each in the first step after the steps that write its
 // operands or read its destination, so the operations of one step are
 // independent and every value sees the same operations in the same order
-// as in the column-by-column path (the same results). The instance's lanes
-// take a step's operations in parallel; the next step's first operation is
-// loaded while the current one runs. The warp's instances run the same
-// program in step.
+// as in the column-by-column path (the same results; fused pairs keep both
+// roundings). The instance's lanes take a step's operations in parallel;
+// the next step's operations are loaded while the current one runs. The
+// warp's instances run the same program in step.
 template <int LPI>
 __device__ __forceinline__ void run_steps(const Prog& P, double* R, int sl) {
-  const int2 nop = make_int2((int)(3u << 30), 0);
+  const int2 nop = make_int2((int)(3u << 30), 0);  // kind 3: nothing
   const int2* const ops = P.ops;
   const int* const sp = P.sp;
-  int p0 = sp[0], p1 = sp[1];
-  int2 op = p0 + sl < p1 ? ops[p0 + sl] : nop;
-  for (int t = 0; t < P.nsteps; ++t) {
-    const int q0 = p1, q1 = t + 2 <= P.nsteps ? sp[t + 2] : p1;
-    const int2 next = q0 + sl < q1 ? ops[q0 + sl] : nop;
-    exec_op(op, R);
-    for (int p = p0 + sl + LPI; p < p1; p += LPI) exec_op(ops[p], R);
+  const int ns = P.nsteps;
+  const int nops = sp[ns];
+  // a step's operation and pointer load independently, a step ahead
+  int s0 = sp[0], s1 = sp[1], s2 = ns >= 2 ? sp[2] : s1;
+  int2 o0 = s0 + sl < nops ? ops[s0 + sl] : nop;
+  for (int t = 0; t < ns; ++t) {
+    const int2 o1 = s1 + sl < nops ? ops[s1 + sl] : nop;
+    const int s3 = t + 3 <= ns ? sp[t + 3] : s2;
+    if (s0 + sl < s1) exec_op(o0, R);
+    for (int p = s0 + sl + LPI; p < s1; p += LPI) exec_op(ops[p], R);
     __syncwarp();
-    p0 = q0;
-    p1 = q1;
-    op = next;
+    s0 = s1;
+    s1 = s2;
+    s2 = s3;
+    o0 = o1;
   }
 }
 

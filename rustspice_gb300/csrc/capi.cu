@@ -1649,7 +1649,7 @@ struct gpuklu_batch {
   // continuation kernel: one warp per parked instance from a queue over the
   // groups (cont.cu); off: the warp classes continue them
   bool cont_kernel = false;
-  int cont_grid = 0, cont_wpb = 0;
+  int cont_grid = 0, cont_wpb = 0, cont_m = 1;
   DBuf<i32> d_cont_groups;
   DBuf<unsigned> d_cont_cursor;
   DBuf<double> d_dv;
@@ -2461,12 +2461,19 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       }
       slice = (slice + 1) & ~1;
       dvs = (dvs + 3) & ~3;
-      const int wpb = std::min(16, (int)((size_t)(227 * 1024) / ((size_t)slice * 8)));
+      // instances per warp: one; GPUKLU_CONT_M=2 puts two of a program in a
+      // warp (16 lanes each, a step's FP64 instruction serving both), which
+      // measured slower: the phase waits for its longest instances, and
+      // their iterations take longer with half the lanes
+      const char* ecm = getenv("GPUKLU_CONT_M");
+      const int cm = ecm && ecm[0] == '2' ? 2 : 1;
+      const int wpb = std::min(16, (int)((size_t)(227 * 1024) / ((size_t)cm * slice * 8)));
       if (!(eck && eck[0] == '0') && steps_all && wpb >= 1) {
         int r3 = 0, b3 = 0;
-        gk::cont_kernel_info(wpb, slice, &r3, &b3);
+        gk::cont_kernel_info(cm, wpb, slice, &r3, &b3);
         if (b3 > 0) {
           B->cont_kernel = true;
+          B->cont_m = cm;
           B->cont_wpb = wpb;
           B->cont_grid = sm_count() * b3;
           B->args.slice = slice;
@@ -2475,7 +2482,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
           if (e == cudaSuccess) e = B->d_cont_groups.upload(cg, s);
           if (e == cudaSuccess) e = B->d_cont_cursor.resize(1);
           if (e == cudaSuccess)
-            e = B->d_dv.resize((size_t)B->cont_grid * wpb * (size_t)dvs);
+            e = B->d_dv.resize((size_t)B->cont_grid * wpb * cm * (size_t)dvs);
         }
       }
     } else {
@@ -3008,7 +3015,7 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
     cudaMemsetAsync(b->d_cont_cursor.p, 0, sizeof(unsigned), s);
     gk::BatchArgs ca = b->args;
     ca.cfg = c;
-    gk::launch_batch_cont(ca, b->cont_grid, b->cont_wpb, s);
+    gk::launch_batch_cont(ca, b->cont_m, b->cont_grid, b->cont_wpb, s);
     cudaEventRecord(b->ph_ev[2], s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return b->fail(cuda_msg(e, "batch launch"));

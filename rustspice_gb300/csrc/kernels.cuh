@@ -276,8 +276,9 @@ void launch_batch_newton(const BatchArgs& a, int m, int grid, int warps_per_bloc
                          cudaStream_t s, bool shared = false);
 // Registers per thread and resident blocks per SM of the batched kernel.
 // Lane-per-instance batched Newton (phase 1 of gpuklu_batch_run).
-void launch_batch_cont(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
-void cont_kernel_info(int warps_per_block, int slice, int* regs, int* blocks_per_sm);
+void launch_batch_cont(const BatchArgs& a, int m, int grid, int warps_per_block,
+                       cudaStream_t s);
+void cont_kernel_info(int m, int warps_per_block, int slice, int* regs, int* blocks_per_sm);
 void launch_batch_lanes(const BatchArgs& a, int grid, int warps_per_block, cudaStream_t s);
 void lanes_kernel_info(int warps_per_block, int* regs, int* blocks_per_sm);
 
