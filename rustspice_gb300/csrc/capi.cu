@@ -198,13 +198,64 @@ int make_cta_groups(const gk::Plan& p, int sms, std::vector<i32>& grp, std::vect
   return rows;
 }
 
+// The solve as a step program (k_solve_steps): every operation the column
+// sweeps perform, in their order - per BTF block in solve order the
+// coupling terms of its rows, the forward sweep (L columns ascending), the
+// backward sweep (per column descending: the pivot division, then its U
+// entries) - as (destination row, source row, value index, kind), each
+// placed in the first step after the last step that writes its source or
+// its destination and after the last step that reads its destination. Every
+// row then sees its updates in the sweeps' order, so the results are the
+// sweeps' bit for bit. Plans whose solution vector does not fit one block's
+// shared memory get none.
+void make_solve_steps(const gk::Plan& p, std::vector<int4>& out_ops, std::vector<i32>& out_ptr) {
+  out_ops.clear();
+  out_ptr.clear();
+  if (p.n == 0 || (size_t)8 * p.n + 16 > (size_t)(227 * 1024)) return;
+  std::vector<int4> ops;
+  for (int bb = 0; bb < p.nblocks; ++bb) {
+    const int b = p.offd_lower ? bb : p.nblocks - 1 - bb;
+    const int b0 = p.block_ptr[b], b1 = p.block_ptr[b + 1];
+    for (int i = b0; i < b1; ++i)
+      for (int e = p.offd_ptr[i]; e < p.offd_ptr[i + 1]; ++e)
+        ops.push_back(make_int4(i, p.offd_col[e], p.offd_raw[e], 2));
+    for (int j = b0; j < b1; ++j)
+      for (int q = p.dslot[j] + 1; q < p.col_ptr[j + 1]; ++q)
+        ops.push_back(make_int4(p.slot_row[q], j, q, 0));
+    for (int j = b1 - 1; j >= b0; --j) {
+      ops.push_back(make_int4(j, -1, p.dslot[j], 1));
+      for (int q = p.col_ptr[j]; q < p.dslot[j]; ++q)
+        ops.push_back(make_int4(p.slot_row[q], j, q, 0));
+    }
+  }
+  std::vector<int> lw(p.n, 0), lr(p.n, 0), step(ops.size());
+  int nsteps = 0;
+  for (size_t q = 0; q < ops.size(); ++q) {
+    const int4 o = ops[q];
+    int st = std::max(lw[o.x], lr[o.x]) + 1;
+    if (o.y >= 0) st = std::max(st, lw[o.y] + 1);
+    step[q] = st;
+    lw[o.x] = st;
+    if (o.y >= 0) lr[o.y] = std::max(lr[o.y], st);
+    nsteps = std::max(nsteps, st);
+  }
+  std::vector<i32> cnt(nsteps + 2, 0);
+  for (int st : step) ++cnt[st];
+  out_ptr.assign(nsteps + 1, 0);
+  for (int t = 0; t < nsteps; ++t) out_ptr[t + 1] = out_ptr[t] + cnt[t + 1];
+  std::vector<i32> pos(out_ptr.begin(), out_ptr.end() - 1);
+  out_ops.assign(ops.size(), make_int4(0, 0, 0, 0));
+  for (size_t q = 0; q < ops.size(); ++q) out_ops[pos[step[q] - 1]++] = ops[q];
+}
+
 // Device copy of a Plan.
 struct PlanDev {
   DBuf<i32> col_ptr, dslot, slot_row, upd_ptr, upd_dst, col_single, amap_ptr, amap_idx,
       offd_ptr, offd_col, offd_raw, offdT_ptr, offdT_row, offdT_raw, lrow_ptr, lrow_col,
       lrow_slot, urow_ptr, urow_col,
       urow_slot, in_row, out_col, pcol_ptr, pcol_raw, pcol_q, pos_block, block_ptr, task,
-      ttask, cs_chunk, cs_op, cs_grp, cs_gchunk, cs_gop;
+      ttask, cs_chunk, cs_op, cs_grp, cs_gchunk, cs_gop, ss_ptr;
+  DBuf<int4> ss_ops;
   gk::DPlan dp{}, dpt{};
   int64_t updates = 0;  // multiply-subtract pairs of one refactorization
 
@@ -236,8 +287,17 @@ struct PlanDev {
     if (e == cudaSuccess) e = cs_grp.upload(hg, s);
     if (e == cudaSuccess) e = cs_gchunk.upload(hgc, s);
     if (e == cudaSuccess) e = cs_gop.upload(hgo, s);
+    std::vector<int4> sso;
+    std::vector<i32> ssp;
+    const char* ess = getenv("GPUKLU_SOLVE_STEPS");
+    if (!(ess && ess[0] == '0')) make_solve_steps(p, sso, ssp);
+    if (e == cudaSuccess) e = ss_ops.upload(sso, s);
+    if (e == cudaSuccess) e = ss_ptr.upload(ssp, s);
     updates = (int64_t)p.upd_dst.size();
     gk::DPlan d{};
+    d.ss_nsteps = ssp.empty() ? 0 : (int)ssp.size() - 1;
+    d.ss_ops = ss_ops.p;
+    d.ss_ptr = ss_ptr.p;
     d.n = p.n;
     d.noffd = p.offd_ptr.empty() ? 0 : p.offd_ptr.back();
     d.cs_nchunk = (int)(hc.size() / 4);
@@ -532,6 +592,8 @@ struct gpuklu_handle {
   int64_t factor_count = 0, refactor_count = 0;
   bool cta_ref = false, cta_sol = false;  // one-block refactor / solve for this plan
   bool cta_grp = false;  // the one-block solve over groups of uncoupled BTF blocks
+  bool steps_sol = false;  // the solve as a step program (k_solve_steps)
+  DBuf<double> d_rec;      // its scratch: the pivots' reciprocals
   // Plans with up to this many multiply-subtract pairs refactor in one block.
   // FP64 issue on one SM (a warp instruction per 16 cycles) bounds that
   // kernel: the 32x32 diode mesh (273k pairs) already refactors faster over
@@ -606,6 +668,11 @@ struct gpuklu_handle {
     const bool allow = !(ob && ob[0] == '0');
     cta_ref = allow && pd.updates <= kOneBlockUpdates && gk::refactor_cta_fits(pd.dp);
     cta_sol = allow && gk::solve_cta_fits(pd.dp);
+    // the step-program solve (one block) when the plan has one
+    // (GPUKLU_SOLVE_STEPS=0: no step programs)
+    steps_sol = allow && gk::solve_steps_fits(pd.dp);
+    if (steps_sol && e == cudaSuccess) e = d_rec.resize(std::max<int64_t>(n, 1));
+    if (e != cudaSuccess) return cuda_fail(e, "solve scratch");
     // the solve split over groups of uncoupled BTF blocks when one block does
     // not hold the plan (GPUKLU_SOLVE_GROUPS=1: whenever the plan has groups)
     const char* eg = getenv("GPUKLU_SOLVE_GROUPS");
@@ -917,6 +984,11 @@ struct gpuklu_handle {
       gk::launch_dense_solve((int)n, d_dense.p, d_dpiv.p, d_rhs.p, d_out.p, d_status.p, stream);
       if (!sync) return GPUKLU_OK;
       return check_status("dense solve");
+    }
+    if (steps_sol && !transpose) {
+      gk::launch_solve_steps(pd.dp, d_rhs.p, d_ax.p, d_lu.p, d_rec.p, d_out.p, stream);
+      if (!sync) return GPUKLU_OK;
+      return check_status("solve");
     }
     if ((cta_sol || cta_grp) && !transpose) {
       if (cta_grp)

@@ -883,6 +883,92 @@ __global__ void __launch_bounds__(256) k_solve_cta(DPlan P, const double* __rest
   for (int i = tid; i < m; i += blockDim.x) out[P.out_col[r0 + i]] = w[i];
 }
 
+// a / b correctly rounded, from y = 1/b correctly rounded, by Markstein's
+// correction (P. Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990): q = a y is
+// within an ulp of a / b, the residual r = a - b q is exact in one fma, and
+// q + r y rounded to nearest is the correctly rounded quotient. Three
+// dependent FP64 operations instead of a division's sequence. Operands or a
+// quotient near the ends of the exponent range (zeros, subnormals,
+// infinities, NaN included) take the division itself; the exponent tests are
+// integer operations.
+__device__ __forceinline__ double div_markstein(double a, double b, double y) {
+  const double q = a * y;
+  const unsigned ea = (unsigned)(__double_as_longlong(a) >> 52) & 0x7ffu;
+  const unsigned eb = (unsigned)(__double_as_longlong(b) >> 52) & 0x7ffu;
+  const unsigned eq = (unsigned)(__double_as_longlong(q) >> 52) & 0x7ffu;
+  if (ea - 64u > 1919u || eb - 64u > 1919u || eq - 64u > 1919u) return a / b;
+  const double r = fma(-b, q, a);
+  return fma(r, y, q);
+}
+
+// The solve as a step program, one thread block: the solution vector in
+// shared memory, the pivots' reciprocals computed first (n divisions in
+// parallel), then step by step the operations the column sweeps perform, in
+// the reference's order for every row (each row's updates separately rounded
+// products and differences, the pivot division exact), the operations of a
+// step spread over the block's threads. A step's operation, its matrix value
+// and (for a division) its reciprocal are loaded two steps ahead: none of
+// them depends on the solution.
+constexpr int kSolveStepsThreads = 128;
+
+struct SolveOp {
+  int4 o;
+  double v, y;
+};
+
+__global__ void __launch_bounds__(kSolveStepsThreads)
+    k_solve_steps(DPlan P, const double* __restrict__ rhs, const double* __restrict__ ax,
+                  const double* __restrict__ lu, double* rec, double* out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* const T = reinterpret_cast<double*>(smem_raw);
+  const int tid = threadIdx.x, n = P.n;
+  for (int i = tid; i < n; i += blockDim.x) {
+    T[i] = rhs[P.in_row[i]];
+    rec[i] = 1.0 / lu[P.dslot[i]];
+  }
+  __syncthreads();
+  const int4* const ops = P.ss_ops;
+  const int* const sp = P.ss_ptr;
+  const int ns = P.ss_nsteps;
+  const int nops = sp[ns];
+  auto fetch = [&](int p) {
+    SolveOp f;
+    f.o = make_int4(0, -1, 0, 3);
+    f.v = 0.0;
+    f.y = 0.0;
+    if (p < nops) {
+      f.o = __ldg(ops + p);
+      f.v = f.o.w == 2 ? __ldg(ax + f.o.z) : __ldg(lu + f.o.z);
+      if (f.o.w == 1) f.y = __ldcg(rec + f.o.x);  // written above by this block
+    }
+    return f;
+  };
+  auto exec = [&](const SolveOp& f) {
+    const int d = f.o.x;
+    if (f.o.w == 1)
+      T[d] = div_markstein(T[d], f.v, f.y);
+    else if (f.o.w != 3)
+      T[d] = __dsub_rn(T[d], __dmul_rn(f.v, T[f.o.y]));
+  };
+  int s0 = sp[0], s1 = ns >= 1 ? sp[1] : s0, s2 = ns >= 2 ? sp[2] : s1, s3 = ns >= 3 ? sp[3] : s2;
+  SolveOp f0 = fetch(s0 + tid), f1 = fetch(s1 + tid);
+  for (int t = 0; t < ns; ++t) {
+    const SolveOp f2 = fetch(s2 + tid);
+    const int s4 = t + 4 <= ns ? sp[t + 4] : s3;
+    if (s0 + tid < s1) exec(f0);
+    for (int p = s0 + tid + kSolveStepsThreads; p < s1; p += kSolveStepsThreads) exec(fetch(p));
+    __syncthreads();
+    s0 = s1;
+    s1 = s2;
+    s2 = s3;
+    s3 = s4;
+    f0 = f1;
+    f1 = f2;
+  }
+  for (int i = tid; i < n; i += blockDim.x) out[P.out_col[i]] = T[i];
+}
+
 // --------------------------------------------------------------- devices
 // Level-1 MOSFET exactly as the reference evaluates it
 // (crates/sim-devices/src/bsim/evaluate.rs:285-356 via mod.rs:440-455).
@@ -1568,6 +1654,18 @@ void launch_solve_cta(const DPlan& P, const double* rhs, const double* ax, const
   if (bytes > 48 * 1024)
     cudaFuncSetAttribute(k_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   k_solve_cta<<<1, 256, bytes, s>>>(P, rhs, ax, lu, out, kSolveChunk, 0);
+}
+
+bool solve_steps_fits(const DPlan& P) {
+  return P.n > 0 && P.ss_nsteps > 0 && (size_t)8 * P.n + 16 <= (size_t)smem_optin();
+}
+
+void launch_solve_steps(const DPlan& P, const double* rhs, const double* ax, const double* lu,
+                        double* rec, double* out, cudaStream_t s) {
+  const size_t bytes = (size_t)8 * P.n + 16;
+  if (bytes > 48 * 1024)
+    cudaFuncSetAttribute(k_solve_steps, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k_solve_steps<<<1, kSolveStepsThreads, bytes, s>>>(P, rhs, ax, lu, rec, out);
 }
 
 bool solve_groups_fit(const DPlan& P) {

@@ -29,6 +29,13 @@ struct DPlan {
   // and chunks [grp[4g+2], grp[4g+3]) of cs_gchunk / cs_gop.
   int cs_ngrp, cs_grp_rows;     // groups; rows of the largest
   const int *cs_grp, *cs_gchunk, *cs_gop;
+  // The solve as a step program (k_solve_steps): ss_ptr[ss_nsteps] operations
+  // (destination row, source row or -1, value index, kind: 0 lu value, 2
+  // coupling ax value, 1 division by the pivot lu[value]), ss_nsteps + 1
+  // step pointers; 0 steps: none.
+  int ss_nsteps;
+  const int4* ss_ops;
+  const int* ss_ptr;
   // Polls of a dependency flag before a waiting warp gives up and reports
   // DS_TIMEOUT (kSpinLimit unless the handle sets another).
   unsigned spin_limit;
@@ -245,6 +252,10 @@ bool refactor_cta_fits(const DPlan& P);
 void launch_refactor_cta(const DPlan& P, const double* ax, double* lu, int* status,
                          cudaStream_t s, const PivotCheck& pc = PivotCheck());
 bool solve_cta_fits(const DPlan& P);
+bool solve_steps_fits(const DPlan& P);
+// rec: n doubles of scratch (the pivots' reciprocals)
+void launch_solve_steps(const DPlan& P, const double* rhs, const double* ax, const double* lu,
+                        double* rec, double* out, cudaStream_t s);
 // One block per group of uncoupled BTF blocks (cs_grp); fits when the
 // largest group's rows fit one block's shared memory.
 bool solve_groups_fit(const DPlan& P);
