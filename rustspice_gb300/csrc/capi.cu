@@ -2539,7 +2539,8 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       // their iterations take longer with half the lanes
       const char* ecm = getenv("GPUKLU_CONT_M");
       const int cm = ecm && ecm[0] == '2' ? 2 : 1;
-      const int wpb = std::min(16, (int)((size_t)(227 * 1024) / ((size_t)cm * slice * 8)));
+      int wpb = std::min(16, (int)((size_t)(227 * 1024) / ((size_t)cm * slice * 8)));
+      if (const char* ecw = getenv("GPUKLU_CONT_WARPS")) wpb = std::max(1, std::min(wpb, atoi(ecw)));
       if (!(eck && eck[0] == '0') && steps_all && wpb >= 1) {
         int r3 = 0, b3 = 0;
         gk::cont_kernel_info(cm, wpb, slice, &r3, &b3);
