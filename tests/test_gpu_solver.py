@@ -3,7 +3,7 @@
 Factor and solve results are compared bit for bit where the arithmetic is the
 same (both compile without multiply-add contraction and follow the
 reference's operation order); device stamps of diodes use CUDA's exp, so
-those are compared to 1e-14 relative. Newton results use the north-star
+those are compared to 1e-14 relative. Newton results use the required
 tolerance: relative solution error <= 1e-10.
 """
 import numpy as np
