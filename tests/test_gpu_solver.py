@@ -160,6 +160,22 @@ def test_newton_dc_mesh():
 
 
 def test_batch_matches_oracle():
+    _batch_against_oracle()
+
+
+@pytest.mark.parametrize("switch", ["GPUKLU_CONT_M=2", "GPUKLU_CONT_KERNEL=0",
+                                    "GPUKLU_STEP_PROGRAM=0", "GPUKLU_CONT_WARPS=4",
+                                    "GPUKLU_LANE_CAP=1"])
+def test_batch_paths_match_oracle(switch, monkeypatch):
+    # the batch's other schedules (two instances per continuation warp, the
+    # warp classes, column-order factorization, fewer resident warps, a lane
+    # phase of one iteration) give the oracle's results as well
+    name, value = switch.split("=")
+    monkeypatch.setenv(name, value)
+    _batch_against_oracle()
+
+
+def _batch_against_oracle():
     B = wl.inverter_batch(12, 61, seed=11)
     it_o, rs_o, x_o = po.dc_batch(B.circuits, B.inst_circ, B.inst_dev, B.inst_val,
                                   "nativeklu_exact", nthreads=4,
