@@ -2523,16 +2523,18 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       // values of the largest program, its global slice the device records;
       // as many warps per block as the slices fit (at most 16)
       const char* eck = getenv("GPUKLU_CONT_KERNEL");
-      int slice = 0, dvs = 0;
+      int slice = 0, dvs = 0, ncs = 0;
       bool steps_all = true;
       for (int g : gorder) {
         const gk::GroupHdr& h = B->groups[g];
-        slice = std::max(slice, h.node_count + h.n + h.nslots + h.noffd);
+        slice = std::max(slice, h.n + h.nslots + h.noffd);
         dvs = std::max(dvs, h.ndv);
+        ncs = std::max(ncs, h.node_count);
         if (h.inst_count > 0 && h.nsteps == 0) steps_all = false;
       }
       slice = (slice + 1) & ~1;
-      dvs = (dvs + 3) & ~3;
+      const int dvx = (dvs + 3) & ~3;  // the iterate after the records
+      dvs = dvx + ((ncs + 3) & ~3);
       // instances per warp: one; GPUKLU_CONT_M=2 puts two of a program in a
       // warp (16 lanes each, a step's FP64 instruction serving both), which
       // measured slower: the phase waits for its longest instances, and
@@ -2551,6 +2553,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
           B->cont_grid = sm_count() * b3;
           B->args.slice = slice;
           B->args.dv_stride = dvs;
+          B->args.dv_x = dvx;
           std::vector<i32> cg(gorder.begin(), gorder.end());
           if (e == cudaSuccess) e = B->d_cont_groups.upload(cg, s);
           if (e == cudaSuccess) e = B->d_cont_cursor.resize(1);
@@ -2644,6 +2647,7 @@ gpuklu_batch* batch_build(int64_t ncirc, const int64_t* dev_off, const int64_t* 
       a.cont_cursor = B->d_cont_cursor.p;
       a.dv_scratch = B->d_dv.p;
       a.dv_stride = B->args.dv_stride;
+      a.dv_x = B->args.dv_x;
       a.slice = B->args.slice;
     }
   }

@@ -5,12 +5,12 @@
 // left is mostly the few instances per circuit program that never converge
 // and run to the iteration cap. Here each warp takes one parked instance at
 // a time from a queue over every program (most expensive programs first)
-// and runs its Newton loop to the end: the iterate, the permuted right-hand
-// side and the LU values in the warp's slice of shared memory (the serial
-// factorization chain runs at shared-memory latency), the device records in
-// the warp's slice of a global scratch (written and read by the warp's own
-// lanes, L2 resident), the factorization and substitutions as the program's
-// step program read through the read-only path. A warp that finishes an
+// and runs its Newton loop to the end: the permuted right-hand side and the
+// LU values in the warp's slice of shared memory (the serial factorization
+// chain runs at shared-memory latency), the device records and the iterate
+// in the warp's slice of a global scratch (written and read by the warp's
+// own lanes, L2 resident), the factorization and substitutions as the
+// program's step program read through the read-only path. A warp that finishes an
 // instance takes the next one at once: no warp waits for the others of its
 // block, and no block stages a program.
 #include <cfloat>
@@ -139,9 +139,13 @@ __global__ void k_batch_cont(BatchArgs A) {
     const GroupHdr G = A.groups[g];
     const bt::Prog P = global_view(A, G);
     const int n = P.n, nc = P.nc;
-    double* const X = S;
-    double* const T = X + nc;
+    // shared: T, V; global (L2): the records and the iterate. The step
+    // program addresses T at nc and V at nc + n from a base nc doubles
+    // before the slice (it touches no X entry).
+    double* const X = DV + A.dv_x;
+    double* const T = S;
     double* const V = T + n;
+    double* const R = S - nc;
     int inst = k0 + sub < cnt ? A.cont_list[G.inst_begin + (int)(k0 + sub)] : -1;
     bool exhausted = inst < 0;
     int it = 0, total = 0, gstep = 0, ov_dev = -1;
@@ -191,7 +195,7 @@ __global__ void k_batch_cont(BatchArgs A) {
       __syncwarp();
       bt::assemble<LPI>(P, DV, V, T, sl);
       __syncwarp();
-      run_steps_global<LPI>(P, X, sl);
+      run_steps_global<LPI>(P, R, sl);
       // ---- Newton update (crates/sim-core/src/newton.rs:93-107), as the
       // warp kernel does it
       bool conv = true, fin = true;

@@ -164,9 +164,10 @@ struct BatchArgs {
   const int* cont_groups;      // the groups, most expensive first
   int cont_ngroups;
   unsigned* cont_cursor;       // first entry of cont_groups that may have parked instances
-  double* dv_scratch;          // per warp: device records, dv_stride doubles
-  long long dv_stride;
-  int slice;                   // shared doubles per warp: X, T and the LU values
+  double* dv_scratch;          // per instance slot: device records, then the iterate
+  long long dv_stride;         //   at dv_x (dv_stride doubles per slot)
+  long long dv_x;
+  int slice;                   // shared doubles per instance slot: T and the LU values
 };
 
 // Batched adaptive transient (atran.cu): per instance its time-dependent
