@@ -273,7 +273,7 @@ int gpuklu_dc_sweep(gpuklu_handle* h, gpuklu_circuit* c, const gpuklu_newton_con
  * sources carry the AC magnitude in p[1] and the phase [deg] in p[2]. x_dc:
  * the operating point (node voltages at least); freqs: nf frequencies [Hz];
  * out_re / out_im: nf x n values (n = node_count + one aux per V source, row
- * 0 the ground); *n_out = n. Systems up to n = 119 are factored in one
+ * 0 the ground); *n_out = n. Systems up to n = 118 are factored in one
  * block's shared memory per frequency; larger ones in per-block slices of a
  * global scratch (up to ~2 GB, blocks looping over the frequencies) with the
  * same arithmetic. n above GPUKLU_AC_MAX_N gives GPUKLU_INVALID_MATRIX, a

@@ -2,7 +2,7 @@
 // crates/sim-core/src/engine.rs:829-930, complex_solver.rs:28-144).
 //
 // One thread block per frequency point keeps the dense complex system in
-// shared memory (n up to 112), or, for larger systems, in its own slice of a
+// shared memory (n up to 118), or, for larger systems, in its own slice of a
 // global scratch (L2 / HBM; blocks loop over the frequencies): it fills
 // Y(w) = G + jwC cell by cell (G from the DC stamp at the operating point,
 // the capacitor terms +-w*C in insertion order), then runs the reference's
