@@ -548,10 +548,11 @@ def run_gpu(a):
     fp64_peak = float(N.lib().gpuklu_fp64_peak_tflops())
     cap = phases[0]["lane_cap"]
     lane_it = np.minimum(itt, cap) if cap > 0 else np.zeros_like(itt)
-    second = "k_batch_cont" if cap > 0 and bt.info()["launches"] == 2 else "k_batch_newton"
+    second = "k_batch_cont" if bt.info()["cont_kernel"] else "k_batch_newton"
     kern = {}
-    for name, ms_k, its in (("k_batch_lanes", "lanes_ms", lane_it),
-                            (second, "warps_ms", itt - lane_it)):
+    phases_run = ([("k_batch_lanes", "lanes_ms", lane_it)] if cap > 0 else []) + \
+        [(second, "warps_ms", itt - lane_it)]
+    for name, ms_k, its in phases_run:
         t_ms = float(np.median([p[ms_k] for p in phases]))
         kb = float(np.sum(b_inst * its))
         kf = float(np.sum(f_inst * its))
@@ -571,7 +572,7 @@ def run_gpu(a):
     # the same way (the difference is what the capped ones cost)
     conv_mask = rs == 0
     conv_iters = int(itt[conv_mask].sum())
-    capped = _converged_only_step(B, conv_mask, cfg, flush, dev, a.steps)
+    capped = _converged_only_step(B, conv_mask, cfg, flush, dev, a.steps, tune)
     # one-at-a-time GpuKluSolver: the engine's DC sweep of a chain over the
     # 61 input points, one handle per chain, the pattern analysed on the
     # sweep's first point and reused for the others (engine.rs:684-820)
@@ -653,10 +654,10 @@ def _timed_runs(bt, cfg, flush, steps):
     return float(np.mean([e0.elapsed_time(e1) for e0, e1 in evs]))
 
 
-def _converged_only_step(B, conv, cfg, flush, dev, steps):
+def _converged_only_step(B, conv, cfg, flush, dev, steps, sched=None):
     """The batch restricted to the instances that converged, timed like the
-    full step: what the instances that run to the iteration cap cost is the
-    difference."""
+    full step (with the same schedule): what the instances that run to the
+    iteration cap cost is the difference."""
     from rustspice_gb300.solver import Batch
     idx = np.flatnonzero(conv)
     x0 = np.concatenate([B.x0[B.x0_off[i]:B.x0_off[i] + B.circuits[B.inst_circ[i]].node_count]
@@ -664,6 +665,8 @@ def _converged_only_step(B, conv, cfg, flush, dev, steps):
     off = np.concatenate([[0], np.cumsum([B.circuits[B.inst_circ[i]].node_count
                                           for i in idx])[:-1]]).astype(np.int64)
     bt = Batch(B.circuits, B.inst_circ[idx], B.inst_dev[idx], B.inst_val[idx], x0, off)
+    if sched is not None:
+        bt.set_schedule(sched["lane_cap"], sched["cont_tiles"])
     ms = _timed_runs(bt, cfg, flush, max(3, steps // 2))
     _, itt, rs, _ = bt.results(with_x=False)
     ph = bt.phase_ms()

@@ -350,14 +350,16 @@ void* gpuklu_batch_stream(gpuklu_batch* b);
 int gpuklu_batch_phase_ms(gpuklu_batch* b, double* out);
 /* The batch's schedule; no counterpart in the reference. lane_cap: Newton
  * iterations an instance runs in the lane-per-instance phase before it is
- * parked for the warp kernels (default 6; ignored when that phase is off);
- * cont_tiles: shared-program tiles per circuit program in the continuation
- * (default 2). Results agree across schedules to the batch's 1e-10 bar
- * (an instance's arithmetic differs between the lane and warp kernels only
- * in rounding). */
+ * parked for the continuation (default 6; ignored when that phase is off;
+ * 0 with the continuation kernel: no lane phase, the continuation starts
+ * every instance); cont_tiles: shared-program tiles per circuit program in
+ * the warp classes' continuation (default 2; the continuation kernel has
+ * none). Results agree across schedules to the batch's 1e-10 bar (an
+ * instance's arithmetic differs between the kernels only in rounding). */
 int gpuklu_batch_set_schedule(gpuklu_batch* b, int lane_cap, int cont_tiles);
 /* Autotuner: times one run of the batch per candidate schedule (lane_cap in
- * {3, 4, 5, 6, 8, 10, 12}, cont_tiles in {1, 2, 3, 4}; two rounds of
+ * {0, 1, 2, 3, 4, 5, 6, 8, 10, 12}, cont_tiles in {1, 2, 3, 4} for the warp
+ * classes' continuation; two rounds of
  * coordinate descent from the current schedule, CUDA events around the
  * kernels) and keeps the fastest. out[0..2] = lane_cap, cont_tiles, runs;
  * *best_ms its device time. The batch's results afterwards are those of the

@@ -3082,16 +3082,18 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
     cudaMemsetAsync(b->d_gnext2.p, 0, b->d_gnext2.n * sizeof(unsigned), s);
   }
   cudaEventRecord(b->ph_ev[0], s);
-  if (b->lanes) {
+  const bool fresh = b->lanes && b->cont_kernel && b->lane_cap == 0;
+  if (b->lanes && !fresh) {
     gk::BatchArgs la = b->args;
     la.cfg = c;
     gk::launch_batch_lanes(la, b->lane_grid, b->lane_wpb, s);
   }
   cudaEventRecord(b->ph_ev[1], s);
-  if (b->lanes && b->cont_kernel) {  // phase 2: one warp per parked instance
+  if (b->lanes && b->cont_kernel) {  // phase 2: one warp per parked instance (or all)
     cudaMemsetAsync(b->d_cont_cursor.p, 0, sizeof(unsigned), s);
     gk::BatchArgs ca = b->args;
     ca.cfg = c;
+    ca.cont_fresh = fresh ? 1 : 0;
     gk::launch_batch_cont(ca, b->cont_m, b->cont_grid, b->cont_wpb, s);
     cudaEventRecord(b->ph_ev[2], s);
     cudaError_t e = cudaGetLastError();
@@ -3122,9 +3124,12 @@ int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg) {
 
 int gpuklu_batch_set_schedule(gpuklu_batch* b, int lane_cap, int cont_tiles) {
   if (!b) return GPUKLU_INVALID_MATRIX;
-  if (cont_tiles < 1 || cont_tiles > 16 || (b->lanes && (lane_cap < 1 || lane_cap > 100)))
-  {
-    b->err = "gpuklu_batch_set_schedule: lane_cap in 1..100 and cont_tiles in 1..16";
+  // lane cap 0: no lane phase, the continuation kernel starts every instance
+  const int cap_lo = b->cont_kernel ? 0 : 1;
+  if (cont_tiles < 1 || cont_tiles > 16 ||
+      (b->lanes && (lane_cap < cap_lo || lane_cap > 100))) {
+    b->err = std::string("gpuklu_batch_set_schedule: lane_cap in ") + std::to_string(cap_lo) +
+             "..100 and cont_tiles in 1..16";
     return GPUKLU_INVALID_MATRIX;
   }
   cudaError_t e = cudaStreamSynchronize(b->stream);  // no run may still read the tiles
@@ -3165,8 +3170,10 @@ int gpuklu_batch_autotune(gpuklu_batch* b, const gpuklu_newton_config* cfg, int6
     *ms = ph[0] + ph[1];
     return st;
   };
-  static const int caps[] = {3, 4, 5, 6, 8, 10, 12};
+  static const int caps[] = {0, 1, 2, 3, 4, 5, 6, 8, 10, 12};
   static const int cts[] = {1, 2, 3, 4};
+  // the continuation kernel has no tiles: only the cap is searched then
+  const bool tiles = !(b->lanes && b->cont_kernel);
   int cap = b->lanes ? b->lane_cap : 1, ct = b->cont_tiles, trials = 0;
   double best = 0.0;
   int st = timed(cap, ct, &best);  // warm-up, then the current schedule
@@ -3176,14 +3183,14 @@ int gpuklu_batch_autotune(gpuklu_batch* b, const gpuklu_newton_config* cfg, int6
     const int cap0 = cap, ct0 = ct;
     if (b->lanes)
       for (int c : caps) {
-        if (c == cap || st != GPUKLU_OK) continue;
+        if (c == cap || st != GPUKLU_OK || (c == 0 && !b->cont_kernel)) continue;
         double ms = 0.0;
         st = timed(c, ct, &ms);
         ++trials;
         if (st == GPUKLU_OK && ms < best) best = ms, cap = c;
       }
     for (int c : cts) {
-      if (c == ct || st != GPUKLU_OK) continue;
+      if (!tiles || c == ct || st != GPUKLU_OK) continue;
       double ms = 0.0;
       st = timed(cap, c, &ms);
       ++trials;
@@ -3272,7 +3279,9 @@ int gpuklu_batch_info(const gpuklu_batch* b, int64_t* out) {
   if (!b) return GPUKLU_INVALID_MATRIX;
   for (int q = 0; q < 8; ++q) out[q] = 0;
   out[2] = (int64_t)b->groups.size();
-  out[6] = b->lanes && b->cont_kernel ? 2 : (int64_t)b->classes.size() + (b->lanes ? 1 : 0);
+  out[6] = b->lanes && b->cont_kernel ? (b->lane_cap == 0 ? 1 : 2)
+                                       : (int64_t)b->classes.size() + (b->lanes ? 1 : 0);
+  out[7] = b->lanes && b->cont_kernel ? 1 : 0;  // the continuation kernel runs
   for (auto& C : b->classes) {  // the largest class (first) describes the launch
     out[0] += C->grid;
     if (out[1] == 0) {

@@ -123,10 +123,11 @@ __global__ void k_batch_cont(BatchArgs A) {
         if (c >= (unsigned)A.cont_ngroups) break;
         const int gg = A.cont_groups[c];
         const unsigned k = atomicAdd(&A.gnext2[gg], (unsigned)M);
-        if (k < A.cont_count[gg]) {
+        const unsigned count = A.cont_fresh ? (unsigned)A.groups[gg].inst_count : A.cont_count[gg];
+        if (k < count) {
           g = gg;
           k0 = k;
-          cnt = A.cont_count[gg];
+          cnt = count;
           break;
         }
         atomicCAS(A.cont_cursor, c, c + 1);
@@ -146,17 +147,28 @@ __global__ void k_batch_cont(BatchArgs A) {
     double* const T = S;
     double* const V = T + n;
     double* const R = S - nc;
-    int inst = k0 + sub < cnt ? A.cont_list[G.inst_begin + (int)(k0 + sub)] : -1;
+    // a program's instances: those the lane phase parked, or all of them
+    const int* const list = A.cont_fresh ? A.order : A.cont_list;
+    int inst = k0 + sub < cnt ? list[G.inst_begin + (int)(k0 + sub)] : -1;
     bool exhausted = inst < 0;
     int it = 0, total = 0, gstep = 0, ov_dev = -1;
     long long xo = 0;
     double damp = 0.0, prev = 0.0, gmin = 0.0, ov_val = 0.0;
     const double* dparams = nullptr;
-    auto resume = [&]() {  // where the lane phase parked the instance
+    auto resume = [&]() {  // where the lane phase parked the instance, or its start
       dparams = A.dparams + A.inst_p_off[inst];
       ov_dev = A.inst_ov_dev[inst];
       ov_val = A.inst_ov_val[inst];
       xo = A.inst_x_off[inst];
+      if (A.cont_fresh) {
+        const long long x0o = A.inst_x0_off[inst];
+        for (int i = sl; i < nc; i += LPI) X[i] = x0o >= 0 ? A.x0[x0o + i] : 0.0;
+        it = total = gstep = 0;
+        damp = cfg.damping;
+        prev = DBL_MAX;
+        gmin = cfg.gmin_steps == 0 ? cfg.gmin : gstart;
+        return;
+      }
       for (int i = sl; i < nc; i += LPI) X[i] = A.x_out[xo + i];
       it = A.cont_it[inst];
       total = A.cont_total[inst];

@@ -168,6 +168,7 @@ struct BatchArgs {
   long long dv_stride;         //   at dv_x (dv_stride doubles per slot)
   long long dv_x;
   int slice;                   // shared doubles per instance slot: T and the LU values
+  int cont_fresh;              // 1: no lane phase ran, the continuation starts every instance
 };
 
 // Batched adaptive transient (atran.cu): per instance its time-dependent

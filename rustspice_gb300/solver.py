@@ -391,7 +391,7 @@ class Batch:
         N.lib().gpuklu_batch_info(self._h, N.ptr(out))
         return dict(grid=int(out[0]), block=int(out[1]), groups=int(out[2]),
                     smem_per_warp=int(out[3]), regs=int(out[4]), blocks_per_sm=int(out[5]),
-                    launches=int(out[6]))
+                    launches=int(out[6]), cont_kernel=bool(out[7]))
 
     def work(self):
         """Per instance: FP64 operations and on-chip value bytes of one iteration."""

@@ -279,8 +279,8 @@ def test_batch_autotune_and_schedules():
     bt.run(cfg)
     _, itt, rs, x = bt.results()
     ch = bt.autotune(cfg)
-    assert ch["lane_cap"] in (3, 4, 5, 6, 8, 10, 12) and ch["cont_tiles"] in (1, 2, 3, 4)
-    assert ch["runs"] >= 11 and ch["best_ms"] > 0.0
+    assert ch["lane_cap"] in (0, 1, 2, 3, 4, 5, 6, 8, 10, 12) and ch["cont_tiles"] in (1, 2, 3, 4)
+    assert ch["runs"] >= 10 and ch["best_ms"] > 0.0
     bt.run(cfg)
     _, itt2, rs2, x2 = bt.results()
     assert np.mean(rs == rs2) >= 0.98
@@ -289,7 +289,7 @@ def test_batch_autotune_and_schedules():
         n = B.circuits[B.inst_circ[i]].n
         a, b = x[bt.x_off[i]:bt.x_off[i] + n], x2[bt.x_off[i]:bt.x_off[i] + n]
         assert np.max(np.abs(a - b)) <= 1e-10 * max(1.0, np.max(np.abs(a)))
-    for cap, ct in ((3, 1), (12, 4)):
+    for cap, ct in ((0, 2), (3, 1), (12, 4)):  # 0: the continuation starts every instance
         bt.set_schedule(cap, ct)
         bt.run(cfg)
         assert bt.phase_ms()["lane_cap"] == cap
@@ -300,5 +300,5 @@ def test_batch_autotune_and_schedules():
     _, itt4, rs4, x4 = bt.results()
     assert np.array_equal(x, x4) and np.array_equal(itt, itt4) and np.array_equal(rs, rs4)
     with pytest.raises(SolverError) as e:
-        bt.set_schedule(0, 2)
+        bt.set_schedule(-1, 2)
     assert e.value.status == N.INVALID_MATRIX
