@@ -518,6 +518,15 @@ void gpuklu_plan_free(gpuklu_plan* p);
  * offsets); copies when the capacities (in int32) suffice. */
 int64_t gpuklu_plan_steps(const gpuklu_plan* p, int32_t nc, int32_t ndv, int32_t* ops,
                           int64_t ops_cap, int32_t* step_ptr, int64_t steps_cap);
+/* The single-system solve's step program (k_solve_steps) for this plan: four
+ * int32 per operation (destination row, source row or -1, value index, kind:
+ * 0 x[d] -= lu[v] x[s], 2 x[d] -= ax[v] x[s] (block coupling), 1 x[d] /= lu[v]
+ * (the pivot)) in step order, with the rows in the plan's positions, and the
+ * step pointers. Returns nops << 32 | (nsteps + 1) (0: no program, the
+ * solution exceeds one block's shared memory); copies when the capacities
+ * (in int32) suffice. */
+int64_t gpuklu_plan_solve_steps(const gpuklu_plan* p, int32_t* ops, int64_t ops_cap,
+                                int32_t* step_ptr, int64_t steps_cap);
 /* btf_decompose (crates/sim-core/src/btf.rs:143-550) on the host: out[0] the
  * number of blocks, out[1] the largest block's size - what
  * MatrixProperties::analyze (solver.rs:276-301) reads for the solver

@@ -3985,6 +3985,23 @@ int64_t gpuklu_plan_steps(const gpuklu_plan* p, int32_t nc, int32_t ndv, int32_t
   return (int64_t)(o.size() / 2) * ((int64_t)1 << 32) + (int64_t)sp.size();
 }
 
+int64_t gpuklu_plan_solve_steps(const gpuklu_plan* p, int32_t* ops, int64_t ops_cap,
+                                int32_t* step_ptr, int64_t steps_cap) {
+  if (!p) return -1;
+  std::vector<int4> o;
+  std::vector<i32> sp;
+  make_solve_steps(p->p, o, sp);
+  if (ops && (int64_t)o.size() * 4 <= ops_cap)
+    for (size_t q = 0; q < o.size(); ++q) {
+      ops[4 * q] = o[q].x;
+      ops[4 * q + 1] = o[q].y;
+      ops[4 * q + 2] = o[q].z;
+      ops[4 * q + 3] = o[q].w;
+    }
+  if (step_ptr && (int64_t)sp.size() <= steps_cap) std::copy(sp.begin(), sp.end(), step_ptr);
+  return (int64_t)o.size() * ((int64_t)1 << 32) + (int64_t)sp.size();
+}
+
 gpuklu_plan* gpuklu_plan_build(int64_t n, const int64_t* ap, const int64_t* ai, int pivot_mode,
                                int kind, const int32_t* row_perm) {
   auto P = std::make_unique<gpuklu_plan>();

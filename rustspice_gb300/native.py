@@ -38,7 +38,7 @@ SYMBOLS = [
     "gpuklu_batch_update_inputs", "gpuklu_batch_last_error", "gpuklu_batch_info",
     "gpuklu_batch_stream", "gpuklu_batch_work", "gpuklu_batch_phase_ms", "gpuklu_batch_set_schedule", "gpuklu_batch_autotune", "gpuklu_ac_sweep", "gpuklu_tran_create", "gpuklu_tran_forward", "gpuklu_atran_create", "gpuklu_atran_run",
     "gpuklu_tran_backward", "gpuklu_bbd_create", "gpuklu_bbd_destroy", "gpuklu_bbd_last_error",
-    "gpuklu_bbd_info", "gpuklu_bbd_perm", "gpuklu_bbd_factor", "gpuklu_bbd_solve", "gpuklu_bbd_newton_dc", "gpuklu_fp64_peak_tflops", "gpuklu_fp64_mma_peak_tflops", "gpuklu_dense_lu_nopivot", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free", "gpuklu_plan_steps", "gpuklu_btf_info",
+    "gpuklu_bbd_info", "gpuklu_bbd_perm", "gpuklu_bbd_factor", "gpuklu_bbd_solve", "gpuklu_bbd_newton_dc", "gpuklu_fp64_peak_tflops", "gpuklu_fp64_mma_peak_tflops", "gpuklu_dense_lu_nopivot", "gpuklu_solve_device_noalloc", "gpuklu_dc_backward", "gpuklu_plan_build", "gpuklu_plan_array", "gpuklu_plan_free", "gpuklu_plan_steps", "gpuklu_plan_solve_steps", "gpuklu_btf_info",
 ]
 
 
@@ -142,6 +142,7 @@ def lib(build_if_missing: bool = True):
         "gpuklu_plan_array": (_I64, [_P, C.c_char_p, _P, _I64]),
         "gpuklu_plan_free": (None, [_P]),
         "gpuklu_plan_steps": (_I64, [_P, C.c_int32, C.c_int32, _P, _I64, _P, _I64]),
+        "gpuklu_plan_solve_steps": (_I64, [_P, _P, _I64, _P, _I64]),
         "gpuklu_btf_info": (C.c_int, [_I64, _P, _P, _P]),
     }
     for name, (res, args) in sig.items():
@@ -196,6 +197,31 @@ def step_program(n, ap, ai, nc, ndv, pivot_mode=PIVOT_REFERENCE, row_perm=None,
         sp = np.zeros(nsp, np.int32)
         L.gpuklu_plan_steps(h, nc, ndv, ptr(ops), len(ops), ptr(sp), len(sp))
         return ops.reshape(nops, 2), sp
+    finally:
+        L.gpuklu_plan_free(h)
+
+
+def solve_step_program(n, ap, ai, pivot_mode=PIVOT_REFERENCE, row_perm=None,
+                       kind="nativeklu"):
+    """The single-system solve's step program for a pattern's plan
+    (gpuklu_plan_solve_steps): (ops[nops, 4] int32, step_ptr[nsteps + 1]), or
+    None when the solution exceeds one block's shared memory."""
+    L = lib()
+    ap, ai = i64(ap), i64(ai)
+    rp = i32(row_perm) if row_perm is not None else None
+    h = L.gpuklu_plan_build(n, ptr(ap), ptr(ai), pivot_mode, KINDS[kind],
+                            ptr(rp) if rp is not None else None)
+    if not h:
+        raise ValueError("plan build failed")
+    try:
+        r = L.gpuklu_plan_solve_steps(h, None, 0, None, 0)
+        nops, nsp = r >> 32, r & 0xffffffff
+        if nsp == 0:
+            return None
+        ops = np.zeros(4 * nops, np.int32)
+        sp = np.zeros(nsp, np.int32)
+        L.gpuklu_plan_solve_steps(h, ptr(ops), len(ops), ptr(sp), len(sp))
+        return ops.reshape(nops, 4), sp
     finally:
         L.gpuklu_plan_free(h)
 

@@ -61,3 +61,51 @@ def test_step_program_absent_beyond_16_bit_offsets():
     n, ap, ai, ax, rhs = po.mna(c, np.zeros(c.node_count))
     assert N.step_program(n, ap, ai, 32700, 13) is None
     assert N.step_program(n, ap, ai, 7, 13) is not None
+
+
+def _run_solve_steps(ops, sp, P, ax, lu, rhs, order=None):
+    """The single-system solve's step program (gpuklu_plan_solve_steps) on
+    the CPU: products and differences separately rounded, the pivot division
+    exact, a step's operations in the given order."""
+    T = np.zeros(P.n)
+    T[P.in_pos] = rhs
+    for t in range(len(sp) - 1):
+        idx = list(range(sp[t], sp[t + 1]))
+        if order == "reverse":
+            idx.reverse()
+        elif order is not None:
+            order.shuffle(idx)
+        for p in idx:
+            d, s, v, k = (int(x) for x in ops[p])
+            if k == 1:
+                T[d] = T[d] / lu[v]
+            else:
+                T[d] = T[d] - (ax[v] if k == 2 else lu[v]) * T[s]
+    return T[P.out_pos]
+
+
+@pytest.mark.parametrize("mode", [N.PIVOT_REFERENCE, N.PIVOT_EXACT], ids=["reference", "exact"])
+@pytest.mark.parametrize("sysm", STEP_SYSTEMS, ids=[s[0] for s in STEP_SYSTEMS])
+def test_solve_step_program_matches_the_sweeps(sysm, mode):
+    """The solve's step program, run step by step with each step's
+    operations in listed, reversed or shuffled order, gives the device
+    solve's results bit for bit (the row-oriented emulation the plan-parity
+    tests pin to the oracle): every row sees its updates in the sweeps'
+    order."""
+    from plan_emulator import first_factor, solve
+    name, ap, ai, ax, rhs = sysm
+    n = len(ap) - 1
+    es = EmulatedSolver(mode)
+    es.factor(n, ap, ai, ax)
+    _, rperm = first_factor(N.Plan(n, ap, ai, mode), ax)
+    prog = N.solve_step_program(n, ap, ai, mode, rperm)
+    assert prog is not None
+    ops, sp = prog
+    assert sp[0] == 0 and sp[-1] == len(ops) and np.all(np.diff(sp) > 0)
+    assert np.sum(ops[:, 3] == 1) == n  # one pivot division per row
+    want = solve(es.plan, es.ax, es.lu, np.asarray(rhs, np.float64))
+    for order in (None, "reverse", np.random.default_rng(3)):
+        got = _run_solve_steps(ops, sp, es.plan, es.ax, es.lu, np.asarray(rhs, np.float64),
+                               order)
+        assert np.array_equal(got, want), (name, order, np.max(np.abs(got - want)))
+    assert len(sp) - 1 <= len(ops)
