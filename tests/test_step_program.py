@@ -1,9 +1,11 @@
-"""The batched warp kernel's step program (gpuklu_plan_steps) on the CPU:
-its operations, executed step by step with each step's operations in
-reverse or shuffled order, give bit for bit the factors and the solution of
-the column-by-column path they replace, on the exact-pivot plans of the
-circuits and matrices of the plan-parity tests; the solution also agrees
-with a dense solve."""
+"""Step programs on the CPU. The batched kernels' (gpuklu_plan_steps): its
+operations, executed step by step with each step's operations in reverse or
+shuffled order, give bit for bit the factors and the solution of the
+column-by-column path they replace, on the exact-pivot plans of the circuits
+and matrices of the plan-parity tests; the solution also agrees with a dense
+solve. The single-system solve's (gpuklu_plan_solve_steps): on the same
+systems in both pivot modes, in any order within a step, it gives the device
+solve's results bit for bit."""
 import numpy as np
 import pytest
 
