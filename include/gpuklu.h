@@ -313,8 +313,9 @@ gpuklu_batch* gpuklu_batch_create(int64_t ncirc, const int64_t* dev_off,
                                   const int64_t* x0_off, int64_t x0_len);
 void gpuklu_batch_destroy(gpuklu_batch* b);
 /* Runs every instance's Newton loop on the device: a lane-per-instance
- * kernel for the first iterations, then the warp kernels for the instances
- * still iterating. */
+ * kernel for the first lane_cap iterations, then the continuation kernel (one
+ * warp per instance still iterating; the warp classes when it is off); with
+ * lane_cap 0 the continuation kernel starts every instance. */
 int gpuklu_batch_run(gpuklu_batch* b, const gpuklu_newton_config* cfg);
 /* Results: per instance iterations (final run), total iterations, exit
  * reason, and x (n of its circuit values, at x_out + x_off[i]; x_off may be
